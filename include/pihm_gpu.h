@@ -1,0 +1,197 @@
+/*
+ * pihm_gpu.h -- C ABI of the GB300 (sm_103a) PIHM right-hand-side library.
+ *
+ * The library evaluates the CVODE right-hand side of the PIHM hydrologic
+ * model -- surface, unsaturated and groundwater storage of every triangular
+ * element plus stage and bed groundwater of every river segment -- with
+ * hand-written FP64 CUDA kernels, and supplies a device-resident N_Vector
+ * whose operations run on the same GPU.
+ *
+ * Everything here is plain C: pointers, sizes and status codes.  No CUDA or
+ * torch type appears in a signature; CUDA streams travel as `void *`
+ * (a cudaStream_t, NULL = the legacy default stream).
+ *
+ * Conventions shared with the reference model (lj-cug/PIHM-CUDA):
+ *   - state vector y, length NEQ = 3*nelem + 2*nriver, blocks
+ *     [surf | unsat | gw | stage | rivgw]      (src/include/pihm_func.h:7-11)
+ *   - element neighbour ids are 1-based, a negative id -k is river segment k,
+ *     0 is the domain boundary                 (src/include/elem_struct.h:1561,
+ *                                               src/init_river.c:23-33)
+ *   - river `down` is a 1-based segment id, or an outlet boundary type
+ *     -1..-4 (DIRICHLET, NEUMANN, ZERO_DPTH_GRAD, CRIT_DPTH)
+ *                                              (src/include/pihm_const.h:140-143)
+ *   - all arithmetic is IEEE double.
+ *
+ * Ordering.  Host arrays passed to or returned from this library are in the
+ * reference's element / segment order.  Inside the library elements are
+ * renumbered for locality (reverse Cuthill-McKee over the element adjacency)
+ * and device state vectors (the `*_dev` arguments and the device N_Vector) are
+ * stored in that internal order; pihm_gpu_to_internal / pihm_gpu_to_reference
+ * convert between the two.
+ *
+ * Status codes: 0 = success, > 0 = recoverable (CVODE retries the step),
+ * < 0 = unrecoverable (see PIHM_GPU_ERR_*).  The CVODE-facing callback follows
+ * CVODE's CVRhsFn contract (cvode/include/cvode/cvode.h, CVRhsFn).
+ */
+#ifndef PIHM_GPU_H
+#define PIHM_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PIHM_GPU_NUM_EDGE   3
+#define PIHM_GPU_NUM_RIVFLX 11
+
+/* Overland / river flow formulation (src/include/pihm_const.h:152-153). */
+#define PIHM_GPU_KINEMATIC 1
+#define PIHM_GPU_DIFF_WAVE 2
+
+/* Element ordering inside the library. */
+#define PIHM_GPU_ORDER_REFERENCE 0 /* keep the caller's order */
+#define PIHM_GPU_ORDER_RCM       1 /* reverse Cuthill-McKee (default) */
+
+enum {
+    PIHM_GPU_OK = 0,
+    PIHM_GPU_ERR_ARG = -1,     /* bad argument or size */
+    PIHM_GPU_ERR_CUDA = -2,    /* a CUDA runtime call failed */
+    PIHM_GPU_ERR_NAN = -3,     /* a derivative came out NaN (reference CheckDy,
+                                  src/ode.c:401-410, exits instead) */
+    PIHM_GPU_ERR_MESH = -4,    /* inconsistent mesh / river topology */
+    PIHM_GPU_ERR_NOMEM = -5,   /* device allocation failed */
+    PIHM_GPU_ERR_BCTYPE = -6   /* unknown river outlet or shape type
+                                  (reference PIHMexit, src/river_flow.c:384-389) */
+};
+
+/*
+ * Static description of one watershed, structure of arrays, reference order.
+ * Field meanings follow the reference element and river records
+ * (src/include/elem_struct.h:28-99, src/include/river_struct.h:5-120); only the
+ * fields read by the right-hand side are present.  Per-edge arrays are
+ * row-major [nelem][3].  All pointers are host pointers and are copied by
+ * pihm_gpu_create; the caller keeps ownership.
+ */
+typedef struct pihm_gpu_mesh {
+    int32_t nelem;
+    int32_t nriver;
+    /* element topology */
+    const int32_t *nabr;      /* [nelem*3] neighbour ids (see conventions) */
+    const int32_t *bc_type;   /* [nelem*3] 0 no-flow, >0 Dirichlet, <0 Neumann */
+    /* element topography (topo_struct) */
+    const double *area;       /* [nelem] m2 */
+    const double *zmin;       /* [nelem] soil bottom elevation, m */
+    const double *zmax;       /* [nelem] surface elevation, m */
+    const double *edge;       /* [nelem*3] edge length, m */
+    const double *nabrdist;   /* [nelem*3] distance to neighbour, m */
+    const double *nabr_x;     /* [nelem*3] neighbour centroid x, m */
+    const double *nabr_y;     /* [nelem*3] neighbour centroid y, m */
+    /* element soil (soil_struct) */
+    const double *depth, *ksath, *ksatv, *kinfv, *dinf, *alpha, *beta,
+                 *porosity, *dmac, *kmach, *kmacv, *areafv, *areafh;
+    /* land cover / plant (lc.rough, ps.rzd) */
+    const double *rough;      /* [nelem] Manning n, s m-1/3 */
+    const double *rzd;        /* [nelem] root zone depth, m */
+    /* river topology */
+    const int32_t *down;       /* [nriver] */
+    const int32_t *leftele;    /* [nriver] 1-based */
+    const int32_t *rightele;   /* [nriver] 1-based */
+    const int32_t *intrpl_ord; /* [nriver] 1 rectangle .. 4 cubic */
+    const int32_t *riverbc_type; /* [nriver] upstream boundary type */
+    /* river topography, shape and material */
+    const double *riv_area, *riv_zmin, *riv_zmax, *riv_zbed, *riv_node_zmax,
+                 *riv_dist_left, *riv_dist_right;
+    const double *riv_depth, *riv_coeff, *riv_length, *riv_width;
+    const double *riv_rough, *riv_cwr, *riv_ksath, *riv_ksatv, *riv_bedthick,
+                 *riv_porosity;
+} pihm_gpu_mesh;
+
+typedef struct pihm_gpu_ctx pihm_gpu_ctx;
+
+/* ---------------------------------------------------------------------
+ * Lifetime.  Replaces the reference's per-field cudaMallocManaged mirror
+ * (src/initialize_cuda.c:5, AoS_to_SoA :430) with one packed device image.
+ * --------------------------------------------------------------------- */
+
+/* Validate the mesh, renumber it (`order`), upload it and allocate all
+ * persistent device buffers.  `surf_mode` / `riv_mode` are KINEMATIC or
+ * DIFF_WAVE (ctrl.surf_mode / ctrl.riv_mode, src/hydrol.c:24-28);
+ * `stepsize` is the model step in seconds that caps infiltration
+ * (src/hydrol.c:26, src/vert_flow.c:124).  Forcing, boundary values and the
+ * carried fluxes start at zero. */
+int pihm_gpu_create(const pihm_gpu_mesh *mesh, int surf_mode, int riv_mode,
+                    double stepsize, int order, pihm_gpu_ctx **out);
+void pihm_gpu_destroy(pihm_gpu_ctx *ctx);
+
+/* Stream all later work of this context is issued on (cudaStream_t). */
+int pihm_gpu_set_stream(pihm_gpu_ctx *ctx, void *stream);
+int pihm_gpu_sizes(const pihm_gpu_ctx *ctx, int32_t *nelem, int32_t *nriver,
+                   int64_t *neq);
+/* Internal position of every element and segment: perm[internal] = reference
+ * index (0-based).  Either pointer may be NULL. */
+int pihm_gpu_get_permutation(const pihm_gpu_ctx *ctx, int32_t *elem_perm,
+                             int32_t *river_perm);
+
+/* ---------------------------------------------------------------------
+ * Inputs the right-hand side reads besides y (reference order, host arrays).
+ * They stand for ApplyBc / ApplyForc / IntcpSnowEt (src/pihm.c:21-66) and the
+ * post-step update (src/update.c:3-99).  NULL leaves a field unchanged.
+ * --------------------------------------------------------------------- */
+int pihm_gpu_set_forcing(pihm_gpu_ctx *ctx, const double *pcpdrp,
+                         const double *edir, const double *ett);
+/* Element boundary values, [nelem*3] (bc.head or bc.flux, one union per edge,
+ * src/include/elem_struct.h:720-728) and river boundary values [nriver]. */
+int pihm_gpu_set_bc(pihm_gpu_ctx *ctx, const double *elem_bc,
+                    const double *river_bc);
+/* ws0.surf of the previous model step (read by Infil, src/vert_flow.c:122). */
+int pihm_gpu_set_ws0_surf(pihm_gpu_ctx *ctx, const double *ws0_surf);
+/* Seed of the river-edge overland fluxes that Infil reads before RiverToElem
+ * overwrites them (src/vert_flow.c:61 vs src/river_flow.c:159-182):
+ * [nelem*3] wf.ovlflow, only entries on river edges are used. */
+int pihm_gpu_set_river_edge_ovlflow(pihm_gpu_ctx *ctx, const double *ovlflow);
+
+/* ---------------------------------------------------------------------
+ * Right-hand side.
+ * --------------------------------------------------------------------- */
+
+/* ydot = f(t, y) on the context's stream, device pointers in internal order.
+ * Asynchronous: it neither synchronises nor allocates.  A NaN derivative sets
+ * a device error word that pihm_gpu_status reads. */
+int pihm_gpu_rhs(pihm_gpu_ctx *ctx, double t, const double *y_dev,
+                 double *ydot_dev);
+/* Synchronise the context's stream and return (then clear) the error word:
+ * 0 or PIHM_GPU_ERR_NAN / PIHM_GPU_ERR_CUDA. */
+int pihm_gpu_status(pihm_gpu_ctx *ctx);
+
+/* Same evaluation from host arrays in reference order: copy y in, run, copy
+ * ydot out, synchronise.  This is the call a CPU-side integrator makes in
+ * place of the serial ODE() (src/ode.c:4-399). */
+int pihm_gpu_rhs_host(pihm_gpu_ctx *ctx, double t, const double *y_host,
+                      double *ydot_host);
+
+/* Keep per-element and per-segment fluxes of every later call so that
+ * pihm_gpu_get_fluxes can read them (costs extra stores). */
+int pihm_gpu_set_diagnostics(pihm_gpu_ctx *ctx, int on);
+/* Fluxes of the last right-hand side evaluated with diagnostics on, reference
+ * order, host arrays, any may be NULL:
+ *   ovlflow, subsurf [nelem*3] (wf.ovlflow / wf.subsurf, m3 s-1)
+ *   infil, rechg     [nelem]   (wf.infil / wf.rechg, m s-1)
+ *   et_split         [nelem*5] (edir_surf, edir_unsat, edir_gw, ett_unsat, ett_gw)
+ *   rivflow          [nriver*11] (river wf.rivflow, m3 s-1) */
+int pihm_gpu_get_fluxes(pihm_gpu_ctx *ctx, double *ovlflow, double *subsurf,
+                        double *infil, double *rechg, double *et_split,
+                        double *rivflow);
+
+/* Reorder a device state vector (length NEQ) between the reference order and
+ * the internal order.  src and dst must not overlap. */
+int pihm_gpu_to_internal(pihm_gpu_ctx *ctx, const double *src_ref_dev,
+                         double *dst_int_dev);
+int pihm_gpu_to_reference(pihm_gpu_ctx *ctx, const double *src_int_dev,
+                          double *dst_ref_dev);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PIHM_GPU_H */

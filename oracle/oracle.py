@@ -1,0 +1,210 @@
+"""Python bindings of the CPU checkers (test infrastructure only).
+
+`Oracle`    -- the C restatement of the reference right-hand side
+               (oracle/pihm_oracle.c), serial or OpenMP build.
+`Reference` -- the reference's own serial/OpenMP code compiled from its
+               sources (oracle/ref_harness.c + oracle/Makefile target `ref`);
+               present only where the reference sources were available at
+               build time.
+
+Only tests/, the smoke check and the benchmark's CPU-baseline leg use this
+module; the GPU library never does.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+sys.path.insert(0, os.path.join(ROOT, "pihm-cuda_gb300"))
+
+from pihm_gpu.meshdesc import MeshDesc, f64p  # noqa: E402
+
+_F64P = ctypes.POINTER(ctypes.c_double)
+_I32P = ctypes.POINTER(ctypes.c_int32)
+
+
+def build(ref: bool = False) -> None:
+    """Compile the restatement (and, when the reference sources exist, the
+    reference harness) in place."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    if ref:
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+
+
+def ref_available() -> bool:
+    return os.path.exists(os.path.join(HERE, "_ref", "libpihm_ref.so"))
+
+
+def _lib(path: str) -> ctypes.CDLL:
+    if not os.path.exists(path):
+        build()
+    return ctypes.CDLL(path)
+
+
+class Oracle:
+    """The restatement, one watershed per instance."""
+
+    def __init__(self, ws, omp: bool = False, threads: int | None = None):
+        name = "liboracle_omp.so" if omp else "liboracle.so"
+        lib = _lib(os.path.join(HERE, "_build", name))
+        lib.oracle_create.restype = ctypes.c_void_p
+        lib.oracle_create.argtypes = [ctypes.POINTER(MeshDesc), ctypes.c_int,
+                                      ctypes.c_int, ctypes.c_double]
+        for fn in ("oracle_set_forcing",):
+            getattr(lib, fn).argtypes = [ctypes.c_void_p, _F64P, _F64P, _F64P]
+        lib.oracle_set_bc.argtypes = [ctypes.c_void_p, _F64P, _F64P]
+        lib.oracle_set_ws0_surf.argtypes = [ctypes.c_void_p, _F64P]
+        lib.oracle_set_river_edge_ovlflow.argtypes = [ctypes.c_void_p, _F64P]
+        lib.oracle_rhs.argtypes = [ctypes.c_void_p, ctypes.c_double, _F64P, _F64P]
+        lib.oracle_get_fluxes.argtypes = [ctypes.c_void_p] + [_F64P] * 6
+        lib.oracle_post_step.argtypes = [ctypes.c_void_p, _F64P]
+        lib.oracle_destroy.argtypes = [ctypes.c_void_p]
+        lib.oracle_num_threads.restype = ctypes.c_int
+        lib.oracle_set_num_threads.argtypes = [ctypes.c_int]
+        self.lib = lib
+        self.ws = ws
+        self.desc = MeshDesc.from_arrays(ws.nelem, ws.nriver, ws.arrays)
+        if threads:
+            lib.oracle_set_num_threads(int(threads))
+        self.h = lib.oracle_create(ctypes.byref(self.desc), ws.surf_mode,
+                                   ws.riv_mode, ws.stepsize)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.oracle_destroy(self.h)
+            self.h = None
+
+    @property
+    def threads(self) -> int:
+        return self.lib.oracle_num_threads()
+
+    def set_forcing(self, pcpdrp=None, edir=None, ett=None):
+        self.lib.oracle_set_forcing(self.h, f64p(_c(pcpdrp)), f64p(_c(edir)),
+                                    f64p(_c(ett)))
+
+    def set_bc(self, elem_bc=None, river_bc=None):
+        self.lib.oracle_set_bc(self.h, f64p(_c(elem_bc)), f64p(_c(river_bc)))
+
+    def set_ws0_surf(self, ws0):
+        self.lib.oracle_set_ws0_surf(self.h, f64p(_c(ws0)))
+
+    def set_river_edge_ovlflow(self, ovl):
+        self.lib.oracle_set_river_edge_ovlflow(self.h, f64p(_c(ovl)))
+
+    def rhs(self, y, t: float = 0.0):
+        y = _c(y)
+        out = np.zeros_like(y)
+        rc = self.lib.oracle_rhs(self.h, t, f64p(y), f64p(out))
+        return out, rc
+
+    def post_step(self, y):
+        self.lib.oracle_post_step(self.h, f64p(_c(y)))
+
+    def fluxes(self):
+        ne, nr = self.ws.nelem, self.ws.nriver
+        out = dict(ovlflow=np.zeros(3 * ne), subsurf=np.zeros(3 * ne),
+                   infil=np.zeros(ne), rechg=np.zeros(ne),
+                   et_split=np.zeros(5 * ne), rivflow=np.zeros(11 * nr))
+        self.lib.oracle_get_fluxes(self.h, *(f64p(out[k]) for k in (
+            "ovlflow", "subsurf", "infil", "rechg", "et_split", "rivflow")))
+        return out
+
+
+class Reference:
+    """The reference's own code (compiled from its sources).  The reference
+    keeps its model in globals, so one instance at a time."""
+
+    def __init__(self, omp: bool = False):
+        name = "libpihm_ref_omp.so" if omp else "libpihm_ref.so"
+        path = os.path.join(HERE, "_ref", name)
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        lib = ctypes.CDLL(path)
+        lib.ref_build.argtypes = [ctypes.POINTER(MeshDesc), ctypes.c_int,
+                                  ctypes.c_int, ctypes.c_int]
+        lib.ref_load_example.argtypes = [ctypes.c_char_p, ctypes.c_char_p,
+                                         _F64P, ctypes.c_int]
+        lib.ref_sizes.argtypes = [ctypes.POINTER(ctypes.c_int)] * 5
+        lib.ref_export_double.argtypes = [ctypes.c_char_p, _F64P]
+        lib.ref_export_int.argtypes = [ctypes.c_char_p, _I32P]
+        lib.ref_set_forcing.argtypes = [_F64P, _F64P, _F64P]
+        lib.ref_set_bc.argtypes = [_F64P, _F64P]
+        lib.ref_set_ws0_surf.argtypes = [_F64P]
+        lib.ref_set_river_edge_ovlflow.argtypes = [_F64P]
+        lib.ref_ode.argtypes = [ctypes.c_double, _F64P, _F64P]
+        lib.ref_get_fluxes.argtypes = [_F64P] * 6
+        lib.ref_apply_forcing.argtypes = [ctypes.c_int]
+        lib.ref_model_times.argtypes = [ctypes.POINTER(ctypes.c_int)] * 4
+        lib.ref_num_threads.restype = ctypes.c_int
+        lib.ref_set_num_threads.argtypes = [ctypes.c_int]
+        self.lib = lib
+        self.ne = self.nr = 0
+
+    def build(self, ws):
+        self.desc = MeshDesc.from_arrays(ws.nelem, ws.nriver, ws.arrays)
+        self.lib.ref_build(ctypes.byref(self.desc), ws.surf_mode, ws.riv_mode,
+                           int(ws.stepsize))
+        self.ne, self.nr = ws.nelem, ws.nriver
+
+    def load_deck(self, workdir: str, project: str):
+        """Read an input deck with the reference's readers; returns y0."""
+        y0 = np.zeros(8 * 1024 * 1024)
+        rc = self.lib.ref_load_example(workdir.encode(), project.encode(),
+                                       f64p(y0), y0.shape[0])
+        assert rc == 0
+        vals = [ctypes.c_int() for _ in range(5)]
+        self.lib.ref_sizes(*[ctypes.byref(v) for v in vals])
+        self.ne, self.nr = vals[0].value, vals[1].value
+        self.stepsize, self.surf_mode, self.riv_mode = (vals[2].value,
+                                                       vals[3].value,
+                                                       vals[4].value)
+        return y0[:3 * self.ne + 2 * self.nr].copy()
+
+    def export(self, name: str, n: int, kind=np.float64):
+        out = np.zeros(n, kind)
+        if kind == np.float64:
+            rc = self.lib.ref_export_double(name.encode(), f64p(out))
+        else:
+            rc = self.lib.ref_export_int(name.encode(),
+                                         out.ctypes.data_as(_I32P))
+        assert rc == 0, name
+        return out
+
+    def set_forcing(self, pcpdrp=None, edir=None, ett=None):
+        self.lib.ref_set_forcing(f64p(_c(pcpdrp)), f64p(_c(edir)), f64p(_c(ett)))
+
+    def set_bc(self, elem_bc=None, river_bc=None):
+        self.lib.ref_set_bc(f64p(_c(elem_bc)), f64p(_c(river_bc)))
+
+    def set_ws0_surf(self, ws0):
+        self.lib.ref_set_ws0_surf(f64p(_c(ws0)))
+
+    def set_river_edge_ovlflow(self, ovl):
+        self.lib.ref_set_river_edge_ovlflow(f64p(_c(ovl)))
+
+    def rhs(self, y, t: float = 0.0):
+        y = _c(y)
+        out = np.zeros_like(y)
+        rc = self.lib.ref_ode(t, f64p(y), f64p(out))
+        return out, rc
+
+    def fluxes(self):
+        ne, nr = self.ne, self.nr
+        out = dict(ovlflow=np.zeros(3 * ne), subsurf=np.zeros(3 * ne),
+                   infil=np.zeros(ne), rechg=np.zeros(ne),
+                   et_split=np.zeros(5 * ne), rivflow=np.zeros(11 * nr))
+        self.lib.ref_get_fluxes(*(f64p(out[k]) for k in (
+            "ovlflow", "subsurf", "infil", "rechg", "et_split", "rivflow")))
+        return out
+
+
+def _c(a):
+    if a is None:
+        return None
+    return np.ascontiguousarray(a, np.float64)

@@ -1,0 +1,49 @@
+/*
+ * pihm_oracle.h -- CPU restatement of the PIHM right-hand side (test
+ * infrastructure only).
+ *
+ * This is the checker for the GPU library, not part of the product: only the
+ * test-suite, the smoke check and the CPU-baseline leg of the benchmark load
+ * it.  It restates, loop for loop and in the same floating-point operation
+ * order, the reference's serial/OpenMP ODE() (lj-cug/PIHM-CUDA src/ode.c:4-399)
+ * and its callees in src/hydrol.c, src/lat_flow.c, src/vert_flow.c,
+ * src/river_flow.c and src/soil.c, reading the watershed from the same
+ * structure-of-arrays description the GPU library takes (include/pihm_gpu.h).
+ * Built with -fopenmp it parallelises the same loops the reference does.
+ */
+#ifndef PIHM_ORACLE_H
+#define PIHM_ORACLE_H
+
+#include "pihm_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct oracle_model oracle_model;
+
+oracle_model *oracle_create(const pihm_gpu_mesh *mesh, int surf_mode,
+                            int riv_mode, double stepsize);
+void oracle_destroy(oracle_model *m);
+void oracle_set_forcing(oracle_model *m, const double *pcpdrp,
+                        const double *edir, const double *ett);
+void oracle_set_bc(oracle_model *m, const double *elem_bc,
+                   const double *river_bc);
+void oracle_set_ws0_surf(oracle_model *m, const double *ws0_surf);
+void oracle_set_river_edge_ovlflow(oracle_model *m, const double *ovlflow);
+/* ydot = f(t, y); returns 0, or -3 when a derivative is NaN (the reference
+ * exits there, src/ode.c:401-410). */
+int oracle_rhs(oracle_model *m, double t, const double *y, double *ydot);
+void oracle_get_fluxes(const oracle_model *m, double *ovlflow, double *subsurf,
+                       double *infil, double *rechg, double *et_split,
+                       double *rivflow);
+/* Post-step update (Summary, src/update.c:3-99): ws0 <- y. */
+void oracle_post_step(oracle_model *m, const double *y);
+/* Number of OpenMP threads the oracle runs with (1 without OpenMP). */
+int oracle_num_threads(void);
+void oracle_set_num_threads(int n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

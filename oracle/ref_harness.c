@@ -1,0 +1,356 @@
+/*
+ * ref_harness.c -- drives the reference's own serial/OpenMP PIHM code, built
+ * from its sources by oracle/Makefile (target `ref`) into oracle/_ref/.
+ * Test infrastructure only: it exists to pin the CPU restatement
+ * (pihm_oracle.c) and to produce golden vectors, never on a product path.
+ *
+ * It links every reference object except src/main.c, so it defines the
+ * globals of src/main.c:10-24 and NumStateVar (src/main.c:313-339) itself.
+ * Two ways in:
+ *   - ref_build():        fill the reference's element/river records from the
+ *                         structure-of-arrays mesh description used everywhere
+ *                         else (include/pihm_gpu.h);
+ *   - ref_load_example(): read a reference input deck with the reference's own
+ *                         ReadAlloc/Initialize (src/read_alloc.c:3,
+ *                         src/initialize.c:16), e.g. benchmark/input/example.
+ * Then ref_ode() calls the reference ODE() (src/ode.c:4) directly, and
+ * ref_run() steps the model the way src/main.c:217-254 and src/pihm.c:7-187 do.
+ */
+#include "pihm.h"
+#include "pihm_gpu.h"
+
+#include <unistd.h>
+
+/* globals of src/main.c:10-24 */
+int verbose_mode;
+int debug_mode;
+int append_mode;
+int corr_mode;
+int spinup_mode;
+int tecplot;
+char project[MAXSTRING];
+int nelem;
+int nriver;
+#if defined(_OPENMP)
+int nthreads = 1;
+#endif
+
+int NumStateVar(void) { return 3 * nelem + 2 * nriver; }
+
+static pihm_struct g_pihm = NULL;
+static int g_have_tables = 0; /* 1 when loaded through ReadAlloc */
+
+int ref_num_threads(void)
+{
+#if defined(_OPENMP)
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+void ref_set_num_threads(int n)
+{
+#if defined(_OPENMP)
+    if (n > 0) {
+        omp_set_num_threads(n);
+        nthreads = n;
+    }
+#else
+    (void)n;
+#endif
+}
+
+static void free_model(void)
+{
+    if (g_pihm) {
+        free(g_pihm->elem);
+        free(g_pihm->river);
+        free(g_pihm);
+        g_pihm = NULL;
+    }
+}
+
+int ref_build(const pihm_gpu_mesh *g, int surf_mode, int riv_mode,
+              int stepsize)
+{
+    int i, j;
+    free_model();
+    g_pihm = (pihm_struct)calloc(1, sizeof(*g_pihm));
+    nelem = g->nelem;
+    nriver = g->nriver;
+    g_pihm->elem = (elem_struct *)calloc(nelem, sizeof(elem_struct));
+    g_pihm->river = (river_struct *)calloc(nriver > 0 ? nriver : 1,
+                                           sizeof(river_struct));
+    g_pihm->ctrl.surf_mode = surf_mode;
+    g_pihm->ctrl.riv_mode = riv_mode;
+    g_pihm->ctrl.stepsize = stepsize;
+    g_have_tables = 0;
+    for (i = 0; i < nelem; i++) {
+        elem_struct *e = &g_pihm->elem[i];
+        e->ind = i + 1;
+        for (j = 0; j < NUM_EDGE; j++) {
+            e->nabr[j] = g->nabr[3 * i + j];
+            e->attrib.bc_type[j] = g->bc_type[3 * i + j];
+            e->topo.edge[j] = g->edge[3 * i + j];
+            e->topo.nabrdist[j] = g->nabrdist[3 * i + j];
+            e->topo.nabr_x[j] = g->nabr_x[3 * i + j];
+            e->topo.nabr_y[j] = g->nabr_y[3 * i + j];
+        }
+        e->topo.area = g->area[i];
+        e->topo.zmin = g->zmin[i];
+        e->topo.zmax = g->zmax[i];
+        e->soil.depth = g->depth[i];
+        e->soil.ksath = g->ksath[i];
+        e->soil.ksatv = g->ksatv[i];
+        e->soil.kinfv = g->kinfv[i];
+        e->soil.dinf = g->dinf[i];
+        e->soil.alpha = g->alpha[i];
+        e->soil.beta = g->beta[i];
+        e->soil.porosity = g->porosity[i];
+        e->soil.dmac = g->dmac[i];
+        e->soil.kmach = g->kmach[i];
+        e->soil.kmacv = g->kmacv[i];
+        e->soil.areafv = g->areafv[i];
+        e->soil.areafh = g->areafh[i];
+        e->lc.rough = g->rough[i];
+        e->ps.rzd = g->rzd[i];
+    }
+    for (i = 0; i < nriver; i++) {
+        river_struct *r = &g_pihm->river[i];
+        r->ind = i + 1;
+        r->down = g->down[i];
+        r->leftele = g->leftele[i];
+        r->rightele = g->rightele[i];
+        r->shp.intrpl_ord = g->intrpl_ord[i];
+        r->attrib.riverbc_type = g->riverbc_type[i];
+        r->topo.area = g->riv_area[i];
+        r->topo.zmin = g->riv_zmin[i];
+        r->topo.zmax = g->riv_zmax[i];
+        r->topo.zbed = g->riv_zbed[i];
+        r->topo.node_zmax = g->riv_node_zmax[i];
+        r->topo.dist_left = g->riv_dist_left[i];
+        r->topo.dist_right = g->riv_dist_right[i];
+        r->shp.depth = g->riv_depth[i];
+        r->shp.coeff = g->riv_coeff[i];
+        r->shp.length = g->riv_length[i];
+        r->shp.width = g->riv_width[i];
+        r->matl.rough = g->riv_rough[i];
+        r->matl.cwr = g->riv_cwr[i];
+        r->matl.ksath = g->riv_ksath[i];
+        r->matl.ksatv = g->riv_ksatv[i];
+        r->matl.bedthick = g->riv_bedthick[i];
+        r->matl.porosity = g->riv_porosity[i];
+    }
+    return 0;
+}
+
+/* Read an input deck `<workdir>/input/<proj>/<proj>.*` with the reference's
+ * readers and initialise it (RelaxIc or ReadIc per the .para file). */
+int ref_load_example(const char *workdir, const char *proj, double *y0,
+                     int ny0)
+{
+    char cwd[4096];
+    N_Vector cv_y;
+    free_model();
+    if (!getcwd(cwd, sizeof(cwd))) return -1;
+    if (chdir(workdir) != 0) return -1;
+    strncpy(project, proj, MAXSTRING - 1);
+    verbose_mode = VL_SILENT;
+    g_pihm = (pihm_struct)calloc(1, sizeof(*g_pihm));
+    ReadAlloc(g_pihm);
+    cv_y = N_VNew(NumStateVar());
+    Initialize(g_pihm, cv_y);
+    if (y0 && ny0 >= NumStateVar())
+        memcpy(y0, NV_DATA(cv_y), sizeof(double) * NumStateVar());
+    N_VDestroy(cv_y);
+    g_have_tables = 1;
+    if (chdir(cwd) != 0) return -1;
+    return 0;
+}
+
+int ref_sizes(int *ne, int *nr, int *stepsize, int *surf_mode, int *riv_mode)
+{
+    if (!g_pihm) return -1;
+    if (ne) *ne = nelem;
+    if (nr) *nr = nriver;
+    if (stepsize) *stepsize = g_pihm->ctrl.stepsize;
+    if (surf_mode) *surf_mode = g_pihm->ctrl.surf_mode;
+    if (riv_mode) *riv_mode = g_pihm->ctrl.riv_mode;
+    return 0;
+}
+
+/* Copy one field of the loaded model out (by name) so that the same
+ * watershed can be handed to the GPU library and to the restatement. */
+int ref_export_double(const char *name, double *out)
+{
+    int i, j;
+    if (!g_pihm) return -1;
+#define EF(nm, expr)                                                       \
+    if (strcmp(name, nm) == 0) {                                           \
+        for (i = 0; i < nelem; i++) out[i] = g_pihm->elem[i].expr;         \
+        return 0;                                                          \
+    }
+#define EF3(nm, expr)                                                      \
+    if (strcmp(name, nm) == 0) {                                           \
+        for (i = 0; i < nelem; i++)                                        \
+            for (j = 0; j < NUM_EDGE; j++)                                 \
+                out[3 * i + j] = g_pihm->elem[i].expr[j];                  \
+        return 0;                                                          \
+    }
+#define RF(nm, expr)                                                       \
+    if (strcmp(name, nm) == 0) {                                           \
+        for (i = 0; i < nriver; i++) out[i] = g_pihm->river[i].expr;       \
+        return 0;                                                          \
+    }
+    EF("area", topo.area) EF("x", topo.x) EF("y", topo.y)
+    EF("zmin", topo.zmin) EF("zmax", topo.zmax)
+    EF3("edge", topo.edge) EF3("nabrdist", topo.nabrdist)
+    EF3("nabr_x", topo.nabr_x) EF3("nabr_y", topo.nabr_y)
+    EF("depth", soil.depth) EF("ksath", soil.ksath) EF("ksatv", soil.ksatv)
+    EF("kinfv", soil.kinfv) EF("dinf", soil.dinf) EF("alpha", soil.alpha)
+    EF("beta", soil.beta) EF("porosity", soil.porosity) EF("dmac", soil.dmac)
+    EF("kmach", soil.kmach) EF("kmacv", soil.kmacv)
+    EF("areafv", soil.areafv) EF("areafh", soil.areafh)
+    EF("rough", lc.rough) EF("rzd", ps.rzd)
+    EF("pcpdrp", wf.pcpdrp) EF("edir", wf.edir) EF("ett", wf.ett)
+    EF("ws0_surf", ws0.surf) EF3("bc", bc.head)
+    EF3("ovlflow", wf.ovlflow) EF3("subsurf", wf.subsurf)
+    EF("infil", wf.infil) EF("rechg", wf.rechg)
+    RF("riv_area", topo.area) RF("riv_zmin", topo.zmin)
+    RF("riv_zmax", topo.zmax) RF("riv_zbed", topo.zbed)
+    RF("riv_node_zmax", topo.node_zmax) RF("riv_dist_left", topo.dist_left)
+    RF("riv_dist_right", topo.dist_right) RF("riv_depth", shp.depth)
+    RF("riv_coeff", shp.coeff) RF("riv_length", shp.length)
+    RF("riv_width", shp.width) RF("riv_rough", matl.rough)
+    RF("riv_cwr", matl.cwr) RF("riv_ksath", matl.ksath)
+    RF("riv_ksatv", matl.ksatv) RF("riv_bedthick", matl.bedthick)
+    RF("riv_porosity", matl.porosity) RF("river_bc", bc.head)
+#undef EF
+#undef EF3
+#undef RF
+    return -2;
+}
+
+int ref_export_int(const char *name, int *out)
+{
+    int i, j;
+    if (!g_pihm) return -1;
+    if (strcmp(name, "nabr") == 0) {
+        for (i = 0; i < nelem; i++)
+            for (j = 0; j < NUM_EDGE; j++) out[3 * i + j] = g_pihm->elem[i].nabr[j];
+        return 0;
+    }
+    if (strcmp(name, "bc_type") == 0) {
+        for (i = 0; i < nelem; i++)
+            for (j = 0; j < NUM_EDGE; j++)
+                out[3 * i + j] = g_pihm->elem[i].attrib.bc_type[j];
+        return 0;
+    }
+#define RI(nm, expr)                                                       \
+    if (strcmp(name, nm) == 0) {                                           \
+        for (i = 0; i < nriver; i++) out[i] = g_pihm->river[i].expr;       \
+        return 0;                                                          \
+    }
+    RI("down", down) RI("leftele", leftele) RI("rightele", rightele)
+    RI("intrpl_ord", shp.intrpl_ord) RI("riverbc_type", attrib.riverbc_type)
+#undef RI
+    return -2;
+}
+
+void ref_set_forcing(const double *pcpdrp, const double *edir,
+                     const double *ett)
+{
+    int i;
+    for (i = 0; i < nelem; i++) {
+        if (pcpdrp) g_pihm->elem[i].wf.pcpdrp = pcpdrp[i];
+        if (edir) g_pihm->elem[i].wf.edir = edir[i];
+        if (ett) g_pihm->elem[i].wf.ett = ett[i];
+    }
+}
+
+void ref_set_bc(const double *elem_bc, const double *river_bc)
+{
+    int i, j;
+    if (elem_bc)
+        for (i = 0; i < nelem; i++)
+            for (j = 0; j < NUM_EDGE; j++)
+                g_pihm->elem[i].bc.head[j] = elem_bc[3 * i + j];
+    if (river_bc)
+        for (i = 0; i < nriver; i++) g_pihm->river[i].bc.head = river_bc[i];
+}
+
+void ref_set_ws0_surf(const double *ws0_surf)
+{
+    int i;
+    for (i = 0; i < nelem; i++) g_pihm->elem[i].ws0.surf = ws0_surf[i];
+}
+
+void ref_set_river_edge_ovlflow(const double *ovl)
+{
+    int i, j;
+    for (i = 0; i < nelem; i++)
+        for (j = 0; j < NUM_EDGE; j++)
+            if (g_pihm->elem[i].nabr[j] < 0)
+                g_pihm->elem[i].wf.ovlflow[j] = ovl[3 * i + j];
+}
+
+/* One call of the reference right-hand side. */
+int ref_ode(double t, const double *y, double *ydot)
+{
+    int n = NumStateVar();
+    N_Vector vy = N_VMake_Serial(n, (realtype *)y);
+    N_Vector vd = N_VMake_Serial(n, ydot);
+    int rc = ODE(t, vy, vd, g_pihm);
+    N_VDestroy(vy);
+    N_VDestroy(vd);
+    return rc;
+}
+
+void ref_get_fluxes(double *ovlflow, double *subsurf, double *infil,
+                    double *rechg, double *et_split, double *rivflow)
+{
+    int i, j;
+    for (i = 0; i < nelem; i++) {
+        const elem_struct *e = &g_pihm->elem[i];
+        for (j = 0; j < NUM_EDGE; j++) {
+            if (ovlflow) ovlflow[3 * i + j] = e->wf.ovlflow[j];
+            if (subsurf) subsurf[3 * i + j] = e->wf.subsurf[j];
+        }
+        if (infil) infil[i] = e->wf.infil;
+        if (rechg) rechg[i] = e->wf.rechg;
+        if (et_split) {
+            et_split[5 * i + 0] = e->wf.edir_surf;
+            et_split[5 * i + 1] = e->wf.edir_unsat;
+            et_split[5 * i + 2] = e->wf.edir_gw;
+            et_split[5 * i + 3] = e->wf.ett_unsat;
+            et_split[5 * i + 4] = e->wf.ett_gw;
+        }
+    }
+    if (rivflow)
+        for (i = 0; i < nriver; i++)
+            for (j = 0; j < NUM_RIVFLX; j++)
+                rivflow[NUM_RIVFLX * i + j] = g_pihm->river[i].wf.rivflow[j];
+}
+
+/* Forcing step of src/pihm.c:21-66 for a model loaded by ref_load_example:
+ * boundary conditions, meteorological forcing, interception/snow/ET, at model
+ * time t (seconds since the epoch, as ctrl.tout). */
+int ref_apply_forcing(int t)
+{
+    if (!g_pihm || !g_have_tables) return -1;
+    ApplyBc(&g_pihm->forc, g_pihm->elem, g_pihm->river, t);
+    ApplyForc(&g_pihm->forc, g_pihm->elem, t);
+    IntcpSnowEt(t, (realtype)g_pihm->ctrl.etstep, g_pihm->elem, &g_pihm->cal);
+    return 0;
+}
+
+int ref_model_times(int *starttime, int *endtime, int *etstep, int *nstep)
+{
+    if (!g_pihm || !g_have_tables) return -1;
+    *starttime = g_pihm->ctrl.starttime;
+    *endtime = g_pihm->ctrl.endtime;
+    *etstep = g_pihm->ctrl.etstep;
+    *nstep = g_pihm->ctrl.nstep;
+    return 0;
+}
