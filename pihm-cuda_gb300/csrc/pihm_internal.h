@@ -1,0 +1,96 @@
+// Internal layout of the GB300 PIHM right-hand-side library.
+//
+// All element data live in internal (renumbered) order as structure-of-arrays
+// FP64 planes; per-edge quantities are three planes [3][nelem] so that thread
+// i reading edge j touches consecutive addresses.  River segments keep the
+// reference order (they are ~3 % of the work and their upstream sums must run
+// in reference order anyway).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "pihm_gpu.h"
+
+namespace pihm {
+
+// Physical and numerical constants of the reference model
+// (src/include/pihm_const.h:64-156).
+constexpr double kGrav = 9.80665;
+constexpr double kPsiMin = -70.0;
+constexpr double kDeprStg = 1E-4;
+constexpr double kGradMin = 5E-8;
+constexpr double kSatMin = 0.1;
+constexpr double kRivGradMin = 0.05;
+constexpr int kRectangle = 1, kTriangle = 2, kQuadratic = 3, kCubic = 4;
+constexpr int kDirichlet = -1, kNeumann = -2, kZeroDpthGrad = -3, kCritDpth = -4;
+constexpr int kKinematic = 1, kDiffWave = 2;
+// river flux slots (src/include/pihm_const.h:127-137)
+enum RivFlx {
+  UP_CHANL2CHANL = 0, DOWN_CHANL2CHANL, LEFT_SURF2CHANL, RIGHT_SURF2CHANL,
+  LEFT_AQUIF2CHANL, RIGHT_AQUIF2CHANL, CHANL_LKG, LEFT_AQUIF2AQUIF,
+  RIGHT_AQUIF2AQUIF, DOWN_AQUIF2AQUIF, UP_AQUIF2AQUIF, NUM_RIVFLX
+};
+
+// Neighbour encoding inside the library: >= 0 internal element index,
+// -1 - s for river segment s, kBoundary for the domain edge.
+constexpr int32_t kBoundary = INT32_MIN;
+
+// Device view of one watershed, passed by value to the kernels.
+struct DevMesh {
+  int32_t ne, nr, nbank;
+  int surf_mode, riv_mode;
+  double dt;  // model step (s), caps infiltration
+
+  // element static data [ne]
+  const double *area, *zmin, *zmax;
+  const double *depth, *ksath, *ksatv, *kinfv, *dinf, *alpha, *beta, *porosity,
+      *dmac, *kmach, *kmacv, *areafv, *areafh, *rough, *rzd;
+  // per edge [3][ne]
+  const int32_t *nb;        // neighbour (encoded as above)
+  const int32_t *bctype;    // boundary condition type (boundary edges)
+  const double *edge, *nabrdist, *nabr_x, *nabr_y;
+  const double *den_x, *den_y;  // [ne] geometric denominators of the gradient
+  const int32_t *bank_slot;     // [ne] slot of an element with river edges
+  const int32_t *bank_elem;     // [nbank]
+
+  // river static data [nr], reference order
+  const int32_t *down, *left, *right, *intrpl_ord, *bctype_riv;  // left/right internal
+  const double *r_area, *r_zmin, *r_zmax, *r_zbed, *r_node_zmax, *r_dist_left,
+      *r_dist_right, *r_depth, *r_coeff, *r_length, *r_width, *r_rough, *r_cwr,
+      *r_ksath, *r_ksatv, *r_bedthick, *r_porosity;
+  const int32_t *up_ptr, *up_idx;  // CSR of upstream segments, reference order
+
+  // inputs besides y
+  const double *pcpdrp, *edir, *ett, *ws0_surf;  // [ne]
+  const double *elem_bc;   // [3][ne]
+  const double *river_bc;  // [nr]
+
+  // scratch written and read inside one evaluation
+  double *surfh, *head, *effk, *gradmag;  // [ne]
+  double *rivflow;                        // [11][nr]; slots 2/3 carry over
+  double *bank_part;                      // [8][nbank]
+  // diagnostics (optional)
+  double *d_ovl, *d_sub, *d_infil, *d_rechg, *d_et;  // [3][ne],[3][ne],[ne],[ne],[5][ne]
+  int diag;
+
+  unsigned int *err;  // error word
+};
+
+}  // namespace pihm
+
+struct pihm_gpu_ctx {
+  pihm::DevMesh m;
+  int32_t ne, nr;
+  int64_t neq;
+  cudaStream_t stream;
+  // device allocations
+  void *d_static;  // one block for every static plane
+  size_t static_bytes;
+  void *d_dyn;     // inputs + scratch
+  size_t dyn_bytes;
+  double *d_stage_in, *d_stage_out;   // host-path staging [neq]
+  int32_t *d_perm;                    // internal -> reference element index
+  int32_t *h_perm, *h_iperm;          // host copies (perm, inverse)
+  int diag;
+};

@@ -1,0 +1,718 @@
+// FP64 right-hand-side kernels of the PIHM hydrologic model for sm_103a.
+//
+// One evaluation of f(t, y) (the reference ODE(), src/ode.c:4-399) runs as
+// five stream-ordered launches with no host synchronisation:
+//
+//   k_elem_prep   per element: clamp y (src/ode.c:25-49), SurfH
+//                 (src/hydrol.c:100-134), surface head zmax + surfh and the
+//                 macropore-weighted conductivity EffKh(gw)
+//                 (src/lat_flow.c:248-277), each computed once per element
+//                 instead of once per edge side as in the reference.
+//   k_elem_grad   per element: FrictSlope/DhByDl water-surface gradient
+//                 (src/lat_flow.c:130-185,239-246) reduced to its magnitude,
+//                 with the purely geometric denominators precomputed.
+//   k_elem_main   per element: edge fluxes (SubFlowElemToElem,
+//                 OvlFlowElemToElem, BoundFluxElem, src/lat_flow.c:285-382),
+//                 EtExtract (src/hydrol.c:33-97), Infil/Recharge/EffKinf/AvgKv
+//                 (src/vert_flow.c:33-270) and the element rows of ydot
+//                 (src/ode.c:111-209).  Elements with river edges hand their
+//                 partial sums to k_finish, because their river-edge fluxes are
+//                 written by the river kernel of the same evaluation.
+//   k_river       per segment: RiverFlow (src/river_flow.c:3-94) and
+//                 RiverToElem (:113-183), ChanLeak, OutletFlux, BoundFluxRiver.
+//   k_finish      per segment: upstream accumulation in reference order
+//                 (src/river_flow.c:96-110, a CSR list instead of a serial
+//                 loop) and the river rows of ydot (src/ode.c:228-300); per
+//                 river-bank element: the rest of its element rows.
+//
+// Infil reads the river-edge overland flux of the previous evaluation
+// (src/vert_flow.c:61 runs before src/river_flow.c:159-182 rewrites it); that
+// value is the previous evaluation's rivflow slot LEFT/RIGHT_SURF2CHANL, which
+// k_elem_main reads before k_river of this evaluation overwrites it.
+#include <cmath>
+
+#include "pihm_internal.h"
+
+namespace pihm {
+
+#define RESTRICT __restrict__
+
+__device__ __forceinline__ double clamp0(double v) { return (v >= 0.0) ? v : 0.0; }
+
+// SurfH, src/hydrol.c:100-134
+__device__ __forceinline__ double surf_h(double surfeqv) {
+  if (surfeqv < 0.0) return 0.0;
+  if (surfeqv <= 0.5 * kDeprStg) return sqrt(2.0 * kDeprStg * surfeqv);
+  return kDeprStg + (surfeqv - 0.5 * kDeprStg);
+}
+
+// EffKh, src/lat_flow.c:248-277
+__device__ __forceinline__ double eff_kh(double depth, double dmac, double kmach,
+                                         double areafv, double ksath, double gw) {
+  gw = (gw > 0.0) ? gw : 0.0;
+  if (gw > depth - dmac) {
+    const double k1 = kmach * areafv + ksath * (1.0 - areafv);
+    const double k2 = ksath;
+    double d1, d2;
+    if (gw > depth) {
+      d1 = dmac;
+      d2 = depth - dmac;
+    } else {
+      d1 = gw - (depth - dmac);
+      d2 = depth - dmac;
+    }
+    return (k1 * d1 + k2 * d2) / (d1 + d2);
+  }
+  return ksath;
+}
+
+// AvgH, src/lat_flow.c:217-237
+__device__ __forceinline__ double avg_h_sub(double diff, double hsub, double hnabr) {
+  if (diff > 0.0) return (hsub > 0.0) ? hsub : 0.0;
+  return (hnabr > 0.0) ? hnabr : 0.0;
+}
+
+// AvgHsurf, src/lat_flow.c:187-215
+__device__ __forceinline__ double avg_h_surf(double diff, double hsurf, double hnabr) {
+  if (diff > 0.0) return (hsurf > kDeprStg) ? 1.0 * (hsurf - kDeprStg) : 0.0;
+  return (hnabr > kDeprStg) ? 1.0 * (hnabr - kDeprStg) : 0.0;
+}
+
+// OverLandFlow, src/lat_flow.c:279-283
+__device__ __forceinline__ double overland_flow(double avg_h, double grad_h, double avg_sf,
+                                                double crossa, double avg_rough) {
+  return crossa * pow(avg_h, 0.6666667) * grad_h / (sqrt(avg_sf) * avg_rough);
+}
+
+// KrFunc, src/soil.c:8-13, with the repeated power evaluated once
+__device__ __forceinline__ double kr_func(double beta, double satn) {
+  const double t = 1.0 - pow(1.0 - pow(satn, beta / (beta - 1.0)), (beta - 1.0) / beta);
+  return sqrt(satn) * t * t;
+}
+
+// Psi, src/vert_flow.c:272-278
+__device__ __forceinline__ double psi_vg(double satn, double alpha, double beta) {
+  satn = (satn < kSatMin) ? kSatMin : satn;
+  return -pow(pow(1.0 / satn, beta / (beta - 1.0)) - 1.0, 1.0 / beta) / alpha;
+}
+
+// EffKinf, src/vert_flow.c:211-270
+__device__ __forceinline__ double eff_kinf(double kinfv, double kmacv, double areafh,
+                                           double dh_by_dz, double ksatfunc, double elemsatn,
+                                           double applrate, double surfh) {
+  if (areafh == 0.0) return kinfv * ksatfunc;
+  if (surfh > kDeprStg) return kinfv * (1.0 - areafh) * ksatfunc + kmacv * areafh;
+  if (applrate <= dh_by_dz * kinfv * ksatfunc) return kinfv * ksatfunc;
+  const double kmax = dh_by_dz * (kmacv * areafh + kinfv * (1.0 - areafh) * ksatfunc);
+  if (applrate < kmax)
+    return kinfv * (1.0 - areafh) * ksatfunc + kmacv * areafh * kr_func(2.0, elemsatn);
+  return kinfv * (1.0 - areafh) * ksatfunc + kmacv * areafh;
+}
+
+// ---------------------------------------------------------------------------
+// river geometry, src/river_flow.c:520-583
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double riv_cs_area(int order, double depth, double coeff) {
+  depth = (depth > 0.0) ? depth : 0.0;
+  switch (order) {
+    case kRectangle: return depth * coeff;
+    case kTriangle: return depth * depth / coeff;
+    case kQuadratic: return 4.0 * depth * sqrt(depth) / (3.0 * sqrt(coeff));
+    case kCubic: return 3.0 * pow(depth, 4.0 / 3.0) / (2.0 * pow(coeff, 1.0 / 3.0));
+  }
+  return 0.0;
+}
+
+__device__ __forceinline__ double riv_perim(int order, double depth, double coeff) {
+  depth = (depth > 0.0) ? depth : 0.0;
+  switch (order) {
+    case kRectangle: return 2.0 * depth + coeff;
+    case kTriangle: return 2.0 * depth * sqrt(1.0 + coeff * coeff) / coeff;
+    case kQuadratic:
+      return sqrt(depth * (1.0 + 4.0 * coeff * depth) / coeff) +
+             log(2.0 * sqrt(coeff * depth) + sqrt(1.0 + 4.0 * coeff * depth)) / (2.0 * coeff);
+    case kCubic: {
+      const double c23 = pow(coeff, 2.0 / 3.0);
+      const double c13 = pow(coeff, 1.0 / 3.0);
+      return 2.0 * ((pow(depth * (1.0 + 9.0 * c23 * depth), 0.5) / 3.0) +
+                    (log(3.0 * c13 * sqrt(depth) + pow(1.0 + 9.0 * c23 * depth, 0.5)) /
+                     (9.0 * c13)));
+    }
+  }
+  return 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// k_elem_prep
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_elem_prep(DevMesh m, const double *RESTRICT y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m.ne) return;
+  const double surfh = surf_h(clamp0(y[i]));
+  const double gw = clamp0(y[2 * m.ne + i]);
+  m.surfh[i] = surfh;
+  m.head[i] = surfh + m.zmax[i];
+  m.effk[i] = eff_kh(m.depth[i], m.dmac[i], m.kmach[i], m.areafv[i], m.ksath[i], gw);
+}
+
+// ---------------------------------------------------------------------------
+// k_elem_grad
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_elem_grad(DevMesh m, const double *RESTRICT y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m.ne) return;
+  const int ne = m.ne;
+  double h[3];
+  const double hself = m.head[i];
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    const int32_t nb = m.nb[j * ne + i];
+    if (nb >= 0) {
+      h[j] = m.head[nb];
+    } else if (nb != kBoundary) {
+      const int s = -1 - nb;
+      const double stage = clamp0(y[3 * ne + s]);
+      h[j] = (stage > m.r_depth[s]) ? m.r_zbed[s] + stage : m.r_zmax[s];
+    } else {
+      h[j] = (m.bctype[j * ne + i] == 0) ? hself : m.elem_bc[j * ne + i];
+    }
+  }
+  const double y0 = m.nabr_y[i], y1 = m.nabr_y[ne + i], y2 = m.nabr_y[2 * ne + i];
+  const double x0 = m.nabr_x[i], x1 = m.nabr_x[ne + i], x2 = m.nabr_x[2 * ne + i];
+  // DhByDl(nabr_y, nabr_x, h) and DhByDl(nabr_x, nabr_y, h)
+  const double dhdx = -1.0 * (y2 * (h[1] - h[0]) + y1 * (h[0] - h[2]) + y0 * (h[2] - h[1])) / m.den_x[i];
+  const double dhdy = -1.0 * (x2 * (h[1] - h[0]) + x1 * (h[0] - h[2]) + x0 * (h[2] - h[1])) / m.den_y[i];
+  m.gradmag[i] = sqrt(dhdx * dhdx + dhdy * dhdy);
+}
+
+// ---------------------------------------------------------------------------
+// k_elem_main
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_elem_main(DevMesh m, const double *RESTRICT y,
+                                                    double *RESTRICT ydot) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m.ne) return;
+  const int ne = m.ne;
+  const double gw = clamp0(y[2 * ne + i]);
+  const double unsat = clamp0(y[ne + i]);
+  const double surfh = m.surfh[i];
+  const double head = m.head[i];
+  const double zmin = m.zmin[i];
+  const double effk = m.effk[i];
+  const double gm = m.gradmag[i];
+  const double rough = m.rough[i];
+  const double area = m.area[i];
+  const double gwhead = gw + zmin;
+
+  double ovl[3], sub[3];
+  bool riv[3];
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    const int32_t nb = m.nb[j * ne + i];
+    riv[j] = false;
+    if (nb >= 0) {
+      // SubFlowElemToElem, src/lat_flow.c:285-309
+      const double gw_k = clamp0(y[2 * ne + nb]);
+      const double dist = m.nabrdist[j * ne + i];
+      const double edge = m.edge[j * ne + i];
+      double diff_h = gwhead - (gw_k + m.zmin[nb]);
+      double avg_h = avg_h_sub(diff_h, gw, gw_k);
+      double grad_h = diff_h / dist;
+      const double avg_ksat = 0.5 * (effk + m.effk[nb]);
+      sub[j] = avg_ksat * grad_h * avg_h * edge;
+      // OvlFlowElemToElem, src/lat_flow.c:311-338
+      const double surfh_k = m.surfh[nb];
+      double avg_sf;
+      if (m.surf_mode == kKinematic) {
+        diff_h = m.zmax[i] - m.zmax[nb];
+        avg_h = avg_h_surf(diff_h, surfh, surfh_k);
+        grad_h = diff_h / dist;
+        avg_sf = (grad_h > 0.0) ? grad_h : kGradMin;
+      } else {
+        diff_h = head - m.head[nb];
+        avg_h = avg_h_surf(diff_h, surfh, surfh_k);
+        grad_h = diff_h / dist;
+        avg_sf = 0.5 * (gm + m.gradmag[nb]);
+        avg_sf = (avg_sf > kGradMin) ? avg_sf : kGradMin;
+      }
+      const double avg_rough = 0.5 * (rough + m.rough[nb]);
+      const double crossa = avg_h * edge;
+      ovl[j] = overland_flow(avg_h, grad_h, avg_sf, crossa, avg_rough);
+    } else if (nb != kBoundary) {
+      // river edge: Infil sees the previous evaluation's value
+      const int s = -1 - nb;
+      const int slot = (m.left[s] == i) ? LEFT_SURF2CHANL : RIGHT_SURF2CHANL;
+      ovl[j] = -m.rivflow[slot * m.nr + s];
+      sub[j] = 0.0;
+      riv[j] = true;
+    } else {
+      // BoundFluxElem, src/lat_flow.c:340-382
+      const int bct = m.bctype[j * ne + i];
+      ovl[j] = 0.0;
+      if (bct == 0) {
+        sub[j] = 0.0;
+      } else if (bct > 0) {
+        const double bc = m.elem_bc[j * ne + i];
+        const double diff_h = gwhead - bc;
+        const double avg_h = avg_h_sub(diff_h, gw, bc - zmin);
+        const double grad_h = diff_h / m.nabrdist[j * ne + i];
+        sub[j] = effk * grad_h * avg_h * m.edge[j * ne + i];
+      } else {
+        sub[j] = -m.elem_bc[j * ne + i];
+      }
+    }
+  }
+
+  // EtExtract, src/hydrol.c:33-97
+  const double depth = m.depth[i];
+  const double dinf = m.dinf[i];
+  const double edir = m.edir[i], ett = m.ett[i];
+  double edir_surf = 0.0, edir_unsat = 0.0, edir_gw = 0.0, ett_unsat = 0.0, ett_gw = 0.0;
+  if (surfh >= kDeprStg) edir_surf = edir;
+  else if (gw > depth - dinf) edir_gw = edir;
+  else edir_unsat = edir;
+  if (gw > depth - m.rzd[i]) ett_gw = ett;
+  else ett_unsat = ett;
+
+  // Infil, src/vert_flow.c:33-130, and Recharge, :132-170
+  const double beta = m.beta[i], alpha = m.alpha[i];
+  const double kinfv = m.kinfv[i], kmacv = m.kmacv[i], areafh = m.areafh[i];
+  const double ksatv = m.ksatv[i], dmac = m.dmac[i];
+  const double pcpdrp = m.pcpdrp[i];
+  const double zmax = m.zmax[i];
+  const bool gw_in_dinf = gw > depth - dinf;
+  double satn = 1.0, satkfunc = 1.0, psi_u = 0.0;
+  if (!gw_in_dinf) {
+    const double deficit = depth - gw;
+    satn = unsat / deficit;
+    satn = (satn > 1.0) ? 1.0 : satn;
+    satn = (satn < kSatMin) ? kSatMin : satn;
+    satkfunc = kr_func(beta, satn);
+    psi_u = psi_vg(satn, alpha, beta);
+  } else {
+    satkfunc = kr_func(beta, 1.0);
+  }
+  double infil;
+  if (unsat + gw > depth) {
+    infil = 0.0;
+  } else {
+    double applrate = 0.0;
+#pragma unroll
+    for (int j = 0; j < 3; j++) applrate += -ovl[j] / area;
+    applrate = (applrate > 0.0) ? applrate : 0.0;
+    applrate += pcpdrp;
+    double wetfrac = surfh / kDeprStg;
+    wetfrac = (wetfrac > 0.0) ? wetfrac : 0.0;
+    wetfrac = (wetfrac < 1.0) ? wetfrac : 1.0;
+    double dh_by_dz;
+    if (gw_in_dinf) {
+      dh_by_dz = (surfh + zmax - gwhead) / (0.5 * (surfh + dinf));
+      dh_by_dz = (surfh <= 0.0 && dh_by_dz > 0.0) ? 0.0 : dh_by_dz;
+      const double kinf = eff_kinf(kinfv, kmacv, areafh, dh_by_dz, satkfunc, 1.0, applrate, surfh);
+      infil = kinf * dh_by_dz;
+    } else {
+      const double psi_c = (psi_u > kPsiMin) ? psi_u : kPsiMin;
+      const double h_u = psi_c + zmax - 0.5 * dinf;
+      dh_by_dz = (surfh + zmax - h_u) / (0.5 * (surfh + dinf));
+      dh_by_dz = (surfh <= 0.0 && dh_by_dz > 0.0) ? 0.0 : dh_by_dz;
+      const double kinf = eff_kinf(kinfv, kmacv, areafh, dh_by_dz, satkfunc, satn, applrate, surfh);
+      infil = kinf * dh_by_dz;
+      infil = (infil > 0.0) ? infil : 0.0;
+    }
+    const double ws0 = m.ws0_surf[i];
+    const double infil_max = applrate + ((ws0 > 0.0) ? ws0 / m.dt : 0.0);
+    infil = (infil > infil_max) ? infil_max : infil;
+    infil *= wetfrac;
+  }
+  double rechg;
+  if (gw_in_dinf) {
+    rechg = infil;
+  } else {
+    const double deficit = depth - gw;
+    const double dh_by_dz = (0.5 * deficit + psi_u) / (0.5 * (deficit + gw));
+    // AvgKv, src/vert_flow.c:172-209, arithmetic mean (_ARITH_ is defined at
+    // src/include/pihm_func.h:4)
+    double k1, k2, k3, d1, d2, d3;
+    if (deficit > dmac) {
+      k1 = satkfunc * ksatv;
+      d1 = dmac;
+      k2 = satkfunc * ksatv;
+      d2 = deficit - dmac;
+      k3 = ksatv;
+      d3 = gw;
+    } else {
+      k1 = satkfunc * ksatv;
+      d1 = deficit;
+      k2 = (areafh > 0.0) ? kmacv * areafh + ksatv * (1.0 - areafh) : ksatv;
+      d2 = dmac - deficit;
+      k3 = ksatv;
+      d3 = gw - (dmac - deficit);
+    }
+    const double kavg = (k1 * d1 + k2 * d2 + k3 * d3) / (d1 + d2 + d3);
+    rechg = kavg * dh_by_dz;
+    rechg = (rechg > 0.0 && unsat <= 0.0) ? 0.0 : rechg;
+    rechg = (rechg < 0.0 && gw <= 0.0) ? 0.0 : rechg;
+  }
+
+  if (m.diag) {
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      if (!riv[j]) {
+        m.d_ovl[j * ne + i] = ovl[j];
+        m.d_sub[j * ne + i] = sub[j];
+      }
+    }
+    m.d_infil[i] = infil;
+    m.d_rechg[i] = rechg;
+    m.d_et[i] = edir_surf;
+    m.d_et[ne + i] = edir_unsat;
+    m.d_et[2 * ne + i] = edir_gw;
+    m.d_et[3 * ne + i] = ett_unsat;
+    m.d_et[4 * ne + i] = ett_gw;
+  }
+
+  // element rows of ydot, src/ode.c:111-209
+  const double porosity = m.porosity[i];
+  const double base_surf = pcpdrp - infil - edir_surf;
+  const double base_gw = rechg - edir_gw - ett_gw;
+  double du = infil - rechg - edir_unsat - ett_unsat;
+  du /= porosity;
+  ydot[ne + i] = du;
+  unsigned int bad = isnan(du);
+  if (riv[0] || riv[1] || riv[2]) {
+    const int b = m.bank_slot[i];
+    const int nbk = m.nbank;
+    double *bp = m.bank_part;
+    bp[b] = base_surf;
+    bp[nbk + b] = base_gw;
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      bp[(2 + j) * nbk + b] = ovl[j];
+      bp[(5 + j) * nbk + b] = sub[j];
+    }
+  } else {
+    double ds = base_surf, dg = base_gw;
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      ds -= ovl[j] / area;
+      dg -= sub[j] / area;
+    }
+    dg /= porosity;
+    ydot[i] = ds;
+    ydot[2 * ne + i] = dg;
+    bad |= isnan(ds) | isnan(dg);
+  }
+  if (bad) atomicOr(m.err, 1u);
+}
+
+// ---------------------------------------------------------------------------
+// k_river
+// ---------------------------------------------------------------------------
+struct RivState {
+  int order;
+  double stage, gw, zbed, zmin, zmax, coeff, length, width, rough;
+};
+
+__device__ __forceinline__ RivState load_riv(const DevMesh &m, const double *y, int s) {
+  RivState r;
+  r.order = m.intrpl_ord[s];
+  r.stage = clamp0(y[3 * m.ne + s]);
+  r.gw = clamp0(y[3 * m.ne + m.nr + s]);
+  r.zbed = m.r_zbed[s];
+  r.zmin = m.r_zmin[s];
+  r.zmax = m.r_zmax[s];
+  r.coeff = m.r_coeff[s];
+  r.length = m.r_length[s];
+  r.width = m.r_width[s];
+  r.rough = m.r_rough[s];
+  return r;
+}
+
+// OvlFlowElemToRiver, src/river_flow.c:185-255
+__device__ __forceinline__ double ovl_elem_to_river(double e_zmax, double e_surfh, const RivState &r,
+                                                    double cwr) {
+  const double zbank = (r.zmax > e_zmax) ? r.zmax : e_zmax;
+  const double elem_h = e_zmax + e_surfh;
+  const double rivseg_h = r.zbed + r.stage;
+  if (rivseg_h > elem_h) {
+    if (elem_h > zbank)
+      return cwr * 2.0 * sqrt(2.0 * kGrav) * r.length * sqrt(rivseg_h - elem_h) * (rivseg_h - zbank) / 3.0;
+    if (zbank < rivseg_h)
+      return cwr * 2.0 * sqrt(2.0 * kGrav) * r.length * sqrt(rivseg_h - zbank) * (rivseg_h - zbank) / 3.0;
+    return 0.0;
+  }
+  if (e_surfh > kDeprStg) {
+    if (rivseg_h > zbank)
+      return -cwr * 2.0 * sqrt(2.0 * kGrav) * r.length * sqrt(elem_h - rivseg_h) * (elem_h - zbank) / 3.0;
+    if (zbank < elem_h)
+      return -cwr * 2.0 * sqrt(2.0 * kGrav) * r.length * sqrt(elem_h - zbank) * (elem_h - zbank) / 3.0;
+    return 0.0;
+  }
+  return 0.0;
+}
+
+// ChanFlowElemToRiver, src/river_flow.c:429-460
+__device__ __forceinline__ double chan_elem_to_river(double e_gw, double e_zmin, double effk,
+                                                     const RivState &r, double r_ksath,
+                                                     double distance) {
+  const double diff_h = (r.stage + r.zbed) - (e_gw + e_zmin);
+  double avg_h;
+  if (e_zmin > r.zbed) avg_h = e_gw;
+  else if (e_zmin + e_gw > r.zbed) avg_h = e_zmin + e_gw - r.zbed;
+  else avg_h = 0.0;
+  avg_h = avg_h_sub(diff_h, r.stage, avg_h);
+  const double grad_h = diff_h / distance;
+  const double avg_ksat = 0.5 * (effk + r_ksath);
+  return r.length * avg_ksat * grad_h * avg_h;
+}
+
+// SubFlowElemToRiver, src/river_flow.c:462-498 (arithmetic mean)
+__device__ __forceinline__ double sub_elem_to_river(double e_gw, double e_zmin, double effk,
+                                                    const RivState &r, double effk_riv,
+                                                    double distance) {
+  const double diff_h = (r.gw + r.zmin) - (e_gw + e_zmin);
+  double avg_h;
+  if (e_zmin > r.zbed) avg_h = 0.0;
+  else if (e_zmin + e_gw > r.zbed) avg_h = r.zbed - e_zmin;
+  else avg_h = e_gw;
+  avg_h = avg_h_sub(diff_h, r.gw, avg_h);
+  const double avg_ksat = 0.5 * (effk + effk_riv);
+  const double grad_h = diff_h / distance;
+  return r.length * avg_ksat * grad_h * avg_h;
+}
+
+__global__ void __launch_bounds__(128) k_river(DevMesh m, const double *RESTRICT y) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= m.nr) return;
+  const int nr = m.nr, ne = m.ne;
+  const RivState r = load_riv(m, y, s);
+  const int down = m.down[s];
+  double f[NUM_RIVFLX];
+  f[UP_CHANL2CHANL] = 0.0;
+  f[UP_AQUIF2AQUIF] = 0.0;
+  const int L = m.left[s], R = m.right[s];
+  const double effk_l = m.effk[L], effk_r = m.effk[R];
+  if (down > 0) {
+    const int bct = m.bctype_riv[s];
+    if (bct != 0) {
+      // BoundFluxRiver, src/river_flow.c:392-427
+      double flux = 0.0;
+      const double bc = m.river_bc[s];
+      if (bct > 0) {
+        const double total_h = r.stage + r.zbed;
+        const double distance = 0.5 * r.length;
+        const double grad_h = (total_h - bc) / distance;
+        const double avg_perim = riv_perim(r.order, r.stage, r.coeff);
+        const double crossa = riv_cs_area(r.order, r.stage, r.coeff);
+        const double avg_h = (avg_perim == 0.0) ? 0.0 : (crossa / avg_perim);
+        flux = overland_flow(avg_h, grad_h, grad_h, crossa, r.rough);
+      } else {
+        flux = -bc;
+      }
+      f[UP_CHANL2CHANL] += flux;
+    }
+    const int d = down - 1;
+    const RivState dn = load_riv(m, y, d);
+    // ChanFlowRiverToRiver, src/river_flow.c:257-300
+    {
+      const double total_h = r.stage + r.zbed;
+      const double perim = riv_perim(r.order, r.stage, r.coeff);
+      const double total_h_down = dn.stage + dn.zbed;
+      const double perim_down = riv_perim(dn.order, dn.stage, dn.coeff);
+      const double avg_perim = (perim + perim_down) / 2.0;
+      const double avg_rough = (r.rough + dn.rough) / 2.0;
+      const double distance = 0.5 * (r.length + dn.length);
+      const double diff_h = (m.riv_mode == kKinematic) ? (r.zbed - dn.zbed) : (total_h - total_h_down);
+      const double grad_h = diff_h / distance;
+      const double avg_sf = (grad_h > 0.0) ? grad_h : kRivGradMin;
+      const double crossa = riv_cs_area(r.order, r.stage, r.coeff);
+      const double crossa_down = riv_cs_area(dn.order, dn.stage, dn.coeff);
+      const double avg_crossa = 0.5 * (crossa + crossa_down);
+      const double avg_h = (avg_perim == 0.0) ? 0.0 : (avg_crossa / avg_perim);
+      f[DOWN_CHANL2CHANL] = overland_flow(avg_h, grad_h, avg_sf, crossa, avg_rough);
+    }
+    // SubFlowRiverToRiver, src/river_flow.c:302-331 (arithmetic mean)
+    {
+      const double effk = 0.5 * (effk_l + effk_r);
+      const double effk_nabr = 0.5 * (m.effk[m.left[d]] + m.effk[m.right[d]]);
+      const double total_h = r.gw + r.zmin;
+      const double total_h_down = dn.gw + dn.zmin;
+      const double avg_wid = (r.width + dn.width) / 2.0;
+      const double diff_h = total_h - total_h_down;
+      const double avg_h = avg_h_sub(diff_h, r.gw, dn.gw);
+      const double distance = 0.5 * (r.length + dn.length);
+      const double grad_h = diff_h / distance;
+      const double avg_ksat = 0.5 * (effk + effk_nabr);
+      f[DOWN_AQUIF2AQUIF] = avg_ksat * grad_h * avg_h * avg_wid;
+    }
+  } else {
+    // OutletFlux, src/river_flow.c:333-390
+    const double depth = m.r_depth[s];
+    const double bc = m.river_bc[s];
+    double q = 0.0;
+    if (down == kDirichlet) {
+      const double total_h = r.stage + r.zbed;
+      const double distance = 0.5 * r.length;
+      const double grad_h = (total_h - bc) / distance;
+      const double avg_perim = riv_perim(r.order, r.stage, r.coeff);
+      const double crossa = riv_cs_area(r.order, r.stage, r.coeff);
+      const double avg_h = (avg_perim == 0.0) ? 0.0 : (crossa / avg_perim);
+      q = overland_flow(avg_h, grad_h, grad_h, crossa, r.rough);
+    } else if (down == kNeumann) {
+      q = -bc;
+    } else if (down == kZeroDpthGrad) {
+      const double distance = 0.5 * r.length;
+      const double grad_h = (r.zbed - (m.r_node_zmax[s] - depth)) / distance;
+      const double avg_perim = riv_perim(r.order, r.stage, r.coeff);
+      const double crossa = riv_cs_area(r.order, r.stage, r.coeff);
+      q = sqrt(grad_h) * crossa * ((avg_perim > 0.0) ? pow(crossa / avg_perim, 2.0 / 3.0) : 0.0) / r.rough;
+    } else {  // kCritDpth (other values are rejected at load)
+      const double crossa = riv_cs_area(r.order, r.stage, r.coeff);
+      q = crossa * sqrt(kGrav * r.stage);
+    }
+    f[DOWN_CHANL2CHANL] = q;
+    f[DOWN_AQUIF2AQUIF] = 0.0;
+  }
+  // RiverToElem, src/river_flow.c:113-183
+  const double cwr = m.r_cwr[s];
+  const double gw_l = clamp0(y[2 * ne + L]), gw_r = clamp0(y[2 * ne + R]);
+  const double zmin_l = m.zmin[L], zmin_r = m.zmin[R];
+  f[LEFT_SURF2CHANL] = ovl_elem_to_river(m.zmax[L], m.surfh[L], r, cwr);
+  f[RIGHT_SURF2CHANL] = ovl_elem_to_river(m.zmax[R], m.surfh[R], r, cwr);
+  const double r_ksath = m.r_ksath[s];
+  f[LEFT_AQUIF2CHANL] = chan_elem_to_river(gw_l, zmin_l, effk_l, r, r_ksath, m.r_dist_left[s]);
+  f[RIGHT_AQUIF2CHANL] = chan_elem_to_river(gw_r, zmin_r, effk_r, r, r_ksath, m.r_dist_right[s]);
+  const double effk_avg = 0.5 * (effk_l + effk_r);
+  f[LEFT_AQUIF2AQUIF] = sub_elem_to_river(gw_l, zmin_l, effk_l, r, effk_avg, m.r_dist_left[s]);
+  f[RIGHT_AQUIF2AQUIF] = sub_elem_to_river(gw_r, zmin_r, effk_r, r, effk_avg, m.r_dist_right[s]);
+  // ChanLeak, src/river_flow.c:500-518
+  {
+    double diff_h;
+    if (r.zbed - (r.gw + r.zmin) > 0.0) diff_h = r.stage;
+    else diff_h = r.stage + r.zbed - (r.gw + r.zmin);
+    const double grad_h = diff_h / m.r_bedthick[s];
+    f[CHANL_LKG] = m.r_ksatv[s] * r.width * r.length * grad_h;
+  }
+#pragma unroll
+  for (int k = 0; k < NUM_RIVFLX; k++) m.rivflow[k * nr + s] = f[k];
+}
+
+// ---------------------------------------------------------------------------
+// k_finish
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_finish(DevMesh m, double *RESTRICT ydot) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nr = m.nr, ne = m.ne;
+  const double *F = m.rivflow;
+  if (t < nr) {
+    const int s = t;
+    double up_c = F[UP_CHANL2CHANL * nr + s];
+    double up_a = 0.0;
+    for (int k = m.up_ptr[s]; k < m.up_ptr[s + 1]; k++) {
+      const int u = m.up_idx[k];
+      up_c -= F[DOWN_CHANL2CHANL * nr + u];
+      up_a -= F[DOWN_AQUIF2AQUIF * nr + u];
+    }
+    const double area = m.r_area[s];
+    double ds = 0.0;
+    ds -= up_c / area;
+#pragma unroll
+    for (int j = 1; j <= 6; j++) ds -= F[j * nr + s] / area;
+    double dg = -F[LEFT_AQUIF2AQUIF * nr + s] - F[RIGHT_AQUIF2AQUIF * nr + s] -
+                F[DOWN_AQUIF2AQUIF * nr + s] - up_a + F[CHANL_LKG * nr + s];
+    dg /= m.r_porosity[s] * area;
+    ydot[3 * ne + s] = ds;
+    ydot[3 * ne + nr + s] = dg;
+    if (m.diag) {
+      m.rivflow[UP_CHANL2CHANL * nr + s] = up_c;
+      m.rivflow[UP_AQUIF2AQUIF * nr + s] = up_a;
+    }
+    if (isnan(ds) | isnan(dg)) atomicOr(m.err, 1u);
+    return;
+  }
+  const int b = t - nr;
+  if (b >= m.nbank) return;
+  const int i = m.bank_elem[b];
+  const int nbk = m.nbank;
+  const double *bp = m.bank_part;
+  double ds = bp[b], dg = bp[nbk + b];
+  const double area = m.area[i];
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    const int32_t nb = m.nb[j * ne + i];
+    double o, u;
+    if (nb < 0 && nb != kBoundary) {
+      const int s = -1 - nb;
+      if (m.left[s] == i) {
+        o = -F[LEFT_SURF2CHANL * nr + s];
+        u = -(F[LEFT_AQUIF2CHANL * nr + s] + F[LEFT_AQUIF2AQUIF * nr + s]);
+      } else {
+        o = -F[RIGHT_SURF2CHANL * nr + s];
+        u = -(F[RIGHT_AQUIF2CHANL * nr + s] + F[RIGHT_AQUIF2AQUIF * nr + s]);
+      }
+      if (m.diag) {
+        m.d_ovl[j * ne + i] = o;
+        m.d_sub[j * ne + i] = u;
+      }
+    } else {
+      o = bp[(2 + j) * nbk + b];
+      u = bp[(5 + j) * nbk + b];
+    }
+    ds -= o / area;
+    dg -= u / area;
+  }
+  dg /= m.porosity[i];
+  ydot[i] = ds;
+  ydot[2 * ne + i] = dg;
+  if (isnan(ds) | isnan(dg)) atomicOr(m.err, 1u);
+}
+
+// ---------------------------------------------------------------------------
+// state reordering between reference and internal order
+// ---------------------------------------------------------------------------
+__global__ void k_permute(const double *RESTRICT src, double *RESTRICT dst, const int32_t *RESTRICT perm,
+                          int ne, int nr, int to_internal) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long n_el = 3LL * ne;
+  if (t < n_el) {
+    const int blk = (int)(t / ne);
+    const int i = (int)(t - (long long)blk * ne);
+    const long long ref = (long long)blk * ne + perm[i];
+    if (to_internal) dst[t] = src[ref];
+    else dst[ref] = src[t];
+  } else if (t < n_el + 2LL * nr) {
+    dst[t] = src[t];
+  }
+}
+
+}  // namespace pihm
+
+// ---------------------------------------------------------------------------
+// launch helpers used by the host side
+// ---------------------------------------------------------------------------
+namespace pihm {
+
+static inline unsigned blocks_for(long long n, int threads) {
+  return (unsigned)((n + threads - 1) / threads);
+}
+
+cudaError_t launch_rhs(const DevMesh &m, const double *y, double *ydot, cudaStream_t st) {
+  if (m.ne > 0) {
+    k_elem_prep<<<blocks_for(m.ne, 256), 256, 0, st>>>(m, y);
+    if (m.surf_mode == kDiffWave) k_elem_grad<<<blocks_for(m.ne, 256), 256, 0, st>>>(m, y);
+    k_elem_main<<<blocks_for(m.ne, 256), 256, 0, st>>>(m, y, ydot);
+  }
+  if (m.nr > 0) k_river<<<blocks_for(m.nr, 128), 128, 0, st>>>(m, y);
+  if (m.nr + m.nbank > 0) k_finish<<<blocks_for((long long)m.nr + m.nbank, 128), 128, 0, st>>>(m, ydot);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_permute(const double *src, double *dst, const int32_t *perm, int ne, int nr,
+                           int to_internal, cudaStream_t st) {
+  const long long n = 3LL * ne + 2LL * nr;
+  if (n == 0) return cudaSuccess;
+  k_permute<<<blocks_for(n, 256), 256, 0, st>>>(src, dst, perm, ne, nr, to_internal);
+  return cudaGetLastError();
+}
+
+}  // namespace pihm

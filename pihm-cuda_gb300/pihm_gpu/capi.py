@@ -1,0 +1,162 @@
+"""ctypes binding of the C ABI in include/pihm_gpu.h.
+
+The shared library is built in place (`make -C pihm-cuda_gb300`, or
+`__graft_entry__.build()`); this module never falls back to anything else:
+if lib/libpihm_gpu.so is missing or a call fails, it raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .meshdesc import MeshDesc, f64p, i32p
+
+PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG_DIR, "lib", "libpihm_gpu.so")
+
+ERRORS = {
+    -1: "PIHM_GPU_ERR_ARG", -2: "PIHM_GPU_ERR_CUDA", -3: "PIHM_GPU_ERR_NAN",
+    -4: "PIHM_GPU_ERR_MESH", -5: "PIHM_GPU_ERR_NOMEM", -6: "PIHM_GPU_ERR_BCTYPE",
+}
+ORDER_REFERENCE, ORDER_RCM = 0, 1
+
+_lib = None
+_F64P = ctypes.POINTER(ctypes.c_double)
+_I32P = ctypes.POINTER(ctypes.c_int32)
+_VP = ctypes.c_void_p
+
+
+class PihmGpuError(RuntimeError):
+    def __init__(self, fn: str, rc: int):
+        super().__init__(f"{fn} failed: {ERRORS.get(rc, rc)}")
+        self.rc = rc
+
+
+def load() -> ctypes.CDLL:
+    """Load lib/libpihm_gpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise FileNotFoundError(
+            f"{LIB_PATH} is missing: build it with `make -C {PKG_DIR}` "
+            "(or __graft_entry__.build()); there is no fallback path")
+    lib = ctypes.CDLL(LIB_PATH)
+    sig = {
+        "pihm_gpu_create": ([ctypes.POINTER(MeshDesc), ctypes.c_int, ctypes.c_int,
+                             ctypes.c_double, ctypes.c_int, ctypes.POINTER(_VP)], ctypes.c_int),
+        "pihm_gpu_destroy": ([_VP], None),
+        "pihm_gpu_set_stream": ([_VP, _VP], ctypes.c_int),
+        "pihm_gpu_sizes": ([_VP, _I32P, _I32P, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
+        "pihm_gpu_get_permutation": ([_VP, _I32P, _I32P], ctypes.c_int),
+        "pihm_gpu_set_forcing": ([_VP, _F64P, _F64P, _F64P], ctypes.c_int),
+        "pihm_gpu_set_bc": ([_VP, _F64P, _F64P], ctypes.c_int),
+        "pihm_gpu_set_ws0_surf": ([_VP, _F64P], ctypes.c_int),
+        "pihm_gpu_set_river_edge_ovlflow": ([_VP, _F64P], ctypes.c_int),
+        "pihm_gpu_rhs": ([_VP, ctypes.c_double, _VP, _VP], ctypes.c_int),
+        "pihm_gpu_status": ([_VP], ctypes.c_int),
+        "pihm_gpu_rhs_host": ([_VP, ctypes.c_double, _F64P, _F64P], ctypes.c_int),
+        "pihm_gpu_set_diagnostics": ([_VP, ctypes.c_int], ctypes.c_int),
+        "pihm_gpu_get_fluxes": ([_VP] + [_F64P] * 6, ctypes.c_int),
+        "pihm_gpu_to_internal": ([_VP, _VP, _VP], ctypes.c_int),
+        "pihm_gpu_to_reference": ([_VP, _VP, _VP], ctypes.c_int),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+def _check(fn: str, rc: int) -> int:
+    if rc < 0:
+        raise PihmGpuError(fn, rc)
+    return rc
+
+
+def _c(a):
+    return None if a is None else np.ascontiguousarray(a, np.float64)
+
+
+class GpuRhs:
+    """One watershed resident on the GPU (wraps pihm_gpu_ctx)."""
+
+    def __init__(self, ws, order: int = ORDER_RCM, stream: int | None = None):
+        self.lib = load()
+        self.ws = ws
+        self.desc = MeshDesc.from_arrays(ws.nelem, ws.nriver, ws.arrays)
+        h = _VP()
+        _check("pihm_gpu_create",
+               self.lib.pihm_gpu_create(ctypes.byref(self.desc), ws.surf_mode, ws.riv_mode,
+                                        float(ws.stepsize), order, ctypes.byref(h)))
+        self.h = h
+        if stream is not None:
+            self.set_stream(stream)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pihm_gpu_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    @property
+    def neq(self) -> int:
+        return self.ws.neq
+
+    def set_stream(self, stream: int):
+        _check("pihm_gpu_set_stream", self.lib.pihm_gpu_set_stream(self.h, _VP(stream)))
+
+    def permutation(self) -> np.ndarray:
+        p = np.zeros(self.ws.nelem, np.int32)
+        _check("pihm_gpu_get_permutation", self.lib.pihm_gpu_get_permutation(self.h, i32p(p), None))
+        return p
+
+    def set_forcing(self, pcpdrp=None, edir=None, ett=None):
+        _check("pihm_gpu_set_forcing", self.lib.pihm_gpu_set_forcing(
+            self.h, f64p(_c(pcpdrp)), f64p(_c(edir)), f64p(_c(ett))))
+
+    def set_bc(self, elem_bc=None, river_bc=None):
+        _check("pihm_gpu_set_bc", self.lib.pihm_gpu_set_bc(self.h, f64p(_c(elem_bc)),
+                                                           f64p(_c(river_bc))))
+
+    def set_ws0_surf(self, ws0):
+        _check("pihm_gpu_set_ws0_surf", self.lib.pihm_gpu_set_ws0_surf(self.h, f64p(_c(ws0))))
+
+    def set_river_edge_ovlflow(self, ovl):
+        _check("pihm_gpu_set_river_edge_ovlflow",
+               self.lib.pihm_gpu_set_river_edge_ovlflow(self.h, f64p(_c(ovl))))
+
+    def set_diagnostics(self, on: bool):
+        _check("pihm_gpu_set_diagnostics", self.lib.pihm_gpu_set_diagnostics(self.h, int(on)))
+
+    def rhs_host(self, y, t: float = 0.0):
+        """Host arrays in reference order (copy in, evaluate, copy out)."""
+        y = _c(y)
+        out = np.empty_like(y)
+        rc = self.lib.pihm_gpu_rhs_host(self.h, t, f64p(y), f64p(out))
+        return out, rc
+
+    def rhs_device(self, y_ptr: int, ydot_ptr: int, t: float = 0.0):
+        """Device pointers in internal order; asynchronous."""
+        _check("pihm_gpu_rhs", self.lib.pihm_gpu_rhs(self.h, t, _VP(y_ptr), _VP(ydot_ptr)))
+
+    def status(self) -> int:
+        return self.lib.pihm_gpu_status(self.h)
+
+    def to_internal(self, src_ptr: int, dst_ptr: int):
+        _check("pihm_gpu_to_internal", self.lib.pihm_gpu_to_internal(self.h, _VP(src_ptr), _VP(dst_ptr)))
+
+    def to_reference(self, src_ptr: int, dst_ptr: int):
+        _check("pihm_gpu_to_reference", self.lib.pihm_gpu_to_reference(self.h, _VP(src_ptr), _VP(dst_ptr)))
+
+    def fluxes(self):
+        ne, nr = self.ws.nelem, self.ws.nriver
+        out = dict(ovlflow=np.zeros(3 * ne), subsurf=np.zeros(3 * ne), infil=np.zeros(ne),
+                   rechg=np.zeros(ne), et_split=np.zeros(5 * ne), rivflow=np.zeros(11 * nr))
+        _check("pihm_gpu_get_fluxes", self.lib.pihm_gpu_get_fluxes(self.h, *(f64p(out[k]) for k in (
+            "ovlflow", "subsurf", "infil", "rechg", "et_split", "rivflow"))))
+        return out

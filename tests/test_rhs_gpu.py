@@ -1,0 +1,75 @@
+"""GPU right-hand side against the CPU oracle (same inputs, reference order)."""
+import numpy as np
+import pytest
+
+import pihm_gpu.watershed as W
+from parity import RTOL, apply, compare, row_scales, scenario
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair(ws, order=1):
+    from oracle import Oracle
+    from pihm_gpu.capi import GpuRhs
+    return Oracle(ws), GpuRhs(ws, order=order)
+
+
+def _check_call(o, g, ws, sc, calls=3, label=""):
+    y = sc["y"]
+    for k in range(calls):
+        yk = W.jitter(y, 77 + k) if k else y
+        want, rc_o = o.rhs(yk)
+        got, rc_g = g.rhs_host(yk)
+        assert rc_o == 0 and rc_g == 0
+        fx = o.fluxes()
+        scale = row_scales(ws, fx, sc["pcpdrp"], sc["edir"], sc["ett"])
+        ok, worst, idx = compare(got, want, scale)
+        assert ok, f"{label} call {k}: worst {worst:.3e} at {idx} got {got[idx]!r} want {want[idx]!r}"
+
+
+@pytest.mark.parametrize("order", [0, 1])
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_c0_parity(seed, order):
+    ws = W.generate(1000, 100, seed=seed)
+    ws, sc = scenario(ws, seed)
+    o, g = _pair(ws, order)
+    apply(o, sc)
+    apply(g, sc)
+    _check_call(o, g, ws, sc, label=f"seed {seed}")
+
+
+def test_boundary_conditions():
+    ws = W.generate(1000, 100, seed=5)
+    ws, sc = scenario(ws, 5, bc=True)
+    o, g = _pair(ws)
+    apply(o, sc)
+    apply(g, sc)
+    _check_call(o, g, ws, sc, label="bc")
+
+
+@pytest.mark.parametrize("surf_mode,riv_mode", [(1, 1), (1, 2), (2, 1)])
+def test_kinematic_modes(surf_mode, riv_mode):
+    ws = W.generate(1000, 100, seed=7)
+    ws.surf_mode, ws.riv_mode = surf_mode, riv_mode
+    ws, sc = scenario(ws, 7)
+    o, g = _pair(ws)
+    apply(o, sc)
+    apply(g, sc)
+    _check_call(o, g, ws, sc, label=f"modes {surf_mode}{riv_mode}")
+
+
+def test_fluxes_match():
+    ws = W.generate(1000, 100, seed=3)
+    ws, sc = scenario(ws, 3)
+    o, g = _pair(ws)
+    apply(o, sc)
+    apply(g, sc)
+    g.set_diagnostics(True)
+    o.rhs(sc["y"])
+    g.rhs_host(sc["y"])
+    fo, fg = o.fluxes(), g.fluxes()
+    for k in fo:
+        a, b = fg[k], fo[k]
+        den = np.maximum(np.abs(b), np.abs(b).max() * 1e-3)
+        err = np.abs(a - b) / np.where(den > 0, den, 1)
+        assert err.max() <= 1e-11, (k, err.max(), int(err.argmax()))
