@@ -1,0 +1,361 @@
+"""Benchmark of the PIHM right-hand side on GB300.
+
+Workload (the configuration the headline metric is quoted on): one synthetic
+watershed of 1,000,000 triangular elements and 30,000 river segments (the
+generator of pihm_gpu.watershed, seed 0), evaluated on 100 perturbed states
+(a wet reference state with every storage jittered x U(0.9, 1.1)).  One
+"step" evaluates the right-hand side on STATES_PER_STEP consecutive states of
+that set; 10 states are 245 MB of y alone, more than the 129 MB L2, so no L2
+flush is needed between evaluations.
+
+Printed (one JSON line, rank 0):
+  value     element-evals/s with the states resident in HBM (device pointers,
+            internal order), CUDA events on the library's stream
+  e2e       the same metric through the host-buffer C-ABI call
+            (pihm_gpu_rhs_host: pinned host y -> device, evaluate, -> host)
+  roofline  the right-hand-side evaluation against the measured HBM copy
+            bandwidth: algorithmic bytes (332 B per element + 184 B per
+            segment) / device time of one evaluation
+  cpu_baseline  the CPU restatement of the reference ODE() (oracle/, OpenMP
+            build, all host cores) on a bounded sample of the same states
+
+`--impl reference` times that CPU implementation alone as the reference arm.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "pihm-cuda_gb300"))
+
+NELEM, NRIVER = 1_000_000, 30_000
+NSTATES = 100
+STATES_PER_STEP = 10
+BYTES_PER_ELEM, BYTES_PER_SEG = 332, 184
+METRIC = "RHS element-evals/s"
+UNIT = "elem-evals/s"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ""
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_time_oracle(ws, states_host, threads, max_seconds=12.0, min_evals=2):
+    """Time the CPU restatement (test infrastructure) on a bounded sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    from oracle import Oracle
+    import pihm_gpu.watershed as W
+    o = Oracle(ws, omp=True, threads=threads)
+    pcpdrp, edir, ett = W.random_forcing(ws, 3)
+    o.set_forcing(pcpdrp, edir, ett)
+    o.set_ws0_surf(states_host[0][:ws.nelem])
+    o.rhs(states_host[0])  # warm
+    n = 0
+    t0 = time.perf_counter()
+    while True:
+        o.rhs(states_host[n % len(states_host)])
+        n += 1
+        el = time.perf_counter() - t0
+        if (el >= max_seconds and n >= min_evals) or n >= 200:
+            break
+    return n, el, o.threads
+
+
+def make_states(ws, n, device):
+    """n jittered copies of the reference state on the device (reference
+    order), x U(0.9, 1.1) per storage, seeded."""
+    import numpy as np
+    import torch
+    import pihm_gpu.watershed as W
+    base = torch.from_numpy(W.reference_state(ws, 1)).to(device)
+    g = torch.Generator(device=device)
+    g.manual_seed(1234)
+    out = torch.empty((n, ws.neq), dtype=torch.float64, device=device)
+    for k in range(n):
+        out[k] = base * (0.9 + 0.2 * torch.rand(ws.neq, generator=g, device=device, dtype=torch.float64))
+    return out
+
+
+def run_reference_arm(args):
+    """CPU implementation of the path on the host cores (bounded sample per
+    step), same workload and metric."""
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import numpy as np
+    import pihm_gpu.watershed as W
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    ws = W.generate(NELEM, NRIVER, seed=0)
+    base = W.reference_state(ws, 1)
+    states = [W.jitter(base, 100 + k) for k in range(4)]
+    threads = os.cpu_count() or 1
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import Oracle
+    o = Oracle(ws, omp=True, threads=threads)
+    pcpdrp, edir, ett = W.random_forcing(ws, 3)
+    o.set_forcing(pcpdrp, edir, ett)
+    o.set_ws0_surf(base[:ws.nelem])
+    evals_per_step = 2
+    for w in range(args.warmup):
+        o.rhs(states[w % len(states)])
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        for e in range(evals_per_step):
+            o.rhs(states[(s * evals_per_step + e) % len(states)])
+    el = time.perf_counter() - t0
+    value = NELEM * evals_per_step * args.steps / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"rhs_{NELEM}elem_{NRIVER}seg", "evals_per_step": evals_per_step,
+                   "nelem": NELEM, "nriver": NRIVER},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": o.threads, "kind": "port",
+                         "sample": f"{evals_per_step} RHS evaluations of the {NELEM}-element mesh per step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--nelem", type=int, default=NELEM, help="smaller meshes for profiling only")
+    ap.add_argument("--nriver", type=int, default=NRIVER)
+    args = ap.parse_args()
+    globals()["NELEM"], globals()["NRIVER"] = args.nelem, args.nriver
+    if args.impl == "reference":
+        return run_reference_arm(args)
+
+    import numpy as np
+    import torch
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    import pihm_gpu.watershed as W
+    from pihm_gpu.capi import GpuRhs
+    t_setup = time.perf_counter()
+    ws = W.generate(NELEM, NRIVER, seed=0)
+    stream = torch.cuda.Stream(device=dev)
+    g = GpuRhs(ws, stream=stream.cuda_stream)
+    pcpdrp, edir, ett = W.random_forcing(ws, 3)
+    g.set_forcing(pcpdrp, edir, ett)
+    base = W.reference_state(ws, 1)
+    g.set_ws0_surf(base[:ws.nelem])
+    with torch.cuda.stream(stream):
+        ref_states = make_states(ws, NSTATES, dev)            # reference order
+        states = torch.empty_like(ref_states)                  # internal order
+        for k in range(NSTATES):
+            g.to_internal(ref_states[k].data_ptr(), states[k].data_ptr())
+        ydot = torch.empty((STATES_PER_STEP, ws.neq), dtype=torch.float64, device=dev)
+    stream.synchronize()
+    setup_s = time.perf_counter() - t_setup
+
+    def step(s):
+        for e in range(STATES_PER_STEP):
+            k = (s * STATES_PER_STEP + e) % NSTATES
+            g.rhs_device(states[k].data_ptr(), ydot[e].data_ptr())
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---- device-resident throughput ----
+    for s in range(args.warmup):
+        step(s)
+    stream.synchronize()
+    assert g.status() == 0, "NaN in warm-up evaluations"
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    launches0 = g.launch_count()
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for s in range(args.steps):
+            step(args.warmup + s)
+        ev1.record(stream)
+        ev1.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    launches = g.launch_count() - launches0
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    evals = args.steps * STATES_PER_STEP
+    value = world * NELEM * evals / (ms * 1e-3)
+    ms_per_eval = ms / evals
+    assert g.status() == 0, "NaN in timed evaluations"
+
+    # ---- per-kernel device time (separate pass, events around each kernel) ----
+    g.set_profiling(True)
+    for s in range(2):
+        step(s)
+    kt = g.kernel_times()
+    g.set_profiling(False)
+    tot = sum(v[0] for v in kt.values())
+    kernels = {k: {"ms_per_call": v[0] / v[1], "share": v[0] / tot} for k, v in kt.items()}
+    dominant = max(kernels, key=lambda k: kernels[k]["share"])
+
+    # ---- end to end through the host-buffer C-ABI call ----
+    e2e_evals = min(evals, 3 * STATES_PER_STEP)
+    y_host = torch.empty((STATES_PER_STEP, ws.neq), dtype=torch.float64, pin_memory=True)
+    yd_host = torch.empty((STATES_PER_STEP, ws.neq), dtype=torch.float64, pin_memory=True)
+    y_host.copy_(ref_states[:STATES_PER_STEP].cpu())
+    import ctypes
+    f64p = ctypes.POINTER(ctypes.c_double)
+    lib = g.lib
+    def e2e_one(k):
+        rc = lib.pihm_gpu_rhs_host(g.h, 0.0, ctypes.cast(y_host[k].data_ptr(), f64p),
+                                   ctypes.cast(yd_host[k].data_ptr(), f64p))
+        assert rc == 0, rc
+    for k in range(2):
+        e2e_one(k)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for k in range(e2e_evals):
+        e2e_one(k % STATES_PER_STEP)
+    e1.record(stream)
+    e1.synchronize()
+    e2e_ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = world * NELEM * e2e_evals / (e2e_ms * 1e-3)
+    bytes_state = ws.neq * 8
+
+    # ---- roofline of one right-hand-side evaluation ----
+    peak, peak_kind = peaks()
+    alg_bytes = NELEM * BYTES_PER_ELEM + NRIVER * BYTES_PER_SEG
+    achieved = alg_bytes / (ms_per_eval * 1e-3) / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "rhs_traffic.json")
+    if os.path.exists(tp):
+        try:
+            traffic = json.load(open(tp)).get("dram_bytes_per_eval")
+        except Exception:
+            traffic = None
+
+    # ---- CPU baseline (rank 0, N = 1 only) ----
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        host_states = [ref_states[k].cpu().numpy() for k in range(2)]
+        try:
+            n, el, thr = cpu_time_oracle(ws, host_states, os.cpu_count() or 1)
+            cpu = {"value": NELEM * n / el, "unit": UNIT, "cores": thr, "kind": "port",
+                   "sample": f"{n} RHS evaluations of the {NELEM}-element mesh, "
+                             f"{el:.1f} s wall, OpenMP restatement of the reference ODE()"}
+        except Exception as exc:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"rhs_{NELEM}elem_{NRIVER}seg", "nelem": NELEM, "nriver": NRIVER,
+                       "states": NSTATES, "evals_per_step": STATES_PER_STEP,
+                       "l2": "inputs larger than L2 (10 states x 24.5 MB per step)",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "peak_kind": peak_kind, "scope": "one RHS evaluation (all its kernels)",
+                         "alg_bytes_per_eval": alg_bytes, "ms_per_eval": ms_per_eval},
+            "kernels": kernels, "dominant_kernel": dominant,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": bytes_state * STATES_PER_STEP,
+                    "d2h_bytes_per_step": bytes_state * STATES_PER_STEP, "evals": e2e_evals},
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+            "cpu_baseline": cpu,
+            "setup_s": setup_s,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

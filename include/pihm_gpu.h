@@ -191,6 +191,20 @@ int pihm_gpu_to_internal(pihm_gpu_ctx *ctx, const double *src_ref_dev,
 int pihm_gpu_to_reference(pihm_gpu_ctx *ctx, const double *src_int_dev,
                           double *dst_ref_dev);
 
+/* ---------------------------------------------------------------------
+ * Instrumentation (no counterpart in the reference, which has no GPU timers).
+ * --------------------------------------------------------------------- */
+
+/* Number of kernels this context has launched so far. */
+int pihm_gpu_launch_count(const pihm_gpu_ctx *ctx, int64_t *count);
+/* Bracket every later kernel launch with CUDA events on the context's
+ * stream. */
+int pihm_gpu_set_profiling(pihm_gpu_ctx *ctx, int on);
+/* Synchronise, then return and reset the accumulated device time (ms) and
+ * launch count per kernel: 0 prep, 1 gradient, 2 element, 3 river,
+ * 4 finish, 5 fused, 6 permute; n entries are written. */
+int pihm_gpu_kernel_times(pihm_gpu_ctx *ctx, double *ms, int64_t *calls, int n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -10,7 +10,8 @@
 #include "pihm_internal.h"
 
 namespace pihm {
-cudaError_t launch_rhs(const DevMesh &m, const double *y, double *ydot, cudaStream_t st);
+cudaError_t launch_rhs(const DevMesh &m, const double *y, double *ydot, cudaStream_t st,
+                       long long *launches, Profiler *prof);
 cudaError_t launch_permute(const double *src, double *dst, const int32_t *perm, int ne, int nr,
                            int to_internal, cudaStream_t st);
 }  // namespace pihm
@@ -133,6 +134,8 @@ int pihm_gpu_create(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double 
   c->neq = 3LL * ne + 2LL * nr;
   c->stream = nullptr;
   c->diag = 0;
+  c->launches = 0;
+  c->prof = nullptr;
 
   // ---- renumbering ----
   std::vector<int32_t> perm(ne);
@@ -332,8 +335,17 @@ int pihm_gpu_create(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double 
   return PIHM_GPU_OK;
 }
 
+static void free_profiler(Profiler *p) {
+  if (!p) return;
+  for (int k = 0; k < p->npool; k++) cudaEventDestroy(p->pool[k]);
+  free(p->pool);
+  free(p->recs);
+  delete p;
+}
+
 void pihm_gpu_destroy(pihm_gpu_ctx *c) {
   if (!c) return;
+  free_profiler(c->prof);
   if (c->d_static) cudaFree(c->d_static);
   if (c->d_dyn) cudaFree(c->d_dyn);
   std::free(c->h_perm);
@@ -431,7 +443,7 @@ int pihm_gpu_rhs(pihm_gpu_ctx *c, double t, const double *y, double *ydot) {
   (void)t;
   if (!c || !y || !ydot) return PIHM_GPU_ERR_ARG;
   c->m.diag = c->diag;
-  return cuda_fail(launch_rhs(c->m, y, ydot, c->stream));
+  return cuda_fail(launch_rhs(c->m, y, ydot, c->stream, &c->launches, c->prof));
 }
 
 int pihm_gpu_status(pihm_gpu_ctx *c) {
@@ -452,15 +464,19 @@ int pihm_gpu_rhs_host(pihm_gpu_ctx *c, double t, const double *y_host, double *y
   if (!c || !y_host || !ydot_host) return PIHM_GPU_ERR_ARG;
   const size_t bytes = sizeof(double) * c->neq;
   cudaError_t e = cudaMemcpyAsync(c->d_stage_in, y_host, bytes, cudaMemcpyHostToDevice, c->stream);
-  if (e == cudaSuccess)
+  if (e == cudaSuccess) {
     e = launch_permute(c->d_stage_in, c->d_stage_out, c->d_perm, c->ne, c->nr, 1, c->stream);
+    c->launches++;
+  }
   double *y_int = c->d_stage_out, *ydot_int = c->d_stage_in;
   if (e == cudaSuccess) {
     c->m.diag = c->diag;
-    e = launch_rhs(c->m, y_int, ydot_int, c->stream);
+    e = launch_rhs(c->m, y_int, ydot_int, c->stream, &c->launches, c->prof);
   }
-  if (e == cudaSuccess)
+  if (e == cudaSuccess) {
     e = launch_permute(ydot_int, c->d_stage_out, c->d_perm, c->ne, c->nr, 0, c->stream);
+    c->launches++;
+  }
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(ydot_host, c->d_stage_out, bytes, cudaMemcpyDeviceToHost, c->stream);
   if (e != cudaSuccess) return PIHM_GPU_ERR_CUDA;
@@ -498,13 +514,54 @@ int pihm_gpu_get_fluxes(pihm_gpu_ctx *c, double *ovlflow, double *subsurf, doubl
   return cudaGetLastError() == cudaSuccess ? PIHM_GPU_OK : PIHM_GPU_ERR_CUDA;
 }
 
+int pihm_gpu_launch_count(const pihm_gpu_ctx *c, int64_t *count) {
+  if (!c || !count) return PIHM_GPU_ERR_ARG;
+  *count = c->launches;
+  return PIHM_GPU_OK;
+}
+
+int pihm_gpu_set_profiling(pihm_gpu_ctx *c, int on) {
+  if (!c) return PIHM_GPU_ERR_ARG;
+  if (on && !c->prof) c->prof = new Profiler();
+  if (!on && c->prof) {
+    cudaStreamSynchronize(c->stream);
+    free_profiler(c->prof);
+    c->prof = nullptr;
+  }
+  return PIHM_GPU_OK;
+}
+
+int pihm_gpu_kernel_times(pihm_gpu_ctx *c, double *ms, int64_t *calls, int n) {
+  if (!c || !c->prof || n <= 0) return PIHM_GPU_ERR_ARG;
+  Profiler *p = c->prof;
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) return PIHM_GPU_ERR_CUDA;
+  for (int r = 0; r < p->nrec; r++) {
+    float t = 0.f;
+    if (cudaEventElapsedTime(&t, p->recs[r].a, p->recs[r].b) == cudaSuccess) {
+      p->ms[p->recs[r].kernel] += t;
+      p->calls[p->recs[r].kernel] += 1;
+    }
+  }
+  p->nrec = 0;
+  p->used = 0;
+  for (int k = 0; k < n && k < Profiler::kKernels; k++) {
+    if (ms) ms[k] = p->ms[k];
+    if (calls) calls[k] = p->calls[k];
+    p->ms[k] = 0;
+    p->calls[k] = 0;
+  }
+  return PIHM_GPU_OK;
+}
+
 int pihm_gpu_to_internal(pihm_gpu_ctx *c, const double *src, double *dst) {
   if (!c || !src || !dst || src == dst) return PIHM_GPU_ERR_ARG;
+  c->launches++;
   return cuda_fail(launch_permute(src, dst, c->d_perm, c->ne, c->nr, 1, c->stream));
 }
 
 int pihm_gpu_to_reference(pihm_gpu_ctx *c, const double *src, double *dst) {
   if (!c || !src || !dst || src == dst) return PIHM_GPU_ERR_ARG;
+  c->launches++;
   return cuda_fail(launch_permute(src, dst, c->d_perm, c->ne, c->nr, 0, c->stream));
 }
 

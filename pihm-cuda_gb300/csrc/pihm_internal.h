@@ -77,6 +77,20 @@ struct DevMesh {
   unsigned int *err;  // error word
 };
 
+// Optional per-kernel CUDA-event timing of the right-hand-side launches.
+struct Profiler {
+  static constexpr int kKernels = 8;
+  struct Rec { int kernel; cudaEvent_t a, b; };
+  Rec *recs = nullptr;
+  int nrec = 0, cap = 0;
+  cudaEvent_t *pool = nullptr;
+  int npool = 0, used = 0;
+  double ms[kKernels] = {0};
+  long long calls[kKernels] = {0};
+};
+
+enum KernelId { K_PREP = 0, K_GRAD, K_MAIN, K_RIVER, K_FINISH, K_FUSED, K_PERMUTE };
+
 }  // namespace pihm
 
 struct pihm_gpu_ctx {
@@ -93,4 +107,6 @@ struct pihm_gpu_ctx {
   int32_t *d_perm;                    // internal -> reference element index
   int32_t *h_perm, *h_iperm;          // host copies (perm, inverse)
   int diag;
+  long long launches;      // kernels launched by this context so far
+  pihm::Profiler *prof;    // non-null while profiling is on
 };

@@ -696,14 +696,66 @@ static inline unsigned blocks_for(long long n, int threads) {
   return (unsigned)((n + threads - 1) / threads);
 }
 
-cudaError_t launch_rhs(const DevMesh &m, const double *y, double *ydot, cudaStream_t st) {
-  if (m.ne > 0) {
-    k_elem_prep<<<blocks_for(m.ne, 256), 256, 0, st>>>(m, y);
-    if (m.surf_mode == kDiffWave) k_elem_grad<<<blocks_for(m.ne, 256), 256, 0, st>>>(m, y);
-    k_elem_main<<<blocks_for(m.ne, 256), 256, 0, st>>>(m, y, ydot);
+// Take two events from the profiler's pool (grown on demand).
+static bool prof_begin(Profiler *p, int kernel, cudaStream_t st) {
+  if (!p) return false;
+  if (p->used + 2 > p->npool) {
+    int n = p->npool ? 2 * p->npool : 256;
+    cudaEvent_t *np_ = (cudaEvent_t *)realloc(p->pool, sizeof(cudaEvent_t) * n);
+    if (!np_) return false;
+    p->pool = np_;
+    for (int k = p->npool; k < n; k++) cudaEventCreate(&p->pool[k]);
+    p->npool = n;
   }
-  if (m.nr > 0) k_river<<<blocks_for(m.nr, 128), 128, 0, st>>>(m, y);
-  if (m.nr + m.nbank > 0) k_finish<<<blocks_for((long long)m.nr + m.nbank, 128), 128, 0, st>>>(m, ydot);
+  if (p->nrec + 1 > p->cap) {
+    int n = p->cap ? 2 * p->cap : 128;
+    Profiler::Rec *nr_ = (Profiler::Rec *)realloc(p->recs, sizeof(Profiler::Rec) * n);
+    if (!nr_) return false;
+    p->recs = nr_;
+    p->cap = n;
+  }
+  Profiler::Rec &r = p->recs[p->nrec++];
+  r.kernel = kernel;
+  r.a = p->pool[p->used++];
+  r.b = p->pool[p->used++];
+  cudaEventRecord(r.a, st);
+  return true;
+}
+static void prof_end(Profiler *p, bool on, cudaStream_t st) {
+  if (on) cudaEventRecord(p->recs[p->nrec - 1].b, st);
+}
+
+cudaError_t launch_rhs(const DevMesh &m, const double *y, double *ydot, cudaStream_t st,
+                       long long *launches, Profiler *prof) {
+  bool on;
+  if (m.ne > 0) {
+    on = prof_begin(prof, K_PREP, st);
+    k_elem_prep<<<blocks_for(m.ne, 256), 256, 0, st>>>(m, y);
+    prof_end(prof, on, st);
+    ++*launches;
+    if (m.surf_mode == kDiffWave) {
+      on = prof_begin(prof, K_GRAD, st);
+      k_elem_grad<<<blocks_for(m.ne, 256), 256, 0, st>>>(m, y);
+      prof_end(prof, on, st);
+      ++*launches;
+    }
+    on = prof_begin(prof, K_MAIN, st);
+    k_elem_main<<<blocks_for(m.ne, 256), 256, 0, st>>>(m, y, ydot);
+    prof_end(prof, on, st);
+    ++*launches;
+  }
+  if (m.nr > 0) {
+    on = prof_begin(prof, K_RIVER, st);
+    k_river<<<blocks_for(m.nr, 128), 128, 0, st>>>(m, y);
+    prof_end(prof, on, st);
+    ++*launches;
+  }
+  if (m.nr + m.nbank > 0) {
+    on = prof_begin(prof, K_FINISH, st);
+    k_finish<<<blocks_for((long long)m.nr + m.nbank, 128), 128, 0, st>>>(m, ydot);
+    prof_end(prof, on, st);
+    ++*launches;
+  }
   return cudaGetLastError();
 }
 

@@ -62,6 +62,10 @@ def load() -> ctypes.CDLL:
         "pihm_gpu_get_fluxes": ([_VP] + [_F64P] * 6, ctypes.c_int),
         "pihm_gpu_to_internal": ([_VP, _VP, _VP], ctypes.c_int),
         "pihm_gpu_to_reference": ([_VP, _VP, _VP], ctypes.c_int),
+        "pihm_gpu_launch_count": ([_VP, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
+        "pihm_gpu_set_profiling": ([_VP, ctypes.c_int], ctypes.c_int),
+        "pihm_gpu_kernel_times": ([_VP, _F64P, ctypes.POINTER(ctypes.c_int64), ctypes.c_int],
+                                  ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -152,6 +156,24 @@ class GpuRhs:
 
     def to_reference(self, src_ptr: int, dst_ptr: int):
         _check("pihm_gpu_to_reference", self.lib.pihm_gpu_to_reference(self.h, _VP(src_ptr), _VP(dst_ptr)))
+
+    def launch_count(self) -> int:
+        n = ctypes.c_int64()
+        _check("pihm_gpu_launch_count", self.lib.pihm_gpu_launch_count(self.h, ctypes.byref(n)))
+        return n.value
+
+    def set_profiling(self, on: bool):
+        _check("pihm_gpu_set_profiling", self.lib.pihm_gpu_set_profiling(self.h, int(on)))
+
+    KERNEL_NAMES = ("k_elem_prep", "k_elem_grad", "k_elem_main", "k_river", "k_finish",
+                    "k_rhs_fused", "k_permute", "unused")
+
+    def kernel_times(self):
+        ms = np.zeros(8)
+        calls = np.zeros(8, np.int64)
+        _check("pihm_gpu_kernel_times", self.lib.pihm_gpu_kernel_times(
+            self.h, f64p(ms), calls.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), 8))
+        return {self.KERNEL_NAMES[k]: (float(ms[k]), int(calls[k])) for k in range(8) if calls[k]}
 
     def fluxes(self):
         ne, nr = self.ws.nelem, self.ws.nriver

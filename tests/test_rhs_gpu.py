@@ -73,3 +73,61 @@ def test_fluxes_match():
         den = np.maximum(np.abs(b), np.abs(b).max() * 1e-3)
         err = np.abs(a - b) / np.where(den > 0, den, 1)
         assert err.max() <= 1e-11, (k, err.max(), int(err.argmax()))
+
+
+def test_device_path_internal_order():
+    """pihm_gpu_rhs on device pointers in internal order agrees with the
+    host-buffer path after reordering."""
+    import torch
+    ws = W.generate(1000, 100, seed=11)
+    ws, sc = scenario(ws, 11)
+    o, g = _pair(ws)
+    apply(o, sc)
+    apply(g, sc)
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    g.set_stream(stream.cuda_stream)
+    y_ref = torch.from_numpy(sc["y"]).to(dev)
+    y_int = torch.empty_like(y_ref)
+    yd_int = torch.empty_like(y_ref)
+    yd_ref = torch.empty_like(y_ref)
+    g.to_internal(y_ref.data_ptr(), y_int.data_ptr())
+    g.rhs_device(y_int.data_ptr(), yd_int.data_ptr())
+    g.to_reference(yd_int.data_ptr(), yd_ref.data_ptr())
+    assert g.status() == 0
+    got = yd_ref.cpu().numpy()
+    want, _ = o.rhs(sc["y"])
+    scale = row_scales(ws, o.fluxes(), sc["pcpdrp"], sc["edir"], sc["ett"])
+    ok, worst, idx = compare(got, want, scale)
+    assert ok, (worst, idx)
+    # permutation round trip is exact
+    back = torch.empty_like(y_ref)
+    g.to_reference(y_int.data_ptr(), back.data_ptr())
+    assert torch.equal(back, y_ref)
+
+
+def test_nan_reports_error_without_exit():
+    """An upstream Dirichlet head above the water surface makes the
+    reference's BoundFluxRiver take sqrt of a negative gradient
+    (src/river_flow.c:410-413) and exit through CheckDy; the library reports
+    PIHM_GPU_ERR_NAN and stays usable."""
+    import copy
+    ws = copy.deepcopy(W.generate(1000, 100, seed=2))
+    ws.arrays["riverbc_type"][0] = 1
+    river_bc = np.zeros(ws.nriver)
+    river_bc[0] = ws.arrays["riv_zbed"][0] + 50.0
+    ws, sc = scenario(ws, 2)
+    o, g = _pair(ws)
+    apply(o, sc)
+    apply(g, sc)
+    o.set_bc(None, river_bc)
+    g.set_bc(None, river_bc)
+    _, rc_o = o.rhs(sc["y"])
+    _, rc_g = g.rhs_host(sc["y"])
+    assert rc_o == -3 and rc_g == -3
+    # context still usable: clear the bad boundary and evaluate again
+    o.set_bc(None, np.zeros(ws.nriver))
+    g.set_bc(None, np.zeros(ws.nriver))
+    want, rc_o = o.rhs(sc["y"])
+    got, rc_g = g.rhs_host(sc["y"])
+    assert rc_o == 0 and rc_g == 0
