@@ -171,6 +171,14 @@ int pihm_gpu_status(pihm_gpu_ctx *ctx);
 int pihm_gpu_rhs_host(pihm_gpu_ctx *ctx, double t, const double *y_host,
                       double *ydot_host);
 
+/* pihm_gpu_ode on device vectors synchronises after each evaluation to read
+ * the NaN error word (the reference checks every call).  deferred = 1 skips
+ * that; the word is then read by the next pihm_gpu_status. */
+int pihm_gpu_set_nan_check(pihm_gpu_ctx *ctx, int deferred);
+/* Post-step update on device state (internal order): ws0.surf <- y_dev[0:nelem]
+ * (Summary, src/update.c:3-99; asynchronous on the context's stream). */
+int pihm_gpu_post_step(pihm_gpu_ctx *ctx, const double *y_dev);
+
 /* Keep per-element and per-segment fluxes of every later call so that
  * pihm_gpu_get_fluxes can read them (costs extra stores). */
 int pihm_gpu_set_diagnostics(pihm_gpu_ctx *ctx, int on);

@@ -1,0 +1,145 @@
+/*
+ * pihm_nvector.h -- device-resident N_Vector for CVODE 2.9 (SUNDIALS 2.7).
+ *
+ * The data of these vectors live in GPU memory and every operation of the
+ * SUNDIALS 2.7 operations table (cvode/include/sundials/sundials_nvector.h:
+ * 90-117 in the reference tree) runs as a kernel on the vector family's CUDA
+ * stream.  Element-wise operations reproduce the serial N_Vector's arithmetic
+ * exactly, special cases included (cvode/src/nvec_ser/nvector_serial.c:
+ * 421-1060), so they agree bit for bit with it; reductions (dot product and
+ * norms) use a fixed two-level tree, so they are deterministic run to run and
+ * differ from the serial left-to-right sum only by rounding.
+ *
+ * Reductions return their value to the host, which synchronises the stream.
+ *
+ * Include order: when the SUNDIALS headers are used too, include them first;
+ * otherwise this header declares the layout-compatible N_Vector types itself.
+ */
+#ifndef PIHM_NVECTOR_H
+#define PIHM_NVECTOR_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#ifndef _NVECTOR_H
+/* Same layout as SUNDIALS 2.7.0 (cvode/include/sundials/sundials_nvector.h:
+ * 64-130 of the reference): the ops table order is the ABI CVODE calls. */
+typedef enum {
+    SUNDIALS_NVEC_SERIAL,
+    SUNDIALS_NVEC_PARALLEL,
+    SUNDIALS_NVEC_OPENMP,
+    SUNDIALS_NVEC_PTHREADS,
+    SUNDIALS_NVEC_PARHYP,
+    SUNDIALS_NVEC_PETSC,
+    SUNDIALS_NVEC_CUSTOM
+} N_Vector_ID;
+typedef struct _generic_N_Vector_Ops *N_Vector_Ops;
+typedef struct _generic_N_Vector *N_Vector;
+struct _generic_N_Vector_Ops {
+    N_Vector_ID (*nvgetvectorid)(N_Vector);
+    N_Vector (*nvclone)(N_Vector);
+    N_Vector (*nvcloneempty)(N_Vector);
+    void (*nvdestroy)(N_Vector);
+    void (*nvspace)(N_Vector, long int *, long int *);
+    double *(*nvgetarraypointer)(N_Vector);
+    void (*nvsetarraypointer)(double *, N_Vector);
+    void (*nvlinearsum)(double, N_Vector, double, N_Vector, N_Vector);
+    void (*nvconst)(double, N_Vector);
+    void (*nvprod)(N_Vector, N_Vector, N_Vector);
+    void (*nvdiv)(N_Vector, N_Vector, N_Vector);
+    void (*nvscale)(double, N_Vector, N_Vector);
+    void (*nvabs)(N_Vector, N_Vector);
+    void (*nvinv)(N_Vector, N_Vector);
+    void (*nvaddconst)(N_Vector, double, N_Vector);
+    double (*nvdotprod)(N_Vector, N_Vector);
+    double (*nvmaxnorm)(N_Vector);
+    double (*nvwrmsnorm)(N_Vector, N_Vector);
+    double (*nvwrmsnormmask)(N_Vector, N_Vector, N_Vector);
+    double (*nvmin)(N_Vector);
+    double (*nvwl2norm)(N_Vector, N_Vector);
+    double (*nvl1norm)(N_Vector);
+    void (*nvcompare)(double, N_Vector, N_Vector);
+    int (*nvinvtest)(N_Vector, N_Vector);
+    int (*nvconstrmask)(N_Vector, N_Vector, N_Vector);
+    double (*nvminquotient)(N_Vector, N_Vector);
+};
+struct _generic_N_Vector {
+    void *content;
+    struct _generic_N_Vector_Ops *ops;
+};
+#endif
+
+/* ---------------------------------------------------------------------
+ * Drop-in CVODE callback and post-step update.
+ * --------------------------------------------------------------------- */
+struct pihm_gpu_ctx;
+
+/* CVRhsFn replacing the reference's ODE() (src/ode.c:4, registered with
+ * CVodeInit at src/ode.c:436): user_data is the pihm_gpu_ctx.  y and ydot are
+ * either device N_Vectors of this library (internal element order, evaluated
+ * in place on the context's stream) or SUNDIALS serial/OpenMP vectors (host
+ * memory, reference order; copied in and out).  Returns 0, or -1 when a
+ * derivative is NaN (the reference exits there, src/ode.c:401-410) or the
+ * vectors do not fit the context. */
+int pihm_gpu_ode(double t, N_Vector y, N_Vector ydot, void *user_data);
+/* Summary's effect on later right-hand sides (src/update.c:3-99): ws0 <- y
+ * (the previous-step surface storage that caps infiltration,
+ * src/vert_flow.c:122).  y as for pihm_gpu_ode. */
+int pihm_gpu_summary(struct pihm_gpu_ctx *ctx, N_Vector y);
+
+/* Create a vector family's first member: `length` doubles of device memory,
+ * operations on `stream` (cudaStream_t, NULL = legacy default stream).
+ * Clones share the family's stream and reduction scratch. */
+N_Vector N_VNew_PihmGpu(long int length, void *stream);
+/* Wrap caller-owned device memory (not freed by N_VDestroy). */
+N_Vector N_VMake_PihmGpu(long int length, double *dev_data, void *stream);
+double *N_VGetDeviceArrayPointer_PihmGpu(N_Vector v);
+long int N_VGetLength_PihmGpu(N_Vector v);
+/* Host <-> device copies of the whole vector (synchronous). */
+int N_VCopyFromHost_PihmGpu(N_Vector v, const double *host);
+int N_VCopyToHost_PihmGpu(N_Vector v, double *host);
+
+/* The operations table, callable directly as well. */
+N_Vector_ID N_VGetVectorID_PihmGpu(N_Vector v);
+N_Vector N_VClone_PihmGpu(N_Vector w);
+N_Vector N_VCloneEmpty_PihmGpu(N_Vector w);
+void N_VDestroy_PihmGpu(N_Vector v);
+void N_VSpace_PihmGpu(N_Vector v, long int *lrw, long int *liw);
+double *N_VGetArrayPointer_PihmGpu(N_Vector v);
+void N_VSetArrayPointer_PihmGpu(double *v_data, N_Vector v);
+void N_VLinearSum_PihmGpu(double a, N_Vector x, double b, N_Vector y, N_Vector z);
+void N_VConst_PihmGpu(double c, N_Vector z);
+void N_VProd_PihmGpu(N_Vector x, N_Vector y, N_Vector z);
+void N_VDiv_PihmGpu(N_Vector x, N_Vector y, N_Vector z);
+void N_VScale_PihmGpu(double c, N_Vector x, N_Vector z);
+void N_VAbs_PihmGpu(N_Vector x, N_Vector z);
+void N_VInv_PihmGpu(N_Vector x, N_Vector z);
+void N_VAddConst_PihmGpu(N_Vector x, double b, N_Vector z);
+double N_VDotProd_PihmGpu(N_Vector x, N_Vector y);
+double N_VMaxNorm_PihmGpu(N_Vector x);
+double N_VWrmsNorm_PihmGpu(N_Vector x, N_Vector w);
+double N_VWrmsNormMask_PihmGpu(N_Vector x, N_Vector w, N_Vector id);
+double N_VMin_PihmGpu(N_Vector x);
+double N_VWL2Norm_PihmGpu(N_Vector x, N_Vector w);
+double N_VL1Norm_PihmGpu(N_Vector x);
+void N_VCompare_PihmGpu(double c, N_Vector x, N_Vector z);
+int N_VInvTest_PihmGpu(N_Vector x, N_Vector z);
+int N_VConstrMask_PihmGpu(N_Vector c, N_Vector x, N_Vector m);
+double N_VMinQuotient_PihmGpu(N_Vector num, N_Vector denom);
+
+/* Raw-pointer entry points (device pointers, length n, the given stream):
+ * the same kernels for callers that keep their own vector objects. */
+int pihm_gpu_nv_linear_sum(double a, const double *x, double b, const double *y, double *z,
+                           int64_t n, void *stream);
+int pihm_gpu_nv_wrms_norm(const double *x, const double *w, int64_t n, void *stream,
+                          double *result);
+int pihm_gpu_nv_dot_prod(const double *x, const double *y, int64_t n, void *stream,
+                         double *result);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PIHM_NVECTOR_H */

@@ -135,6 +135,7 @@ int pihm_gpu_create(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double 
   c->stream = nullptr;
   c->diag = 0;
   c->launches = 0;
+  c->nan_check_deferred = 0;
   c->prof = nullptr;
 
   // ---- renumbering ----

@@ -107,6 +107,7 @@ struct pihm_gpu_ctx {
   int32_t *d_perm;                    // internal -> reference element index
   int32_t *h_perm, *h_iperm;          // host copies (perm, inverse)
   int diag;
+  int nan_check_deferred;  // 1: pihm_gpu_ode does not synchronise to read the error word
   long long launches;      // kernels launched by this context so far
   pihm::Profiler *prof;    // non-null while profiling is on
 };
