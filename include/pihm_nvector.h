@@ -139,6 +139,28 @@ int pihm_gpu_nv_wrms_norm(const double *x, const double *w, int64_t n, void *str
 int pihm_gpu_nv_dot_prod(const double *x, const double *y, int64_t n, void *stream,
                          double *result);
 
+/* WRMS norm, sqrt(sum_i (x_i w_i)^2 / n), for callers that cannot allocate
+ * device memory (no counterpart in the reference).  pihm_gpu_nv_wrms_norm
+ * creates a workspace with cudaMalloc the first time a stream uses it; code
+ * running during CUDA-graph capture, inside a framework that owns every
+ * device allocation, or in a per-call integrator callback cannot do that.
+ * This entry point allocates nothing: it works in a fixed library-static
+ * device array (about 64 KiB, held by every GPU that loads the library until
+ * the process exits) and writes the norm to `result_dev`, caller-owned device
+ * memory, on `stream` without synchronising.
+ *   - n must be 1 .. PIHM_GPU_NOALLOC_MAX_LEN; longer vectors return
+ *     PIHM_GPU_NOALLOC_ERR_TOO_LONG and launch nothing.
+ *   - All calls share the array: calls that overlap on the GPU (different
+ *     streams without ordering) race and give wrong results.
+ *   - The first call on a device looks up the array's device address with
+ *     that device current; make it before any stream capture begins.
+ * Returns 0, -1 (bad argument), -2 (CUDA error) or
+ * PIHM_GPU_NOALLOC_ERR_TOO_LONG. */
+#define PIHM_GPU_NOALLOC_MAX_LEN 33554432L
+#define PIHM_GPU_NOALLOC_ERR_TOO_LONG (-7)
+int pihm_gpu_nv_wrms_norm_noalloc(const double *x, const double *w, int64_t n, void *stream,
+                                  double *result_dev);
+
 #ifdef __cplusplus
 }
 #endif
