@@ -173,9 +173,48 @@ int pihm_gpu_create(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double 
       if (g->down[s] > 0) up_idx[fill[g->down[s] - 1]++] = s;
   }
 
+  // ---- interior edges, internal order ----
+  // An edge is owned by the element with the smaller internal index when the
+  // flux is antisymmetric: diffusion wave, both sides list each other, and the
+  // distance and edge length agree bit for bit.  Otherwise every element side
+  // is a one-sided edge evaluated from that side, as in the reference.
+  std::vector<int32_t> e_i, e_k, emap(3 * (size_t)ne, 0);
+  std::vector<double> e_invdist, e_len, e_invrough;
+  for (int i = 0; i < ne; i++) {
+    const int ri = perm[i];
+    for (int j = 0; j < 3; j++) {
+      const int nbr = g->nabr[3 * ri + j];
+      if (nbr <= 0) continue;
+      const int rk = nbr - 1, k = iperm[rk];
+      int jr = -1;
+      for (int q = 0; q < 3; q++)
+        if (g->nabr[3 * rk + q] == ri + 1) {
+          jr = q;
+          break;
+        }
+      const bool sym = surf_mode == kDiffWave && jr >= 0 &&
+                       g->nabrdist[3 * ri + j] == g->nabrdist[3 * rk + jr] &&
+                       g->edge[3 * ri + j] == g->edge[3 * rk + jr];
+      if (sym && k < i) continue;  // owned by k, recorded when k was visited
+      const int e = (int)e_i.size();
+      e_i.push_back(i);
+      e_k.push_back(k);
+      e_invdist.push_back(1.0 / g->nabrdist[3 * ri + j]);
+      e_len.push_back(g->edge[3 * ri + j]);
+      e_invrough.push_back(1.0 / (0.5 * (g->rough[ri] + g->rough[rk])));
+      emap[(size_t)j * ne + i] = e + 1;
+      if (sym) emap[(size_t)jr * ne + k] = -(e + 1);
+    }
+  }
+  const int nedge = (int)e_i.size();
+
   // ---- host images of the static planes ----
   const size_t NE = ne, NR = nr > 0 ? nr : 1, NB = nbank > 0 ? nbank : 1;
+  const size_t NED = nedge > 0 ? nedge : 1;
   size_t sbytes = 0;
+  sbytes += 13 * carve_size<double>(NE);                       // derived element constants
+  sbytes += 2 * carve_size<int32_t>(NED) + 3 * carve_size<double>(NED);  // edge list
+  sbytes += carve_size<int32_t>(3 * NE);                       // emap
   sbytes += 18 * carve_size<double>(NE);                       // element scalars
   sbytes += 4 * carve_size<double>(3 * NE);                    // edge, nabrdist, nabr_x, nabr_y
   sbytes += 2 * carve_size<double>(NE);                        // den_x, den_y
@@ -254,6 +293,44 @@ int pihm_gpu_create(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double 
   int32_t *h_permd = carve<int32_t>(hp, NE);
   std::memcpy(h_permd, perm.data(), sizeof(int32_t) * ne);
 
+  // derived element constants (see DevMesh); same expressions as the
+  // reference's inline ones, evaluated without contraction
+  double *h_inv_area = carve<double>(hp, NE), *h_inv_por = carve<double>(hp, NE);
+  double *h_inv_alpha = carve<double>(hp, NE), *h_vg_m = carve<double>(hp, NE);
+  double *h_vg_e = carve<double>(hp, NE), *h_vg_ib = carve<double>(hp, NE);
+  double *h_kinf_mat = carve<double>(hp, NE), *h_kmac_a = carve<double>(hp, NE);
+  double *h_kv2_mac = carve<double>(hp, NE), *h_d_dinf = carve<double>(hp, NE);
+  double *h_d_rzd = carve<double>(hp, NE), *h_d_dmac = carve<double>(hp, NE);
+  double *h_kh_k1 = carve<double>(hp, NE);
+  for (int i = 0; i < ne; i++) {
+    h_inv_area[i] = 1.0 / h_area[i];
+    h_inv_por[i] = 1.0 / h_por[i];
+    h_inv_alpha[i] = 1.0 / h_alpha[i];
+    h_vg_m[i] = h_beta[i] / (h_beta[i] - 1.0);
+    h_vg_e[i] = (h_beta[i] - 1.0) / h_beta[i];
+    h_vg_ib[i] = 1.0 / h_beta[i];
+    h_kinf_mat[i] = h_kinfv[i] * (1.0 - h_areafh[i]);
+    h_kmac_a[i] = h_kmacv[i] * h_areafh[i];
+    h_kv2_mac[i] = (h_areafh[i] > 0.0) ? h_kmacv[i] * h_areafh[i] + h_ksatv[i] * (1.0 - h_areafh[i])
+                                       : h_ksatv[i];
+    h_d_dinf[i] = h_depth[i] - h_dinf[i];
+    h_d_rzd[i] = h_depth[i] - h_rzd[i];
+    h_d_dmac[i] = h_depth[i] - h_dmac[i];
+    h_kh_k1[i] = h_kmach[i] * h_areafv[i] + h_ksath[i] * (1.0 - h_areafv[i]);
+  }
+  int32_t *h_ei = carve<int32_t>(hp, NED), *h_ek = carve<int32_t>(hp, NED);
+  double *h_einvd = carve<double>(hp, NED), *h_elen = carve<double>(hp, NED);
+  double *h_einvr = carve<double>(hp, NED);
+  int32_t *h_emap = carve<int32_t>(hp, 3 * NE);
+  if (nedge) {
+    std::memcpy(h_ei, e_i.data(), sizeof(int32_t) * nedge);
+    std::memcpy(h_ek, e_k.data(), sizeof(int32_t) * nedge);
+    std::memcpy(h_einvd, e_invdist.data(), sizeof(double) * nedge);
+    std::memcpy(h_elen, e_len.data(), sizeof(double) * nedge);
+    std::memcpy(h_einvr, e_invrough.data(), sizeof(double) * nedge);
+  }
+  std::memcpy(h_emap, emap.data(), sizeof(int32_t) * 3 * ne);
+
   // ---- device allocations ----
   if (cudaMalloc(&c->d_static, sbytes) != cudaSuccess) {
     pihm_gpu_destroy(c);
@@ -296,6 +373,18 @@ int pihm_gpu_create(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double 
   m.r_porosity = (double *)dev(h_rpor);
   m.up_ptr = (int32_t *)dev(h_upp); m.up_idx = (int32_t *)dev(h_upi);
   c->d_perm = (int32_t *)dev(h_permd);
+  m.inv_area = (double *)dev(h_inv_area); m.inv_por = (double *)dev(h_inv_por);
+  m.inv_alpha = (double *)dev(h_inv_alpha); m.vg_m = (double *)dev(h_vg_m);
+  m.vg_e = (double *)dev(h_vg_e); m.vg_ib = (double *)dev(h_vg_ib);
+  m.kinf_mat = (double *)dev(h_kinf_mat); m.kmac_a = (double *)dev(h_kmac_a);
+  m.kv2_mac = (double *)dev(h_kv2_mac); m.d_dinf = (double *)dev(h_d_dinf);
+  m.d_rzd = (double *)dev(h_d_rzd); m.d_dmac = (double *)dev(h_d_dmac);
+  m.kh_k1 = (double *)dev(h_kh_k1);
+  m.nedge = nedge;
+  m.e_i = (int32_t *)dev(h_ei); m.e_k = (int32_t *)dev(h_ek);
+  m.e_invdist = (double *)dev(h_einvd); m.e_len = (double *)dev(h_elen);
+  m.e_invrough = (double *)dev(h_einvr);
+  m.emap = (int32_t *)dev(h_emap);
 
   // dynamic block: inputs, scratch, diagnostics, staging, error word
   size_t dbytes = 0;
@@ -304,6 +393,7 @@ int pihm_gpu_create(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double 
   dbytes += carve_size<double>(NR);           // river_bc
   dbytes += 4 * carve_size<double>(NE);       // surfh, head, effk, gradmag
   dbytes += carve_size<double>(11 * NR);      // rivflow
+  dbytes += 2 * carve_size<double>(NED);      // edge fluxes
   dbytes += carve_size<double>(8 * NB);       // bank_part
   dbytes += 2 * carve_size<double>(3 * NE) + 2 * carve_size<double>(NE) + carve_size<double>(5 * NE);
   dbytes += 2 * carve_size<double>(c->neq);   // staging
@@ -325,6 +415,7 @@ int pihm_gpu_create(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double 
   m.surfh = carve<double>(dp, NE); m.head = carve<double>(dp, NE); m.effk = carve<double>(dp, NE);
   m.gradmag = carve<double>(dp, NE);
   m.rivflow = carve<double>(dp, 11 * NR);
+  m.eflux_ovl = carve<double>(dp, NED); m.eflux_sub = carve<double>(dp, NED);
   m.bank_part = carve<double>(dp, 8 * NB);
   m.d_ovl = carve<double>(dp, 3 * NE); m.d_sub = carve<double>(dp, 3 * NE);
   m.d_infil = carve<double>(dp, NE); m.d_rechg = carve<double>(dp, NE); m.d_et = carve<double>(dp, 5 * NE);

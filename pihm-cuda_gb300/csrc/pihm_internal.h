@@ -51,6 +51,20 @@ struct DevMesh {
   const int32_t *bctype;    // boundary condition type (boundary edges)
   const double *edge, *nabrdist, *nabr_x, *nabr_y;
   const double *den_x, *den_y;  // [ne] geometric denominators of the gradient
+  // element constants derived once at load: the reference evaluates these
+  // sub-expressions inline with the same operation order (bit-identical),
+  // except the reciprocals, which replace divisions (<= 1 ulp apart)
+  const double *inv_area, *inv_por, *inv_alpha;
+  const double *vg_m, *vg_e, *vg_ib;         // beta/(beta-1), (beta-1)/beta, 1/beta
+  const double *kinf_mat, *kmac_a, *kv2_mac; // kinfv(1-areafh), kmacv areafh, AvgKv k2
+  const double *d_dinf, *d_rzd, *d_dmac;     // depth-dinf, depth-rzd, depth-dmac
+  const double *kh_k1;                       // EffKh k1 = kmach areafv + ksath (1-areafv)
+  // interior edges: each pair of neighbouring elements is evaluated once by
+  // its owner and read with a sign by the other side
+  int32_t nedge;
+  const int32_t *e_i, *e_k;                  // owner, neighbour (internal)
+  const double *e_invdist, *e_len, *e_invrough;
+  const int32_t *emap;                       // [3][ne] +(e+1) owner, -(e+1) other, 0 none
   const int32_t *bank_slot;     // [ne] slot of an element with river edges
   const int32_t *bank_elem;     // [nbank]
 
@@ -68,6 +82,7 @@ struct DevMesh {
 
   // scratch written and read inside one evaluation
   double *surfh, *head, *effk, *gradmag;  // [ne]
+  double *eflux_ovl, *eflux_sub;          // [nedge]
   double *rivflow;                        // [11][nr]; slots 2/3 carry over
   double *bank_part;                      // [8][nbank]
   // diagnostics (optional)
@@ -89,7 +104,7 @@ struct Profiler {
   long long calls[kKernels] = {0};
 };
 
-enum KernelId { K_PREP = 0, K_GRAD, K_MAIN, K_RIVER, K_FINISH, K_FUSED, K_PERMUTE };
+enum KernelId { K_PREP = 0, K_GRAD, K_MAIN, K_RIVER, K_FINISH, K_EDGE, K_PERMUTE };
 
 }  // namespace pihm
 

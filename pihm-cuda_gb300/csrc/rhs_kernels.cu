@@ -66,6 +66,18 @@ __device__ __forceinline__ double eff_kh(double depth, double dmac, double kmach
   return ksath;
 }
 
+// EffKh with k1 = kmach*areafv + ksath*(1-areafv) and depth-dmac precomputed
+// (the reference evaluates both inline with the same operations)
+__device__ __forceinline__ double eff_kh_pre(double k1, double ksath, double depth, double dmac,
+                                             double d_dmac, double gw) {
+  gw = (gw > 0.0) ? gw : 0.0;
+  if (gw > d_dmac) {
+    const double d1 = (gw > depth) ? dmac : gw - d_dmac;
+    return (k1 * d1 + ksath * d_dmac) / (d1 + d_dmac);
+  }
+  return ksath;
+}
+
 // AvgH, src/lat_flow.c:217-237
 __device__ __forceinline__ double avg_h_sub(double diff, double hsub, double hnabr) {
   if (diff > 0.0) return (hsub > 0.0) ? hsub : 0.0;
@@ -152,7 +164,7 @@ __global__ void __launch_bounds__(256) k_elem_prep(DevMesh m, const double *REST
   const double gw = clamp0(y[2 * m.ne + i]);
   m.surfh[i] = surfh;
   m.head[i] = surfh + m.zmax[i];
-  m.effk[i] = eff_kh(m.depth[i], m.dmac[i], m.kmach[i], m.areafv[i], m.ksath[i], gw);
+  m.effk[i] = eff_kh_pre(m.kh_k1[i], m.ksath[i], m.depth[i], m.dmac[i], m.d_dmac[i], gw);
 }
 
 // ---------------------------------------------------------------------------
@@ -186,6 +198,52 @@ __global__ void __launch_bounds__(256) k_elem_grad(DevMesh m, const double *REST
 }
 
 // ---------------------------------------------------------------------------
+// k_edge: one thread per interior edge.  SubFlowElemToElem and
+// OvlFlowElemToElem (src/lat_flow.c:285-338) are antisymmetric in IEEE
+// arithmetic under the diffusion wave (negated head difference, commutative
+// averages, the same distance and edge length on both sides, which the host
+// checks bit for bit), so the owner evaluates each edge once and the
+// neighbour reads the negated value.  Kinematic overland flow is not
+// antisymmetric (avg_sf depends on the sign of the gradient): there every
+// element side is its own one-sided edge.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_edge(DevMesh m, const double *RESTRICT y) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m.nedge) return;
+  const int ne = m.ne;
+  const int i = m.e_i[e], k = m.e_k[e];
+  const double invdist = m.e_invdist[e], len = m.e_len[e];
+  // Darcy flux between the two groundwater columns
+  const double gw_i = clamp0(y[2 * ne + i]), gw_k = clamp0(y[2 * ne + k]);
+  double diff_h = (gw_i + m.zmin[i]) - (gw_k + m.zmin[k]);
+  double avg_h = avg_h_sub(diff_h, gw_i, gw_k);
+  double grad_h = diff_h * invdist;
+  const double avg_ksat = 0.5 * (m.effk[i] + m.effk[k]);
+  m.eflux_sub[e] = avg_ksat * grad_h * avg_h * len;
+  // Manning overland flux
+  const double s_i = m.surfh[i], s_k = m.surfh[k];
+  double avg_sf;
+  if (m.surf_mode == kKinematic) {
+    diff_h = m.zmax[i] - m.zmax[k];
+    avg_h = avg_h_surf(diff_h, s_i, s_k);
+    grad_h = diff_h * invdist;
+    avg_sf = (grad_h > 0.0) ? grad_h : kGradMin;
+  } else {
+    diff_h = m.head[i] - m.head[k];
+    avg_h = avg_h_surf(diff_h, s_i, s_k);
+    grad_h = diff_h * invdist;
+    avg_sf = 0.5 * (m.gradmag[i] + m.gradmag[k]);
+    avg_sf = (avg_sf > kGradMin) ? avg_sf : kGradMin;
+  }
+  double ovl = 0.0;
+  if (avg_h > 0.0) {  // avg_h == 0 gives crossa == 0: the flux is zero
+    const double crossa = avg_h * len;
+    ovl = crossa * pow(avg_h, 0.6666667) * grad_h * rsqrt(avg_sf) * m.e_invrough[e];
+  }
+  m.eflux_ovl[e] = ovl;
+}
+
+// ---------------------------------------------------------------------------
 // k_elem_main
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_elem_main(DevMesh m, const double *RESTRICT y,
@@ -196,129 +254,123 @@ __global__ void __launch_bounds__(256) k_elem_main(DevMesh m, const double *REST
   const double gw = clamp0(y[2 * ne + i]);
   const double unsat = clamp0(y[ne + i]);
   const double surfh = m.surfh[i];
-  const double head = m.head[i];
   const double zmin = m.zmin[i];
-  const double effk = m.effk[i];
-  const double gm = m.gradmag[i];
-  const double rough = m.rough[i];
-  const double area = m.area[i];
+  const double inv_area = m.inv_area[i];
   const double gwhead = gw + zmin;
 
   double ovl[3], sub[3];
   bool riv[3];
 #pragma unroll
   for (int j = 0; j < 3; j++) {
-    const int32_t nb = m.nb[j * ne + i];
+    const int32_t code = m.emap[j * ne + i];
     riv[j] = false;
-    if (nb >= 0) {
-      // SubFlowElemToElem, src/lat_flow.c:285-309
-      const double gw_k = clamp0(y[2 * ne + nb]);
-      const double dist = m.nabrdist[j * ne + i];
-      const double edge = m.edge[j * ne + i];
-      double diff_h = gwhead - (gw_k + m.zmin[nb]);
-      double avg_h = avg_h_sub(diff_h, gw, gw_k);
-      double grad_h = diff_h / dist;
-      const double avg_ksat = 0.5 * (effk + m.effk[nb]);
-      sub[j] = avg_ksat * grad_h * avg_h * edge;
-      // OvlFlowElemToElem, src/lat_flow.c:311-338
-      const double surfh_k = m.surfh[nb];
-      double avg_sf;
-      if (m.surf_mode == kKinematic) {
-        diff_h = m.zmax[i] - m.zmax[nb];
-        avg_h = avg_h_surf(diff_h, surfh, surfh_k);
-        grad_h = diff_h / dist;
-        avg_sf = (grad_h > 0.0) ? grad_h : kGradMin;
-      } else {
-        diff_h = head - m.head[nb];
-        avg_h = avg_h_surf(diff_h, surfh, surfh_k);
-        grad_h = diff_h / dist;
-        avg_sf = 0.5 * (gm + m.gradmag[nb]);
-        avg_sf = (avg_sf > kGradMin) ? avg_sf : kGradMin;
-      }
-      const double avg_rough = 0.5 * (rough + m.rough[nb]);
-      const double crossa = avg_h * edge;
-      ovl[j] = overland_flow(avg_h, grad_h, avg_sf, crossa, avg_rough);
-    } else if (nb != kBoundary) {
-      // river edge: Infil sees the previous evaluation's value
-      const int s = -1 - nb;
-      const int slot = (m.left[s] == i) ? LEFT_SURF2CHANL : RIGHT_SURF2CHANL;
-      ovl[j] = -m.rivflow[slot * m.nr + s];
-      sub[j] = 0.0;
-      riv[j] = true;
+    if (code > 0) {
+      ovl[j] = m.eflux_ovl[code - 1];
+      sub[j] = m.eflux_sub[code - 1];
+    } else if (code < 0) {
+      ovl[j] = -m.eflux_ovl[-code - 1];
+      sub[j] = -m.eflux_sub[-code - 1];
     } else {
-      // BoundFluxElem, src/lat_flow.c:340-382
-      const int bct = m.bctype[j * ne + i];
-      ovl[j] = 0.0;
-      if (bct == 0) {
+      const int32_t nb = m.nb[j * ne + i];
+      if (nb != kBoundary) {
+        // river edge: Infil sees the previous evaluation's value
+        const int s = -1 - nb;
+        const int slot = (m.left[s] == i) ? LEFT_SURF2CHANL : RIGHT_SURF2CHANL;
+        ovl[j] = -m.rivflow[slot * m.nr + s];
         sub[j] = 0.0;
-      } else if (bct > 0) {
-        const double bc = m.elem_bc[j * ne + i];
-        const double diff_h = gwhead - bc;
-        const double avg_h = avg_h_sub(diff_h, gw, bc - zmin);
-        const double grad_h = diff_h / m.nabrdist[j * ne + i];
-        sub[j] = effk * grad_h * avg_h * m.edge[j * ne + i];
+        riv[j] = true;
       } else {
-        sub[j] = -m.elem_bc[j * ne + i];
+        // BoundFluxElem, src/lat_flow.c:340-382
+        const int bct = m.bctype[j * ne + i];
+        ovl[j] = 0.0;
+        if (bct == 0) {
+          sub[j] = 0.0;
+        } else if (bct > 0) {
+          const double bc = m.elem_bc[j * ne + i];
+          const double diff_h = gwhead - bc;
+          const double avg_h = avg_h_sub(diff_h, gw, bc - zmin);
+          const double grad_h = diff_h / m.nabrdist[j * ne + i];
+          sub[j] = m.effk[i] * grad_h * avg_h * m.edge[j * ne + i];
+        } else {
+          sub[j] = -m.elem_bc[j * ne + i];
+        }
       }
     }
   }
 
   // EtExtract, src/hydrol.c:33-97
   const double depth = m.depth[i];
-  const double dinf = m.dinf[i];
+  const double d_dinf = m.d_dinf[i];
   const double edir = m.edir[i], ett = m.ett[i];
   double edir_surf = 0.0, edir_unsat = 0.0, edir_gw = 0.0, ett_unsat = 0.0, ett_gw = 0.0;
+  const bool gw_in_dinf = gw > d_dinf;
   if (surfh >= kDeprStg) edir_surf = edir;
-  else if (gw > depth - dinf) edir_gw = edir;
+  else if (gw_in_dinf) edir_gw = edir;
   else edir_unsat = edir;
-  if (gw > depth - m.rzd[i]) ett_gw = ett;
+  if (gw > m.d_rzd[i]) ett_gw = ett;
   else ett_unsat = ett;
 
-  // Infil, src/vert_flow.c:33-130, and Recharge, :132-170
-  const double beta = m.beta[i], alpha = m.alpha[i];
-  const double kinfv = m.kinfv[i], kmacv = m.kmacv[i], areafh = m.areafh[i];
-  const double ksatv = m.ksatv[i], dmac = m.dmac[i];
+  // Infil, src/vert_flow.c:33-130, and Recharge, :132-170, sharing KrFunc and
+  // Psi of the same saturation
+  const double kinf_mat = m.kinf_mat[i], kmac_a = m.kmac_a[i], areafh = m.areafh[i];
+  const double kinfv = m.kinfv[i], ksatv = m.ksatv[i], dmac = m.dmac[i];
   const double pcpdrp = m.pcpdrp[i];
   const double zmax = m.zmax[i];
-  const bool gw_in_dinf = gw > depth - dinf;
+  const double dinf = m.dinf[i];
   double satn = 1.0, satkfunc = 1.0, psi_u = 0.0;
   if (!gw_in_dinf) {
     const double deficit = depth - gw;
     satn = unsat / deficit;
     satn = (satn > 1.0) ? 1.0 : satn;
     satn = (satn < kSatMin) ? kSatMin : satn;
-    satkfunc = kr_func(beta, satn);
-    psi_u = psi_vg(satn, alpha, beta);
-  } else {
-    satkfunc = kr_func(beta, 1.0);
+    const double vm = m.vg_m[i];
+    // KrFunc, src/soil.c:8-13
+    const double t = 1.0 - pow(1.0 - pow(satn, vm), m.vg_e[i]);
+    satkfunc = sqrt(satn) * t * t;
+    // Psi, src/vert_flow.c:272-278
+    psi_u = -pow(pow(1.0 / satn, vm) - 1.0, m.vg_ib[i]) * m.inv_alpha[i];
   }
+  // KrFunc(beta, 1) == 1 exactly: pow(1 - pow(1, m), e) == pow(0, e) == 0
   double infil;
   if (unsat + gw > depth) {
     infil = 0.0;
   } else {
     double applrate = 0.0;
 #pragma unroll
-    for (int j = 0; j < 3; j++) applrate += -ovl[j] / area;
+    for (int j = 0; j < 3; j++) applrate += -ovl[j] * inv_area;
     applrate = (applrate > 0.0) ? applrate : 0.0;
     applrate += pcpdrp;
-    double wetfrac = surfh / kDeprStg;
+    double wetfrac = surfh * (1.0 / kDeprStg);
     wetfrac = (wetfrac > 0.0) ? wetfrac : 0.0;
     wetfrac = (wetfrac < 1.0) ? wetfrac : 1.0;
     double dh_by_dz;
+    double esatn = satn;
     if (gw_in_dinf) {
       dh_by_dz = (surfh + zmax - gwhead) / (0.5 * (surfh + dinf));
-      dh_by_dz = (surfh <= 0.0 && dh_by_dz > 0.0) ? 0.0 : dh_by_dz;
-      const double kinf = eff_kinf(kinfv, kmacv, areafh, dh_by_dz, satkfunc, 1.0, applrate, surfh);
-      infil = kinf * dh_by_dz;
+      esatn = 1.0;
     } else {
       const double psi_c = (psi_u > kPsiMin) ? psi_u : kPsiMin;
       const double h_u = psi_c + zmax - 0.5 * dinf;
       dh_by_dz = (surfh + zmax - h_u) / (0.5 * (surfh + dinf));
-      dh_by_dz = (surfh <= 0.0 && dh_by_dz > 0.0) ? 0.0 : dh_by_dz;
-      const double kinf = eff_kinf(kinfv, kmacv, areafh, dh_by_dz, satkfunc, satn, applrate, surfh);
-      infil = kinf * dh_by_dz;
-      infil = (infil > 0.0) ? infil : 0.0;
     }
+    dh_by_dz = (surfh <= 0.0 && dh_by_dz > 0.0) ? 0.0 : dh_by_dz;
+    // EffKinf, src/vert_flow.c:211-270
+    double kinf;
+    if (areafh == 0.0) {
+      kinf = kinfv * satkfunc;
+    } else if (surfh > kDeprStg) {
+      kinf = kinf_mat * satkfunc + kmac_a;
+    } else if (applrate <= dh_by_dz * kinfv * satkfunc) {
+      kinf = kinfv * satkfunc;
+    } else if (applrate < dh_by_dz * (kmac_a + kinf_mat * satkfunc)) {
+      // KrFunc(2, satn): pow(satn, 2) and pow(., 0.5) are a product and sqrt
+      const double t2 = 1.0 - sqrt(1.0 - esatn * esatn);
+      kinf = kinf_mat * satkfunc + kmac_a * (sqrt(esatn) * t2 * t2);
+    } else {
+      kinf = kinf_mat * satkfunc + kmac_a;
+    }
+    infil = kinf * dh_by_dz;
+    if (!gw_in_dinf) infil = (infil > 0.0) ? infil : 0.0;
     const double ws0 = m.ws0_surf[i];
     const double infil_max = applrate + ((ws0 > 0.0) ? ws0 / m.dt : 0.0);
     infil = (infil > infil_max) ? infil_max : infil;
@@ -343,7 +395,7 @@ __global__ void __launch_bounds__(256) k_elem_main(DevMesh m, const double *REST
     } else {
       k1 = satkfunc * ksatv;
       d1 = deficit;
-      k2 = (areafh > 0.0) ? kmacv * areafh + ksatv * (1.0 - areafh) : ksatv;
+      k2 = m.kv2_mac[i];
       d2 = dmac - deficit;
       k3 = ksatv;
       d3 = gw - (dmac - deficit);
@@ -372,11 +424,10 @@ __global__ void __launch_bounds__(256) k_elem_main(DevMesh m, const double *REST
   }
 
   // element rows of ydot, src/ode.c:111-209
-  const double porosity = m.porosity[i];
+  const double inv_por = m.inv_por[i];
   const double base_surf = pcpdrp - infil - edir_surf;
   const double base_gw = rechg - edir_gw - ett_gw;
-  double du = infil - rechg - edir_unsat - ett_unsat;
-  du /= porosity;
+  const double du = (infil - rechg - edir_unsat - ett_unsat) * inv_por;
   ydot[ne + i] = du;
   unsigned int bad = isnan(du);
   if (riv[0] || riv[1] || riv[2]) {
@@ -394,10 +445,10 @@ __global__ void __launch_bounds__(256) k_elem_main(DevMesh m, const double *REST
     double ds = base_surf, dg = base_gw;
 #pragma unroll
     for (int j = 0; j < 3; j++) {
-      ds -= ovl[j] / area;
-      dg -= sub[j] / area;
+      ds -= ovl[j] * inv_area;
+      dg -= sub[j] * inv_area;
     }
-    dg /= porosity;
+    dg *= inv_por;
     ydot[i] = ds;
     ydot[2 * ne + i] = dg;
     bad |= isnan(ds) | isnan(dg);
@@ -636,7 +687,7 @@ __global__ void __launch_bounds__(128) k_finish(DevMesh m, double *RESTRICT ydot
   const int nbk = m.nbank;
   const double *bp = m.bank_part;
   double ds = bp[b], dg = bp[nbk + b];
-  const double area = m.area[i];
+  const double inv_area = m.inv_area[i];
 #pragma unroll
   for (int j = 0; j < 3; j++) {
     const int32_t nb = m.nb[j * ne + i];
@@ -658,10 +709,10 @@ __global__ void __launch_bounds__(128) k_finish(DevMesh m, double *RESTRICT ydot
       o = bp[(2 + j) * nbk + b];
       u = bp[(5 + j) * nbk + b];
     }
-    ds -= o / area;
-    dg -= u / area;
+    ds -= o * inv_area;
+    dg -= u * inv_area;
   }
-  dg /= m.porosity[i];
+  dg *= m.inv_por[i];
   ydot[i] = ds;
   ydot[2 * ne + i] = dg;
   if (isnan(ds) | isnan(dg)) atomicOr(m.err, 1u);
@@ -736,6 +787,12 @@ cudaError_t launch_rhs(const DevMesh &m, const double *y, double *ydot, cudaStre
     if (m.surf_mode == kDiffWave) {
       on = prof_begin(prof, K_GRAD, st);
       k_elem_grad<<<blocks_for(m.ne, 256), 256, 0, st>>>(m, y);
+      prof_end(prof, on, st);
+      ++*launches;
+    }
+    if (m.nedge > 0) {
+      on = prof_begin(prof, K_EDGE, st);
+      k_edge<<<blocks_for(m.nedge, 256), 256, 0, st>>>(m, y);
       prof_end(prof, on, st);
       ++*launches;
     }

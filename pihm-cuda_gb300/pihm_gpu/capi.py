@@ -166,7 +166,7 @@ class GpuRhs:
         _check("pihm_gpu_set_profiling", self.lib.pihm_gpu_set_profiling(self.h, int(on)))
 
     KERNEL_NAMES = ("k_elem_prep", "k_elem_grad", "k_elem_main", "k_river", "k_finish",
-                    "k_rhs_fused", "k_permute", "unused")
+                    "k_edge", "k_permute", "unused")
 
     def kernel_times(self):
         ms = np.zeros(8)
