@@ -210,8 +210,15 @@ int pihm_gpu_launch_count(const pihm_gpu_ctx *ctx, int64_t *count);
 int pihm_gpu_set_profiling(pihm_gpu_ctx *ctx, int on);
 /* Synchronise, then return and reset the accumulated device time (ms) and
  * launch count per kernel: 0 prep, 1 gradient, 2 element, 3 river,
- * 4 finish, 5 fused, 6 permute; n entries are written. */
+ * 4 finish, 5 edge, 6 permute; n entries are written. */
 int pihm_gpu_kernel_times(pihm_gpu_ctx *ctx, double *ms, int64_t *calls, int n);
+
+/* Diagnostic: the table-driven pow of the right-hand-side kernels,
+ * fast[i] = pow(x[i], y[i]), and CUDA's pow into cuda_pow[i] when it is not
+ * NULL; device arrays of length n, asynchronous on `stream`.  Used by the
+ * tests to measure the error of the fast path. */
+int pihm_gpu_selftest_pow(const double *x, const double *y, double *fast,
+                          double *cuda_pow, int64_t n, void *stream);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,87 @@
+// Table-driven FP64 pow for the right-hand-side kernels (sm_103a).
+//
+// GB300 issues about two FP64 instructions per clock per SM, so the dozens of
+// FP64 operations inside a general-purpose pow dominate the PIHM right-hand
+// side.  pow_fast(x, y) = exp(y ln x) follows P. T. P. Tang's table-driven
+// algorithms ("Table-driven implementation of the exponential function in
+// IEEE floating-point arithmetic", ACM TOMS 15(2) 1989; "... of the logarithm
+// function ...", ACM TOMS 16(4) 1990) with 256-entry tables generated by
+// gen_fp64_tables.py:
+//
+//   ln x:  x = 2^k m, m in [1,2); i = top 8 fraction bits; r = m F_i - 1 is
+//          formed exactly (two-product, Sterbenz); ln x = k ln2 + G_i +
+//          log1p(r), log1p by its Taylor series to r^7 (|r| < 2^-8.9),
+//          carried as a double-double;
+//   y ln x: double-double product;
+//   exp:   z = (256 q + j) ln2/256 + r, |r| <= ln2/512;
+//          exp z = 2^q T_j (1 + expm1 r), expm1 by its Taylor series to r^5.
+//
+// Error: about 0.51 ulp for the arguments the model produces (checked against
+// 60-digit references and CUDA's pow in tests/test_fp64_math_gpu.py).  The
+// fast path needs x positive and normal and |y ln x| < 700; everything else
+// (x <= 0, zero, subnormal, inf, nan, overflow, underflow) goes to pow().
+#pragma once
+
+#include <cmath>
+
+#include "fp64_tables.h"
+
+namespace pihm {
+
+__device__ __forceinline__ double exp_dd_fast(double zh, double zl) {
+  const double shifter = 0x1.8p52;  // 1.5 * 2^52: rounds to an integer in the low bits
+  const double u = fma(zh, k256ByLn2, shifter);
+  const int kk = __double2loint(u);
+  const double nd = u - shifter;
+  double r = fma(-nd, kLn2By256Hi, zh);
+  r = fma(-nd, kLn2By256Lo, r) + zl;
+  double p = fma(r, 1.0 / 120.0, 1.0 / 24.0);
+  p = fma(p, r, 1.0 / 6.0);
+  p = fma(p, r, 0.5);
+  p = fma(p, r * r, r);  // expm1(r)
+  const int j = kk & 255;
+  const int q = kk >> 8;
+  const double th = __ldg(&kExpThi[j]);
+  const double tl = __ldg(&kExpTlo[j]);
+  const double res = th + fma(th, p, tl);
+  return __longlong_as_double(__double_as_longlong(res) + ((long long)q << 52));
+}
+
+__device__ __forceinline__ double pow_fast(double x, double y) {
+  const long long xb = __double_as_longlong(x);
+  const unsigned top = (unsigned)((unsigned long long)xb >> 52);  // sign and exponent
+  if (top - 1u >= 2046u) return pow(x, y);  // x <= 0, zero, subnormal, inf or nan
+  const int k = (int)top - 1023;
+  const double m = __longlong_as_double((xb & 0x000FFFFFFFFFFFFFLL) | 0x3FF0000000000000LL);
+  const int i = (int)((xb >> 44) & 0xFF);
+  const double F = __ldg(&kLogF[i]);
+  const double gh = __ldg(&kLogGhi[i]);
+  const double gl = __ldg(&kLogGlo[i]);
+  // r = m F - 1 = rh + pe exactly
+  const double p = m * F;
+  const double pe = fma(m, F, -p);
+  const double rh = p - 1.0;
+  // log1p(rh) - rh = rh^2 (-1/2 + rh (1/3 + rh (-1/4 + rh (1/5 + rh (-1/6 + rh/7)))))
+  double q = fma(rh, 1.0 / 7.0, -1.0 / 6.0);
+  q = fma(q, rh, 0.2);
+  q = fma(q, rh, -0.25);
+  q = fma(q, rh, 1.0 / 3.0);
+  q = fma(q, rh, -0.5);
+  const double t = (rh * rh) * q;
+  // k ln2 + G_hi is exact; add rh with an exact two-sum
+  const double kd = (double)k;
+  const double s1 = fma(kd, kLn2Hi, gh);
+  const double sh = s1 + rh;
+  const double bb = sh - s1;
+  const double se = (s1 - (sh - bb)) + (rh - bb);
+  // low part: two-sum error, the low half of r (times 1 - rh), the series
+  // tail, k ln2_lo + G_lo
+  const double lo = se + (fma(-pe, rh, pe) + (t + fma(kd, kLn2Lo, gl)));
+  // z = y (sh + lo) as a double-double
+  const double zh = y * sh;
+  const double zl = fma(y, lo, fma(y, sh, -zh));
+  if (!(fabs(zh) < 700.0)) return pow(x, y);
+  return exp_dd_fast(zh, zl);
+}
+
+}  // namespace pihm

@@ -1,7 +1,14 @@
 // FP64 right-hand-side kernels of the PIHM hydrologic model for sm_103a.
 //
 // One evaluation of f(t, y) (the reference ODE(), src/ode.c:4-399) runs as
-// five stream-ordered launches with no host synchronisation:
+// six stream-ordered launches with no host synchronisation (k_edge is listed
+// at its definition: each interior edge is evaluated once and read with a
+// sign by both elements).  GB300 issues ~2 FP64 instructions per clock per SM,
+// so the kernels are FP64-issue bound: powers go through the table-driven
+// pow_fast (fp64_math.cuh), divisions by static quantities are multiplications
+// by reciprocals computed at load, and sub-expressions the reference
+// re-evaluates (EffKh per edge side, KrFunc/Psi in Infil and Recharge) are
+// computed once.
 //
 //   k_elem_prep   per element: clamp y (src/ode.c:25-49), SurfH
 //                 (src/hydrol.c:100-134), surface head zmax + surfh and the
@@ -31,6 +38,7 @@
 // k_elem_main reads before k_river of this evaluation overwrites it.
 #include <cmath>
 
+#include "fp64_math.cuh"
 #include "pihm_internal.h"
 
 namespace pihm {
@@ -44,26 +52,6 @@ __device__ __forceinline__ double surf_h(double surfeqv) {
   if (surfeqv < 0.0) return 0.0;
   if (surfeqv <= 0.5 * kDeprStg) return sqrt(2.0 * kDeprStg * surfeqv);
   return kDeprStg + (surfeqv - 0.5 * kDeprStg);
-}
-
-// EffKh, src/lat_flow.c:248-277
-__device__ __forceinline__ double eff_kh(double depth, double dmac, double kmach,
-                                         double areafv, double ksath, double gw) {
-  gw = (gw > 0.0) ? gw : 0.0;
-  if (gw > depth - dmac) {
-    const double k1 = kmach * areafv + ksath * (1.0 - areafv);
-    const double k2 = ksath;
-    double d1, d2;
-    if (gw > depth) {
-      d1 = dmac;
-      d2 = depth - dmac;
-    } else {
-      d1 = gw - (depth - dmac);
-      d2 = depth - dmac;
-    }
-    return (k1 * d1 + k2 * d2) / (d1 + d2);
-  }
-  return ksath;
 }
 
 // EffKh with k1 = kmach*areafv + ksath*(1-areafv) and depth-dmac precomputed
@@ -93,32 +81,7 @@ __device__ __forceinline__ double avg_h_surf(double diff, double hsurf, double h
 // OverLandFlow, src/lat_flow.c:279-283
 __device__ __forceinline__ double overland_flow(double avg_h, double grad_h, double avg_sf,
                                                 double crossa, double avg_rough) {
-  return crossa * pow(avg_h, 0.6666667) * grad_h / (sqrt(avg_sf) * avg_rough);
-}
-
-// KrFunc, src/soil.c:8-13, with the repeated power evaluated once
-__device__ __forceinline__ double kr_func(double beta, double satn) {
-  const double t = 1.0 - pow(1.0 - pow(satn, beta / (beta - 1.0)), (beta - 1.0) / beta);
-  return sqrt(satn) * t * t;
-}
-
-// Psi, src/vert_flow.c:272-278
-__device__ __forceinline__ double psi_vg(double satn, double alpha, double beta) {
-  satn = (satn < kSatMin) ? kSatMin : satn;
-  return -pow(pow(1.0 / satn, beta / (beta - 1.0)) - 1.0, 1.0 / beta) / alpha;
-}
-
-// EffKinf, src/vert_flow.c:211-270
-__device__ __forceinline__ double eff_kinf(double kinfv, double kmacv, double areafh,
-                                           double dh_by_dz, double ksatfunc, double elemsatn,
-                                           double applrate, double surfh) {
-  if (areafh == 0.0) return kinfv * ksatfunc;
-  if (surfh > kDeprStg) return kinfv * (1.0 - areafh) * ksatfunc + kmacv * areafh;
-  if (applrate <= dh_by_dz * kinfv * ksatfunc) return kinfv * ksatfunc;
-  const double kmax = dh_by_dz * (kmacv * areafh + kinfv * (1.0 - areafh) * ksatfunc);
-  if (applrate < kmax)
-    return kinfv * (1.0 - areafh) * ksatfunc + kmacv * areafh * kr_func(2.0, elemsatn);
-  return kinfv * (1.0 - areafh) * ksatfunc + kmacv * areafh;
+  return crossa * pow_fast(avg_h, 0.6666667) * grad_h / (sqrt(avg_sf) * avg_rough);
 }
 
 // ---------------------------------------------------------------------------
@@ -130,7 +93,7 @@ __device__ __forceinline__ double riv_cs_area(int order, double depth, double co
     case kRectangle: return depth * coeff;
     case kTriangle: return depth * depth / coeff;
     case kQuadratic: return 4.0 * depth * sqrt(depth) / (3.0 * sqrt(coeff));
-    case kCubic: return 3.0 * pow(depth, 4.0 / 3.0) / (2.0 * pow(coeff, 1.0 / 3.0));
+    case kCubic: return 3.0 * pow_fast(depth, 4.0 / 3.0) / (2.0 * pow_fast(coeff, 1.0 / 3.0));
   }
   return 0.0;
 }
@@ -144,10 +107,10 @@ __device__ __forceinline__ double riv_perim(int order, double depth, double coef
       return sqrt(depth * (1.0 + 4.0 * coeff * depth) / coeff) +
              log(2.0 * sqrt(coeff * depth) + sqrt(1.0 + 4.0 * coeff * depth)) / (2.0 * coeff);
     case kCubic: {
-      const double c23 = pow(coeff, 2.0 / 3.0);
-      const double c13 = pow(coeff, 1.0 / 3.0);
-      return 2.0 * ((pow(depth * (1.0 + 9.0 * c23 * depth), 0.5) / 3.0) +
-                    (log(3.0 * c13 * sqrt(depth) + pow(1.0 + 9.0 * c23 * depth, 0.5)) /
+      const double c23 = pow_fast(coeff, 2.0 / 3.0);
+      const double c13 = pow_fast(coeff, 1.0 / 3.0);
+      return 2.0 * ((pow_fast(depth * (1.0 + 9.0 * c23 * depth), 0.5) / 3.0) +
+                    (log(3.0 * c13 * sqrt(depth) + pow_fast(1.0 + 9.0 * c23 * depth, 0.5)) /
                      (9.0 * c13)));
     }
   }
@@ -238,7 +201,7 @@ __global__ void __launch_bounds__(256) k_edge(DevMesh m, const double *RESTRICT 
   double ovl = 0.0;
   if (avg_h > 0.0) {  // avg_h == 0 gives crossa == 0: the flux is zero
     const double crossa = avg_h * len;
-    ovl = crossa * pow(avg_h, 0.6666667) * grad_h * rsqrt(avg_sf) * m.e_invrough[e];
+    ovl = crossa * pow_fast(avg_h, 0.6666667) * grad_h * rsqrt(avg_sf) * m.e_invrough[e];
   }
   m.eflux_ovl[e] = ovl;
 }
@@ -325,10 +288,10 @@ __global__ void __launch_bounds__(256) k_elem_main(DevMesh m, const double *REST
     satn = (satn < kSatMin) ? kSatMin : satn;
     const double vm = m.vg_m[i];
     // KrFunc, src/soil.c:8-13
-    const double t = 1.0 - pow(1.0 - pow(satn, vm), m.vg_e[i]);
+    const double t = 1.0 - pow_fast(1.0 - pow_fast(satn, vm), m.vg_e[i]);
     satkfunc = sqrt(satn) * t * t;
     // Psi, src/vert_flow.c:272-278
-    psi_u = -pow(pow(1.0 / satn, vm) - 1.0, m.vg_ib[i]) * m.inv_alpha[i];
+    psi_u = -pow_fast(pow_fast(1.0 / satn, vm) - 1.0, m.vg_ib[i]) * m.inv_alpha[i];
   }
   // KrFunc(beta, 1) == 1 exactly: pow(1 - pow(1, m), e) == pow(0, e) == 0
   double infil;
@@ -616,7 +579,7 @@ __global__ void __launch_bounds__(128) k_river(DevMesh m, const double *RESTRICT
       const double grad_h = (r.zbed - (m.r_node_zmax[s] - depth)) / distance;
       const double avg_perim = riv_perim(r.order, r.stage, r.coeff);
       const double crossa = riv_cs_area(r.order, r.stage, r.coeff);
-      q = sqrt(grad_h) * crossa * ((avg_perim > 0.0) ? pow(crossa / avg_perim, 2.0 / 3.0) : 0.0) / r.rough;
+      q = sqrt(grad_h) * crossa * ((avg_perim > 0.0) ? pow_fast(crossa / avg_perim, 2.0 / 3.0) : 0.0) / r.rough;
     } else {  // kCritDpth (other values are rejected at load)
       const double crossa = riv_cs_area(r.order, r.stage, r.coeff);
       q = crossa * sqrt(kGrav * r.stage);

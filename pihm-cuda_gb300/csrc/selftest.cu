@@ -1,0 +1,21 @@
+// Diagnostic entry point: the table-driven pow of the right-hand-side kernels
+// next to CUDA's pow, element by element, so tests can measure its error.
+#include <cstdint>
+
+#include "fp64_math.cuh"
+
+namespace {
+__global__ void k_pow_pair(const double *x, const double *y, double *fast, double *ref, long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  fast[i] = pihm::pow_fast(x[i], y[i]);
+  if (ref) ref[i] = pow(x[i], y[i]);
+}
+}  // namespace
+
+extern "C" int pihm_gpu_selftest_pow(const double *x, const double *y, double *fast, double *cuda_pow,
+                                     int64_t n, void *stream) {
+  if (n <= 0 || !x || !y || !fast) return -1;
+  k_pow_pair<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(x, y, fast, cuda_pow, n);
+  return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
