@@ -1074,3 +1074,25 @@ void oracle_post_step(oracle_model *m, const double *y)
     int i;
     for (i = 0; i < m->nelem; i++) m->elem[i].ws0_surf = y[i];
 }
+
+/* CVRhsFn over SUNDIALS serial N_Vectors (content: length, own_data, data;
+ * cvode/include/nvector/nvector_serial.h:69-73), user_data = oracle_model:
+ * lets an integrator call the restatement the way CVODE calls ODE(). */
+struct serial_content_prefix {
+    long int length;
+    int own_data;
+    double *data;
+};
+struct nvector_prefix {
+    void *content;
+    void *ops;
+};
+
+int oracle_cvrhs(double t, void *y, void *ydot, void *user_data)
+{
+    const double *yd =
+        ((struct serial_content_prefix *)((struct nvector_prefix *)y)->content)->data;
+    double *dd =
+        ((struct serial_content_prefix *)((struct nvector_prefix *)ydot)->content)->data;
+    return oracle_rhs((oracle_model *)user_data, t, yd, dd) == 0 ? 0 : -1;
+}

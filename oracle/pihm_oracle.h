@@ -39,6 +39,8 @@ void oracle_get_fluxes(const oracle_model *m, double *ovlflow, double *subsurf,
                        double *rivflow);
 /* Post-step update (Summary, src/update.c:3-99): ws0 <- y. */
 void oracle_post_step(oracle_model *m, const double *y);
+/* CVRhsFn over SUNDIALS serial N_Vectors, user_data = oracle_model. */
+int oracle_cvrhs(double t, void *y, void *ydot, void *user_data);
 /* Number of OpenMP threads the oracle runs with (1 without OpenMP). */
 int oracle_num_threads(void);
 void oracle_set_num_threads(int n);

@@ -354,3 +354,69 @@ int ref_model_times(int *starttime, int *endtime, int *etstep, int *nstep)
     *nstep = g_pihm->ctrl.nstep;
     return 0;
 }
+
+/* The reference's per-step loop (src/main.c:217-254, src/pihm.c:7-187) on a
+ * model built by ref_build: every model step sets the element forcing
+ * (uniform pcpdrp/edir/ett of that step, standing in for ApplyForc and
+ * IntcpSnowEt), calls SolveCVode (src/ode.c:555), Summary (src/update.c:3)
+ * and AdjCVodeMaxStep (src/ode.c:601).  Records the state every `every`
+ * steps, the outlet segment's DOWN_CHANL2CHANL flux after every step (the
+ * value PIHM prints as rivflx1) and CVODE's counters. */
+int ref_run_pihm(double *y, int nsteps, int stepsize, double reltol, double abstol,
+                 double initstep, double nncfn, double nnimax, double nnimin, double decr,
+                 double incr, double stmin, const double *pcp, const double *edir,
+                 const double *ett, int outlet, int every, double *y_out, double *q_out,
+                 long *stats)
+{
+    int n = NumStateVar();
+    int i, s;
+    N_Vector cv_y = N_VMake_Serial(n, y);
+    void *cvode_mem = CVodeCreate(CV_BDF, CV_NEWTON);
+    pihm_struct p = g_pihm;
+    p->ctrl.stepsize = stepsize;
+    p->ctrl.reltol = reltol;
+    p->ctrl.abstol = abstol;
+    p->ctrl.initstep = initstep;
+    p->ctrl.nncfn = nncfn;
+    p->ctrl.nnimax = nnimax;
+    p->ctrl.nnimin = nnimin;
+    p->ctrl.decr = decr;
+    p->ctrl.incr = incr;
+    p->ctrl.stmin = stmin;
+    /* InitVar: ws0 <- initial state (src/initialize.c:576-640) */
+    for (i = 0; i < nelem; i++) {
+        p->elem[i].ws0.surf = y[i];
+        p->elem[i].ws0.unsat = y[i + nelem];
+        p->elem[i].ws0.gw = y[i + 2 * nelem];
+    }
+    SetCVodeParam(p, cvode_mem, cv_y);
+    for (s = 0; s < nsteps; s++) {
+        int t = 0;
+        double pc[1];
+        for (i = 0; i < nelem; i++) {
+            p->elem[i].wf.pcpdrp = pcp[s];
+            p->elem[i].wf.edir = edir[s];
+            p->elem[i].wf.ett = ett[s];
+        }
+        (void)pc;
+        SolveCVode(0, &t, (s + 1) * stepsize, 0.0, cvode_mem, cv_y);
+        Summary(p->elem, p->river, cv_y, (double)stepsize);
+        AdjCVodeMaxStep(cvode_mem, &p->ctrl);
+        if (q_out) q_out[s] = p->river[outlet].wf.rivflow[DOWN_CHANL2CHANL];
+        if (y_out && every > 0 && (s + 1) % every == 0)
+            memcpy(y_out + (size_t)((s + 1) / every - 1) * n, y, sizeof(double) * n);
+    }
+    if (stats) {
+        long v;
+        CVodeGetNumSteps(cvode_mem, &v); stats[0] = v;
+        CVodeGetNumRhsEvals(cvode_mem, &v); stats[1] = v;
+        CVodeGetNumNonlinSolvIters(cvode_mem, &v); stats[2] = v;
+        CVodeGetNumNonlinSolvConvFails(cvode_mem, &v); stats[3] = v;
+        CVodeGetNumErrTestFails(cvode_mem, &v); stats[4] = v;
+        CVSpilsGetNumLinIters(cvode_mem, &v); stats[5] = v;
+        CVSpilsGetNumRhsEvals(cvode_mem, &v); stats[6] = v;
+    }
+    CVodeFree(&cvode_mem);
+    N_VDestroy(cv_y);
+    return 0;
+}

@@ -344,6 +344,23 @@ def generate(nelem: int = 1000, nriver: int = 100, seed: int = 0,
     assert np.all(leftele > 0) and np.all(rightele > 0)
     down = np.where(seg_of_from[to_n] >= 0, seg_of_from[to_n] + 1, 0)
 
+    # Stream burning: every river node lies at least 0.1 % of the segment
+    # length below its upstream node.  The reference's channel routing moves
+    # water upstream through a segment whose bed is above its upstream
+    # neighbour's water surface even when that segment is empty
+    # (ChanFlowRiverToRiver uses the upstream cross-section,
+    # src/river_flow.c:257-300), so channels must fall downstream, as mesh
+    # tools ensure by correcting river elevations (cf. CorrElev,
+    # src/initialize.c:225-383).  Segments are visited upstream first.
+    for s in range(nr):
+        f, tn = int(from_n[s]), int(to_n[s])
+        seglen = math.hypot(px[f] - px[tn], py[f] - py[tn])
+        zcap = zmax_n[f] - 1e-3 * seglen
+        if zmax_n[tn] > zcap:
+            dz = zmax_n[tn] - zcap
+            zmax_n[tn] -= dz
+            zmin_n[tn] -= dz
+
     # ---- element geometry: InitTopo, src/init_topo.c:6-52 ----
     x = px[tri]
     y = py[tri]

@@ -1,0 +1,69 @@
+"""End-to-end solves: the BDF integrator (include/pihm_bdf.h, a restatement of
+CVODE 2.9) driving the right-hand side through the reference's model-step
+loop, against the reference's own CVODE + ODE() run
+(tests/golden/make_golden_solve.py: 1,000 elements, 2 days, 60 s steps).
+
+On the CPU, with the right-hand-side restatement over host vectors, the
+integrator reproduces the reference run step for step (same counters, same
+states).  On the GPU the hydrograph and storages must agree within 1e-6
+relative (the bar for the end-to-end run)."""
+import os
+
+import numpy as np
+import pytest
+
+import pihm_gpu.watershed as W
+from backends import GpuBackend, OracleBackend
+from pihm_gpu.solver import StepControl, run_steps
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _golden():
+    z = np.load(os.path.join(GOLD, "c0_solve.npz"))
+    ws = W.Watershed.load(os.path.join(GOLD, "c0_watershed.npz"))
+    ctrl = StepControl(**{str(k): (int(v) if str(k) == "stepsize" else float(v))
+                          for k, v in zip(z["ctrl_names"], z["ctrl"])})
+    return ws, z, ctrl
+
+
+def _run(backend_cls, ws, z, ctrl, **kw):
+    nsteps = z["outlet_q"].shape[0]
+    b = backend_cls(ws, z["y0"], z["pcp"], z["edir"], z["ett"], **kw)
+    try:
+        return run_steps(b, ctrl, nsteps, b.set_forcing, record_every=int(z["every"]),
+                         outlet=int(z["outlet"]))
+    finally:
+        b.close()
+
+
+def test_integrator_reproduces_reference_cvode_on_cpu():
+    ws, z, ctrl = _golden()
+    res = _run(OracleBackend, ws, z, ctrl)
+    s = res["stats"]
+    got = [s.nst, s.nfe, s.nni, s.ncfn, s.netf, s.nli, s.nfes]
+    assert got == list(z["stats"]), (got, list(z["stats"]))
+    assert np.array_equal(res["states"], z["states"])
+    assert np.array_equal(res["outlet"], z["outlet_q"])
+
+
+def _rel(a, b, floor=1e-5):
+    """Relative error with the solver's absolute tolerance as the floor
+    (storages that are zero in the reference compare absolutely)."""
+    den = np.maximum(np.abs(b), floor)
+    return float(np.max(np.abs(a - b) / den))
+
+
+@pytest.mark.gpu
+def test_gpu_solve_hydrograph_and_storages():
+    ws, z, ctrl = _golden()
+    res = _run(GpuBackend, ws, z, ctrl)
+    q_ref = z["outlet_q"]
+    # hydrograph: relative to the peak flow, per step
+    qerr = np.max(np.abs(res["outlet"] - q_ref)) / np.max(np.abs(q_ref))
+    serr = _rel(res["states"][-1], z["states"][-1])
+    s = res["stats"]
+    print(f"GPU solve: nst {s.nst} nfe {s.nfe} (reference {z['stats'][0]} {z['stats'][1]}); "
+          f"hydrograph err {qerr:.2e}, final storage err {serr:.2e}")
+    assert qerr <= 1e-6
+    assert serr <= 1e-6
