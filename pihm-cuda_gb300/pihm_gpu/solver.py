@@ -67,6 +67,7 @@ class StepControl:
     decr: float = 1.2      # DECR_FACTOR
     incr: float = 1.2      # INCR_FACTOR
     stmin: float = 1.0     # MIN_MAXSTEP
+    mxstep: int = 0        # internal steps per model step; 0 = 10 * stepsize (src/ode.c:497)
 
 
 class Bdf:
@@ -113,7 +114,7 @@ def run_steps(backend, ctrl: StepControl, nsteps: int, forcing, record_every: in
     bdf.check("stald", lib.pihm_bdf_set_stab_lim_det(bdf.h, 1))
     maxstep = float(ctrl.stepsize)
     bdf.check("hmax", lib.pihm_bdf_set_max_step(bdf.h, maxstep))
-    bdf.check("mxstep", lib.pihm_bdf_set_max_num_steps(bdf.h, ctrl.stepsize * 10))
+    bdf.check("mxstep", lib.pihm_bdf_set_max_num_steps(bdf.h, ctrl.mxstep or ctrl.stepsize * 10))
     states, qout = [], []
     nst0 = ncfn0 = nni0 = 0
     tret = _D()
