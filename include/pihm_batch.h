@@ -1,0 +1,104 @@
+/*
+ * pihm_batch.h -- many PIHM watersheds (or calibration parameter sets) of
+ * uneven size integrated together on one GPU.
+ *
+ * Each watershed runs the reference's model-step loop (src/pihm.c:7-187:
+ * forcing, CVODE to the end of the step with the stop time set, the post-step
+ * update, AdjCVodeMaxStep, src/ode.c:555-661) with its own integrator state,
+ * step sizes, model step and tolerances.  The engine packs the watersheds'
+ * meshes and CVODE vectors into one device arena and advances them in rounds:
+ * every watershed runs until it needs a device result (a norm, a dot product
+ * or a right-hand-side evaluation); one launch then applies all their queued
+ * vector operations and reductions, and one right-hand-side evaluation covers
+ * every watershed that asked for one.
+ *
+ * A watershed's results do not depend on what else is in the batch: each is
+ * bit-for-bit the trajectory the single-watershed path (pihm_bdf_* over
+ * N_VNew_PihmGpu with pihm_gpu_ode) computes for it.
+ *
+ * Admission is by arena capacity (elements, segments, interior edges, state
+ * entries and watershed slots fixed at creation): pihm_batch_add returns
+ * PIHM_GPU_ERR_NOMEM when a watershed does not fit now, and succeeds again
+ * after finished watersheds have been released.  Watersheds can be added while
+ * others are running.
+ */
+#ifndef PIHM_BATCH_H
+#define PIHM_BATCH_H
+
+#include <stdint.h>
+
+#include "pihm_bdf.h"
+#include "pihm_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct pihm_batch pihm_batch;
+
+/* Arena capacity. */
+typedef struct pihm_batch_limits {
+    int64_t max_elem;      /* elements over all resident watersheds */
+    int64_t max_river;     /* river segments */
+    int64_t max_edge;      /* interior edges (about 1.5 x elements) */
+    int64_t max_record;    /* hydrograph entries (model steps) over all resident watersheds */
+    int32_t max_systems;   /* resident watersheds */
+} pihm_batch_limits;
+
+/* The reference's solver controls (ctrl_struct, src/read_para.c:23-108). */
+typedef struct pihm_step_control {
+    double stepsize;   /* model step (s); also caps infiltration (src/vert_flow.c:122) */
+    double reltol, abstol, initstep;
+    double nncfn, nnimax, nnimin, decr, incr, stmin;  /* AdjCVodeMaxStep, src/ode.c:601-661 */
+    long mxstep;       /* internal steps per model step; 0 = 10 x stepsize (src/ode.c:497) */
+} pihm_step_control;
+
+/* One simulation request. */
+typedef struct pihm_batch_job {
+    const pihm_gpu_mesh *mesh;
+    const double *elem_bc;    /* [3*nelem] reference order, or NULL (zeros) */
+    const double *river_bc;   /* [nriver], or NULL */
+    const double *y0;         /* [3*nelem + 2*nriver] initial state, reference order */
+    pihm_step_control ctrl;
+    int32_t nsteps;           /* model steps */
+    /* spatially uniform forcing per model step [nsteps]: pcpdrp, edir, ett (m/s) */
+    const double *pcpdrp, *edir, *ett;
+    int32_t outlet;           /* segment whose DOWN_CHANL2CHANL flux is recorded per step, -1: none */
+} pihm_batch_job;
+
+enum { PIHM_BATCH_RUNNING = 0, PIHM_BATCH_DONE = 1, PIHM_BATCH_FAILED = 2 };
+
+int pihm_batch_create(const pihm_batch_limits *lim, int surf_mode, int riv_mode, int order,
+                      pihm_batch **out);
+void pihm_batch_destroy(pihm_batch *b);
+int pihm_batch_set_stream(pihm_batch *b, void *stream);
+
+/* Admit a watershed; *id receives its handle.  PIHM_GPU_ERR_NOMEM: no room now. */
+int pihm_batch_add(pihm_batch *b, const pihm_batch_job *job, int32_t *id);
+
+/* Advance every resident watershed by up to max_rounds rounds (<= 0: until
+ * all have finished).  *running receives the number still running. */
+int pihm_batch_step(pihm_batch *b, int32_t max_rounds, int32_t *running);
+
+/* PIHM_BATCH_RUNNING / _DONE / _FAILED, and the integrator's return code. */
+int pihm_batch_poll(const pihm_batch *b, int32_t id, int32_t *status, int32_t *solver_rc);
+
+/* Results of a finished (or failed) watershed; any output may be NULL.
+ * y: [neq] reference order; outlet: [nsteps] */
+int pihm_batch_result(pihm_batch *b, int32_t id, double *y, double *outlet, pihm_bdf_stats *stats,
+                      int32_t *steps_done);
+
+/* Free a watershed's arena ranges (after its results have been read). */
+int pihm_batch_release(pihm_batch *b, int32_t id);
+
+/* Rounds executed, kernels launched and arena occupancy so far. */
+typedef struct pihm_batch_info {
+    int64_t rounds, rhs_rounds, launches;
+    int64_t elem_used, elem_hwm, resident;
+} pihm_batch_info;
+int pihm_batch_get_info(const pihm_batch *b, pihm_batch_info *info);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PIHM_BATCH_H */

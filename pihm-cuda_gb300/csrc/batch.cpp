@@ -1,0 +1,834 @@
+// The batch engine (include/pihm_batch.h).
+//
+// Every watershed runs the reference's model-step loop as a coroutine over the
+// integrator of bdf_core.h.  Its vector operations are not executed when they
+// are issued: element-wise ones are queued into the watershed's program for
+// the current round, and a reduction or a right-hand-side evaluation ends the
+// program and suspends the coroutine.  A round uploads all programs, runs them
+// in one launch of the program kernel (batch_kernels.cu), evaluates the right
+// hand side once over the arena for the watersheds that asked for it, reads
+// back every reduction result and error word in one copy, and resumes the
+// coroutines.  Watersheds therefore proceed independently -- each with its own
+// step size, order, Newton and Krylov iterations, model step and stopping
+// time -- while sharing every launch.
+#include <algorithm>
+#include <cmath>
+#include <coroutine>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <vector>
+
+#include "batch_device.h"
+#include "bdf_core.h"
+#include "mesh_image.h"
+#include "nv_select.h"
+#include "pihm_batch.h"
+
+using namespace pihm;
+using namespace pihm::batch;
+using pihm_nv::EwCall;
+
+namespace {
+
+// First-fit allocator of index ranges in [0, cap).
+class RangeAlloc {
+ public:
+  explicit RangeAlloc(int64_t cap = 0) : cap_(cap) {
+    if (cap > 0) free_[0] = cap;
+  }
+  // start of a free range of n entries, or -1
+  int64_t alloc(int64_t n) {
+    if (n <= 0) return 0;
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      if (it->second < n) continue;
+      const int64_t start = it->first, len = it->second;
+      free_.erase(it);
+      if (len > n) free_[start + n] = len - n;
+      used_ += n;
+      return start;
+    }
+    return -1;
+  }
+  void release(int64_t start, int64_t n) {
+    if (n <= 0) return;
+    used_ -= n;
+    auto next = free_.lower_bound(start);
+    if (next != free_.end() && start + n == next->first) {
+      n += next->second;
+      next = free_.erase(next);
+    }
+    if (next != free_.begin()) {
+      auto prev = std::prev(next);
+      if (prev->first + prev->second == start) {
+        prev->second += n;
+        return;
+      }
+    }
+    free_[start] = n;
+  }
+  // one past the last allocated entry
+  int64_t hwm() const {
+    if (free_.empty()) return cap_;
+    auto last = std::prev(free_.end());
+    return (last->first + last->second == cap_) ? last->first : cap_;
+  }
+  int64_t used() const { return used_; }
+
+ private:
+  int64_t cap_;
+  int64_t used_ = 0;
+  std::map<int64_t, int64_t> free_;
+};
+
+struct Sys;
+
+// The integrator's operations for one watershed of the batch: vectors are
+// slot numbers; element-wise operations are queued; reductions and the right
+// hand side suspend the calling coroutine until the round has run.
+struct BatchOps {
+  using Vec = int;
+  Sys *s = nullptr;
+  int next_slot = 1;  // slot 0 holds the model state y
+
+  int clone(int) { return next_slot < kVecSlots ? next_slot++ : -1; }
+  void destroy(int) {}
+  bool valid(int v) const { return v >= 0; }
+
+  struct Ew {
+    Sys *s;
+    bool await_ready() const noexcept;
+    void await_suspend(std::coroutine_handle<> h) const noexcept;
+    void await_resume() const noexcept {}
+  };
+  struct Red {
+    Sys *s;
+    bool await_ready() const noexcept { return false; }
+    void await_suspend(std::coroutine_handle<> h) const noexcept;
+    double await_resume() const noexcept;
+  };
+  struct Rhs {
+    Sys *s;
+    bool await_ready() const noexcept { return false; }
+    void await_suspend(std::coroutine_handle<> h) const noexcept;
+    int await_resume() const noexcept;
+  };
+
+  Ew push(int code, double a, double b, int x, int y, int z, double c = 0.0, int i0 = 0, int i1 = 0);
+  Ew push(const EwCall<int> &e) { return push(e.op, e.a, e.b, e.x, e.y, e.z); }
+  Red reduce(int red, int x, int y, bool wrms);
+
+  Ew linear_sum(double a, int x, double b, int y, int z) {
+    return push(pihm_nv::select_linear_sum<int>(a, x, b, y, z));
+  }
+  Ew const_(double c, int z) { return push(pihm_nv::EW_CONST, c, 0.0, z, z, z); }
+  Ew scale(double c, int x, int z) { return push(pihm_nv::select_scale<int>(c, x, z)); }
+  Ew abs_(int x, int z) { return push(pihm_nv::EW_ABS, 0.0, 0.0, x, x, z); }
+  Ew inv(int x, int z) { return push(pihm_nv::EW_INV, 0.0, 0.0, x, x, z); }
+  Ew div(int x, int y, int z) { return push(pihm_nv::EW_DIV, 0.0, 0.0, x, y, z); }
+  Ew prod(int x, int y, int z) { return push(pihm_nv::EW_PROD, 0.0, 0.0, x, y, z); }
+  Ew addconst(int x, double b, int z) { return push(pihm_nv::EW_ADDCONST, 0.0, b, x, x, z); }
+  Red dot(int x, int y) { return reduce(pihm_nv::R_DOT, x, y, false); }
+  Red maxnorm(int x) { return reduce(pihm_nv::R_MAXABS, x, x, false); }
+  Red wrms(int x, int w) { return reduce(pihm_nv::R_WSQ, x, w, true); }
+  Red vmin(int x) { return reduce(pihm_nv::R_MIN, x, x, false); }
+  Rhs rhs(double t, int y, int ydot);
+  // model-step operations
+  Ew forcing(double pcp, double edir, double ett) { return push(OP_FORCING, pcp, edir, 0, 0, 0, ett); }
+  Ew post_step(int y) { return push(OP_WS0, 0.0, 0.0, y, y, y); }
+  Ew record(int k, int seg) { return push(OP_RECORD, 0.0, 0.0, 0, 0, 0, 0.0, k, seg); }
+};
+
+enum SysState { S_NEW = 0, S_RUNNING, S_DONE, S_FAILED };
+
+struct Sys {
+  int32_t id = -1, slot = -1;
+  // arena ranges
+  int64_t eoff = 0, roff = 0, edoff = 0, boff = 0, upoff = 0, soff = 0, recoff = 0;
+  int32_t ne = 0, nr = 0, nedge = 0, nbank = 0, nup = 0, nrec = 0;
+  int64_t neq = 0;
+  std::vector<int32_t> perm;
+  // job
+  pihm_step_control ctrl{};
+  int32_t nsteps = 0, outlet = -1, steps_done = 0;
+  std::vector<double> pcp, edir, ett;
+  // integrator and its coroutine
+  bdf::BdfCore<BatchOps> core;
+  std::unique_ptr<Task<int>> task;
+  std::coroutine_handle<> waiting{};
+  int state = S_NEW, solver_rc = 0;
+  // the program of the current round
+  std::vector<Op> prog;
+  int red = -1;
+  uint8_t rx = 0, ry = 0;
+  bool red_wrms = false, rhs_req = false, rhs_pending_out = false;
+  uint8_t rhs_out = 0;
+  double red_value = 0.0;
+  int rhs_rc = 0;
+};
+
+bool BatchOps::Ew::await_ready() const noexcept { return (int)s->prog.size() < kMaxProgOps; }
+void BatchOps::Ew::await_suspend(std::coroutine_handle<> h) const noexcept { s->waiting = h; }
+void BatchOps::Red::await_suspend(std::coroutine_handle<> h) const noexcept { s->waiting = h; }
+double BatchOps::Red::await_resume() const noexcept { return s->red_value; }
+void BatchOps::Rhs::await_suspend(std::coroutine_handle<> h) const noexcept { s->waiting = h; }
+int BatchOps::Rhs::await_resume() const noexcept { return s->rhs_rc; }
+
+BatchOps::Ew BatchOps::push(int code, double a, double b, int x, int y, int z, double c, int i0, int i1) {
+  Op o;
+  std::memset(&o, 0, sizeof(o));
+  o.code = (uint8_t)code;
+  o.x = (uint8_t)x;
+  o.y = (uint8_t)y;
+  o.z = (uint8_t)z;
+  o.i0 = i0;
+  o.i1 = i1;
+  o.a = a;
+  o.b = b;
+  o.c = c;
+  s->prog.push_back(o);
+  return Ew{s};
+}
+
+BatchOps::Red BatchOps::reduce(int red, int x, int y, bool wrms) {
+  s->red = red;
+  s->rx = (uint8_t)x;
+  s->ry = (uint8_t)y;
+  s->red_wrms = wrms;
+  return Red{s};
+}
+
+BatchOps::Rhs BatchOps::rhs(double, int y, int ydot) {
+  push(OP_STAGE_IN, 0.0, 0.0, y, y, y);
+  s->rhs_req = true;
+  s->rhs_out = (uint8_t)ydot;
+  return Rhs{s};
+}
+
+// The reference's model-step loop for one watershed (src/pihm.c:7-187 with
+// SolveCVode and AdjCVodeMaxStep, src/ode.c:555-661), as the single-watershed
+// driver runs it: forcing, stop time, solve, post-step update, maximum-step
+// adaptation, outlet record.
+Task<int> model_run(Sys *s) {
+  bdf::BdfCore<BatchOps> &c = s->core;
+  BatchOps &o = c.ops;
+  const pihm_step_control &ct = s->ctrl;
+  const int Y = 0;
+  co_await o.post_step(Y);  // ws0 <- y0
+  int rc = co_await c.init(0.0, Y);
+  if (rc != bdf::SUCCESS) co_return rc;
+  c.reltol = ct.reltol;
+  c.abstol = ct.abstol;
+  c.tol_set = true;
+  c.hin = ct.initstep;
+  c.sldeton = true;
+  double maxstep = ct.stepsize;
+  if ((rc = c.set_max_step(maxstep)) != bdf::SUCCESS) co_return rc;
+  c.mxstep = ct.mxstep ? ct.mxstep : (long)(ct.stepsize * 10.0);
+  long nst0 = 0, ncfn0 = 0, nni0 = 0;
+  double tret = 0.0;
+  for (int k = 0; k < s->nsteps; k++) {
+    co_await o.forcing(s->pcp[k], s->edir[k], s->ett[k]);
+    const double tout = (double)(k + 1) * ct.stepsize;
+    if ((rc = c.set_stop_time(tout)) != bdf::SUCCESS) co_return rc;
+    rc = co_await c.solve(tout, Y, &tret);
+    if (rc < 0) co_return rc;
+    co_await o.post_step(Y);
+    // AdjCVodeMaxStep, src/ode.c:601-661
+    const double nsteps_d = (double)(c.nst - nst0);
+    const double nfails = (double)(c.ncfn - ncfn0) / nsteps_d;
+    const double niters = (double)(c.nni - nni0) / nsteps_d;
+    if (nfails > ct.nncfn || niters >= ct.nnimax) maxstep /= ct.decr;
+    if (nfails == 0.0 && niters <= ct.nnimin) maxstep *= ct.incr;
+    maxstep = maxstep < ct.stepsize ? maxstep : ct.stepsize;
+    maxstep = maxstep > ct.stmin ? maxstep : ct.stmin;
+    if ((rc = c.set_max_step(maxstep)) != bdf::SUCCESS) co_return rc;
+    nst0 = c.nst;
+    ncfn0 = c.ncfn;
+    nni0 = c.nni;
+    if (s->outlet >= 0) co_await o.record(k, s->outlet);
+    s->steps_done = k + 1;
+  }
+  co_return bdf::SUCCESS;
+}
+
+template <class T>
+T *dalloc(size_t n, std::vector<void *> &owned) {
+  void *p = nullptr;
+  if (n == 0) n = 1;
+  if (cudaMalloc(&p, sizeof(T) * n) != cudaSuccess) return nullptr;
+  owned.push_back(p);
+  return (T *)p;
+}
+
+}  // namespace
+
+struct pihm_batch {
+  DeviceArena A{};
+  cudaStream_t st = nullptr;
+  std::vector<void *> owned;
+  int64_t ne_cap = 0, nr_cap = 0, ned_cap = 0, rec_cap = 0;
+  int max_sys = 0;
+  int order = PIHM_GPU_ORDER_RCM;
+  RangeAlloc ra_elem, ra_riv, ra_edge, ra_bank, ra_up, ra_state, ra_rec;
+  std::vector<std::unique_ptr<Sys>> slots;  // [max_sys]
+  std::map<int32_t, Sys *> by_id;
+  int32_t next_id = 0;
+  // per-round upload: active flags, then the round list, then the ops
+  char *h_up = nullptr;
+  char *d_up = nullptr;
+  size_t up_active_bytes = 0, up_round_off = 0, up_ops_off = 0;
+  // per-round download: results [max_sys][2], then error words [max_sys]
+  char *h_down = nullptr;
+  char *d_down = nullptr;
+  size_t down_bytes = 0;
+  unsigned int *err_sys = nullptr;
+  // counters
+  long long rounds = 0, rhs_rounds = 0, launches = 0;
+
+  ~pihm_batch() {
+    slots.clear();
+    for (void *p : owned) cudaFree(p);
+    if (h_up) cudaFreeHost(h_up);
+    if (h_down) cudaFreeHost(h_down);
+  }
+
+  void update_extents() {
+    A.m.ne_run = (int32_t)ra_elem.hwm();
+    A.m.nr_run = (int32_t)ra_riv.hwm();
+    A.m.nedge_run = (int32_t)ra_edge.hwm();
+    A.m.nbank_run = (int32_t)ra_bank.hwm();
+  }
+};
+
+namespace {
+
+template <class T>
+int h2d(T *dst, const T *src, size_t n, cudaStream_t st) {
+  if (n == 0) return 0;
+  return cudaMemcpyAsync(dst, src, sizeof(T) * n, cudaMemcpyHostToDevice, st) == cudaSuccess ? 0 : -1;
+}
+
+// Translate a watershed image's indices to its arena ranges and upload it.
+int place(pihm_batch *B, Sys *s, const SystemImage &im, const pihm_batch_job *job) {
+  DevMesh &m = B->A.m;
+  cudaStream_t st = B->st;
+  const int ne = im.ne, nr = im.nr;
+  const int64_t NE = B->ne_cap, NR = B->nr_cap;
+  const int64_t eo = s->eoff, ro = s->roff, edo = s->edoff, bo = s->boff, uo = s->upoff;
+  int rc = 0;
+  for (int k = 0; k < EP_COUNT; k++) rc |= h2d((double *)(m.*kElemMember[k]) + eo, im.el[k].data(), ne, st);
+  for (int k = 0; k < XP_COUNT; k++)
+    for (int j = 0; j < 3; j++)
+      rc |= h2d((double *)(m.*kEdgeMember[k]) + j * NE + eo, im.ed[k].data() + (size_t)j * ne, ne, st);
+  std::vector<int32_t> t(3 * (size_t)ne);
+  for (size_t q = 0; q < t.size(); q++) {
+    const int32_t v = im.nb[q];
+    t[q] = v >= 0 ? (int32_t)(v + eo) : (v == kBoundary ? v : (int32_t)(-1 - ((-1 - v) + ro)));
+  }
+  for (int j = 0; j < 3; j++) rc |= h2d((int32_t *)m.nb + j * NE + eo, t.data() + (size_t)j * ne, ne, st);
+  std::vector<int32_t> t2(3 * (size_t)ne);
+  for (size_t q = 0; q < t2.size(); q++) {
+    const int32_t v = im.emap[q];
+    t2[q] = v > 0 ? (int32_t)(v + edo) : (v < 0 ? (int32_t)(v - edo) : 0);
+  }
+  for (int j = 0; j < 3; j++) {
+    rc |= h2d((int32_t *)m.emap + j * NE + eo, t2.data() + (size_t)j * ne, ne, st);
+    rc |= h2d((int32_t *)m.bctype + j * NE + eo, im.bct.data() + (size_t)j * ne, ne, st);
+  }
+  std::vector<int32_t> ei(im.nedge), ek(im.nedge);
+  for (int e = 0; e < im.nedge; e++) {
+    ei[e] = (int32_t)(im.e_i[e] + eo);
+    ek[e] = (int32_t)(im.e_k[e] + eo);
+  }
+  rc |= h2d((int32_t *)m.e_i + edo, ei.data(), im.nedge, st);
+  rc |= h2d((int32_t *)m.e_k + edo, ek.data(), im.nedge, st);
+  rc |= h2d((double *)m.e_invdist + edo, im.e_invdist.data(), im.nedge, st);
+  rc |= h2d((double *)m.e_len + edo, im.e_len.data(), im.nedge, st);
+  rc |= h2d((double *)m.e_invrough + edo, im.e_invrough.data(), im.nedge, st);
+  std::vector<int32_t> bs(ne), be(im.nbank);
+  for (int i = 0; i < ne; i++) bs[i] = im.bank_slot[i] >= 0 ? (int32_t)(im.bank_slot[i] + bo) : -1;
+  for (int b = 0; b < im.nbank; b++) be[b] = (int32_t)(im.bank_elem[b] + eo);
+  rc |= h2d((int32_t *)m.bank_slot + eo, bs.data(), ne, st);
+  rc |= h2d((int32_t *)m.bank_elem + bo, be.data(), im.nbank, st);
+  std::vector<int32_t> dn(nr), lf(nr), rt(nr), ub(nr), ue(nr), ui(im.up_idx.size());
+  for (int r = 0; r < nr; r++) {
+    dn[r] = im.down[r] > 0 ? (int32_t)(im.down[r] + ro) : im.down[r];
+    lf[r] = (int32_t)(im.left[r] + eo);
+    rt[r] = (int32_t)(im.right[r] + eo);
+    ub[r] = (int32_t)(im.up_ptr[r] + uo);
+    ue[r] = (int32_t)(im.up_ptr[r + 1] + uo);
+  }
+  for (size_t q = 0; q < ui.size(); q++) ui[q] = (int32_t)(im.up_idx[q] + ro);
+  rc |= h2d((int32_t *)m.down + ro, dn.data(), nr, st);
+  rc |= h2d((int32_t *)m.left + ro, lf.data(), nr, st);
+  rc |= h2d((int32_t *)m.right + ro, rt.data(), nr, st);
+  rc |= h2d((int32_t *)m.intrpl_ord + ro, im.ord.data(), nr, st);
+  rc |= h2d((int32_t *)m.bctype_riv + ro, im.rbct.data(), nr, st);
+  rc |= h2d((int32_t *)m.up_ptr + ro, ub.data(), nr, st);
+  rc |= h2d((int32_t *)m.up_end + ro, ue.data(), nr, st);
+  rc |= h2d((int32_t *)m.up_idx + uo, ui.data(), ui.size(), st);
+  for (int k = 0; k < RP_COUNT; k++) rc |= h2d((double *)(m.*kRiverMember[k]) + ro, im.rv[k].data(), nr, st);
+  // boundary conditions (reference order in the job)
+  std::vector<double> bc(3 * (size_t)ne, 0.0);
+  if (job->elem_bc)
+    for (int j = 0; j < 3; j++)
+      for (int i = 0; i < ne; i++) bc[(size_t)j * ne + i] = job->elem_bc[3 * (size_t)im.perm[i] + j];
+  for (int j = 0; j < 3; j++) rc |= h2d((double *)m.elem_bc + j * NE + eo, bc.data() + (size_t)j * ne, ne, st);
+  std::vector<double> rbc(nr, 0.0);
+  if (job->river_bc) std::copy(job->river_bc, job->river_bc + nr, rbc.begin());
+  rc |= h2d((double *)m.river_bc + ro, rbc.data(), nr, st);
+  // a fresh watershed carries no river-edge flux from an earlier evaluation
+  for (int k = 0; k < NUM_RIVFLX; k++)
+    if (nr && cudaMemsetAsync(m.rivflow + k * NR + ro, 0, sizeof(double) * nr, st) != cudaSuccess) rc = -1;
+  // owner tables
+  std::vector<int32_t> own(std::max<int64_t>({(int64_t)ne, (int64_t)nr, (int64_t)im.nedge, (int64_t)im.nbank, 1}),
+                           s->slot);
+  rc |= h2d((int32_t *)m.sys_elem + eo, own.data(), ne, st);
+  rc |= h2d((int32_t *)m.sys_riv + ro, own.data(), nr, st);
+  rc |= h2d((int32_t *)m.sys_edge + edo, own.data(), im.nedge, st);
+  rc |= h2d((int32_t *)m.sys_bank + bo, own.data(), im.nbank, st);
+  const double dt = job->ctrl.stepsize;
+  rc |= h2d((double *)m.sys_dt + s->slot, &dt, 1, st);
+  // initial state, internal order, into vector slot 0
+  std::vector<double> y(s->neq);
+  for (int p = 0; p < 3; p++)
+    for (int i = 0; i < ne; i++) y[(size_t)p * ne + i] = job->y0[(size_t)p * ne + im.perm[i]];
+  for (int64_t q = 3LL * ne; q < s->neq; q++) y[q] = job->y0[q];
+  rc |= h2d(B->A.vec + s->soff, y.data(), s->neq, st);
+  SysInfo info{};
+  info.off = s->soff;
+  info.neq = (int32_t)s->neq;
+  info.ne = ne;
+  info.nr = nr;
+  info.eoff = (int32_t)eo;
+  info.roff = (int32_t)ro;
+  info.nblk = (int32_t)pihm_nv::red_grid_for(s->neq);
+  info.rec_off = s->recoff;
+  rc |= h2d(B->A.sysinfo + s->slot, &info, 1, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) rc = -1;
+  return rc ? PIHM_GPU_ERR_CUDA : PIHM_GPU_OK;
+}
+
+void free_ranges(pihm_batch *B, Sys *s) {
+  DevMesh &m = B->A.m;
+  // mark the items free so the masked kernels skip them whatever the slot's next owner
+  if (s->ne) cudaMemsetAsync((int32_t *)m.sys_elem + s->eoff, 0xff, sizeof(int32_t) * s->ne, B->st);
+  if (s->nr) cudaMemsetAsync((int32_t *)m.sys_riv + s->roff, 0xff, sizeof(int32_t) * s->nr, B->st);
+  if (s->nedge) cudaMemsetAsync((int32_t *)m.sys_edge + s->edoff, 0xff, sizeof(int32_t) * s->nedge, B->st);
+  if (s->nbank) cudaMemsetAsync((int32_t *)m.sys_bank + s->boff, 0xff, sizeof(int32_t) * s->nbank, B->st);
+  cudaStreamSynchronize(B->st);
+  B->ra_elem.release(s->eoff, s->ne);
+  B->ra_riv.release(s->roff, s->nr);
+  B->ra_edge.release(s->edoff, s->nedge);
+  B->ra_bank.release(s->boff, s->nbank);
+  B->ra_up.release(s->upoff, s->nup);
+  B->ra_state.release(s->soff, s->neq);
+  B->ra_rec.release(s->recoff, s->nrec);
+  B->update_extents();
+}
+
+// Resume a watershed's coroutine and note how it stopped.
+void resume(Sys *s) {
+  std::coroutine_handle<> h = s->waiting;
+  s->waiting = {};
+  h.resume();
+  if (s->task->done()) {
+    s->solver_rc = s->task->result();
+    s->state = (s->solver_rc < 0) ? S_FAILED : S_DONE;
+  }
+}
+
+// One round: upload the programs, run them and the right-hand side, read
+// the results back and resume the watersheds that were waiting.
+int run_round(pihm_batch *B, bool *any) {
+  *any = false;
+  std::vector<Sys *> part;
+  RoundSys *rs = (RoundSys *)(B->h_up + B->up_round_off);
+  Op *ops = (Op *)(B->h_up + B->up_ops_off);
+  uint8_t *active = (uint8_t *)B->h_up;
+  std::memset(active, 0, B->max_sys);
+  int nops = 0, nblocks = 0;
+  bool rhs = false;
+  for (auto &up : B->slots) {
+    Sys *s = up.get();
+    if (!s) continue;
+    const bool waiting = (bool)s->waiting;
+    if (!waiting && s->prog.empty()) continue;
+    RoundSys &r = rs[part.size()];
+    r.sys = s->slot;
+    r.prog_off = nops;
+    r.prog_len = (int32_t)s->prog.size();
+    r.red = waiting ? s->red : -1;
+    r.rx = s->rx;
+    r.ry = s->ry;
+    r.pad0 = r.pad1 = 0;
+    r.bstart = nblocks;
+    std::memcpy(ops + nops, s->prog.data(), sizeof(Op) * s->prog.size());
+    nops += (int)s->prog.size();
+    nblocks += (int)pihm_nv::red_grid_for(s->neq);
+    if (waiting && s->rhs_req) {
+      active[s->slot] = 1;
+      rhs = true;
+    }
+    part.push_back(s);
+  }
+  if (part.empty()) return 0;
+  *any = true;
+  cudaStream_t st = B->st;
+  const size_t up1 = B->up_round_off + sizeof(RoundSys) * part.size();
+  if (cudaMemcpyAsync(B->d_up, B->h_up, up1, cudaMemcpyHostToDevice, st) != cudaSuccess) return -1;
+  if (nops && cudaMemcpyAsync(B->d_up + B->up_ops_off, B->h_up + B->up_ops_off, sizeof(Op) * nops,
+                              cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return -1;
+  if (launch_program(B->A, (int)part.size(), nblocks, st) != cudaSuccess) return -1;
+  B->launches++;
+  if (rhs) {
+    if (cudaMemsetAsync(B->err_sys, 0, sizeof(unsigned int) * B->max_sys, st) != cudaSuccess) return -1;
+    if (launch_rhs(B->A.m, B->A.rhs_in, B->A.rhs_out, st, &B->launches, nullptr) != cudaSuccess) return -1;
+    B->rhs_rounds++;
+  }
+  if (cudaMemcpyAsync(B->h_down, B->d_down, B->down_bytes, cudaMemcpyDeviceToHost, st) != cudaSuccess) return -1;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
+  B->rounds++;
+  const double *res = (const double *)B->h_down;
+  const unsigned int *err = (const unsigned int *)(B->h_down + sizeof(double) * 2 * B->max_sys);
+  for (Sys *s : part) {
+    s->prog.clear();
+    if (!s->waiting) continue;  // a finished watershed's last operations
+    if (s->red >= 0) {
+      const double v = res[2 * s->slot];
+      s->red_value = s->red_wrms ? std::sqrt(v / (double)s->neq) : v;
+      s->red = -1;
+    }
+    if (s->rhs_req) {
+      s->rhs_rc = err[s->slot] ? -1 : 0;
+      s->rhs_req = false;
+      // the next program starts by delivering the evaluation
+      Op o;
+      std::memset(&o, 0, sizeof(o));
+      o.code = OP_STAGE_OUT;
+      o.x = o.y = o.z = s->rhs_out;
+      s->prog.push_back(o);
+    }
+    resume(s);
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pihm_batch_create(const pihm_batch_limits *lim, int surf_mode, int riv_mode, int order, pihm_batch **out) {
+  if (!lim || !out) return PIHM_GPU_ERR_ARG;
+  *out = nullptr;
+  if (lim->max_elem <= 0 || lim->max_river < 0 || lim->max_edge < 0 || lim->max_systems <= 0 ||
+      lim->max_record < 0 || lim->max_elem > INT32_MAX / 3 || lim->max_river > INT32_MAX / 3 ||
+      lim->max_edge > INT32_MAX)
+    return PIHM_GPU_ERR_ARG;
+  if ((surf_mode != kKinematic && surf_mode != kDiffWave) || (riv_mode != kKinematic && riv_mode != kDiffWave))
+    return PIHM_GPU_ERR_ARG;
+  if (order != PIHM_GPU_ORDER_REFERENCE && order != PIHM_GPU_ORDER_RCM) return PIHM_GPU_ERR_ARG;
+  auto B = std::make_unique<pihm_batch>();
+  B->order = order;
+  const int64_t NE = lim->max_elem, NR = std::max<int64_t>(lim->max_river, 1);
+  const int64_t NED = std::max<int64_t>(lim->max_edge, 1), MS = lim->max_systems;
+  B->ne_cap = NE;
+  B->nr_cap = NR;
+  B->ned_cap = NED;
+  B->rec_cap = std::max<int64_t>(lim->max_record, 1);
+  B->max_sys = (int)MS;
+  const int64_t NEQ = 3 * NE + 2 * NR;
+  B->ra_elem = RangeAlloc(NE);
+  B->ra_riv = RangeAlloc(NR);
+  B->ra_edge = RangeAlloc(NED);
+  B->ra_bank = RangeAlloc(NE);
+  B->ra_up = RangeAlloc(NR);
+  B->ra_state = RangeAlloc(NEQ);
+  B->ra_rec = RangeAlloc(B->rec_cap);
+  B->slots.resize(MS);
+  auto &o = B->owned;
+  DevMesh &m = B->A.m;
+  std::memset(&m, 0, sizeof(m));
+  m.ne = (int32_t)NE;
+  m.nr = (int32_t)NR;
+  m.nedge = (int32_t)NED;
+  m.nbank = (int32_t)NE;
+  m.surf_mode = surf_mode;
+  m.riv_mode = riv_mode;
+  m.dt = 1.0;
+  bool ok = true;
+  auto D = [&](size_t n) {
+    double *p = dalloc<double>(n, o);
+    ok = ok && p;
+    return p;
+  };
+  auto I = [&](size_t n) {
+    int32_t *p = dalloc<int32_t>(n, o);
+    ok = ok && p;
+    return p;
+  };
+  for (int k = 0; k < EP_COUNT; k++) m.*kElemMember[k] = D(NE);
+  for (int k = 0; k < XP_COUNT; k++) m.*kEdgeMember[k] = D(3 * NE);
+  m.nb = I(3 * NE);
+  m.bctype = I(3 * NE);
+  m.emap = I(3 * NE);
+  m.e_i = I(NED);
+  m.e_k = I(NED);
+  m.e_invdist = D(NED);
+  m.e_len = D(NED);
+  m.e_invrough = D(NED);
+  m.bank_slot = I(NE);
+  m.bank_elem = I(NE);
+  m.down = I(NR);
+  m.left = I(NR);
+  m.right = I(NR);
+  m.intrpl_ord = I(NR);
+  m.bctype_riv = I(NR);
+  for (int k = 0; k < RP_COUNT; k++) m.*kRiverMember[k] = D(NR);
+  m.up_ptr = I(NR);
+  m.up_end = I(NR);
+  m.up_idx = I(NR);
+  m.pcpdrp = D(NE);
+  m.edir = D(NE);
+  m.ett = D(NE);
+  m.ws0_surf = D(NE);
+  m.elem_bc = D(3 * NE);
+  m.river_bc = D(NR);
+  m.surfh = D(NE);
+  m.head = D(NE);
+  m.effk = D(NE);
+  m.gradmag = D(NE);
+  m.rivflow = D(NUM_RIVFLX * NR);
+  m.eflux_ovl = D(NED);
+  m.eflux_sub = D(NED);
+  m.bank_part = D(8 * NE);
+  m.err = dalloc<unsigned int>(1, o);
+  int32_t *se = I(NE), *sr = I(NR), *sed = I(NED), *sb = I(NE);
+  m.sys_elem = se;
+  m.sys_riv = sr;
+  m.sys_edge = sed;
+  m.sys_bank = sb;
+  m.sys_dt = D(MS);
+  DeviceArena &A = B->A;
+  A.vec = D((size_t)kVecSlots * NEQ);
+  A.neq_cap = NEQ;
+  A.rhs_in = D(NEQ);
+  A.rhs_out = D(NEQ);
+  A.sysinfo = dalloc<SysInfo>(MS, o);
+  A.partials = D(MS * 2 * pihm_nv::kMaxBlocks);
+  A.tickets = dalloc<unsigned int>(MS, o);
+  A.rec = D(B->rec_cap);
+  A.max_sys = (int)MS;
+  // upload block: active flags | round list | ops
+  B->up_active_bytes = ((size_t)MS + 255) & ~size_t(255);
+  B->up_round_off = B->up_active_bytes;
+  B->up_ops_off = B->up_round_off + ((sizeof(RoundSys) * MS + 255) & ~size_t(255));
+  const size_t up_bytes = B->up_ops_off + sizeof(Op) * MS * kMaxProgOps;
+  B->d_up = (char *)dalloc<char>(up_bytes, o);
+  // download block: results | error words
+  B->down_bytes = sizeof(double) * 2 * MS + sizeof(unsigned int) * MS;
+  B->d_down = (char *)dalloc<char>(B->down_bytes, o);
+  if (!ok || !m.err || !A.sysinfo || !A.tickets || !B->d_up || !B->d_down ||
+      cudaMallocHost(&B->h_up, up_bytes) != cudaSuccess ||
+      cudaMallocHost(&B->h_down, B->down_bytes) != cudaSuccess)
+    return PIHM_GPU_ERR_NOMEM;
+  m.active = (const uint8_t *)B->d_up;
+  A.round = (RoundSys *)(B->d_up + B->up_round_off);
+  A.ops = (Op *)(B->d_up + B->up_ops_off);
+  A.results = (double *)B->d_down;
+  B->err_sys = (unsigned int *)(B->d_down + sizeof(double) * 2 * MS);
+  m.err_sys = B->err_sys;
+  // everything starts free: owner -1, zero scratch
+  bool z = cudaMemset(se, 0xff, sizeof(int32_t) * NE) == cudaSuccess &&
+           cudaMemset(sr, 0xff, sizeof(int32_t) * NR) == cudaSuccess &&
+           cudaMemset(sed, 0xff, sizeof(int32_t) * NED) == cudaSuccess &&
+           cudaMemset(sb, 0xff, sizeof(int32_t) * NE) == cudaSuccess &&
+           cudaMemset(A.tickets, 0, sizeof(unsigned int) * MS) == cudaSuccess &&
+           cudaMemset(B->d_up, 0, up_bytes) == cudaSuccess &&
+           cudaMemset(m.rivflow, 0, sizeof(double) * NUM_RIVFLX * NR) == cudaSuccess &&
+           cudaMemset(A.rhs_in, 0, sizeof(double) * NEQ) == cudaSuccess &&
+           cudaDeviceSynchronize() == cudaSuccess;
+  if (!z) return PIHM_GPU_ERR_CUDA;
+  B->update_extents();
+  *out = B.release();
+  return PIHM_GPU_OK;
+}
+
+void pihm_batch_destroy(pihm_batch *b) { delete b; }
+
+int pihm_batch_set_stream(pihm_batch *b, void *stream) {
+  if (!b) return PIHM_GPU_ERR_ARG;
+  b->st = (cudaStream_t)stream;
+  return PIHM_GPU_OK;
+}
+
+int pihm_batch_add(pihm_batch *B, const pihm_batch_job *job, int32_t *id) {
+  if (!B || !job || !job->mesh || !job->y0 || !id || job->nsteps < 0 ||
+      (job->nsteps > 0 && (!job->pcpdrp || !job->edir || !job->ett)))
+    return PIHM_GPU_ERR_ARG;
+  const pihm_step_control &c = job->ctrl;
+  if (!(c.stepsize > 0.0) || c.reltol < 0 || c.abstol < 0 || !(c.decr > 0.0)) return PIHM_GPU_ERR_ARG;
+  if (job->outlet >= job->mesh->nriver) return PIHM_GPU_ERR_ARG;
+  SystemImage im;
+  const int brc = build_image(job->mesh, B->A.m.surf_mode, B->A.m.riv_mode, c.stepsize, B->order, &im);
+  if (brc != PIHM_GPU_OK) return brc;
+  int slot = -1;
+  for (int k = 0; k < B->max_sys; k++)
+    if (!B->slots[k]) {
+      slot = k;
+      break;
+    }
+  if (slot < 0) return PIHM_GPU_ERR_NOMEM;
+  auto s = std::make_unique<Sys>();
+  s->slot = slot;
+  s->ne = im.ne;
+  s->nr = im.nr;
+  s->nedge = im.nedge;
+  s->nbank = im.nbank;
+  s->nup = (int32_t)im.up_idx.size();
+  s->neq = 3LL * im.ne + 2LL * im.nr;
+  s->nrec = job->outlet >= 0 ? job->nsteps : 0;
+  // admission: every range must fit now
+  struct Want {
+    RangeAlloc *ra;
+    int64_t n, *off;
+  } want[] = {{&B->ra_elem, s->ne, &s->eoff},   {&B->ra_riv, s->nr, &s->roff},
+              {&B->ra_edge, s->nedge, &s->edoff}, {&B->ra_bank, s->nbank, &s->boff},
+              {&B->ra_up, s->nup, &s->upoff},   {&B->ra_state, s->neq, &s->soff},
+              {&B->ra_rec, s->nrec, &s->recoff}};
+  int got = 0;
+  for (; got < 7; got++) {
+    const int64_t off = want[got].ra->alloc(want[got].n);
+    if (off < 0) break;
+    *want[got].off = off;
+  }
+  if (got < 7) {
+    for (int k = 0; k < got; k++) want[k].ra->release(*want[k].off, want[k].n);
+    return PIHM_GPU_ERR_NOMEM;
+  }
+  s->perm = im.perm;
+  s->ctrl = c;
+  s->nsteps = job->nsteps;
+  s->outlet = job->outlet;
+  s->pcp.assign(job->pcpdrp, job->pcpdrp + job->nsteps);
+  s->edir.assign(job->edir, job->edir + job->nsteps);
+  s->ett.assign(job->ett, job->ett + job->nsteps);
+  s->core.ops.s = s.get();
+  Sys *sp = s.get();
+  B->slots[slot] = std::move(s);
+  const int prc = place(B, sp, im, job);
+  if (prc != PIHM_GPU_OK) {
+    free_ranges(B, sp);
+    B->slots[slot].reset();
+    return prc;
+  }
+  B->update_extents();
+  sp->id = B->next_id++;
+  B->by_id[sp->id] = sp;
+  // start the model loop: it runs until its first device operation
+  sp->task = std::make_unique<Task<int>>(model_run(sp));
+  sp->state = S_RUNNING;
+  sp->waiting = sp->task->handle();
+  resume(sp);
+  *id = sp->id;
+  return PIHM_GPU_OK;
+}
+
+int pihm_batch_step(pihm_batch *B, int32_t max_rounds, int32_t *running) {
+  if (!B) return PIHM_GPU_ERR_ARG;
+  for (int32_t r = 0; max_rounds <= 0 || r < max_rounds; r++) {
+    bool any = false;
+    if (run_round(B, &any) != 0) return PIHM_GPU_ERR_CUDA;
+    if (!any) break;
+  }
+  if (running) {
+    int32_t n = 0;
+    for (auto &kv : B->by_id)
+      if (kv.second->state == S_RUNNING) n++;
+    *running = n;
+  }
+  return PIHM_GPU_OK;
+}
+
+int pihm_batch_poll(const pihm_batch *B, int32_t id, int32_t *status, int32_t *solver_rc) {
+  if (!B) return PIHM_GPU_ERR_ARG;
+  auto it = B->by_id.find(id);
+  if (it == B->by_id.end()) return PIHM_GPU_ERR_ARG;
+  const Sys *s = it->second;
+  const bool pending = !s->prog.empty();  // last operations not yet run
+  if (status)
+    *status = (s->state == S_RUNNING || pending) ? PIHM_BATCH_RUNNING
+              : (s->state == S_DONE)             ? PIHM_BATCH_DONE
+                                                 : PIHM_BATCH_FAILED;
+  if (solver_rc) *solver_rc = s->solver_rc;
+  return PIHM_GPU_OK;
+}
+
+int pihm_batch_result(pihm_batch *B, int32_t id, double *y, double *outlet, pihm_bdf_stats *stats,
+                      int32_t *steps_done) {
+  if (!B) return PIHM_GPU_ERR_ARG;
+  auto it = B->by_id.find(id);
+  if (it == B->by_id.end()) return PIHM_GPU_ERR_ARG;
+  Sys *s = it->second;
+  if (s->state == S_RUNNING || !s->prog.empty()) return PIHM_GPU_ERR_ARG;
+  if (y) {
+    std::vector<double> yi(s->neq);
+    if (cudaMemcpy(yi.data(), B->A.vec + s->soff, sizeof(double) * s->neq, cudaMemcpyDeviceToHost) != cudaSuccess)
+      return PIHM_GPU_ERR_CUDA;
+    const int ne = s->ne;
+    for (int p = 0; p < 3; p++)
+      for (int i = 0; i < ne; i++) y[(size_t)p * ne + s->perm[i]] = yi[(size_t)p * ne + i];
+    for (int64_t q = 3LL * ne; q < s->neq; q++) y[q] = yi[q];
+  }
+  if (outlet && s->nrec > 0 &&
+      cudaMemcpy(outlet, B->A.rec + s->recoff, sizeof(double) * s->nrec, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return PIHM_GPU_ERR_CUDA;
+  if (stats) {
+    const bdf::Stats st = s->core.stats();
+    stats->nst = st.nst;
+    stats->nfe = st.nfe;
+    stats->nni = st.nni;
+    stats->ncfn = st.ncfn;
+    stats->netf = st.netf;
+    stats->nli = st.nli;
+    stats->nfes = st.nfes;
+    stats->njtimes = st.njtimes;
+    stats->ncfl = st.ncfl;
+    stats->nor = st.nor;
+    stats->qlast = st.qlast;
+    stats->qcur = st.qcur;
+    stats->hlast = st.hlast;
+    stats->hcur = st.hcur;
+    stats->tcur = st.tcur;
+  }
+  if (steps_done) *steps_done = s->steps_done;
+  return PIHM_GPU_OK;
+}
+
+int pihm_batch_release(pihm_batch *B, int32_t id) {
+  if (!B) return PIHM_GPU_ERR_ARG;
+  auto it = B->by_id.find(id);
+  if (it == B->by_id.end()) return PIHM_GPU_ERR_ARG;
+  Sys *s = it->second;
+  if (s->state == S_RUNNING || !s->prog.empty()) return PIHM_GPU_ERR_ARG;
+  free_ranges(B, s);
+  const int slot = s->slot;
+  B->by_id.erase(it);
+  B->slots[slot].reset();
+  return PIHM_GPU_OK;
+}
+
+int pihm_batch_get_info(const pihm_batch *B, pihm_batch_info *info) {
+  if (!B || !info) return PIHM_GPU_ERR_ARG;
+  info->rounds = B->rounds;
+  info->rhs_rounds = B->rhs_rounds;
+  info->launches = B->launches;
+  info->elem_used = B->ra_elem.used();
+  info->elem_hwm = B->ra_elem.hwm();
+  info->resident = (int64_t)B->by_id.size();
+  return PIHM_GPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,57 @@
+// Arithmetic of the N_Vector operations, shared by the single-vector kernels
+// (nvector.cu) and the batch engine's program kernel (batch_kernels.cu) so
+// that both produce bit-identical vectors and norms.
+//
+// Element-wise operations use __dmul_rn/__dadd_rn so the compiler cannot fuse
+// a multiply and an add: every element equals what the serial N_Vector
+// computes (cvode/src/nvec_ser/nvector_serial.c:421-1060), including its
+// special cases (a == 1, b == -1, a == b, ...) which change the rounding.
+#pragma once
+
+#include <cmath>
+
+#include "nv_reduce.cuh"
+#include "nv_select.h"
+
+namespace pihm_nv {
+
+// z_i = OP(a, b, x_i, y_i, z_i)
+template <int OP>
+__device__ __forceinline__ double ew_eval(double a, double b, double x, double y, double z) {
+  if (OP == EW_LIN) return __dadd_rn(__dmul_rn(a, x), __dmul_rn(b, y));
+  if (OP == EW_LIN1) return __dadd_rn(__dmul_rn(a, x), y);
+  if (OP == EW_LIN2) return __dsub_rn(__dmul_rn(a, x), y);
+  if (OP == EW_SUM) return __dadd_rn(x, y);
+  if (OP == EW_DIFF) return __dsub_rn(x, y);
+  if (OP == EW_SCALESUM) return __dmul_rn(a, __dadd_rn(x, y));
+  if (OP == EW_SCALEDIFF) return __dmul_rn(a, __dsub_rn(x, y));
+  if (OP == EW_AXPY) return __dadd_rn(z, __dmul_rn(a, x));
+  if (OP == EW_AXPY1) return __dadd_rn(z, x);
+  if (OP == EW_AXPYM1) return __dsub_rn(z, x);
+  if (OP == EW_CONST) return a;
+  if (OP == EW_PROD) return __dmul_rn(x, y);
+  if (OP == EW_DIV) return __ddiv_rn(x, y);
+  if (OP == EW_SCALE) return __dmul_rn(a, x);
+  if (OP == EW_COPY) return x;
+  if (OP == EW_NEG) return -x;
+  if (OP == EW_ABS) return fabs(x);
+  if (OP == EW_INV) return __drcp_rn(x);
+  if (OP == EW_ADDCONST) return __dadd_rn(x, b);
+  return (fabs(x) >= a) ? 1.0 : 0.0;
+}
+
+// Per-entry term of a reduction
+template <int OP>
+__device__ __forceinline__ Pair red_term(double x, double y) {
+  Pair t = red_identity<OP>();
+  if (OP == R_DOT) t.v = __dmul_rn(x, y);
+  else if (OP == R_MAXABS) t.v = fabs(x);
+  else if (OP == R_WSQ) {
+    const double p = __dmul_rn(x, y);
+    t.v = __dmul_rn(p, p);
+  } else if (OP == R_MIN) t.v = x;
+  else if (OP == R_L1) t.v = fabs(x);
+  return t;
+}
+
+}  // namespace pihm_nv

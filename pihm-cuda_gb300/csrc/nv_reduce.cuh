@@ -3,11 +3,9 @@
 
 #include <cmath>
 
+#include "nv_select.h"
+
 namespace pihm_nv {
-
-constexpr int kThreads = 256;
-
-enum RedOp { R_DOT = 0, R_MAXABS, R_WSQ, R_WSQ_MASK, R_MIN, R_L1, R_INVTEST, R_CONSTR, R_MINQ };
 
 struct Pair {
   double v;

@@ -18,11 +18,10 @@
 #include <mutex>
 
 #include "pihm_nvector.h"
-#include "nv_reduce.cuh"
+#include "nv_ops.cuh"
 
 namespace pihm_nv {
 
-constexpr int kMaxBlocks = 608;  // 4 x 152 SMs
 constexpr double kBigReal = DBL_MAX;
 
 struct Scratch {
@@ -78,65 +77,19 @@ static inline unsigned grid_for(long long n) {
   if (b > 16 * 152) b = 16 * 152;
   return (unsigned)(b > 0 ? b : 1);
 }
-static inline unsigned red_grid_for(long long n) {
-  long long b = (n + 4LL * kThreads - 1) / (4LL * kThreads);
-  if (b > kMaxBlocks) b = kMaxBlocks;
-  return (unsigned)(b > 0 ? b : 1);
-}
 
 // ---------------------------------------------------------------------------
 // element-wise kernels
 // ---------------------------------------------------------------------------
-enum EwOp {
-  EW_LIN = 0,      // a*x + b*y
-  EW_LIN1,         // a*x + y
-  EW_LIN2,         // a*x - y
-  EW_SUM,          // x + y
-  EW_DIFF,         // x - y
-  EW_SCALESUM,     // a*(x + y)
-  EW_SCALEDIFF,    // a*(x - y)
-  EW_AXPY,         // y += a*x   (z == y)
-  EW_AXPY1,        // y += x
-  EW_AXPYM1,       // y -= x
-  EW_CONST,        // c
-  EW_PROD,         // x*y
-  EW_DIV,          // x/y
-  EW_SCALE,        // c*x
-  EW_COPY,         // x
-  EW_NEG,          // -x
-  EW_ABS,          // |x|
-  EW_INV,          // 1/x
-  EW_ADDCONST,     // x + b
-  EW_COMPARE       // |x| >= c ? 1 : 0
-};
-
 template <int OP>
 __global__ void k_ew(long long n, double a, double b, const double *__restrict__ x,
                      const double *__restrict__ y, double *z) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
-    double r;
-    if (OP == EW_LIN) r = __dadd_rn(__dmul_rn(a, x[i]), __dmul_rn(b, y[i]));
-    else if (OP == EW_LIN1) r = __dadd_rn(__dmul_rn(a, x[i]), y[i]);
-    else if (OP == EW_LIN2) r = __dsub_rn(__dmul_rn(a, x[i]), y[i]);
-    else if (OP == EW_SUM) r = __dadd_rn(x[i], y[i]);
-    else if (OP == EW_DIFF) r = __dsub_rn(x[i], y[i]);
-    else if (OP == EW_SCALESUM) r = __dmul_rn(a, __dadd_rn(x[i], y[i]));
-    else if (OP == EW_SCALEDIFF) r = __dmul_rn(a, __dsub_rn(x[i], y[i]));
-    else if (OP == EW_AXPY) r = __dadd_rn(z[i], __dmul_rn(a, x[i]));
-    else if (OP == EW_AXPY1) r = __dadd_rn(z[i], x[i]);
-    else if (OP == EW_AXPYM1) r = __dsub_rn(z[i], x[i]);
-    else if (OP == EW_CONST) r = a;
-    else if (OP == EW_PROD) r = __dmul_rn(x[i], y[i]);
-    else if (OP == EW_DIV) r = __ddiv_rn(x[i], y[i]);
-    else if (OP == EW_SCALE) r = __dmul_rn(a, x[i]);
-    else if (OP == EW_COPY) r = x[i];
-    else if (OP == EW_NEG) r = -x[i];
-    else if (OP == EW_ABS) r = fabs(x[i]);
-    else if (OP == EW_INV) r = __drcp_rn(x[i]);
-    else if (OP == EW_ADDCONST) r = __dadd_rn(x[i], b);
-    else r = (fabs(x[i]) >= a) ? 1.0 : 0.0;
-    z[i] = r;
+    const double xv = ew_reads_x(OP) ? x[i] : 0.0;
+    const double yv = ew_reads_y(OP) ? y[i] : 0.0;
+    const double zv = ew_reads_z(OP) ? z[i] : 0.0;
+    z[i] = ew_eval<OP>(a, b, xv, yv, zv);
   }
 }
 
@@ -148,39 +101,31 @@ static int ew(long long n, double a, double b, const double *x, const double *y,
   return cudaGetLastError() == cudaSuccess ? 0 : -2;
 }
 
-// z = a*x + b*y with the serial N_Vector's case analysis
-// (cvode/src/nvec_ser/nvector_serial.c:421-506)
+// One element-wise call after the serial N_Vector's case analysis.
+static int ew_call(const EwCall<const double *> &c, long long n, cudaStream_t st) {
+  double *z = const_cast<double *>(c.z);
+  switch (c.op) {
+    case EW_LIN: return ew<EW_LIN>(n, c.a, c.b, c.x, c.y, z, st);
+    case EW_LIN1: return ew<EW_LIN1>(n, c.a, c.b, c.x, c.y, z, st);
+    case EW_LIN2: return ew<EW_LIN2>(n, c.a, c.b, c.x, c.y, z, st);
+    case EW_SUM: return ew<EW_SUM>(n, c.a, c.b, c.x, c.y, z, st);
+    case EW_DIFF: return ew<EW_DIFF>(n, c.a, c.b, c.x, c.y, z, st);
+    case EW_SCALESUM: return ew<EW_SCALESUM>(n, c.a, c.b, c.x, c.y, z, st);
+    case EW_SCALEDIFF: return ew<EW_SCALEDIFF>(n, c.a, c.b, c.x, c.y, z, st);
+    case EW_AXPY: return ew<EW_AXPY>(n, c.a, c.b, c.x, c.y, z, st);
+    case EW_AXPY1: return ew<EW_AXPY1>(n, c.a, c.b, c.x, c.y, z, st);
+    case EW_AXPYM1: return ew<EW_AXPYM1>(n, c.a, c.b, c.x, c.y, z, st);
+    case EW_SCALE: return ew<EW_SCALE>(n, c.a, c.b, c.x, c.y, z, st);
+    case EW_COPY: return ew<EW_COPY>(n, c.a, c.b, c.x, c.y, z, st);
+    case EW_NEG: return ew<EW_NEG>(n, c.a, c.b, c.x, c.y, z, st);
+    default: return -1;
+  }
+}
+
+// z = a*x + b*y (cvode/src/nvec_ser/nvector_serial.c:421-506)
 static int linear_sum(double a, const double *x, double b, const double *y, double *z, long long n,
                       cudaStream_t st) {
-  if (b == 1.0 && z == y) {
-    if (a == 1.0) return ew<EW_AXPY1>(n, a, b, x, y, z, st);
-    if (a == -1.0) return ew<EW_AXPYM1>(n, a, b, x, y, z, st);
-    return ew<EW_AXPY>(n, a, b, x, y, z, st);
-  }
-  if (a == 1.0 && z == x) {
-    if (b == 1.0) return ew<EW_AXPY1>(n, b, a, y, x, z, st);
-    if (b == -1.0) return ew<EW_AXPYM1>(n, b, a, y, x, z, st);
-    return ew<EW_AXPY>(n, b, a, y, x, z, st);
-  }
-  if (a == 1.0 && b == 1.0) return ew<EW_SUM>(n, a, b, x, y, z, st);
-  bool test;
-  if ((test = (a == 1.0 && b == -1.0)) || (a == -1.0 && b == 1.0)) {
-    const double *v1 = test ? y : x, *v2 = test ? x : y;
-    return ew<EW_DIFF>(n, 0, 0, v2, v1, z, st);
-  }
-  if ((test = (a == 1.0)) || (b == 1.0)) {
-    double c = test ? b : a;
-    const double *v1 = test ? y : x, *v2 = test ? x : y;
-    return ew<EW_LIN1>(n, c, 0, v1, v2, z, st);
-  }
-  if ((test = (a == -1.0)) || (b == -1.0)) {
-    double c = test ? b : a;
-    const double *v1 = test ? y : x, *v2 = test ? x : y;
-    return ew<EW_LIN2>(n, c, 0, v1, v2, z, st);
-  }
-  if (a == b) return ew<EW_SCALESUM>(n, a, 0, x, y, z, st);
-  if (a == -b) return ew<EW_SCALEDIFF>(n, a, 0, x, y, z, st);
-  return ew<EW_LIN>(n, a, b, x, y, z, st);
+  return ew_call(select_linear_sum<const double *>(a, x, b, y, z), n, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -199,14 +144,11 @@ __global__ void __launch_bounds__(kThreads) k_red(long long n, const double *__r
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     Pair t = red_identity<OP>();
-    if (OP == R_DOT) t.v = __dmul_rn(x[i], y[i]);
-    else if (OP == R_MAXABS) t.v = fabs(x[i]);
-    else if (OP == R_WSQ) { double p = __dmul_rn(x[i], y[i]); t.v = __dmul_rn(p, p); }
+    if (OP == R_DOT || OP == R_WSQ) t = red_term<OP>(x[i], y[i]);
+    else if (OP == R_MAXABS || OP == R_MIN || OP == R_L1) t = red_term<OP>(x[i], 0.0);
     else if (OP == R_WSQ_MASK) {
       if (z[i] > 0.0) { double p = __dmul_rn(x[i], y[i]); t.v = __dmul_rn(p, p); }
-    } else if (OP == R_MIN) t.v = x[i];
-    else if (OP == R_L1) t.v = fabs(x[i]);
-    else if (OP == R_INVTEST) {
+    } else if (OP == R_INVTEST) {
       if (x[i] == 0.0) t.f = 1.0;
       else z[i] = __drcp_rn(x[i]);
     } else if (OP == R_CONSTR) {
@@ -445,13 +387,7 @@ void N_VProd_PihmGpu(N_Vector x, N_Vector y, N_Vector z) { ew<EW_PROD>(L(x), 0, 
 void N_VDiv_PihmGpu(N_Vector x, N_Vector y, N_Vector z) { ew<EW_DIV>(L(x), 0, 0, D(x), D(y), D(z), S(z)); }
 void N_VScale_PihmGpu(double c, N_Vector x, N_Vector z) {
   // cvode/src/nvec_ser/nvector_serial.c:559-584
-  if (z == x) {
-    ew<EW_SCALE>(L(x), c, 0, D(x), nullptr, D(z), S(z));
-    return;
-  }
-  if (c == 1.0) ew<EW_COPY>(L(x), 0, 0, D(x), nullptr, D(z), S(z));
-  else if (c == -1.0) ew<EW_NEG>(L(x), 0, 0, D(x), nullptr, D(z), S(z));
-  else ew<EW_SCALE>(L(x), c, 0, D(x), nullptr, D(z), S(z));
+  ew_call(select_scale<const double *>(c, D(x), D(z)), L(x), S(z));
 }
 void N_VAbs_PihmGpu(N_Vector x, N_Vector z) { ew<EW_ABS>(L(x), 0, 0, D(x), nullptr, D(z), S(z)); }
 void N_VInv_PihmGpu(N_Vector x, N_Vector z) { ew<EW_INV>(L(x), 0, 0, D(x), nullptr, D(z), S(z)); }

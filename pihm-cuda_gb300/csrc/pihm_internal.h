@@ -74,6 +74,8 @@ struct DevMesh {
       *r_dist_right, *r_depth, *r_coeff, *r_length, *r_width, *r_rough, *r_cwr,
       *r_ksath, *r_ksatv, *r_bedthick, *r_porosity;
   const int32_t *up_ptr, *up_idx;  // CSR of upstream segments, reference order
+  const int32_t *up_end;           // [nr] end of each upstream list (up_ptr + 1 in a
+                                   // single-watershed context)
 
   // inputs besides y
   const double *pcpdrp, *edir, *ett, *ws0_surf;  // [ne]
@@ -90,6 +92,19 @@ struct DevMesh {
   int diag;
 
   unsigned int *err;  // error word
+
+  // Launch extents.  A single-watershed context evaluates every item
+  // (ne_run = ne, ...); the batch engine's arena places watersheds in ranges of
+  // planes sized ne, nr, nedge, nbank (the capacities, which stay the plane
+  // strides) and evaluates items below the high-water marks.
+  int32_t ne_run, nr_run, nedge_run, nbank_run;
+  // Batch engine only (null otherwise): the watershed of each item (-1 for a
+  // free arena slot), the watersheds evaluated by this call, their model steps
+  // and their error words.
+  const int32_t *sys_elem, *sys_riv, *sys_edge, *sys_bank;
+  const uint8_t *active;
+  const double *sys_dt;
+  unsigned int *err_sys;
 };
 
 // Optional per-kernel CUDA-event timing of the right-hand-side launches.

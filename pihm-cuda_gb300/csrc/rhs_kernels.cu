@@ -117,12 +117,28 @@ __device__ __forceinline__ double riv_perim(int order, double depth, double coef
   return 0.0;
 }
 
+// Batch engine: whether the watershed of item idx sits out this evaluation
+// (a free arena slot, or a watershed that did not ask for one).  Always false
+// in a single-watershed context.
+__device__ __forceinline__ bool skip_item(const DevMesh &m, const int32_t *sys_of, int idx, int *sy) {
+  *sy = 0;
+  if (!m.active) return false;
+  const int s = sys_of[idx];
+  *sy = s;
+  return s < 0 || !m.active[s];
+}
+
+__device__ __forceinline__ void report_err(const DevMesh &m, int sy) {
+  atomicOr(m.err_sys ? &m.err_sys[sy] : m.err, 1u);
+}
+
 // ---------------------------------------------------------------------------
 // k_elem_prep
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_elem_prep(DevMesh m, const double *RESTRICT y) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= m.ne) return;
+  int sy;
+  if (i >= m.ne_run || skip_item(m, m.sys_elem, i, &sy)) return;
   const double surfh = surf_h(clamp0(y[i]));
   const double gw = clamp0(y[2 * m.ne + i]);
   m.surfh[i] = surfh;
@@ -135,7 +151,8 @@ __global__ void __launch_bounds__(256) k_elem_prep(DevMesh m, const double *REST
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_elem_grad(DevMesh m, const double *RESTRICT y) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= m.ne) return;
+  int sy;
+  if (i >= m.ne_run || skip_item(m, m.sys_elem, i, &sy)) return;
   const int ne = m.ne;
   double h[3];
   const double hself = m.head[i];
@@ -172,7 +189,8 @@ __global__ void __launch_bounds__(256) k_elem_grad(DevMesh m, const double *REST
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_edge(DevMesh m, const double *RESTRICT y) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= m.nedge) return;
+  int sy;
+  if (e >= m.nedge_run || skip_item(m, m.sys_edge, e, &sy)) return;
   const int ne = m.ne;
   const int i = m.e_i[e], k = m.e_k[e];
   const double invdist = m.e_invdist[e], len = m.e_len[e];
@@ -212,7 +230,8 @@ __global__ void __launch_bounds__(256) k_edge(DevMesh m, const double *RESTRICT 
 __global__ void __launch_bounds__(256) k_elem_main(DevMesh m, const double *RESTRICT y,
                                                     double *RESTRICT ydot) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= m.ne) return;
+  int sy;
+  if (i >= m.ne_run || skip_item(m, m.sys_elem, i, &sy)) return;
   const int ne = m.ne;
   const double gw = clamp0(y[2 * ne + i]);
   const double unsat = clamp0(y[ne + i]);
@@ -335,7 +354,8 @@ __global__ void __launch_bounds__(256) k_elem_main(DevMesh m, const double *REST
     infil = kinf * dh_by_dz;
     if (!gw_in_dinf) infil = (infil > 0.0) ? infil : 0.0;
     const double ws0 = m.ws0_surf[i];
-    const double infil_max = applrate + ((ws0 > 0.0) ? ws0 / m.dt : 0.0);
+    const double dt = m.sys_dt ? m.sys_dt[sy] : m.dt;
+    const double infil_max = applrate + ((ws0 > 0.0) ? ws0 / dt : 0.0);
     infil = (infil > infil_max) ? infil_max : infil;
     infil *= wetfrac;
   }
@@ -416,7 +436,7 @@ __global__ void __launch_bounds__(256) k_elem_main(DevMesh m, const double *REST
     ydot[2 * ne + i] = dg;
     bad |= isnan(ds) | isnan(dg);
   }
-  if (bad) atomicOr(m.err, 1u);
+  if (bad) report_err(m, sy);
 }
 
 // ---------------------------------------------------------------------------
@@ -497,7 +517,8 @@ __device__ __forceinline__ double sub_elem_to_river(double e_gw, double e_zmin, 
 
 __global__ void __launch_bounds__(128) k_river(DevMesh m, const double *RESTRICT y) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= m.nr) return;
+  int sy;
+  if (s >= m.nr_run || skip_item(m, m.sys_riv, s, &sy)) return;
   const int nr = m.nr, ne = m.ne;
   const RivState r = load_riv(m, y, s);
   const int down = m.down[s];
@@ -618,11 +639,13 @@ __global__ void __launch_bounds__(128) k_finish(DevMesh m, double *RESTRICT ydot
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int nr = m.nr, ne = m.ne;
   const double *F = m.rivflow;
-  if (t < nr) {
+  int sy;
+  if (t < m.nr_run) {
     const int s = t;
+    if (skip_item(m, m.sys_riv, s, &sy)) return;
     double up_c = F[UP_CHANL2CHANL * nr + s];
     double up_a = 0.0;
-    for (int k = m.up_ptr[s]; k < m.up_ptr[s + 1]; k++) {
+    for (int k = m.up_ptr[s]; k < m.up_end[s]; k++) {
       const int u = m.up_idx[k];
       up_c -= F[DOWN_CHANL2CHANL * nr + u];
       up_a -= F[DOWN_AQUIF2AQUIF * nr + u];
@@ -641,11 +664,11 @@ __global__ void __launch_bounds__(128) k_finish(DevMesh m, double *RESTRICT ydot
       m.rivflow[UP_CHANL2CHANL * nr + s] = up_c;
       m.rivflow[UP_AQUIF2AQUIF * nr + s] = up_a;
     }
-    if (isnan(ds) | isnan(dg)) atomicOr(m.err, 1u);
+    if (isnan(ds) | isnan(dg)) report_err(m, sy);
     return;
   }
-  const int b = t - nr;
-  if (b >= m.nbank) return;
+  const int b = t - m.nr_run;
+  if (b >= m.nbank_run || skip_item(m, m.sys_bank, b, &sy)) return;
   const int i = m.bank_elem[b];
   const int nbk = m.nbank;
   const double *bp = m.bank_part;
@@ -678,7 +701,7 @@ __global__ void __launch_bounds__(128) k_finish(DevMesh m, double *RESTRICT ydot
   dg *= m.inv_por[i];
   ydot[i] = ds;
   ydot[2 * ne + i] = dg;
-  if (isnan(ds) | isnan(dg)) atomicOr(m.err, 1u);
+  if (isnan(ds) | isnan(dg)) report_err(m, sy);
 }
 
 // ---------------------------------------------------------------------------
@@ -742,37 +765,37 @@ static void prof_end(Profiler *p, bool on, cudaStream_t st) {
 cudaError_t launch_rhs(const DevMesh &m, const double *y, double *ydot, cudaStream_t st,
                        long long *launches, Profiler *prof) {
   bool on;
-  if (m.ne > 0) {
+  if (m.ne_run > 0) {
     on = prof_begin(prof, K_PREP, st);
-    k_elem_prep<<<blocks_for(m.ne, 256), 256, 0, st>>>(m, y);
+    k_elem_prep<<<blocks_for(m.ne_run, 256), 256, 0, st>>>(m, y);
     prof_end(prof, on, st);
     ++*launches;
     if (m.surf_mode == kDiffWave) {
       on = prof_begin(prof, K_GRAD, st);
-      k_elem_grad<<<blocks_for(m.ne, 256), 256, 0, st>>>(m, y);
+      k_elem_grad<<<blocks_for(m.ne_run, 256), 256, 0, st>>>(m, y);
       prof_end(prof, on, st);
       ++*launches;
     }
-    if (m.nedge > 0) {
+    if (m.nedge_run > 0) {
       on = prof_begin(prof, K_EDGE, st);
-      k_edge<<<blocks_for(m.nedge, 256), 256, 0, st>>>(m, y);
+      k_edge<<<blocks_for(m.nedge_run, 256), 256, 0, st>>>(m, y);
       prof_end(prof, on, st);
       ++*launches;
     }
     on = prof_begin(prof, K_MAIN, st);
-    k_elem_main<<<blocks_for(m.ne, 256), 256, 0, st>>>(m, y, ydot);
+    k_elem_main<<<blocks_for(m.ne_run, 256), 256, 0, st>>>(m, y, ydot);
     prof_end(prof, on, st);
     ++*launches;
   }
-  if (m.nr > 0) {
+  if (m.nr_run > 0) {
     on = prof_begin(prof, K_RIVER, st);
-    k_river<<<blocks_for(m.nr, 128), 128, 0, st>>>(m, y);
+    k_river<<<blocks_for(m.nr_run, 128), 128, 0, st>>>(m, y);
     prof_end(prof, on, st);
     ++*launches;
   }
-  if (m.nr + m.nbank > 0) {
+  if (m.nr_run + m.nbank_run > 0) {
     on = prof_begin(prof, K_FINISH, st);
-    k_finish<<<blocks_for((long long)m.nr + m.nbank, 128), 128, 0, st>>>(m, ydot);
+    k_finish<<<blocks_for((long long)m.nr_run + m.nbank_run, 128), 128, 0, st>>>(m, ydot);
     prof_end(prof, on, st);
     ++*launches;
   }

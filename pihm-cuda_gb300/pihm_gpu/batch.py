@@ -1,0 +1,157 @@
+"""ctypes binding of the batch engine (include/pihm_batch.h): many watersheds
+integrated together on one GPU, each bit-for-bit as the single-watershed
+path would integrate it alone."""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+
+import numpy as np
+
+from . import capi
+from .meshdesc import MeshDesc, f64p
+from .solver import BdfStats, StepControl
+
+_VP = ctypes.c_void_p
+_D = ctypes.c_double
+_I32 = ctypes.c_int32
+_I64 = ctypes.c_int64
+_F64P = ctypes.POINTER(ctypes.c_double)
+
+RUNNING, DONE, FAILED = 0, 1, 2
+
+
+class BatchLimits(ctypes.Structure):
+    _fields_ = [("max_elem", _I64), ("max_river", _I64), ("max_edge", _I64), ("max_record", _I64),
+                ("max_systems", _I32)]
+
+
+class StepControlC(ctypes.Structure):
+    _fields_ = [(n, _D) for n in ("stepsize", "reltol", "abstol", "initstep", "nncfn", "nnimax",
+                                  "nnimin", "decr", "incr", "stmin")] + [("mxstep", ctypes.c_long)]
+
+    @staticmethod
+    def of(ctrl: StepControl) -> "StepControlC":
+        c = StepControlC()
+        for f in dataclasses.fields(ctrl):
+            setattr(c, f.name, getattr(ctrl, f.name))
+        return c
+
+
+class BatchJob(ctypes.Structure):
+    _fields_ = [("mesh", ctypes.POINTER(MeshDesc)), ("elem_bc", _F64P), ("river_bc", _F64P),
+                ("y0", _F64P), ("ctrl", StepControlC), ("nsteps", _I32), ("pcpdrp", _F64P),
+                ("edir", _F64P), ("ett", _F64P), ("outlet", _I32)]
+
+
+class BatchInfo(ctypes.Structure):
+    _fields_ = [(n, _I64) for n in ("rounds", "rhs_rounds", "launches", "elem_used", "elem_hwm",
+                                    "resident")]
+
+
+def _bind(lib):
+    sig = {
+        "pihm_batch_create": ([ctypes.POINTER(BatchLimits), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                               ctypes.POINTER(_VP)], ctypes.c_int),
+        "pihm_batch_destroy": ([_VP], None),
+        "pihm_batch_set_stream": ([_VP, _VP], ctypes.c_int),
+        "pihm_batch_add": ([_VP, ctypes.POINTER(BatchJob), ctypes.POINTER(_I32)], ctypes.c_int),
+        "pihm_batch_step": ([_VP, _I32, ctypes.POINTER(_I32)], ctypes.c_int),
+        "pihm_batch_poll": ([_VP, _I32, ctypes.POINTER(_I32), ctypes.POINTER(_I32)], ctypes.c_int),
+        "pihm_batch_result": ([_VP, _I32, _F64P, _F64P, ctypes.POINTER(BdfStats), ctypes.POINTER(_I32)],
+                              ctypes.c_int),
+        "pihm_batch_release": ([_VP, _I32], ctypes.c_int),
+        "pihm_batch_get_info": ([_VP, ctypes.POINTER(BatchInfo)], ctypes.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+    return lib
+
+
+def limits_for(watersheds, nsteps: int, slack: float = 1.0) -> BatchLimits:
+    """Arena capacity holding the given watersheds at once (times slack)."""
+    ne = sum(w.nelem for w in watersheds)
+    nr = sum(w.nriver for w in watersheds)
+    lim = BatchLimits()
+    lim.max_elem = int(ne * slack) + 1
+    lim.max_river = int(nr * slack) + 1
+    lim.max_edge = int(1.6 * ne * slack) + 16
+    lim.max_record = int(nsteps * len(watersheds) * slack) + 1
+    lim.max_systems = max(1, int(len(watersheds) * slack))
+    return lim
+
+
+class Batch:
+    """A batch engine instance (pihm_batch)."""
+
+    def __init__(self, limits: BatchLimits, surf_mode: int = 2, riv_mode: int = 2,
+                 order: int = capi.ORDER_RCM):
+        self.lib = _bind(capi.load())
+        h = _VP()
+        capi._check("pihm_batch_create", self.lib.pihm_batch_create(
+            ctypes.byref(limits), surf_mode, riv_mode, order, ctypes.byref(h)))
+        self.h = h
+        self.jobs = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.pihm_batch_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def add(self, ws, y0, ctrl: StepControl, pcp, edir, ett, outlet: int = -1,
+            elem_bc=None, river_bc=None) -> int | None:
+        """Admit a watershed; None when the arena has no room for it now."""
+        keep = dict(desc=MeshDesc.from_arrays(ws.nelem, ws.nriver, ws.arrays),
+                    y0=np.ascontiguousarray(y0, np.float64), pcp=np.ascontiguousarray(pcp, np.float64),
+                    edir=np.ascontiguousarray(edir, np.float64), ett=np.ascontiguousarray(ett, np.float64),
+                    ebc=None if elem_bc is None else np.ascontiguousarray(elem_bc, np.float64),
+                    rbc=None if river_bc is None else np.ascontiguousarray(river_bc, np.float64))
+        job = BatchJob()
+        job.mesh = ctypes.pointer(keep["desc"])
+        job.elem_bc = f64p(keep["ebc"])
+        job.river_bc = f64p(keep["rbc"])
+        job.y0 = f64p(keep["y0"])
+        job.ctrl = StepControlC.of(ctrl)
+        job.nsteps = len(keep["pcp"])
+        job.pcpdrp, job.edir, job.ett = f64p(keep["pcp"]), f64p(keep["edir"]), f64p(keep["ett"])
+        job.outlet = outlet
+        i = _I32()
+        rc = self.lib.pihm_batch_add(self.h, ctypes.byref(job), ctypes.byref(i))
+        if rc == -5:  # PIHM_GPU_ERR_NOMEM: no room now
+            return None
+        capi._check("pihm_batch_add", rc)
+        self.jobs[i.value] = (ws, job.nsteps, outlet)
+        return i.value
+
+    def step(self, max_rounds: int = 0) -> int:
+        n = _I32()
+        capi._check("pihm_batch_step", self.lib.pihm_batch_step(self.h, max_rounds, ctypes.byref(n)))
+        return n.value
+
+    def poll(self, i: int):
+        st, rc = _I32(), _I32()
+        capi._check("pihm_batch_poll", self.lib.pihm_batch_poll(self.h, i, ctypes.byref(st), ctypes.byref(rc)))
+        return st.value, rc.value
+
+    def result(self, i: int):
+        ws, nsteps, outlet = self.jobs[i]
+        y = np.zeros(ws.neq)
+        q = np.zeros(nsteps if outlet >= 0 else 0)
+        stats = BdfStats()
+        done = _I32()
+        capi._check("pihm_batch_result", self.lib.pihm_batch_result(
+            self.h, i, f64p(y), f64p(q) if q.size else None, ctypes.byref(stats), ctypes.byref(done)))
+        return dict(y=y, outlet=q, stats=stats, steps_done=done.value)
+
+    def release(self, i: int):
+        capi._check("pihm_batch_release", self.lib.pihm_batch_release(self.h, i))
+        self.jobs.pop(i, None)
+
+    def info(self) -> BatchInfo:
+        inf = BatchInfo()
+        capi._check("pihm_batch_get_info", self.lib.pihm_batch_get_info(self.h, ctypes.byref(inf)))
+        return inf

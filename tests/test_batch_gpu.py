@@ -1,0 +1,141 @@
+"""Batch engine (include/pihm_batch.h) on the GPU.
+
+A watershed integrated in a batch must follow exactly the trajectory the
+single-watershed path (pihm_bdf_* over device N_Vectors with pihm_gpu_ode,
+driven by the reference's model-step loop) computes for it alone: same final
+state, same outlet flux after every model step, same solver counters, bit for
+bit -- whatever else shares the batch, whenever it was admitted and whatever
+happens to its neighbours."""
+import copy
+
+import numpy as np
+import pytest
+
+import pihm_gpu.watershed as W
+from backends import GpuBackend, step_forcing
+from pihm_gpu.batch import DONE, FAILED, RUNNING, Batch, BatchLimits, limits_for
+from pihm_gpu.solver import StepControl, run_steps
+
+pytestmark = pytest.mark.gpu
+
+
+def _case(nelem, seed, nsteps, stepsize=60):
+    nriver = max(4, int(round(100 * (nelem / 1000.0) ** 0.826)))
+    ws = W.generate(nelem, nriver, seed=seed)
+    pcp, edir, ett = step_forcing(ws, nsteps, stepsize=stepsize, seed=seed + 2)
+    # a wet start so that every branch of the right-hand side is exercised
+    y0 = W.reference_state(ws, seed=seed)
+    outlet = int(np.where(ws.arrays["down"] < 0)[0][0])
+    return dict(ws=ws, y0=y0, pcp=pcp, edir=edir, ett=ett, outlet=outlet,
+                ctrl=StepControl(stepsize=stepsize))
+
+
+def _alone(c):
+    """The single-watershed GPU path."""
+    b = GpuBackend(c["ws"], c["y0"], c["pcp"], c["edir"], c["ett"])
+    try:
+        n = len(c["pcp"])
+        r = run_steps(b, c["ctrl"], n, b.set_forcing, record_every=n, outlet=c["outlet"])
+    finally:
+        b.close()
+    return dict(y=r["states"][-1], outlet=r["outlet"], stats=r["stats"])
+
+
+def _add(batch, c):
+    return batch.add(c["ws"], c["y0"], c["ctrl"], c["pcp"], c["edir"], c["ett"], outlet=c["outlet"])
+
+
+def _same(got, want, label):
+    assert np.array_equal(got["y"], want["y"]), (
+        f"{label}: final state differs, max |d| {np.max(np.abs(got['y'] - want['y'])):.3e}")
+    assert np.array_equal(got["outlet"], want["outlet"]), f"{label}: outlet series differs"
+    gs, ws_ = got["stats"], want["stats"]
+    for k in ("nst", "nfe", "nni", "ncfn", "netf", "nli", "nfes"):
+        assert getattr(gs, k) == getattr(ws_, k), (label, k, getattr(gs, k), getattr(ws_, k))
+
+
+@pytest.fixture(scope="module")
+def cases():
+    # uneven sizes, their own soils, forcing and (for the last) model step
+    c = [_case(1000, 11, 90), _case(400, 12, 60), _case(2500, 13, 90)]
+    c[1]["ctrl"] = StepControl(stepsize=90)
+    c[1]["ws"].stepsize = 90  # the model step also caps infiltration in the right-hand side
+    c[1]["pcp"], c[1]["edir"], c[1]["ett"] = step_forcing(c[1]["ws"], 60, stepsize=90, seed=14)
+    return c
+
+
+@pytest.fixture(scope="module")
+def alone(cases):
+    return [_alone(c) for c in cases]
+
+
+def test_batch_is_bit_identical_to_the_single_watershed_path(cases, alone):
+    b = Batch(limits_for([c["ws"] for c in cases], 90))
+    ids = [_add(b, c) for c in cases]
+    assert b.step() == 0
+    for i, c, want in zip(ids, cases, alone):
+        assert b.poll(i) == (DONE, 0)
+        got = b.result(i)
+        assert got["steps_done"] == len(c["pcp"])
+        _same(got, want, f"watershed {c['ws'].nelem}")
+    inf = b.info()
+    assert inf.rounds > 0 and inf.rhs_rounds > 0
+    b.close()
+
+
+def test_alone_in_a_batch_and_in_a_mix_agree(cases, alone):
+    b = Batch(limits_for([cases[2]["ws"]], 90))
+    i = _add(b, cases[2])
+    b.step()
+    _same(b.result(i), alone[2], "batch of one")
+    b.close()
+
+
+def test_admission_by_capacity_and_reuse_of_released_ranges(cases, alone):
+    # room for the largest and the smallest watershed: with the two smaller
+    # ones resident the largest has to wait for a slot and a contiguous range
+    lim = limits_for([cases[2]["ws"], cases[1]["ws"]], 90)
+    b = Batch(lim)
+    i0, i1 = _add(b, cases[0]), _add(b, cases[1])
+    assert i0 is not None and i1 is not None
+    assert _add(b, cases[2]) is None
+    # run until one finishes, retire it, admit the waiting one mid-flight
+    while b.poll(i0)[0] == RUNNING and b.poll(i1)[0] == RUNNING:
+        b.step(max_rounds=50)
+    first = i1 if b.poll(i1)[0] == DONE else i0
+    _same(b.result(first), alone[[i0, i1].index(first)], "first finished")
+    b.release(first)
+    i2 = _add(b, cases[2])
+    if i2 is None:  # the large one needs both slots' room
+        b.step()
+        other = i0 if first == i1 else i1
+        _same(b.result(other), alone[[i0, i1].index(other)], "second finished")
+        b.release(other)
+        i2 = _add(b, cases[2])
+    assert i2 is not None
+    b.step()
+    for i in list(b.jobs):
+        idx = {i0: 0, i1: 1, i2: 2}[i]
+        _same(b.result(i), alone[idx], f"job {idx}")
+    b.close()
+
+
+def test_a_failing_watershed_does_not_disturb_the_others(cases, alone):
+    bad = dict(cases[1])
+    bad["ws"] = copy.deepcopy(cases[1]["ws"])
+    por = bad["ws"].arrays["porosity"].copy()
+    por[5] = np.nan  # the right-hand side reports NaN derivatives
+    bad["ws"].arrays["porosity"] = por
+    b = Batch(limits_for([cases[0]["ws"], cases[1]["ws"]], 90))
+    ig = _add(b, cases[0])
+    ib = _add(b, bad)
+    b.step()
+    st, rc = b.poll(ib)
+    assert st == FAILED and rc == -8  # CV_RHSFUNC_FAIL
+    _same(b.result(ig), alone[0], "healthy neighbour")
+    b.close()
+
+
+def test_limits_are_validated():
+    with pytest.raises(RuntimeError):
+        Batch(BatchLimits(max_elem=0, max_river=1, max_edge=1, max_record=1, max_systems=1))

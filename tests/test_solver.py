@@ -7,14 +7,15 @@ On the CPU, with the right-hand-side restatement over host vectors, the
 integrator reproduces the reference run step for step (same counters, same
 states, same hydrograph, bit for bit).
 
-A run at reltol 1e-4 is sensitive to the last bit of the right-hand side:
-multiplying the reference right-hand side's output by (1 +- 2^-52) changes
-the step sequence and moves the hydrograph by 2.2e-3 of its peak after
-2 days (1.5e-3 after 12 h).  The GPU right-hand side differs from the
+A run at reltol 1e-4 is sensitive to the last bit of the right-hand side.
+tests/golden/make_sensitivity.py repeats the reference run six times with
+every right-hand-side output multiplied by (1 +- 2^-52) (seeded signs): the
+step counts spread over 11518..11997 (reference 11752), the hydrograph moves
+by up to 6.2e-3 of its peak and single storages by up to 17 % of
+max(|storage|, 1 mm) after 2 days.  The GPU right-hand side differs from the
 reference's by about an ulp (pow, fused multiply-adds, reciprocals, reduction
-order), so its end-to-end run is held to that envelope: hydrograph within
-1e-2 of the peak flow, storages within 1e-2 of max(|storage|, 1 mm), and the
-same step count within 5 %."""
+order), so its end-to-end run is held to that envelope: no farther from the
+reference than twice the farthest perturbed run, in each measure."""
 import os
 
 import numpy as np
@@ -62,17 +63,38 @@ def _rel(a, b, floor=1e-5):
     return float(np.max(np.abs(a - b) / den))
 
 
+def _envelope(z):
+    """Largest deviation of the one-ulp-perturbed reference runs."""
+    e = np.load(os.path.join(GOLD, "c0_sensitivity.npz"))
+    q_ref, fin = z["outlet_q"], z["states"][-1]
+    peak = np.max(np.abs(q_ref))
+    qerr = max(np.max(np.abs(q - q_ref)) / peak for q in e["outlet"])
+    serr = max(_rel(f, fin, floor=1e-3) for f in e["final"])
+    return qerr, serr, int(e["nst"].min()), int(e["nst"].max())
+
+
+def test_sensitivity_envelope_fixture():
+    ws, z, ctrl = _golden()
+    qenv, senv, nmin, nmax = _envelope(z)
+    # the perturbed runs moved, but stayed close to the reference run
+    assert 1e-4 < qenv < 2e-2 and 1e-3 < senv < 0.5
+    assert nmin <= int(z["stats"][0]) <= nmax
+
+
 @pytest.mark.gpu
 def test_gpu_solve_hydrograph_and_storages():
     ws, z, ctrl = _golden()
     res = _run(GpuBackend, ws, z, ctrl)
     q_ref = z["outlet_q"]
+    qenv, senv, nmin, nmax = _envelope(z)
     # hydrograph: relative to the peak flow, per step
     qerr = np.max(np.abs(res["outlet"] - q_ref)) / np.max(np.abs(q_ref))
-    serr = _rel(res["states"][-1], z["states"][-1])
+    serr = _rel(res["states"][-1], z["states"][-1], floor=1e-3)
     s = res["stats"]
     print(f"GPU solve: nst {s.nst} nfe {s.nfe} (reference {z['stats'][0]} {z['stats'][1]}); "
-          f"hydrograph err {qerr:.2e}, final storage err {serr:.2e}")
-    assert qerr <= 1e-2
-    assert _rel(res["states"][-1], z["states"][-1], floor=1e-3) <= 1e-2
-    assert abs(s.nst - int(z["stats"][0])) <= 0.05 * int(z["stats"][0])
+          f"hydrograph err {qerr:.2e} (envelope {qenv:.2e}), storage err {serr:.2e} "
+          f"(envelope {senv:.2e})")
+    assert qerr <= 2 * qenv
+    assert serr <= 2 * senv
+    span = nmax - nmin
+    assert nmin - span <= s.nst <= nmax + span
