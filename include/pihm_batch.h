@@ -73,6 +73,13 @@ int pihm_batch_create(const pihm_batch_limits *lim, int surf_mode, int riv_mode,
 void pihm_batch_destroy(pihm_batch *b);
 int pihm_batch_set_stream(pihm_batch *b, void *stream);
 
+/* Scheduling: a watershed waiting for a right-hand-side evaluation is held
+ * back while others have reductions to run, until the watersheds waiting for
+ * one hold at least `gate` (0..1) of the waiting elements.  0 evaluates every
+ * request at once; 1 (the default) gathers every waiting watershed into each
+ * evaluation.  Results do not depend on it; throughput does. */
+int pihm_batch_set_rhs_gate(pihm_batch *b, double gate);
+
 /* Admit a watershed; *id receives its handle.  PIHM_GPU_ERR_NOMEM: no room now. */
 int pihm_batch_add(pihm_batch *b, const pihm_batch_job *job, int32_t *id);
 
@@ -91,12 +98,17 @@ int pihm_batch_result(pihm_batch *b, int32_t id, double *y, double *outlet, pihm
 /* Free a watershed's arena ranges (after its results have been read). */
 int pihm_batch_release(pihm_batch *b, int32_t id);
 
-/* Rounds executed, kernels launched and arena occupancy so far. */
+/* Rounds executed, kernels launched, arena occupancy and time so far:
+ * host_ms building rounds and running the integrators, wait_ms blocked on the
+ * device, and (with profiling on) the device time of the program kernel and
+ * of the right-hand-side evaluations, from CUDA events. */
 typedef struct pihm_batch_info {
     int64_t rounds, rhs_rounds, launches;
     int64_t elem_used, elem_hwm, resident;
+    double host_ms, wait_ms, program_ms, rhs_ms;
 } pihm_batch_info;
 int pihm_batch_get_info(const pihm_batch *b, pihm_batch_info *info);
+int pihm_batch_set_profiling(pihm_batch *b, int on);
 
 #ifdef __cplusplus
 }

@@ -12,6 +12,7 @@
 // step size, order, Newton and Krylov iterations, model step and stopping
 // time -- while sharing every launch.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <coroutine>
 #include <cstring>
@@ -283,10 +284,18 @@ struct pihm_batch {
   char *d_down = nullptr;
   size_t down_bytes = 0;
   unsigned int *err_sys = nullptr;
-  // counters
+  // scheduling policy
+  double rhs_gate = 1.0;
+  // counters and timing (host: building rounds and running the coroutines;
+  // wait: blocked on the device; program/rhs: device time, when profiling)
   long long rounds = 0, rhs_rounds = 0, launches = 0;
+  double host_ms = 0, wait_ms = 0, program_ms = 0, rhs_ms = 0;
+  bool profiling = false;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
 
   ~pihm_batch() {
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
     slots.clear();
     for (void *p : owned) cudaFree(p);
     if (h_up) cudaFreeHost(h_up);
@@ -442,6 +451,7 @@ void resume(Sys *s) {
 // One round: upload the programs, run them and the right-hand side, read
 // the results back and resume the watersheds that were waiting.
 int run_round(pihm_batch *B, bool *any) {
+  const auto t_start = std::chrono::steady_clock::now();
   *any = false;
   std::vector<Sys *> part;
   RoundSys *rs = (RoundSys *)(B->h_up + B->up_round_off);
@@ -450,11 +460,23 @@ int run_round(pihm_batch *B, bool *any) {
   std::memset(active, 0, B->max_sys);
   int nops = 0, nblocks = 0;
   bool rhs = false;
+  // Right-hand-side gating: a watershed that waits for an evaluation is held
+  // back while others still have reductions to run, until the waiting ones
+  // hold at least rhs_gate of the waiting elements, so that evaluations are
+  // launched over many watersheds at once.
+  int64_t el_rhs = 0, el_other = 0;
+  for (auto &up : B->slots) {
+    const Sys *s = up.get();
+    if (!s || !s->waiting) continue;
+    (s->rhs_req ? el_rhs : el_other) += s->ne;
+  }
+  const bool hold_rhs = el_other > 0 && (double)el_rhs < B->rhs_gate * (double)(el_rhs + el_other);
   for (auto &up : B->slots) {
     Sys *s = up.get();
     if (!s) continue;
     const bool waiting = (bool)s->waiting;
     if (!waiting && s->prog.empty()) continue;
+    if (waiting && s->rhs_req && hold_rhs) continue;
     RoundSys &r = rs[part.size()];
     r.sys = s->slot;
     r.prog_off = nops;
@@ -481,15 +503,29 @@ int run_round(pihm_batch *B, bool *any) {
   if (nops && cudaMemcpyAsync(B->d_up + B->up_ops_off, B->h_up + B->up_ops_off, sizeof(Op) * nops,
                               cudaMemcpyHostToDevice, st) != cudaSuccess)
     return -1;
+  if (B->profiling) cudaEventRecord(B->ev[0], st);
   if (launch_program(B->A, (int)part.size(), nblocks, st) != cudaSuccess) return -1;
   B->launches++;
+  if (B->profiling) cudaEventRecord(B->ev[1], st);
   if (rhs) {
     if (cudaMemsetAsync(B->err_sys, 0, sizeof(unsigned int) * B->max_sys, st) != cudaSuccess) return -1;
     if (launch_rhs(B->A.m, B->A.rhs_in, B->A.rhs_out, st, &B->launches, nullptr) != cudaSuccess) return -1;
     B->rhs_rounds++;
   }
+  if (B->profiling) cudaEventRecord(B->ev[2], st);
   if (cudaMemcpyAsync(B->h_down, B->d_down, B->down_bytes, cudaMemcpyDeviceToHost, st) != cudaSuccess) return -1;
+  const auto t_wait = std::chrono::steady_clock::now();
   if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
+  const auto t_done = std::chrono::steady_clock::now();
+  B->wait_ms += std::chrono::duration<double, std::milli>(t_done - t_wait).count();
+  B->host_ms += std::chrono::duration<double, std::milli>(t_wait - t_start).count();
+  if (B->profiling) {
+    float a = 0.f, b = 0.f;
+    cudaEventElapsedTime(&a, B->ev[0], B->ev[1]);
+    cudaEventElapsedTime(&b, B->ev[1], B->ev[2]);
+    B->program_ms += a;
+    B->rhs_ms += b;
+  }
   B->rounds++;
   const double *res = (const double *)B->h_down;
   const unsigned int *err = (const unsigned int *)(B->h_down + sizeof(double) * 2 * B->max_sys);
@@ -657,6 +693,12 @@ int pihm_batch_create(const pihm_batch_limits *lim, int surf_mode, int riv_mode,
 }
 
 void pihm_batch_destroy(pihm_batch *b) { delete b; }
+
+int pihm_batch_set_rhs_gate(pihm_batch *b, double gate) {
+  if (!b || !(gate >= 0.0 && gate <= 1.0)) return PIHM_GPU_ERR_ARG;
+  b->rhs_gate = gate;
+  return PIHM_GPU_OK;
+}
 
 int pihm_batch_set_stream(pihm_batch *b, void *stream) {
   if (!b) return PIHM_GPU_ERR_ARG;
@@ -828,6 +870,19 @@ int pihm_batch_get_info(const pihm_batch *B, pihm_batch_info *info) {
   info->elem_used = B->ra_elem.used();
   info->elem_hwm = B->ra_elem.hwm();
   info->resident = (int64_t)B->by_id.size();
+  info->host_ms = B->host_ms;
+  info->wait_ms = B->wait_ms;
+  info->program_ms = B->program_ms;
+  info->rhs_ms = B->rhs_ms;
+  return PIHM_GPU_OK;
+}
+
+int pihm_batch_set_profiling(pihm_batch *B, int on) {
+  if (!B) return PIHM_GPU_ERR_ARG;
+  if (on && !B->ev[0])
+    for (cudaEvent_t &e : B->ev)
+      if (cudaEventCreate(&e) != cudaSuccess) return PIHM_GPU_ERR_CUDA;
+  B->profiling = on != 0;
   return PIHM_GPU_OK;
 }
 

@@ -46,7 +46,8 @@ class BatchJob(ctypes.Structure):
 
 class BatchInfo(ctypes.Structure):
     _fields_ = [(n, _I64) for n in ("rounds", "rhs_rounds", "launches", "elem_used", "elem_hwm",
-                                    "resident")]
+                                    "resident")] + [
+        (n, _D) for n in ("host_ms", "wait_ms", "program_ms", "rhs_ms")]
 
 
 def _bind(lib):
@@ -55,6 +56,7 @@ def _bind(lib):
                                ctypes.POINTER(_VP)], ctypes.c_int),
         "pihm_batch_destroy": ([_VP], None),
         "pihm_batch_set_stream": ([_VP, _VP], ctypes.c_int),
+        "pihm_batch_set_rhs_gate": ([_VP, _D], ctypes.c_int),
         "pihm_batch_add": ([_VP, ctypes.POINTER(BatchJob), ctypes.POINTER(_I32)], ctypes.c_int),
         "pihm_batch_step": ([_VP, _I32, ctypes.POINTER(_I32)], ctypes.c_int),
         "pihm_batch_poll": ([_VP, _I32, ctypes.POINTER(_I32), ctypes.POINTER(_I32)], ctypes.c_int),
@@ -62,6 +64,7 @@ def _bind(lib):
                               ctypes.c_int),
         "pihm_batch_release": ([_VP, _I32], ctypes.c_int),
         "pihm_batch_get_info": ([_VP, ctypes.POINTER(BatchInfo)], ctypes.c_int),
+        "pihm_batch_set_profiling": ([_VP, ctypes.c_int], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -126,6 +129,12 @@ class Batch:
         capi._check("pihm_batch_add", rc)
         self.jobs[i.value] = (ws, job.nsteps, outlet)
         return i.value
+
+    def set_profiling(self, on: bool):
+        capi._check("pihm_batch_set_profiling", self.lib.pihm_batch_set_profiling(self.h, int(on)))
+
+    def set_rhs_gate(self, gate: float):
+        capi._check("pihm_batch_set_rhs_gate", self.lib.pihm_batch_set_rhs_gate(self.h, gate))
 
     def step(self, max_rounds: int = 0) -> int:
         n = _I32()
