@@ -110,6 +110,28 @@ typedef struct pihm_batch_info {
 int pihm_batch_get_info(const pihm_batch *b, pihm_batch_info *info);
 int pihm_batch_set_profiling(pihm_batch *b, int on);
 
+/* ---- serving --------------------------------------------------------------
+ * Requests are submitted with an arrival time (seconds after the start of
+ * pihm_serve_run).  From its arrival on, a request is prepared on one of
+ * `workers` host threads while the GPU keeps integrating the resident
+ * watersheds; prepared requests are admitted in arrival order as soon as the
+ * arena has room, join the rounds in flight, and are retired (results copied
+ * to the host, arena ranges freed) the moment they finish.  A request larger
+ * than the whole arena fails with PIHM_GPU_ERR_NOMEM.  Submit every request
+ * before pihm_serve_run; it returns when all have been served. */
+typedef struct pihm_serve_record {
+    int32_t status;      /* PIHM_BATCH_RUNNING (queued or resident), _DONE, _FAILED */
+    int32_t solver_rc;   /* integrator return code, or the admission error */
+    int32_t nelem;
+    double t_arrival, t_admit, t_done;  /* s from the start of pihm_serve_run; -1 if not reached */
+} pihm_serve_record;
+
+int pihm_serve_submit(pihm_batch *b, const pihm_batch_job *job, double arrival_s, int32_t *ticket);
+int pihm_serve_run(pihm_batch *b, int32_t workers);
+int pihm_serve_record_get(const pihm_batch *b, int32_t ticket, pihm_serve_record *rec);
+/* y: [neq] reference order, outlet: [nsteps] (when the job recorded one) */
+int pihm_serve_result(const pihm_batch *b, int32_t ticket, double *y, double *outlet, pihm_bdf_stats *stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -20,153 +20,14 @@
 #include <memory>
 #include <vector>
 
-#include "batch_device.h"
-#include "bdf_core.h"
-#include "mesh_image.h"
-#include "nv_select.h"
-#include "pihm_batch.h"
+#include "batch_engine.h"
 
 using namespace pihm;
 using namespace pihm::batch;
 using pihm_nv::EwCall;
 
-namespace {
-
-// First-fit allocator of index ranges in [0, cap).
-class RangeAlloc {
- public:
-  explicit RangeAlloc(int64_t cap = 0) : cap_(cap) {
-    if (cap > 0) free_[0] = cap;
-  }
-  // start of a free range of n entries, or -1
-  int64_t alloc(int64_t n) {
-    if (n <= 0) return 0;
-    for (auto it = free_.begin(); it != free_.end(); ++it) {
-      if (it->second < n) continue;
-      const int64_t start = it->first, len = it->second;
-      free_.erase(it);
-      if (len > n) free_[start + n] = len - n;
-      used_ += n;
-      return start;
-    }
-    return -1;
-  }
-  void release(int64_t start, int64_t n) {
-    if (n <= 0) return;
-    used_ -= n;
-    auto next = free_.lower_bound(start);
-    if (next != free_.end() && start + n == next->first) {
-      n += next->second;
-      next = free_.erase(next);
-    }
-    if (next != free_.begin()) {
-      auto prev = std::prev(next);
-      if (prev->first + prev->second == start) {
-        prev->second += n;
-        return;
-      }
-    }
-    free_[start] = n;
-  }
-  // one past the last allocated entry
-  int64_t hwm() const {
-    if (free_.empty()) return cap_;
-    auto last = std::prev(free_.end());
-    return (last->first + last->second == cap_) ? last->first : cap_;
-  }
-  int64_t used() const { return used_; }
-
- private:
-  int64_t cap_;
-  int64_t used_ = 0;
-  std::map<int64_t, int64_t> free_;
-};
-
-struct Sys;
-
-// The integrator's operations for one watershed of the batch: vectors are
-// slot numbers; element-wise operations are queued; reductions and the right
-// hand side suspend the calling coroutine until the round has run.
-struct BatchOps {
-  using Vec = int;
-  Sys *s = nullptr;
-  int next_slot = 1;  // slot 0 holds the model state y
-
-  int clone(int) { return next_slot < kVecSlots ? next_slot++ : -1; }
-  void destroy(int) {}
-  bool valid(int v) const { return v >= 0; }
-
-  struct Ew {
-    Sys *s;
-    bool await_ready() const noexcept;
-    void await_suspend(std::coroutine_handle<> h) const noexcept;
-    void await_resume() const noexcept {}
-  };
-  struct Red {
-    Sys *s;
-    bool await_ready() const noexcept { return false; }
-    void await_suspend(std::coroutine_handle<> h) const noexcept;
-    double await_resume() const noexcept;
-  };
-  struct Rhs {
-    Sys *s;
-    bool await_ready() const noexcept { return false; }
-    void await_suspend(std::coroutine_handle<> h) const noexcept;
-    int await_resume() const noexcept;
-  };
-
-  Ew push(int code, double a, double b, int x, int y, int z, double c = 0.0, int i0 = 0, int i1 = 0);
-  Ew push(const EwCall<int> &e) { return push(e.op, e.a, e.b, e.x, e.y, e.z); }
-  Red reduce(int red, int x, int y, bool wrms);
-
-  Ew linear_sum(double a, int x, double b, int y, int z) {
-    return push(pihm_nv::select_linear_sum<int>(a, x, b, y, z));
-  }
-  Ew const_(double c, int z) { return push(pihm_nv::EW_CONST, c, 0.0, z, z, z); }
-  Ew scale(double c, int x, int z) { return push(pihm_nv::select_scale<int>(c, x, z)); }
-  Ew abs_(int x, int z) { return push(pihm_nv::EW_ABS, 0.0, 0.0, x, x, z); }
-  Ew inv(int x, int z) { return push(pihm_nv::EW_INV, 0.0, 0.0, x, x, z); }
-  Ew div(int x, int y, int z) { return push(pihm_nv::EW_DIV, 0.0, 0.0, x, y, z); }
-  Ew prod(int x, int y, int z) { return push(pihm_nv::EW_PROD, 0.0, 0.0, x, y, z); }
-  Ew addconst(int x, double b, int z) { return push(pihm_nv::EW_ADDCONST, 0.0, b, x, x, z); }
-  Red dot(int x, int y) { return reduce(pihm_nv::R_DOT, x, y, false); }
-  Red maxnorm(int x) { return reduce(pihm_nv::R_MAXABS, x, x, false); }
-  Red wrms(int x, int w) { return reduce(pihm_nv::R_WSQ, x, w, true); }
-  Red vmin(int x) { return reduce(pihm_nv::R_MIN, x, x, false); }
-  Rhs rhs(double t, int y, int ydot);
-  // model-step operations
-  Ew forcing(double pcp, double edir, double ett) { return push(OP_FORCING, pcp, edir, 0, 0, 0, ett); }
-  Ew post_step(int y) { return push(OP_WS0, 0.0, 0.0, y, y, y); }
-  Ew record(int k, int seg) { return push(OP_RECORD, 0.0, 0.0, 0, 0, 0, 0.0, k, seg); }
-};
-
-enum SysState { S_NEW = 0, S_RUNNING, S_DONE, S_FAILED };
-
-struct Sys {
-  int32_t id = -1, slot = -1;
-  // arena ranges
-  int64_t eoff = 0, roff = 0, edoff = 0, boff = 0, upoff = 0, soff = 0, recoff = 0;
-  int32_t ne = 0, nr = 0, nedge = 0, nbank = 0, nup = 0, nrec = 0;
-  int64_t neq = 0;
-  std::vector<int32_t> perm;
-  // job
-  pihm_step_control ctrl{};
-  int32_t nsteps = 0, outlet = -1, steps_done = 0;
-  std::vector<double> pcp, edir, ett;
-  // integrator and its coroutine
-  bdf::BdfCore<BatchOps> core;
-  std::unique_ptr<Task<int>> task;
-  std::coroutine_handle<> waiting{};
-  int state = S_NEW, solver_rc = 0;
-  // the program of the current round
-  std::vector<Op> prog;
-  int red = -1;
-  uint8_t rx = 0, ry = 0;
-  bool red_wrms = false, rhs_req = false, rhs_pending_out = false;
-  uint8_t rhs_out = 0;
-  double red_value = 0.0;
-  int rhs_rc = 0;
-};
+namespace pihm {
+namespace batch {
 
 bool BatchOps::Ew::await_ready() const noexcept { return (int)s->prog.size() < kMaxProgOps; }
 void BatchOps::Ew::await_suspend(std::coroutine_handle<> h) const noexcept { s->waiting = h; }
@@ -262,53 +123,9 @@ T *dalloc(size_t n, std::vector<void *> &owned) {
   return (T *)p;
 }
 
-}  // namespace
+}  // namespace batch
+}  // namespace pihm
 
-struct pihm_batch {
-  DeviceArena A{};
-  cudaStream_t st = nullptr;
-  std::vector<void *> owned;
-  int64_t ne_cap = 0, nr_cap = 0, ned_cap = 0, rec_cap = 0;
-  int max_sys = 0;
-  int order = PIHM_GPU_ORDER_RCM;
-  RangeAlloc ra_elem, ra_riv, ra_edge, ra_bank, ra_up, ra_state, ra_rec;
-  std::vector<std::unique_ptr<Sys>> slots;  // [max_sys]
-  std::map<int32_t, Sys *> by_id;
-  int32_t next_id = 0;
-  // per-round upload: active flags, then the round list, then the ops
-  char *h_up = nullptr;
-  char *d_up = nullptr;
-  size_t up_active_bytes = 0, up_round_off = 0, up_ops_off = 0;
-  // per-round download: results [max_sys][2], then error words [max_sys]
-  char *h_down = nullptr;
-  char *d_down = nullptr;
-  size_t down_bytes = 0;
-  unsigned int *err_sys = nullptr;
-  // scheduling policy
-  double rhs_gate = 1.0;
-  // counters and timing (host: building rounds and running the coroutines;
-  // wait: blocked on the device; program/rhs: device time, when profiling)
-  long long rounds = 0, rhs_rounds = 0, launches = 0;
-  double host_ms = 0, wait_ms = 0, program_ms = 0, rhs_ms = 0;
-  bool profiling = false;
-  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
-
-  ~pihm_batch() {
-    for (cudaEvent_t e : ev)
-      if (e) cudaEventDestroy(e);
-    slots.clear();
-    for (void *p : owned) cudaFree(p);
-    if (h_up) cudaFreeHost(h_up);
-    if (h_down) cudaFreeHost(h_down);
-  }
-
-  void update_extents() {
-    A.m.ne_run = (int32_t)ra_elem.hwm();
-    A.m.nr_run = (int32_t)ra_riv.hwm();
-    A.m.nedge_run = (int32_t)ra_edge.hwm();
-    A.m.nbank_run = (int32_t)ra_bank.hwm();
-  }
-};
 
 namespace {
 
@@ -319,7 +136,8 @@ int h2d(T *dst, const T *src, size_t n, cudaStream_t st) {
 }
 
 // Translate a watershed image's indices to its arena ranges and upload it.
-int place(pihm_batch *B, Sys *s, const SystemImage &im, const pihm_batch_job *job) {
+int place(pihm_batch *B, Sys *s, const Prepared &job) {
+  const SystemImage &im = job.im;
   DevMesh &m = B->A.m;
   cudaStream_t st = B->st;
   const int ne = im.ne, nr = im.nr;
@@ -380,12 +198,12 @@ int place(pihm_batch *B, Sys *s, const SystemImage &im, const pihm_batch_job *jo
   for (int k = 0; k < RP_COUNT; k++) rc |= h2d((double *)(m.*kRiverMember[k]) + ro, im.rv[k].data(), nr, st);
   // boundary conditions (reference order in the job)
   std::vector<double> bc(3 * (size_t)ne, 0.0);
-  if (job->elem_bc)
+  if (!job.elem_bc.empty())
     for (int j = 0; j < 3; j++)
-      for (int i = 0; i < ne; i++) bc[(size_t)j * ne + i] = job->elem_bc[3 * (size_t)im.perm[i] + j];
+      for (int i = 0; i < ne; i++) bc[(size_t)j * ne + i] = job.elem_bc[3 * (size_t)im.perm[i] + j];
   for (int j = 0; j < 3; j++) rc |= h2d((double *)m.elem_bc + j * NE + eo, bc.data() + (size_t)j * ne, ne, st);
   std::vector<double> rbc(nr, 0.0);
-  if (job->river_bc) std::copy(job->river_bc, job->river_bc + nr, rbc.begin());
+  if (!job.river_bc.empty()) std::copy(job.river_bc.begin(), job.river_bc.end(), rbc.begin());
   rc |= h2d((double *)m.river_bc + ro, rbc.data(), nr, st);
   // a fresh watershed carries no river-edge flux from an earlier evaluation
   for (int k = 0; k < NUM_RIVFLX; k++)
@@ -397,13 +215,13 @@ int place(pihm_batch *B, Sys *s, const SystemImage &im, const pihm_batch_job *jo
   rc |= h2d((int32_t *)m.sys_riv + ro, own.data(), nr, st);
   rc |= h2d((int32_t *)m.sys_edge + edo, own.data(), im.nedge, st);
   rc |= h2d((int32_t *)m.sys_bank + bo, own.data(), im.nbank, st);
-  const double dt = job->ctrl.stepsize;
+  const double dt = job.ctrl.stepsize;
   rc |= h2d((double *)m.sys_dt + s->slot, &dt, 1, st);
   // initial state, internal order, into vector slot 0
   std::vector<double> y(s->neq);
   for (int p = 0; p < 3; p++)
-    for (int i = 0; i < ne; i++) y[(size_t)p * ne + i] = job->y0[(size_t)p * ne + im.perm[i]];
-  for (int64_t q = 3LL * ne; q < s->neq; q++) y[q] = job->y0[q];
+    for (int i = 0; i < ne; i++) y[(size_t)p * ne + i] = job.y0[(size_t)p * ne + im.perm[i]];
+  for (int64_t q = 3LL * ne; q < s->neq; q++) y[q] = job.y0[q];
   rc |= h2d(B->A.vec + s->soff, y.data(), s->neq, st);
   SysInfo info{};
   info.off = s->soff;
@@ -418,6 +236,11 @@ int place(pihm_batch *B, Sys *s, const SystemImage &im, const pihm_batch_job *jo
   if (cudaStreamSynchronize(st) != cudaSuccess) rc = -1;
   return rc ? PIHM_GPU_ERR_CUDA : PIHM_GPU_OK;
 }
+
+}  // namespace
+
+namespace pihm {
+namespace batch {
 
 void free_ranges(pihm_batch *B, Sys *s) {
   DevMesh &m = B->A.m;
@@ -447,6 +270,98 @@ void resume(Sys *s) {
     s->state = (s->solver_rc < 0) ? S_FAILED : S_DONE;
   }
 }
+
+
+// Validate a job and build everything the arena needs from it on the host.
+int prepare(const pihm_batch_job *job, int surf_mode, int riv_mode, int order, Prepared *p) {
+  if (!job || !job->mesh || !job->y0 || !p || job->nsteps < 0 ||
+      (job->nsteps > 0 && (!job->pcpdrp || !job->edir || !job->ett)))
+    return PIHM_GPU_ERR_ARG;
+  const pihm_step_control &c = job->ctrl;
+  if (!(c.stepsize > 0.0) || c.reltol < 0 || c.abstol < 0 || !(c.decr > 0.0)) return PIHM_GPU_ERR_ARG;
+  if (job->outlet >= job->mesh->nriver) return PIHM_GPU_ERR_ARG;
+  const int brc = build_image(job->mesh, surf_mode, riv_mode, c.stepsize, order, &p->im);
+  if (brc != PIHM_GPU_OK) return brc;
+  const int ne = p->im.ne, nr = p->im.nr;
+  const size_t neq = 3 * (size_t)ne + 2 * (size_t)nr;
+  p->y0.assign(job->y0, job->y0 + neq);
+  if (job->elem_bc) p->elem_bc.assign(job->elem_bc, job->elem_bc + 3 * (size_t)ne);
+  if (job->river_bc) p->river_bc.assign(job->river_bc, job->river_bc + nr);
+  p->pcp.assign(job->pcpdrp, job->pcpdrp + job->nsteps);
+  p->edir.assign(job->edir, job->edir + job->nsteps);
+  p->ett.assign(job->ett, job->ett + job->nsteps);
+  p->ctrl = c;
+  p->nsteps = job->nsteps;
+  p->outlet = job->outlet;
+  return PIHM_GPU_OK;
+}
+
+// Reserve arena ranges for a prepared job, upload it and start its model
+// loop.  PIHM_GPU_ERR_NOMEM when it does not fit now.
+int admit(pihm_batch *B, const Prepared &p, int32_t *id) {
+  const SystemImage &im = p.im;
+  int slot = -1;
+  for (int k = 0; k < B->max_sys; k++)
+    if (!B->slots[k]) {
+      slot = k;
+      break;
+    }
+  if (slot < 0) return PIHM_GPU_ERR_NOMEM;
+  auto s = std::make_unique<Sys>();
+  s->slot = slot;
+  s->ne = im.ne;
+  s->nr = im.nr;
+  s->nedge = im.nedge;
+  s->nbank = im.nbank;
+  s->nup = (int32_t)im.up_idx.size();
+  s->neq = 3LL * im.ne + 2LL * im.nr;
+  s->nrec = p.outlet >= 0 ? p.nsteps : 0;
+  // admission: every range must fit now
+  struct Want {
+    RangeAlloc *ra;
+    int64_t n, *off;
+  } want[] = {{&B->ra_elem, s->ne, &s->eoff},   {&B->ra_riv, s->nr, &s->roff},
+              {&B->ra_edge, s->nedge, &s->edoff}, {&B->ra_bank, s->nbank, &s->boff},
+              {&B->ra_up, s->nup, &s->upoff},   {&B->ra_state, s->neq, &s->soff},
+              {&B->ra_rec, s->nrec, &s->recoff}};
+  int got = 0;
+  for (; got < 7; got++) {
+    const int64_t off = want[got].ra->alloc(want[got].n);
+    if (off < 0) break;
+    *want[got].off = off;
+  }
+  if (got < 7) {
+    for (int k = 0; k < got; k++) want[k].ra->release(*want[k].off, want[k].n);
+    return PIHM_GPU_ERR_NOMEM;
+  }
+  s->perm = im.perm;
+  s->ctrl = p.ctrl;
+  s->nsteps = p.nsteps;
+  s->outlet = p.outlet;
+  s->pcp = p.pcp;
+  s->edir = p.edir;
+  s->ett = p.ett;
+  s->core.ops.s = s.get();
+  Sys *sp = s.get();
+  B->slots[slot] = std::move(s);
+  const int prc = place(B, sp, p);
+  if (prc != PIHM_GPU_OK) {
+    free_ranges(B, sp);
+    B->slots[slot].reset();
+    return prc;
+  }
+  B->update_extents();
+  sp->id = B->next_id++;
+  B->by_id[sp->id] = sp;
+  // start the model loop: it runs until its first device operation
+  sp->task = std::make_unique<Task<int>>(model_run(sp));
+  sp->state = S_RUNNING;
+  sp->waiting = sp->task->handle();
+  resume(sp);
+  *id = sp->id;
+  return PIHM_GPU_OK;
+}
+
 
 // One round: upload the programs, run them and the right-hand side, read
 // the results back and resume the watersheds that were waiting.
@@ -552,7 +467,42 @@ int run_round(pihm_batch *B, bool *any) {
   return 0;
 }
 
-}  // namespace
+int read_result(pihm_batch *B, Sys *s, double *y, double *outlet, pihm_bdf_stats *stats) {
+  if (y) {
+    std::vector<double> yi(s->neq);
+    if (cudaMemcpy(yi.data(), B->A.vec + s->soff, sizeof(double) * s->neq, cudaMemcpyDeviceToHost) != cudaSuccess)
+      return PIHM_GPU_ERR_CUDA;
+    const int ne = s->ne;
+    for (int p = 0; p < 3; p++)
+      for (int i = 0; i < ne; i++) y[(size_t)p * ne + s->perm[i]] = yi[(size_t)p * ne + i];
+    for (int64_t q = 3LL * ne; q < s->neq; q++) y[q] = yi[q];
+  }
+  if (outlet && s->nrec > 0 &&
+      cudaMemcpy(outlet, B->A.rec + s->recoff, sizeof(double) * s->nrec, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return PIHM_GPU_ERR_CUDA;
+  if (stats) {
+    const bdf::Stats st = s->core.stats();
+    stats->nst = st.nst;
+    stats->nfe = st.nfe;
+    stats->nni = st.nni;
+    stats->ncfn = st.ncfn;
+    stats->netf = st.netf;
+    stats->nli = st.nli;
+    stats->nfes = st.nfes;
+    stats->njtimes = st.njtimes;
+    stats->ncfl = st.ncfl;
+    stats->nor = st.nor;
+    stats->qlast = st.qlast;
+    stats->qcur = st.qcur;
+    stats->hlast = st.hlast;
+    stats->hcur = st.hcur;
+    stats->tcur = st.tcur;
+  }
+  return PIHM_GPU_OK;
+}
+
+}  // namespace batch
+}  // namespace pihm
 
 extern "C" {
 
@@ -707,75 +657,11 @@ int pihm_batch_set_stream(pihm_batch *b, void *stream) {
 }
 
 int pihm_batch_add(pihm_batch *B, const pihm_batch_job *job, int32_t *id) {
-  if (!B || !job || !job->mesh || !job->y0 || !id || job->nsteps < 0 ||
-      (job->nsteps > 0 && (!job->pcpdrp || !job->edir || !job->ett)))
-    return PIHM_GPU_ERR_ARG;
-  const pihm_step_control &c = job->ctrl;
-  if (!(c.stepsize > 0.0) || c.reltol < 0 || c.abstol < 0 || !(c.decr > 0.0)) return PIHM_GPU_ERR_ARG;
-  if (job->outlet >= job->mesh->nriver) return PIHM_GPU_ERR_ARG;
-  SystemImage im;
-  const int brc = build_image(job->mesh, B->A.m.surf_mode, B->A.m.riv_mode, c.stepsize, B->order, &im);
-  if (brc != PIHM_GPU_OK) return brc;
-  int slot = -1;
-  for (int k = 0; k < B->max_sys; k++)
-    if (!B->slots[k]) {
-      slot = k;
-      break;
-    }
-  if (slot < 0) return PIHM_GPU_ERR_NOMEM;
-  auto s = std::make_unique<Sys>();
-  s->slot = slot;
-  s->ne = im.ne;
-  s->nr = im.nr;
-  s->nedge = im.nedge;
-  s->nbank = im.nbank;
-  s->nup = (int32_t)im.up_idx.size();
-  s->neq = 3LL * im.ne + 2LL * im.nr;
-  s->nrec = job->outlet >= 0 ? job->nsteps : 0;
-  // admission: every range must fit now
-  struct Want {
-    RangeAlloc *ra;
-    int64_t n, *off;
-  } want[] = {{&B->ra_elem, s->ne, &s->eoff},   {&B->ra_riv, s->nr, &s->roff},
-              {&B->ra_edge, s->nedge, &s->edoff}, {&B->ra_bank, s->nbank, &s->boff},
-              {&B->ra_up, s->nup, &s->upoff},   {&B->ra_state, s->neq, &s->soff},
-              {&B->ra_rec, s->nrec, &s->recoff}};
-  int got = 0;
-  for (; got < 7; got++) {
-    const int64_t off = want[got].ra->alloc(want[got].n);
-    if (off < 0) break;
-    *want[got].off = off;
-  }
-  if (got < 7) {
-    for (int k = 0; k < got; k++) want[k].ra->release(*want[k].off, want[k].n);
-    return PIHM_GPU_ERR_NOMEM;
-  }
-  s->perm = im.perm;
-  s->ctrl = c;
-  s->nsteps = job->nsteps;
-  s->outlet = job->outlet;
-  s->pcp.assign(job->pcpdrp, job->pcpdrp + job->nsteps);
-  s->edir.assign(job->edir, job->edir + job->nsteps);
-  s->ett.assign(job->ett, job->ett + job->nsteps);
-  s->core.ops.s = s.get();
-  Sys *sp = s.get();
-  B->slots[slot] = std::move(s);
-  const int prc = place(B, sp, im, job);
-  if (prc != PIHM_GPU_OK) {
-    free_ranges(B, sp);
-    B->slots[slot].reset();
-    return prc;
-  }
-  B->update_extents();
-  sp->id = B->next_id++;
-  B->by_id[sp->id] = sp;
-  // start the model loop: it runs until its first device operation
-  sp->task = std::make_unique<Task<int>>(model_run(sp));
-  sp->state = S_RUNNING;
-  sp->waiting = sp->task->handle();
-  resume(sp);
-  *id = sp->id;
-  return PIHM_GPU_OK;
+  if (!B || !id) return PIHM_GPU_ERR_ARG;
+  Prepared p;
+  const int rc = prepare(job, B->A.m.surf_mode, B->A.m.riv_mode, B->order, &p);
+  if (rc != PIHM_GPU_OK) return rc;
+  return admit(B, p, id);
 }
 
 int pihm_batch_step(pihm_batch *B, int32_t max_rounds, int32_t *running) {
@@ -815,36 +701,8 @@ int pihm_batch_result(pihm_batch *B, int32_t id, double *y, double *outlet, pihm
   if (it == B->by_id.end()) return PIHM_GPU_ERR_ARG;
   Sys *s = it->second;
   if (s->state == S_RUNNING || !s->prog.empty()) return PIHM_GPU_ERR_ARG;
-  if (y) {
-    std::vector<double> yi(s->neq);
-    if (cudaMemcpy(yi.data(), B->A.vec + s->soff, sizeof(double) * s->neq, cudaMemcpyDeviceToHost) != cudaSuccess)
-      return PIHM_GPU_ERR_CUDA;
-    const int ne = s->ne;
-    for (int p = 0; p < 3; p++)
-      for (int i = 0; i < ne; i++) y[(size_t)p * ne + s->perm[i]] = yi[(size_t)p * ne + i];
-    for (int64_t q = 3LL * ne; q < s->neq; q++) y[q] = yi[q];
-  }
-  if (outlet && s->nrec > 0 &&
-      cudaMemcpy(outlet, B->A.rec + s->recoff, sizeof(double) * s->nrec, cudaMemcpyDeviceToHost) != cudaSuccess)
-    return PIHM_GPU_ERR_CUDA;
-  if (stats) {
-    const bdf::Stats st = s->core.stats();
-    stats->nst = st.nst;
-    stats->nfe = st.nfe;
-    stats->nni = st.nni;
-    stats->ncfn = st.ncfn;
-    stats->netf = st.netf;
-    stats->nli = st.nli;
-    stats->nfes = st.nfes;
-    stats->njtimes = st.njtimes;
-    stats->ncfl = st.ncfl;
-    stats->nor = st.nor;
-    stats->qlast = st.qlast;
-    stats->qcur = st.qcur;
-    stats->hlast = st.hlast;
-    stats->hcur = st.hcur;
-    stats->tcur = st.tcur;
-  }
+  const int rc = read_result(B, s, y, outlet, stats);
+  if (rc != PIHM_GPU_OK) return rc;
   if (steps_done) *steps_done = s->steps_done;
   return PIHM_GPU_OK;
 }

@@ -50,6 +50,30 @@ class BatchInfo(ctypes.Structure):
         (n, _D) for n in ("host_ms", "wait_ms", "program_ms", "rhs_ms")]
 
 
+class ServeRecord(ctypes.Structure):
+    _fields_ = [("status", _I32), ("solver_rc", _I32), ("nelem", _I32), ("t_arrival", _D),
+                ("t_admit", _D), ("t_done", _D)]
+
+
+def _job(ws, y0, ctrl, pcp, edir, ett, outlet, elem_bc, river_bc):
+    """A BatchJob and the arrays it points at (keep both alive)."""
+    keep = dict(desc=MeshDesc.from_arrays(ws.nelem, ws.nriver, ws.arrays),
+                y0=np.ascontiguousarray(y0, np.float64), pcp=np.ascontiguousarray(pcp, np.float64),
+                edir=np.ascontiguousarray(edir, np.float64), ett=np.ascontiguousarray(ett, np.float64),
+                ebc=None if elem_bc is None else np.ascontiguousarray(elem_bc, np.float64),
+                rbc=None if river_bc is None else np.ascontiguousarray(river_bc, np.float64))
+    job = BatchJob()
+    job.mesh = ctypes.pointer(keep["desc"])
+    job.elem_bc = f64p(keep["ebc"])
+    job.river_bc = f64p(keep["rbc"])
+    job.y0 = f64p(keep["y0"])
+    job.ctrl = StepControlC.of(ctrl)
+    job.nsteps = len(keep["pcp"])
+    job.pcpdrp, job.edir, job.ett = f64p(keep["pcp"]), f64p(keep["edir"]), f64p(keep["ett"])
+    job.outlet = outlet
+    return job, keep
+
+
 def _bind(lib):
     sig = {
         "pihm_batch_create": ([ctypes.POINTER(BatchLimits), ctypes.c_int, ctypes.c_int, ctypes.c_int,
@@ -65,6 +89,10 @@ def _bind(lib):
         "pihm_batch_release": ([_VP, _I32], ctypes.c_int),
         "pihm_batch_get_info": ([_VP, ctypes.POINTER(BatchInfo)], ctypes.c_int),
         "pihm_batch_set_profiling": ([_VP, ctypes.c_int], ctypes.c_int),
+        "pihm_serve_submit": ([_VP, ctypes.POINTER(BatchJob), _D, ctypes.POINTER(_I32)], ctypes.c_int),
+        "pihm_serve_run": ([_VP, _I32], ctypes.c_int),
+        "pihm_serve_record_get": ([_VP, _I32, ctypes.POINTER(ServeRecord)], ctypes.c_int),
+        "pihm_serve_result": ([_VP, _I32, _F64P, _F64P, ctypes.POINTER(BdfStats)], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -97,6 +125,7 @@ class Batch:
             ctypes.byref(limits), surf_mode, riv_mode, order, ctypes.byref(h)))
         self.h = h
         self.jobs = {}
+        self.requests = {}
 
     def close(self):
         if getattr(self, "h", None):
@@ -108,20 +137,7 @@ class Batch:
     def add(self, ws, y0, ctrl: StepControl, pcp, edir, ett, outlet: int = -1,
             elem_bc=None, river_bc=None) -> int | None:
         """Admit a watershed; None when the arena has no room for it now."""
-        keep = dict(desc=MeshDesc.from_arrays(ws.nelem, ws.nriver, ws.arrays),
-                    y0=np.ascontiguousarray(y0, np.float64), pcp=np.ascontiguousarray(pcp, np.float64),
-                    edir=np.ascontiguousarray(edir, np.float64), ett=np.ascontiguousarray(ett, np.float64),
-                    ebc=None if elem_bc is None else np.ascontiguousarray(elem_bc, np.float64),
-                    rbc=None if river_bc is None else np.ascontiguousarray(river_bc, np.float64))
-        job = BatchJob()
-        job.mesh = ctypes.pointer(keep["desc"])
-        job.elem_bc = f64p(keep["ebc"])
-        job.river_bc = f64p(keep["rbc"])
-        job.y0 = f64p(keep["y0"])
-        job.ctrl = StepControlC.of(ctrl)
-        job.nsteps = len(keep["pcp"])
-        job.pcpdrp, job.edir, job.ett = f64p(keep["pcp"]), f64p(keep["edir"]), f64p(keep["ett"])
-        job.outlet = outlet
+        job, keep = _job(ws, y0, ctrl, pcp, edir, ett, outlet, elem_bc, river_bc)
         i = _I32()
         rc = self.lib.pihm_batch_add(self.h, ctypes.byref(job), ctypes.byref(i))
         if rc == -5:  # PIHM_GPU_ERR_NOMEM: no room now
@@ -164,3 +180,32 @@ class Batch:
         inf = BatchInfo()
         capi._check("pihm_batch_get_info", self.lib.pihm_batch_get_info(self.h, ctypes.byref(inf)))
         return inf
+
+    # ---- serving ----------------------------------------------------------
+    def submit(self, ws, y0, ctrl: StepControl, pcp, edir, ett, arrival: float, outlet: int = -1,
+               elem_bc=None, river_bc=None) -> int:
+        """Queue a request arriving `arrival` seconds after serve() starts."""
+        job, keep = _job(ws, y0, ctrl, pcp, edir, ett, outlet, elem_bc, river_bc)
+        t = _I32()
+        capi._check("pihm_serve_submit", self.lib.pihm_serve_submit(self.h, ctypes.byref(job), float(arrival),
+                                                                     ctypes.byref(t)))
+        self.requests[t.value] = (ws, job.nsteps, outlet)
+        return t.value
+
+    def serve(self, workers: int = 4):
+        """Serve every submitted request (returns when all are finished)."""
+        capi._check("pihm_serve_run", self.lib.pihm_serve_run(self.h, workers))
+
+    def record(self, ticket: int) -> ServeRecord:
+        r = ServeRecord()
+        capi._check("pihm_serve_record_get", self.lib.pihm_serve_record_get(self.h, ticket, ctypes.byref(r)))
+        return r
+
+    def served(self, ticket: int):
+        ws, nsteps, outlet = self.requests[ticket]
+        y = np.zeros(ws.neq)
+        q = np.zeros(nsteps if outlet >= 0 else 0)
+        stats = BdfStats()
+        capi._check("pihm_serve_result", self.lib.pihm_serve_result(
+            self.h, ticket, f64p(y), f64p(q) if q.size else None, ctypes.byref(stats)))
+        return dict(y=y, outlet=q, stats=stats)

@@ -139,3 +139,34 @@ def test_a_failing_watershed_does_not_disturb_the_others(cases, alone):
 def test_limits_are_validated():
     with pytest.raises(RuntimeError):
         Batch(BatchLimits(max_elem=0, max_river=1, max_edge=1, max_record=1, max_systems=1))
+
+
+def _submit(b, c, arrival):
+    return b.submit(c["ws"], c["y0"], c["ctrl"], c["pcp"], c["edir"], c["ett"], arrival=arrival,
+                    outlet=c["outlet"])
+
+
+def test_served_requests_match_their_solo_runs(cases, alone):
+    # room for about two at a time: requests queue, join the rounds in
+    # flight as others retire, and each still computes its solo trajectory
+    b = Batch(limits_for([cases[2]["ws"], cases[1]["ws"]], 90))
+    plan = [(0, 0.0), (1, 0.001), (2, 0.002), (0, 0.02), (1, 0.03)]
+    tickets = [_submit(b, cases[i], t) for i, t in plan]
+    b.serve(workers=2)
+    for tk, (i, t) in zip(tickets, plan):
+        r = b.record(tk)
+        assert r.status == DONE and r.solver_rc == 0, (tk, r.status, r.solver_rc)
+        assert r.t_arrival == t and r.t_admit >= r.t_arrival and r.t_done >= r.t_admit
+        _same(b.served(tk), alone[i], f"request {tk}")
+    b.close()
+
+
+def test_serving_fails_a_request_larger_than_the_arena(cases, alone):
+    b = Batch(limits_for([cases[0]["ws"]], 90))
+    big = _submit(b, cases[2], 0.0)
+    ok = _submit(b, cases[0], 0.0)
+    b.serve(workers=1)
+    assert b.record(big).status == FAILED and b.record(big).solver_rc == -5  # PIHM_GPU_ERR_NOMEM
+    assert b.record(ok).status == DONE
+    _same(b.served(ok), alone[0], "request behind a rejected one")
+    b.close()
