@@ -185,6 +185,128 @@ def run_reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+BATCH_N, BATCH_LO, BATCH_HI, BATCH_STEPS, BATCH_SEQ_SAMPLE = 256, 2000, 200000, 10, 32
+SERVE_N, SERVE_LO, SERVE_HI, SERVE_STEPS, SERVE_LOAD = 48, 1000, 500000, 10, 0.8
+SERVE_ARENA_ELEM, SERVE_MAX_REQ = 3_000_000, 64
+
+
+def _pct(a, q):
+    import numpy as np
+    return float(np.percentile(np.asarray(a), q)) if len(a) else None
+
+
+def bench_batched():
+    """256 watersheds integrated together vs one by one through the plain path."""
+    import numpy as np
+    import torch
+    from pihm_gpu import workloads as WL
+    from pihm_gpu.batch import Batch, limits_for
+    from pihm_gpu.single import solve_alone
+    t = time.perf_counter()
+    cases = WL.make_cases(WL.batched_specs(BATCH_N, BATCH_LO, BATCH_HI, BATCH_STEPS))
+    gen_s = time.perf_counter() - t
+    torch.cuda.synchronize()
+    b = Batch(limits_for([c["ws"] for c in cases], BATCH_STEPS))
+    t0 = time.perf_counter()
+    ids = b.add_many(cases, threads=min(16, os.cpu_count() or 1))
+    assert all(i is not None for i in ids)
+    t1 = time.perf_counter()
+    b.step()
+    t2 = time.perf_counter()
+    res = [b.result(i) for i in ids]
+    t3 = time.perf_counter()
+    inf = b.info()
+    b.close()
+    evals = sum(c["ws"].nelem * (r["stats"].nfe + r["stats"].nfes) for c, r in zip(cases, res))
+    sizes = np.array([c["ws"].nelem for c in cases])
+    pick = np.argsort(sizes)[np.linspace(0, BATCH_N - 1, BATCH_SEQ_SAMPLE).astype(int)]
+    seq_s, same = 0.0, 0
+    for k in pick:
+        ts = time.perf_counter()
+        r = solve_alone(cases[k])
+        seq_s += time.perf_counter() - ts
+        same += int(np.array_equal(r["y"], res[k]["y"]) and np.array_equal(r["outlet"], res[k]["outlet"]))
+    seq_all = seq_s * BATCH_N / len(pick)
+    return {
+        "metric": "batched solves/s", "unit": "solves/s",
+        "value": BATCH_N / (t2 - t1), "e2e_value": BATCH_N / (t3 - t0),
+        "workload": f"{BATCH_N} watersheds, {int(sizes.sum())} elements (log-uniform {BATCH_LO}..{BATCH_HI}), "
+                    f"{BATCH_STEPS} model steps of 60 s each from RelaxIc",
+        "solve_s": t2 - t1, "admit_s": t1 - t0, "readback_s": t3 - t2, "generate_s": gen_s,
+        "elem_evals_per_s": evals / (t2 - t1), "rounds": inf.rounds, "rhs_rounds": inf.rhs_rounds,
+        "gpu_launches": inf.launches,
+        "sequential": {"value": BATCH_N / seq_all, "unit": "solves/s",
+                       "sample": f"{len(pick)} of {BATCH_N} watersheds stratified by size, plain path "
+                                 f"(create, solve, read back), {seq_s:.2f} s, scaled to all"},
+        "speedup_e2e": (BATCH_N / (t3 - t0)) / (BATCH_N / seq_all),
+        "bit_identical_to_plain_path": f"{same}/{len(pick)}",
+    }
+
+
+def bench_serving():
+    """Poisson stream of calibration requests at SERVE_LOAD of measured capacity."""
+    import numpy as np
+    import torch
+    from pihm_gpu import workloads as WL
+    from pihm_gpu.batch import DONE, Batch, BatchLimits
+    from pihm_gpu.single import solve_alone
+    t = time.perf_counter()
+    cases = WL.make_cases(WL.serving_specs(SERVE_N, SERVE_LO, SERVE_HI, SERVE_STEPS))
+    gen_s = time.perf_counter() - t
+
+    def limits():
+        lim = BatchLimits()
+        lim.max_elem = SERVE_ARENA_ELEM
+        lim.max_river = SERVE_ARENA_ELEM // 10 + 16
+        lim.max_edge = int(1.6 * SERVE_ARENA_ELEM) + 16
+        lim.max_record = SERVE_N * SERVE_STEPS
+        lim.max_systems = SERVE_MAX_REQ
+        return lim
+
+    def serve(arrivals):
+        torch.cuda.synchronize()
+        b = Batch(limits())
+        tk = [b.submit(c["ws"], c["y0"], c["ctrl"], c["pcp"], c["edir"], c["ett"], arrival=float(a),
+                       outlet=c["outlet"]) for c, a in zip(cases, arrivals)]
+        b.serve(workers=8)
+        recs = [b.record(k) for k in tk]
+        out = [b.served(k) for k in tk]
+        inf = b.info()
+        b.close()
+        return recs, out, inf
+
+    # capacity: everything queued at t = 0
+    recs, _, _ = serve(np.zeros(SERVE_N))
+    makespan = max(r.t_done for r in recs)
+    mu = SERVE_N / makespan
+    # the open-loop run
+    arr = WL.poisson_arrivals(SERVE_N, SERVE_LOAD * mu)
+    recs, out, inf = serve(arr)
+    failed = sum(r.status != DONE for r in recs)
+    lat = np.array([r.t_done - r.t_arrival for r in recs if r.status == DONE])
+    span = max(r.t_done for r in recs)
+    # the plain path one request at a time, first come first served
+    service, same = [], 0
+    for c, o in zip(cases, out):
+        ts = time.perf_counter()
+        r = solve_alone(c)
+        service.append(time.perf_counter() - ts)
+        same += int(np.array_equal(r["y"], o["y"]) and np.array_equal(r["outlet"], o["outlet"]))
+    seq_lat, seq_end = WL.fifo_latencies(arr, service)
+    return {
+        "metric": "served solves/s", "unit": "solves/s", "value": SERVE_N / span,
+        "p50_s": _pct(lat, 50), "p99_s": _pct(lat, 99), "mean_s": float(lat.mean()),
+        "workload": f"{SERVE_N} requests, {SERVE_LO}..{SERVE_HI} elements (log-uniform), Ksat x U(0.3,3), "
+                    f"Manning n x U(0.5,2), model step 60 or 120 s, {SERVE_STEPS} model steps each, "
+                    f"Poisson arrivals at {SERVE_LOAD} of the measured capacity {mu:.2f} solves/s",
+        "arena_elements": SERVE_ARENA_ELEM, "rounds": inf.rounds, "generate_s": gen_s,
+        "sequential": {"value": SERVE_N / seq_end, "unit": "solves/s", "p50_s": _pct(seq_lat, 50),
+                       "p99_s": _pct(seq_lat, 99), "service_s_total": float(sum(service)),
+                       "note": "plain path, one request at a time, first come first served, same arrivals"},
+        "bit_identical_to_plain_path": f"{same}/{SERVE_N}", "failed": failed,
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -194,6 +316,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--nelem", type=int, default=NELEM, help="smaller meshes for profiling only")
     ap.add_argument("--nriver", type=int, default=NRIVER)
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-watersheds leg")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving leg")
     args = ap.parse_args()
     globals()["NELEM"], globals()["NRIVER"] = args.nelem, args.nriver
     if args.impl == "reference":
@@ -330,6 +454,21 @@ def main():
         except Exception as exc:  # the baseline is reported, never required
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
 
+    # ---- batched watersheds and serving (N = 1 only) ----
+    batched = serving = None
+    if rank == 0 and world == 1:
+        g.close()
+        if not args.no_batched:
+            try:
+                batched = bench_batched()
+            except Exception as exc:
+                batched = {"error": repr(exc)}
+        if not args.no_serving:
+            try:
+                serving = bench_serving()
+            except Exception as exc:
+                serving = {"error": repr(exc)}
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -351,6 +490,8 @@ def main():
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
             "setup_s": setup_s,
+            "batched": batched,
+            "serving": serving,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -83,6 +83,13 @@ int pihm_batch_set_rhs_gate(pihm_batch *b, double gate);
 /* Admit a watershed; *id receives its handle.  PIHM_GPU_ERR_NOMEM: no room now. */
 int pihm_batch_add(pihm_batch *b, const pihm_batch_job *job, int32_t *id);
 
+/* Admit n watersheds, preparing them (validation, renumbering, derived
+ * constants) on `threads` host threads and admitting them in order; ids[k]
+ * receives each handle, or -1 from the first one that fails or does not fit
+ * on (the return code says why).  *admitted: how many were admitted. */
+int pihm_batch_add_many(pihm_batch *b, const pihm_batch_job *jobs, int32_t n, int32_t threads, int32_t *ids,
+                        int32_t *admitted);
+
 /* Advance every resident watershed by up to max_rounds rounds (<= 0: until
  * all have finished).  *running receives the number still running. */
 int pihm_batch_step(pihm_batch *b, int32_t max_rounds, int32_t *running);
@@ -106,9 +113,17 @@ typedef struct pihm_batch_info {
     int64_t rounds, rhs_rounds, launches;
     int64_t elem_used, elem_hwm, resident;
     double host_ms, wait_ms, program_ms, rhs_ms;
+    int32_t program_variant;  /* variant of the program kernel in use */
+    int32_t tuning;           /* 1 while the tuner is still timing variants */
 } pihm_batch_info;
 int pihm_batch_get_info(const pihm_batch *b, pihm_batch_info *info);
 int pihm_batch_set_profiling(pihm_batch *b, int on);
+
+/* The program kernel comes in variants (0, 1, 2: a thread keeps 1, 2 or 4 of
+ * its grid-stride entries in flight) that give identical results.  By default
+ * (-1) the engine times them on its first large rounds and keeps the fastest;
+ * 0..2 forces one. */
+int pihm_batch_set_program_variant(pihm_batch *b, int32_t variant);
 
 /* ---- serving --------------------------------------------------------------
  * Requests are submitted with an arrival time (seconds after the start of

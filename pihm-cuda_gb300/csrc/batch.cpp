@@ -12,12 +12,14 @@
 // step size, order, Newton and Krylov iterations, model step and stopping
 // time -- while sharing every launch.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <coroutine>
 #include <cstring>
 #include <map>
 #include <memory>
+#include <thread>
 #include <vector>
 
 #include "batch_engine.h"
@@ -418,10 +420,18 @@ int run_round(pihm_batch *B, bool *any) {
   if (nops && cudaMemcpyAsync(B->d_up + B->up_ops_off, B->h_up + B->up_ops_off, sizeof(Op) * nops,
                               cudaMemcpyHostToDevice, st) != cudaSuccess)
     return -1;
+  int variant = B->prog_forced >= 0 ? B->prog_forced : B->prog_variant;
+  const bool tune = B->prog_forced < 0 && B->tuning && nblocks >= pihm_batch::kTuneMinBlocks && B->tev[0];
+  if (tune) {
+    variant = B->tune_next;
+    B->tune_next = (B->tune_next + 1) % kProgramVariants;
+    cudaEventRecord(B->tev[0], st);
+  }
   if (B->profiling) cudaEventRecord(B->ev[0], st);
-  if (launch_program(B->A, (int)part.size(), nblocks, st) != cudaSuccess) return -1;
+  if (launch_program(B->A, (int)part.size(), nblocks, variant, st) != cudaSuccess) return -1;
   B->launches++;
   if (B->profiling) cudaEventRecord(B->ev[1], st);
+  if (tune) cudaEventRecord(B->tev[1], st);
   if (rhs) {
     if (cudaMemsetAsync(B->err_sys, 0, sizeof(unsigned int) * B->max_sys, st) != cudaSuccess) return -1;
     if (launch_rhs(B->A.m, B->A.rhs_in, B->A.rhs_out, st, &B->launches, nullptr) != cudaSuccess) return -1;
@@ -434,6 +444,22 @@ int run_round(pihm_batch *B, bool *any) {
   const auto t_done = std::chrono::steady_clock::now();
   B->wait_ms += std::chrono::duration<double, std::milli>(t_done - t_wait).count();
   B->host_ms += std::chrono::duration<double, std::milli>(t_wait - t_start).count();
+  if (tune) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, B->tev[0], B->tev[1]);
+    B->tune_ms_per_block[variant] += ms / nblocks;
+    if (++B->tune_n[variant] >= pihm_batch::kTuneSamples) {
+      bool all = true;
+      for (int v = 0; v < kProgramVariants; v++) all = all && B->tune_n[v] >= pihm_batch::kTuneSamples;
+      if (all) {
+        int best = 0;
+        for (int v = 1; v < kProgramVariants; v++)
+          if (B->tune_ms_per_block[v] / B->tune_n[v] < B->tune_ms_per_block[best] / B->tune_n[best]) best = v;
+        B->prog_variant = best;
+        B->tuning = false;
+      }
+    }
+  }
   if (B->profiling) {
     float a = 0.f, b = 0.f;
     cudaEventElapsedTime(&a, B->ev[0], B->ev[1]);
@@ -637,6 +663,8 @@ int pihm_batch_create(const pihm_batch_limits *lim, int surf_mode, int riv_mode,
            cudaMemset(A.rhs_in, 0, sizeof(double) * NEQ) == cudaSuccess &&
            cudaDeviceSynchronize() == cudaSuccess;
   if (!z) return PIHM_GPU_ERR_CUDA;
+  for (cudaEvent_t &e : B->tev)
+    if (cudaEventCreate(&e) != cudaSuccess) return PIHM_GPU_ERR_CUDA;
   B->update_extents();
   *out = B.release();
   return PIHM_GPU_OK;
@@ -662,6 +690,41 @@ int pihm_batch_add(pihm_batch *B, const pihm_batch_job *job, int32_t *id) {
   const int rc = prepare(job, B->A.m.surf_mode, B->A.m.riv_mode, B->order, &p);
   if (rc != PIHM_GPU_OK) return rc;
   return admit(B, p, id);
+}
+
+int pihm_batch_add_many(pihm_batch *B, const pihm_batch_job *jobs, int32_t n, int32_t threads, int32_t *ids,
+                        int32_t *admitted) {
+  if (!B || !jobs || !ids || n < 0) return PIHM_GPU_ERR_ARG;
+  std::vector<Prepared> prep(n);
+  std::vector<int> rcs(n, PIHM_GPU_OK);
+  const int nt = std::max(1, std::min<int>(threads, n));
+  std::atomic<int> next{0};
+  auto work = [&] {
+    for (int k; (k = next.fetch_add(1)) < n;)
+      rcs[k] = prepare(&jobs[k], B->A.m.surf_mode, B->A.m.riv_mode, B->order, &prep[k]);
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; t++) pool.emplace_back(work);
+  work();
+  for (auto &t : pool) t.join();
+  int rc = PIHM_GPU_OK, count = 0;
+  for (int k = 0; k < n; k++) {
+    ids[k] = -1;
+    if (rc != PIHM_GPU_OK) continue;
+    if (rcs[k] != PIHM_GPU_OK) {
+      rc = rcs[k];
+      continue;
+    }
+    const int arc = admit(B, prep[k], &ids[k]);
+    if (arc != PIHM_GPU_OK) {
+      rc = arc;
+      continue;
+    }
+    count++;
+    prep[k] = Prepared();  // release the host image early
+  }
+  if (admitted) *admitted = count;
+  return rc;
 }
 
 int pihm_batch_step(pihm_batch *B, int32_t max_rounds, int32_t *running) {
@@ -732,6 +795,14 @@ int pihm_batch_get_info(const pihm_batch *B, pihm_batch_info *info) {
   info->wait_ms = B->wait_ms;
   info->program_ms = B->program_ms;
   info->rhs_ms = B->rhs_ms;
+  info->program_variant = B->prog_forced >= 0 ? B->prog_forced : B->prog_variant;
+  info->tuning = B->prog_forced < 0 && B->tuning;
+  return PIHM_GPU_OK;
+}
+
+int pihm_batch_set_program_variant(pihm_batch *B, int32_t variant) {
+  if (!B || variant < -1 || variant >= kProgramVariants) return PIHM_GPU_ERR_ARG;
+  B->prog_forced = variant;
   return PIHM_GPU_OK;
 }
 

@@ -77,7 +77,9 @@ struct DeviceArena {
 };
 
 // Run one round's programs: nrs watersheds over nblocks blocks in total.
-cudaError_t launch_program(const DeviceArena &a, int nrs, int nblocks, cudaStream_t st);
+// variant 0, 1, 2: entries a thread keeps in flight (1, 2, 4); same results.
+constexpr int kProgramVariants = 3;
+cudaError_t launch_program(const DeviceArena &a, int nrs, int nblocks, int variant, cudaStream_t st);
 
 }  // namespace batch
 

@@ -191,6 +191,16 @@ struct pihm_batch {
   unsigned int *err_sys = nullptr;
   // scheduling policy
   double rhs_gate = 1.0;
+  // Tuner of the program kernel: while exploring, rounds of at least
+  // kTuneMinBlocks blocks rotate through the variants and are timed with
+  // events; after kTuneSamples rounds each, the fastest per block is kept.
+  // Every variant gives the same bits, so tuning mid-run changes no result.
+  static constexpr int kTuneSamples = 12, kTuneMinBlocks = 512;
+  int prog_variant = 1, prog_forced = -1, tune_next = 0;
+  bool tuning = true;
+  double tune_ms_per_block[pihm::batch::kProgramVariants] = {0};
+  int tune_n[pihm::batch::kProgramVariants] = {0};
+  cudaEvent_t tev[2] = {nullptr, nullptr};
   // counters and timing (host: building rounds and running the coroutines;
   // wait: blocked on the device; program/rhs: device time, when profiling)
   long long rounds = 0, rhs_rounds = 0, launches = 0;
@@ -203,6 +213,8 @@ struct pihm_batch {
   ~pihm_batch() {
     pihm_serve_state_free(serve);
     for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : tev)
       if (e) cudaEventDestroy(e);
     slots.clear();
     for (void *p : owned) cudaFree(p);

@@ -141,8 +141,26 @@ __global__ void __launch_bounds__(kThreads) k_red(long long n, const double *__r
   __shared__ Pair sh[kThreads / 32];
   __shared__ bool last;
   Pair acc = red_identity<OP>();
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (OP == R_DOT || OP == R_WSQ || OP == R_MAXABS || OP == R_MIN || OP == R_L1) {
+    // four grid-stride entries at a time (their loads in flight together),
+    // accumulated in grid-stride order
+    constexpr int U = 4;
+    for (; i0 < n; i0 += U * stride) {
+      double xv[U], yv[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const long long i = i0 + u * stride;
+        xv[u] = (i < n) ? x[i] : 0.0;
+        yv[u] = (i < n && (OP == R_DOT || OP == R_WSQ)) ? y[i] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++)
+        if (i0 + u * stride < n) acc = red_combine<OP>(acc, red_term<OP>(xv[u], yv[u]));
+    }
+  }
+  for (long long i = i0; i < n; i += stride) {
     Pair t = red_identity<OP>();
     if (OP == R_DOT || OP == R_WSQ) t = red_term<OP>(x[i], y[i]);
     else if (OP == R_MAXABS || OP == R_MIN || OP == R_L1) t = red_term<OP>(x[i], 0.0);

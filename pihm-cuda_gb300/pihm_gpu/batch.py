@@ -47,7 +47,8 @@ class BatchJob(ctypes.Structure):
 class BatchInfo(ctypes.Structure):
     _fields_ = [(n, _I64) for n in ("rounds", "rhs_rounds", "launches", "elem_used", "elem_hwm",
                                     "resident")] + [
-        (n, _D) for n in ("host_ms", "wait_ms", "program_ms", "rhs_ms")]
+        (n, _D) for n in ("host_ms", "wait_ms", "program_ms", "rhs_ms")] + [
+        ("program_variant", _I32), ("tuning", _I32)]
 
 
 class ServeRecord(ctypes.Structure):
@@ -83,12 +84,15 @@ def _bind(lib):
         "pihm_batch_set_rhs_gate": ([_VP, _D], ctypes.c_int),
         "pihm_batch_add": ([_VP, ctypes.POINTER(BatchJob), ctypes.POINTER(_I32)], ctypes.c_int),
         "pihm_batch_step": ([_VP, _I32, ctypes.POINTER(_I32)], ctypes.c_int),
+        "pihm_batch_add_many": ([_VP, ctypes.POINTER(BatchJob), _I32, _I32, ctypes.POINTER(_I32),
+                                 ctypes.POINTER(_I32)], ctypes.c_int),
         "pihm_batch_poll": ([_VP, _I32, ctypes.POINTER(_I32), ctypes.POINTER(_I32)], ctypes.c_int),
         "pihm_batch_result": ([_VP, _I32, _F64P, _F64P, ctypes.POINTER(BdfStats), ctypes.POINTER(_I32)],
                               ctypes.c_int),
         "pihm_batch_release": ([_VP, _I32], ctypes.c_int),
         "pihm_batch_get_info": ([_VP, ctypes.POINTER(BatchInfo)], ctypes.c_int),
         "pihm_batch_set_profiling": ([_VP, ctypes.c_int], ctypes.c_int),
+        "pihm_batch_set_program_variant": ([_VP, _I32], ctypes.c_int),
         "pihm_serve_submit": ([_VP, ctypes.POINTER(BatchJob), _D, ctypes.POINTER(_I32)], ctypes.c_int),
         "pihm_serve_run": ([_VP, _I32], ctypes.c_int),
         "pihm_serve_record_get": ([_VP, _I32, ctypes.POINTER(ServeRecord)], ctypes.c_int),
@@ -146,8 +150,37 @@ class Batch:
         self.jobs[i.value] = (ws, job.nsteps, outlet)
         return i.value
 
+    def add_many(self, cases, threads: int = 16):
+        """Admit many cases (dicts with ws, y0, ctrl, pcp, edir, ett, outlet),
+        prepared in parallel on host threads; returns their ids (None where a
+        case did not fit)."""
+        n = len(cases)
+        jobs = (BatchJob * n)()
+        keeps = []
+        for k, c in enumerate(cases):
+            job, keep = _job(c["ws"], c["y0"], c["ctrl"], c["pcp"], c["edir"], c["ett"], c.get("outlet", -1),
+                             c.get("elem_bc"), c.get("river_bc"))
+            jobs[k] = job
+            keeps.append(keep)
+        ids = (_I32 * n)()
+        admitted = _I32()
+        rc = self.lib.pihm_batch_add_many(self.h, jobs, n, threads, ids, ctypes.byref(admitted))
+        if rc not in (0, -5):
+            capi._check("pihm_batch_add_many", rc)
+        out = []
+        for k, c in enumerate(cases):
+            if ids[k] < 0:
+                out.append(None)
+                continue
+            self.jobs[ids[k]] = (c["ws"], jobs[k].nsteps, jobs[k].outlet)
+            out.append(ids[k])
+        return out
+
     def set_profiling(self, on: bool):
         capi._check("pihm_batch_set_profiling", self.lib.pihm_batch_set_profiling(self.h, int(on)))
+
+    def set_program_variant(self, variant: int):
+        capi._check("pihm_batch_set_program_variant", self.lib.pihm_batch_set_program_variant(self.h, variant))
 
     def set_rhs_gate(self, gate: float):
         capi._check("pihm_batch_set_rhs_gate", self.lib.pihm_batch_set_rhs_gate(self.h, gate))

@@ -71,7 +71,8 @@ def alone(cases):
 
 def test_batch_is_bit_identical_to_the_single_watershed_path(cases, alone):
     b = Batch(limits_for([c["ws"] for c in cases], 90))
-    ids = [_add(b, c) for c in cases]
+    ids = b.add_many(cases, threads=3)  # prepared on host threads, admitted in order
+    assert None not in ids
     assert b.step() == 0
     for i, c, want in zip(ids, cases, alone):
         assert b.poll(i) == (DONE, 0)
@@ -169,4 +170,16 @@ def test_serving_fails_a_request_larger_than_the_arena(cases, alone):
     assert b.record(big).status == FAILED and b.record(big).solver_rc == -5  # PIHM_GPU_ERR_NOMEM
     assert b.record(ok).status == DONE
     _same(b.served(ok), alone[0], "request behind a rejected one")
+    b.close()
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2])
+def test_program_kernel_variants_give_the_same_bits(cases, alone, variant):
+    b = Batch(limits_for([c["ws"] for c in cases], 90))
+    b.set_program_variant(variant)
+    ids = b.add_many(cases)
+    b.step()
+    assert b.info().program_variant == variant
+    for i, c, want in zip(ids, cases, alone):
+        _same(b.result(i), want, f"variant {variant}, watershed {c['ws'].nelem}")
     b.close()
