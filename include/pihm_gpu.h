@@ -178,6 +178,14 @@ int pihm_gpu_set_nan_check(pihm_gpu_ctx *ctx, int deferred);
 /* Post-step update on device state (internal order): ws0.surf <- y_dev[0:nelem]
  * (Summary, src/update.c:3-99; asynchronous on the context's stream). */
 int pihm_gpu_post_step(pihm_gpu_ctx *ctx, const double *y_dev);
+/* The watershed water balance of a model step of dt seconds, from the state
+ * y_dev (device, internal order) and the current forcing and river fluxes:
+ * out[0] sources (prcp area dt), out[1] sinks ((edir + ett) area dt plus the
+ * outlet segments' discharge dt), out[2] storage (surface, pore water and
+ * river water volume), the three sums of PrintWaterBal (src/print.c:337-542)
+ * with no canopy or snow stores.  The reference's cumulative error is the
+ * running sum of out[0] - out[1] - (out[2] - previous out[2]).  Synchronous. */
+int pihm_gpu_water_balance(pihm_gpu_ctx *ctx, const double *y_dev, double dt, double *out);
 
 /* Keep per-element and per-segment fluxes of every later call so that
  * pihm_gpu_get_fluxes can read them (costs extra stores). */

@@ -362,6 +362,27 @@ int ref_model_times(int *starttime, int *endtime, int *etstep, int *nstep)
  * and AdjCVodeMaxStep (src/ode.c:601).  Records the state every `every`
  * steps, the outlet segment's DOWN_CHANL2CHANL flux after every step (the
  * value PIHM prints as rivflx1) and CVODE's counters. */
+/* Optional water-balance outputs of ref_run_pihm: a file for the reference's
+   own PrintWaterBal and [nsteps][3] (src, snk, storage) at full precision. */
+static FILE *g_wb_file = NULL;
+static double *g_wb_out = NULL;
+
+int ref_set_water_balance(const char *path, double *out)
+{
+    if (g_wb_file) fclose(g_wb_file);
+    g_wb_file = path ? fopen(path, "w") : NULL;
+    g_wb_out = out;
+    return (path && !g_wb_file) ? -1 : 0;
+}
+
+int ref_close_water_balance(void)
+{
+    if (g_wb_file) fclose(g_wb_file);
+    g_wb_file = NULL;
+    g_wb_out = NULL;
+    return 0;
+}
+
 int ref_run_pihm(double *y, int nsteps, int stepsize, double reltol, double abstol,
                  double initstep, double nncfn, double nnimax, double nnimin, double decr,
                  double incr, double stmin, const double *pcp, const double *edir,
@@ -403,6 +424,35 @@ int ref_run_pihm(double *y, int nsteps, int stepsize, double reltol, double abst
         Summary(p->elem, p->river, cv_y, (double)stepsize);
         AdjCVodeMaxStep(cvode_mem, &p->ctrl);
         if (q_out) q_out[s] = p->river[outlet].wf.rivflow[DOWN_CHANL2CHANL];
+        if (g_wb_file || g_wb_out) {
+            /* the watershed water balance of this step: the reference's own
+               PrintWaterBal (src/print.c:337-542, printed with 6 digits) and
+               its three sums at full precision, in its summation order */
+            double src = 0.0, snk = 0.0, strg = 0.0;
+            for (i = 0; i < nelem; i++) {
+                p->elem[i].wf.prcp = pcp[s];  /* no interception: prcp = pcpdrp */
+                p->elem[i].wf.ec = 0.0;
+            }
+            if (g_wb_file)
+                PrintWaterBal(g_wb_file, (s + 1) * stepsize, 0, stepsize, p->elem, p->river);
+            for (i = 0; i < nelem; i++) {
+                const elem_struct *e = &p->elem[i];
+                src += e->wf.prcp * e->topo.area * stepsize;
+                snk += (e->wf.edir + e->wf.ett + e->wf.ec) * e->topo.area * stepsize;
+                strg += (e->ws.cmc + e->ws.sneqv + e->ws.surf + (e->ws.unsat + e->ws.gw) * e->soil.porosity) *
+                        e->topo.area;
+            }
+            for (i = 0; i < nriver; i++) {
+                const river_struct *r = &p->river[i];
+                strg += (r->ws.stage + r->ws.gw * r->matl.porosity) * r->topo.area;
+                if (r->down < 0) snk += r->wf.rivflow[DOWN_CHANL2CHANL] * stepsize;
+            }
+            if (g_wb_out) {
+                g_wb_out[3 * s] = src;
+                g_wb_out[3 * s + 1] = snk;
+                g_wb_out[3 * s + 2] = strg;
+            }
+        }
         if (y_out && every > 0 && (s + 1) % every == 0)
             memcpy(y_out + (size_t)((s + 1) / every - 1) * n, y, sizeof(double) * n);
     }

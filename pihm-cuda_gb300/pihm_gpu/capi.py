@@ -64,6 +64,7 @@ def load() -> ctypes.CDLL:
         "pihm_gpu_to_reference": ([_VP, _VP, _VP], ctypes.c_int),
         "pihm_gpu_launch_count": ([_VP, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
         "pihm_gpu_set_profiling": ([_VP, ctypes.c_int], ctypes.c_int),
+        "pihm_gpu_water_balance": ([_VP, _VP, ctypes.c_double, _F64P], ctypes.c_int),
         "pihm_gpu_kernel_times": ([_VP, _F64P, ctypes.POINTER(ctypes.c_int64), ctypes.c_int],
                                   ctypes.c_int),
     }
@@ -126,6 +127,13 @@ class GpuRhs:
     def set_bc(self, elem_bc=None, river_bc=None):
         _check("pihm_gpu_set_bc", self.lib.pihm_gpu_set_bc(self.h, f64p(_c(elem_bc)),
                                                            f64p(_c(river_bc))))
+
+    def water_balance(self, y_ptr: int, dt: float):
+        """(sources, sinks, storage) of a model step from the device state
+        y_ptr (internal order): the sums of PrintWaterBal."""
+        out = np.zeros(3)
+        _check("pihm_gpu_water_balance", self.lib.pihm_gpu_water_balance(self.h, _VP(y_ptr), float(dt), f64p(out)))
+        return tuple(out)
 
     def set_ws0_surf(self, ws0):
         _check("pihm_gpu_set_ws0_surf", self.lib.pihm_gpu_set_ws0_surf(self.h, f64p(_c(ws0))))

@@ -51,6 +51,9 @@ class GpuWatershed:
         assert self.lib.N_VCopyToHost_PihmGpu(self.scratch, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))) == 0
         return out
 
+    def water_balance(self, dt):
+        return self.g.water_balance(self.lib.N_VGetDeviceArrayPointer_PihmGpu(self.y), dt)
+
     def outlet_flux(self, s):
         return float(self.g.fluxes()["rivflow"][11 * s + 1])
 

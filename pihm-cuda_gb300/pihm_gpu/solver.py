@@ -96,14 +96,16 @@ class Bdf:
 
 
 def run_steps(backend, ctrl: StepControl, nsteps: int, forcing, record_every: int = 0,
-              outlet: int | None = None):
+              outlet: int | None = None, water_balance: bool = False):
     """The reference's model-step loop over `backend`, from t = 0.
 
     backend provides: y (N_Vector handle of the state), rhs (C function
     pointer), user_data, set_forcing(k), post_step(), read_state() ->
     numpy (reference order), outlet_flux(outlet) -> float.
     forcing(k) is called as backend.set_forcing(k) before step k.
-    Returns dict(states=[...], outlet=[...], stats=BdfStats).
+    water_balance: record backend.water_balance(dt) -> (sources, sinks,
+    storage) after every step (PrintWaterBal, src/print.c:337-542).
+    Returns dict(states=[...], outlet=[...], stats=BdfStats, wb=[nsteps][3]).
     """
     bdf = Bdf()
     lib = bdf.lib
@@ -115,7 +117,7 @@ def run_steps(backend, ctrl: StepControl, nsteps: int, forcing, record_every: in
     maxstep = float(ctrl.stepsize)
     bdf.check("hmax", lib.pihm_bdf_set_max_step(bdf.h, maxstep))
     bdf.check("mxstep", lib.pihm_bdf_set_max_num_steps(bdf.h, ctrl.mxstep or ctrl.stepsize * 10))
-    states, qout = [], []
+    states, qout, wb = [], [], []
     nst0 = ncfn0 = nni0 = 0
     tret = _D()
     for k in range(nsteps):
@@ -139,8 +141,10 @@ def run_steps(backend, ctrl: StepControl, nsteps: int, forcing, record_every: in
         nst0, ncfn0, nni0 = st.nst, st.ncfn, st.nni
         if outlet is not None:
             qout.append(backend.outlet_flux(outlet))
+        if water_balance:
+            wb.append(backend.water_balance(ctrl.stepsize))
         if record_every and (k + 1) % record_every == 0:
             states.append(backend.read_state())
-    out = dict(states=np.array(states), outlet=np.array(qout), stats=bdf.stats())
+    out = dict(states=np.array(states), outlet=np.array(qout), stats=bdf.stats(), wb=np.array(wb))
     bdf.close()
     return out

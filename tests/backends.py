@@ -44,6 +44,7 @@ class OracleBackend:
 
     def set_forcing(self, k):
         ne = self.ws.nelem
+        self.k = k
         self.model.set_forcing(np.full(ne, self.pcp[k]), np.full(ne, self.edir[k]),
                                np.full(ne, self.ett[k]))
 
@@ -55,6 +56,22 @@ class OracleBackend:
 
     def outlet_flux(self, s):
         return float(self.model.fluxes()["rivflow"][11 * s + 1])
+
+    def water_balance(self, dt):
+        """PrintWaterBal's sums (src/print.c:337-542) in its summation order
+        (np.cumsum adds left to right), no canopy or snow stores."""
+        a, ne, nr = self.ws.arrays, self.ws.nelem, self.ws.nriver
+        y, k = self.yarr, self.k
+        area = a["area"]
+        src = np.cumsum(self.pcp[k] * area * dt)[-1]
+        e_snk = (self.edir[k] + self.ett[k] + 0.0) * area * dt
+        rivflow = self.model.fluxes()["rivflow"].reshape(nr, 11)[:, 1]
+        r_snk = (rivflow * dt)[a["down"] < 0]
+        snk = np.cumsum(np.concatenate([e_snk, r_snk]))[-1]
+        e_strg = ((0.0 + 0.0 + y[:ne]) + (y[ne:2 * ne] + y[2 * ne:3 * ne]) * a["porosity"]) * area
+        r_strg = (y[3 * ne:3 * ne + nr] + y[3 * ne + nr:] * a["riv_porosity"]) * a["riv_area"]
+        strg = np.cumsum(np.concatenate([e_strg, r_strg]))[-1]
+        return float(src), float(snk), float(strg)
 
     def close(self):
         if self.y:

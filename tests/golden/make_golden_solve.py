@@ -8,7 +8,10 @@ src/main.c:217-254), driven through oracle/ref_harness.c::ref_run_pihm.
 writes tests/golden/c0_solve.npz: the initial state, the per-step forcing,
 the state every 6 hours, the outlet flux (rivflow DOWN_CHANL2CHANL of the
 outlet segment as left by the last right-hand-side call, what PIHM prints as
-rivflx1) after every step, and CVODE's counters.  Runs in its own process:
+rivflx1) after every step, CVODE's counters, and the water balance after
+every step: the sums of PrintWaterBal (src/print.c:337-542: sources, sinks,
+storage) at full precision in `wb` and the reference's own printed lines in
+`wb_printed`.  Runs in its own process:
 the reference keeps solver state in statics (src/ode.c:416,609-611).
 """
 import argparse
@@ -59,6 +62,12 @@ def main():
     P = ctypes.POINTER(D)
     f.argtypes = [P, ctypes.c_int, ctypes.c_int] + [D] * 9 + [P, P, P, ctypes.c_int, ctypes.c_int,
                                                              P, P, ctypes.POINTER(ctypes.c_long)]
+    # the watershed water balance per step: the reference's own PrintWaterBal
+    # (6 printed digits) and its sums at full precision
+    wb = np.zeros((nsteps, 3))
+    wb_path = os.path.join(HERE, "_wb_tmp.txt")
+    ref.lib.ref_set_water_balance.argtypes = [ctypes.c_char_p, P]
+    ref.lib.ref_set_water_balance(wb_path.encode(), wb.ctypes.data_as(P))
     y = y0.copy()
     nrec = nsteps // EVERY
     ys = np.zeros((nrec, ws.neq))
@@ -70,7 +79,10 @@ def main():
            pcp.ctypes.data_as(P), edir.ctypes.data_as(P), ett.ctypes.data_as(P), outlet, EVERY,
            ys.ctypes.data_as(P), q.ctypes.data_as(P), stats)
     assert rc == 0
-    np.savez_compressed(args.out, y0=y0, pcp=pcp, edir=edir, ett=ett,
+    ref.lib.ref_close_water_balance()
+    printed = np.loadtxt(wb_path, skiprows=1)  # t, src, snk, dstrg, src - snk - dstrg, cumulative
+    os.remove(wb_path)
+    np.savez_compressed(args.out, y0=y0, pcp=pcp, edir=edir, ett=ett, wb=wb, wb_printed=printed,
                         states=ys, outlet_q=q, outlet=outlet, every=EVERY,
                         stats=np.array(list(stats)), ctrl=np.array([c[k] for k in CTRL]),
                         ctrl_names=np.array(list(CTRL)))

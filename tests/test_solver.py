@@ -41,7 +41,7 @@ def _run(backend_cls, ws, z, ctrl, **kw):
     b = backend_cls(ws, z["y0"], z["pcp"], z["edir"], z["ett"], **kw)
     try:
         return run_steps(b, ctrl, nsteps, b.set_forcing, record_every=int(z["every"]),
-                         outlet=int(z["outlet"]))
+                         outlet=int(z["outlet"]), water_balance=True)
     finally:
         b.close()
 
@@ -54,6 +54,23 @@ def test_integrator_reproduces_reference_cvode_on_cpu():
     assert got == list(z["stats"]), (got, list(z["stats"]))
     assert np.array_equal(res["states"], z["states"])
     assert np.array_equal(res["outlet"], z["outlet_q"])
+    # the water balance after every step: PrintWaterBal's sums, bit for bit
+    assert np.array_equal(res["wb"], z["wb"])
+
+
+def _wb_error(wb):
+    """PrintWaterBal's cumulative error (src/print.c: from its second call)."""
+    src, snk, strg = wb[:, 0], wb[:, 1], wb[:, 2]
+    return np.cumsum(src[1:] - snk[1:] - (strg[1:] - strg[:-1]))
+
+
+def test_reference_water_balance_fixture():
+    z = np.load(os.path.join(GOLD, "c0_solve.npz"))
+    err = _wb_error(z["wb"])
+    # the full-precision sums round to the reference's own printed lines
+    printed = z["wb_printed"]
+    assert np.allclose(err, printed[:, 5], rtol=1e-5, atol=1e-6 * np.abs(err).max())
+    assert np.allclose(z["wb"][1:, 0], printed[:, 1], rtol=1e-5, atol=1e-300)
 
 
 def _rel(a, b, floor=1e-5):
@@ -98,3 +115,8 @@ def test_gpu_solve_hydrograph_and_storages():
     assert serr <= 2 * senv
     span = nmax - nmin
     assert nmin - span <= s.nst <= nmax + span
+    # mass balance: the cumulative residual is no worse than the reference's
+    e_gpu, e_ref = np.abs(_wb_error(res["wb"])).max(), np.abs(_wb_error(z["wb"])).max()
+    print(f"water-balance residual: GPU {e_gpu:.4g} m3, reference {e_ref:.4g} m3 "
+          f"(storage {z['wb'][-1, 2]:.4g} m3)")
+    assert e_gpu <= 1.05 * e_ref
