@@ -178,6 +178,19 @@ int pihm_gpu_set_nan_check(pihm_gpu_ctx *ctx, int deferred);
 /* Post-step update on device state (internal order): ws0.surf <- y_dev[0:nelem]
  * (Summary, src/update.c:3-99; asynchronous on the context's stream). */
 int pihm_gpu_post_step(pihm_gpu_ctx *ctx, const double *y_dev);
+/* Switch to the Flux-PIHM right-hand side (the reference built with _NOAH_)
+ * and set Noah's per-step inputs, all in reference element order:
+ * transpiration per soil layer et[nelem][nlayers] (wf.et, m/s), the
+ * water-table layer nwtbl and the root layers nroot (ps.nwtbl, ps.nroot;
+ * nroot <= nlayers <= 11), the top layer's unfrozen moisture sh2o0
+ * (ws.sh2o[0]) with the soil's smcmin / smcmax, and the frozen-soil factor
+ * fcr (ps.fcr).  EtExtract then splits ET as src/hydrol.c:43-55,79-83 (with
+ * GwTransp, noah/lsm_func.c:163-185) and Infil takes its saturation from
+ * sh2o0 and is scaled by fcr (src/vert_flow.c:16-19,94-98).  Call again
+ * after every Noah step. */
+int pihm_gpu_set_noah(pihm_gpu_ctx *ctx, const double *et, int nlayers, const int32_t *nwtbl,
+                      const int32_t *nroot, const double *sh2o0, const double *smcmin,
+                      const double *smcmax, const double *fcr);
 /* The watershed water balance of a model step of dt seconds, from the state
  * y_dev (device, internal order) and the current forcing and river fluxes:
  * out[0] sources (prcp area dt), out[1] sinks ((edir + ett) area dt plus the

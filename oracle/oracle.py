@@ -106,6 +106,11 @@ class Oracle:
     def post_step(self, y):
         self.lib.oracle_post_step(self.h, f64p(_c(y)))
 
+    def set_noah(self, noah: dict):
+        """Flux-PIHM (_NOAH_) right-hand side with Noah's per-step inputs
+        (et [nelem, nlayers], nwtbl, nroot, sh2o0, smcmin, smcmax, fcr)."""
+        _set_noah(self.lib.oracle_set_noah, noah, self.h)
+
     def fluxes(self):
         ne, nr = self.ws.nelem, self.ws.nriver
         out = dict(ovlflow=np.zeros(3 * ne), subsurf=np.zeros(3 * ne),
@@ -120,16 +125,14 @@ class Reference:
     """The reference's own code (compiled from its sources).  The reference
     keeps its model in globals, so one instance at a time."""
 
-    def __init__(self, omp: bool = False):
-        name = "libpihm_ref_omp.so" if omp else "libpihm_ref.so"
+    def __init__(self, omp: bool = False, noah: bool = False):
+        name = "libpihm_ref_noah.so" if noah else ("libpihm_ref_omp.so" if omp else "libpihm_ref.so")
         path = os.path.join(HERE, "_ref", name)
         if not os.path.exists(path):
             raise FileNotFoundError(path)
         lib = ctypes.CDLL(path)
         lib.ref_build.argtypes = [ctypes.POINTER(MeshDesc), ctypes.c_int,
                                   ctypes.c_int, ctypes.c_int]
-        lib.ref_load_example.argtypes = [ctypes.c_char_p, ctypes.c_char_p,
-                                         _F64P, ctypes.c_int]
         lib.ref_sizes.argtypes = [ctypes.POINTER(ctypes.c_int)] * 5
         lib.ref_export_double.argtypes = [ctypes.c_char_p, _F64P]
         lib.ref_export_int.argtypes = [ctypes.c_char_p, _I32P]
@@ -139,10 +142,15 @@ class Reference:
         lib.ref_set_river_edge_ovlflow.argtypes = [_F64P]
         lib.ref_ode.argtypes = [ctypes.c_double, _F64P, _F64P]
         lib.ref_get_fluxes.argtypes = [_F64P] * 6
-        lib.ref_apply_forcing.argtypes = [ctypes.c_int]
-        lib.ref_model_times.argtypes = [ctypes.POINTER(ctypes.c_int)] * 4
         lib.ref_num_threads.restype = ctypes.c_int
         lib.ref_set_num_threads.argtypes = [ctypes.c_int]
+        if noah:  # the Flux-PIHM build has the right-hand side only
+            lib.ref_get_gwet.argtypes = [_F64P]
+        else:
+            lib.ref_load_example.argtypes = [ctypes.c_char_p, ctypes.c_char_p,
+                                             _F64P, ctypes.c_int]
+            lib.ref_apply_forcing.argtypes = [ctypes.c_int]
+            lib.ref_model_times.argtypes = [ctypes.POINTER(ctypes.c_int)] * 4
         self.lib = lib
         self.ne = self.nr = 0
 
@@ -194,6 +202,9 @@ class Reference:
         rc = self.lib.ref_ode(t, f64p(y), f64p(out))
         return out, rc
 
+    def set_noah(self, noah: dict):
+        _set_noah(self.lib.ref_set_noah, noah)
+
     def fluxes(self):
         ne, nr = self.ne, self.nr
         out = dict(ovlflow=np.zeros(3 * ne), subsurf=np.zeros(3 * ne),
@@ -202,6 +213,19 @@ class Reference:
         self.lib.ref_get_fluxes(*(f64p(out[k]) for k in (
             "ovlflow", "subsurf", "infil", "rechg", "et_split", "rivflow")))
         return out
+
+
+def _set_noah(fn, noah, *head):
+    """Call oracle_set_noah / ref_set_noah with a dict of Noah inputs."""
+    et = np.ascontiguousarray(noah["et"], np.float64)
+    nl = et.shape[1] if et.ndim == 2 else 0
+    i32 = lambda a: np.ascontiguousarray(a, np.int32)
+    keep = [et, i32(noah["nwtbl"]), i32(noah["nroot"])] + [_c(noah[k]) for k in ("sh2o0", "smcmin", "smcmax", "fcr")]
+    fn.argtypes = ([ctypes.c_void_p] if head else []) + [_F64P, ctypes.c_int, _I32P, _I32P] + [_F64P] * 4
+    fn.restype = ctypes.c_int
+    rc = fn(*head, f64p(keep[0]), nl, keep[1].ctypes.data_as(_I32P), keep[2].ctypes.data_as(_I32P),
+            *(f64p(a) for a in keep[3:]))
+    assert rc == 0
 
 
 def _c(a):

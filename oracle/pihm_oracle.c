@@ -54,6 +54,8 @@
 #define KINEMATIC 1
 #define DIFF_WAVE 2
 
+#define NOAH_MAXLYR 11 /* MAXLYR, src/include/pihm_const.h:84 */
+
 typedef struct soil_p {
     double depth, ksath, ksatv, kinfv, dinf, alpha, beta, porosity, dmac,
         kmach, kmacv, areafv, areafh;
@@ -74,6 +76,9 @@ typedef struct elem_t {
     double ovlflow[NUM_EDGE], subsurf[NUM_EDGE];
     double pcpdrp, infil, rechg, edir, ett;
     double edir_surf, edir_unsat, edir_gw, ett_unsat, ett_gw;
+    /* Flux-PIHM (_NOAH_) inputs Noah sets once per model step */
+    double et[NOAH_MAXLYR], sh2o0, smcmin, smcmax, fcr, gwet;
+    int nwtbl, nroot;
 } elem_t;
 
 typedef struct river_t {
@@ -88,6 +93,7 @@ typedef struct river_t {
 
 struct oracle_model {
     int nelem, nriver;
+    int noah; /* 1: the Flux-PIHM (_NOAH_) variants of EtExtract and Infil */
     int surf_mode, riv_mode;
     double stepsize;
     elem_t *elem;
@@ -224,6 +230,26 @@ void oracle_set_ws0_surf(oracle_model *m, const double *ws0_surf)
 {
     int i;
     for (i = 0; i < m->nelem; i++) m->elem[i].ws0_surf = ws0_surf[i];
+}
+
+/* Flux-PIHM inputs (see oracle_set_noah in pihm_oracle.h). */
+int oracle_set_noah(oracle_model *m, const double *et, int nlayers, const int *nwtbl, const int *nroot,
+                    const double *sh2o0, const double *smcmin, const double *smcmax, const double *fcr)
+{
+    int i, j;
+    if (nlayers < 0 || nlayers > NOAH_MAXLYR) return -1;
+    m->noah = 1;
+    for (i = 0; i < m->nelem; i++) {
+        elem_t *e = &m->elem[i];
+        for (j = 0; j < NOAH_MAXLYR; j++) e->et[j] = (j < nlayers) ? et[(size_t)nlayers * i + j] : 0.0;
+        e->nwtbl = nwtbl[i];
+        e->nroot = nroot[i];
+        e->sh2o0 = sh2o0[i];
+        e->smcmin = smcmin[i];
+        e->smcmax = smcmax[i];
+        e->fcr = fcr[i];
+    }
+    return 0;
 }
 
 void oracle_set_river_edge_ovlflow(oracle_model *m, const double *ovlflow)
@@ -488,8 +514,9 @@ static double EffKinf(const soil_p *soil, double dh_by_dz, double ksatfunc,
     return keff;
 }
 
-/* Infil, src/vert_flow.c:33-130 (no _NOAH_) */
-static double Infil(const elem_t *e, double dt)
+/* Infil, src/vert_flow.c:33-130; with noah, the saturation of the
+ * unsaturated branch is Noah's top layer (src/vert_flow.c:94-98) */
+static double Infil(const elem_t *e, double dt, int noah)
 {
     double applrate, wetfrac, dh_by_dz, satn, satkfunc, infil, infil_max,
         kinf, deficit, psi_u, h_u;
@@ -517,7 +544,10 @@ static double Infil(const elem_t *e, double dt)
             infil = kinf * dh_by_dz;
         } else {
             deficit = soil->depth - e->gw;
-            satn = e->unsat / deficit;
+            if (noah)
+                satn = (e->sh2o0 - e->smcmin) / (e->smcmax - e->smcmin);
+            else
+                satn = e->unsat / deficit;
             satn = (satn > 1.0) ? 1.0 : satn;
             satn = (satn < SATMIN) ? SATMIN : satn;
             psi_u = Psi(satn, soil->alpha, soil->beta);
@@ -594,12 +624,31 @@ static void VerticalFlow(oracle_model *m)
 #pragma omp parallel for
 #endif
     for (i = 0; i < m->nelem; i++) {
-        m->elem[i].infil = Infil(&m->elem[i], m->stepsize);
+        m->elem[i].infil = Infil(&m->elem[i], m->stepsize, m->noah);
+        /* frozen top soil, src/vert_flow.c:16-19 */
+        if (m->noah) m->elem[i].infil *= m->elem[i].fcr;
         m->elem[i].rechg = Recharge(&m->elem[i]);
     }
 }
 
-/* EtExtract, src/hydrol.c:33-97 (no _NOAH_) */
+/* GwTransp, noah/lsm_func.c:163-185: the fraction of transpiration drawn
+ * from the saturated zone */
+static double GwTransp(double ett, const double *et, int nwtbl, int nroot)
+{
+    int j;
+    double gw_transp = 0.0;
+    if (ett > 0.0) {
+        if (nwtbl <= nroot) {
+            for (j = (nwtbl <= 0 ? 0 : nwtbl - 1); j < nroot; j++) gw_transp += et[j];
+            gw_transp = gw_transp / ett;
+            gw_transp = (gw_transp > 1.0) ? 1.0 : gw_transp;
+            gw_transp = (gw_transp < 0.0) ? 0.0 : gw_transp;
+        }
+    }
+    return gw_transp;
+}
+
+/* EtExtract, src/hydrol.c:33-97, with its _NOAH_ branches (:43-55, :79-83) */
 static void EtExtract(oracle_model *m)
 {
     int i;
@@ -608,6 +657,21 @@ static void EtExtract(oracle_model *m)
 #endif
     for (i = 0; i < m->nelem; i++) {
         elem_t *e = &m->elem[i];
+        if (m->noah) {
+            if (e->gw > e->soil.depth - e->soil.dinf) {
+                e->edir_surf = 0.0;
+                e->edir_unsat = 0.0;
+                e->edir_gw = e->edir;
+            } else {
+                e->edir_surf = 0.0;
+                e->edir_unsat = e->edir;
+                e->edir_gw = 0.0;
+            }
+            e->gwet = GwTransp(e->ett, e->et, e->nwtbl, e->nroot);
+            e->ett_unsat = (1.0 - e->gwet) * e->ett;
+            e->ett_gw = e->gwet * e->ett;
+            continue;
+        }
         if (e->surfh >= DEPRSTG) {
             e->edir_surf = e->edir;
             e->edir_unsat = 0.0;

@@ -30,6 +30,12 @@ void oracle_set_forcing(oracle_model *m, const double *pcpdrp,
 void oracle_set_bc(oracle_model *m, const double *elem_bc,
                    const double *river_bc);
 void oracle_set_ws0_surf(oracle_model *m, const double *ws0_surf);
+/* Switch to the Flux-PIHM (_NOAH_) right-hand side with Noah's per-step
+ * inputs: transpiration per soil layer et[nelem][nlayers], water-table and
+ * root layers, top-layer unfrozen moisture with the soil's smcmin/smcmax, and
+ * the frozen-soil infiltration factor. */
+int oracle_set_noah(oracle_model *m, const double *et, int nlayers, const int *nwtbl, const int *nroot,
+                    const double *sh2o0, const double *smcmin, const double *smcmax, const double *fcr);
 void oracle_set_river_edge_ovlflow(oracle_model *m, const double *ovlflow);
 /* ydot = f(t, y); returns 0, or -3 when a derivative is NaN (the reference
  * exits there, src/ode.c:401-410). */

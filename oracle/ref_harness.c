@@ -145,6 +145,7 @@ int ref_build(const pihm_gpu_mesh *g, int surf_mode, int riv_mode,
     return 0;
 }
 
+#if !defined(_NOAH_)
 /* Read an input deck `<workdir>/input/<proj>/<proj>.*` with the reference's
  * readers and initialise it (RelaxIc or ReadIc per the .para file). */
 int ref_load_example(const char *workdir, const char *proj, double *y0,
@@ -168,6 +169,8 @@ int ref_load_example(const char *workdir, const char *proj, double *y0,
     if (chdir(cwd) != 0) return -1;
     return 0;
 }
+
+#endif /* !_NOAH_ */
 
 int ref_sizes(int *ne, int *nr, int *stepsize, int *surf_mode, int *riv_mode)
 {
@@ -333,6 +336,39 @@ void ref_get_fluxes(double *ovlflow, double *subsurf, double *infil,
                 rivflow[NUM_RIVFLX * i + j] = g_pihm->river[i].wf.rivflow[j];
 }
 
+#if defined(_NOAH_)
+/* Flux-PIHM (_NOAH_) inputs of the right-hand side, which Noah computes once
+ * per model step: per-layer transpiration wf.et[0..nlayers) (GwTransp,
+ * noah/lsm_func.c:163-185, splits ett with them), the water-table layer
+ * ps.nwtbl and root layers ps.nroot, the top-layer unfrozen moisture
+ * ws.sh2o[0] with soil.smcmin/smcmax (Infil's saturation,
+ * src/vert_flow.c:94-98) and the frozen-soil factor ps.fcr
+ * (src/vert_flow.c:16-19). */
+int ref_set_noah(const double *et, int nlayers, const int *nwtbl, const int *nroot, const double *sh2o0,
+                 const double *smcmin, const double *smcmax, const double *fcr)
+{
+    int i, j;
+    if (!g_pihm || nlayers < 0 || nlayers > MAXLYR) return -1;
+    for (i = 0; i < nelem; i++) {
+        elem_struct *e = &g_pihm->elem[i];
+        for (j = 0; j < MAXLYR; j++) e->wf.et[j] = (j < nlayers) ? et[(size_t)nlayers * i + j] : 0.0;
+        e->ps.nwtbl = nwtbl[i];
+        e->ps.nroot = nroot[i];
+        e->ws.sh2o[0] = sh2o0[i];
+        e->soil.smcmin = smcmin[i];
+        e->soil.smcmax = smcmax[i];
+        e->ps.fcr = fcr[i];
+    }
+    return 0;
+}
+
+/* gwet of the last evaluation (EtExtract stores it in ps.gwet). */
+void ref_get_gwet(double *gwet)
+{
+    int i;
+    for (i = 0; i < nelem; i++) gwet[i] = g_pihm->elem[i].ps.gwet;
+}
+#else
 /* Forcing step of src/pihm.c:21-66 for a model loaded by ref_load_example:
  * boundary conditions, meteorological forcing, interception/snow/ET, at model
  * time t (seconds since the epoch, as ctrl.tout). */
@@ -470,3 +506,4 @@ int ref_run_pihm(double *y, int nsteps, int stepsize, double reltol, double abst
     N_VDestroy(cv_y);
     return 0;
 }
+#endif /* _NOAH_ */

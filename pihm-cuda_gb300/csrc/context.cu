@@ -60,6 +60,7 @@ int pihm_gpu_create(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double 
   c->launches = 0;
   c->nan_check_deferred = 0;
   c->prof = nullptr;
+  c->d_noah = nullptr;
   c->h_perm = (int32_t *)std::malloc(sizeof(int32_t) * ne);
   c->h_iperm = (int32_t *)std::malloc(sizeof(int32_t) * ne);
   std::memcpy(c->h_perm, im.perm.data(), sizeof(int32_t) * ne);
@@ -186,6 +187,7 @@ void pihm_gpu_destroy(pihm_gpu_ctx *c) {
   free_profiler(c->prof);
   if (c->d_static) cudaFree(c->d_static);
   if (c->d_dyn) cudaFree(c->d_dyn);
+  if (c->d_noah) cudaFree(c->d_noah);
   std::free(c->h_perm);
   std::free(c->h_iperm);
   delete c;
@@ -239,6 +241,57 @@ int pihm_gpu_set_bc(pihm_gpu_ctx *c, const double *elem_bc, const double *river_
     rc = cuda_fail(cudaMemcpyAsync((double *)c->m.river_bc, river_bc, sizeof(double) * c->nr,
                                    cudaMemcpyHostToDevice, c->stream)) ?:
          cuda_fail(cudaStreamSynchronize(c->stream));
+  return rc;
+}
+
+int pihm_gpu_set_noah(pihm_gpu_ctx *c, const double *et, int nlayers, const int32_t *nwtbl,
+                      const int32_t *nroot, const double *sh2o0, const double *smcmin, const double *smcmax,
+                      const double *fcr) {
+  if (!c || !nwtbl || !nroot || !sh2o0 || !smcmin || !smcmax || !fcr || nlayers < 0 || nlayers > 11 ||
+      (nlayers > 0 && !et))
+    return PIHM_GPU_ERR_ARG;
+  const int ne = c->ne;
+  const size_t NE = ne;
+  for (int r = 0; r < ne; r++)
+    if (nroot[r] > nlayers) return PIHM_GPU_ERR_ARG;
+  if (!c->d_noah) {
+    const size_t bytes = 3 * carve_size<double>(NE) + carve_size<int32_t>(NE);
+    if (cudaMalloc(&c->d_noah, bytes) != cudaSuccess) {
+      c->d_noah = nullptr;
+      return PIHM_GPU_ERR_NOMEM;
+    }
+    char *p = (char *)c->d_noah;
+    c->m.noah_etgw = carve<double>(p, NE);
+    c->m.noah_satn = carve<double>(p, NE);
+    c->m.noah_fcr = carve<double>(p, NE);
+    c->m.noah_wtin = carve<int32_t>(p, NE);
+  }
+  // per element, internal order: GwTransp's layer sum in its order
+  // (noah/lsm_func.c:171-177), Infil's top-layer saturation
+  // (src/vert_flow.c:94-98), the frozen-soil factor
+  std::vector<double> etgw(NE), satn(NE), f(NE);
+  std::vector<int32_t> wtin(NE);
+  for (int i = 0; i < ne; i++) {
+    const int r = c->h_perm[i];
+    double g = 0.0;
+    const int top = nwtbl[r], nr = nroot[r];
+    wtin[i] = top <= nr;
+    if (top <= nr)
+      for (int j = (top <= 0 ? 0 : top - 1); j < nr; j++) g += et[(size_t)nlayers * r + j];
+    etgw[i] = g;
+    satn[i] = (sh2o0[r] - smcmin[r]) / (smcmax[r] - smcmin[r]);
+    f[i] = fcr[r];
+  }
+  const int rc = cuda_fail(cudaMemcpyAsync((void *)c->m.noah_etgw, etgw.data(), sizeof(double) * NE,
+                                           cudaMemcpyHostToDevice, c->stream)) ?:
+                 cuda_fail(cudaMemcpyAsync((void *)c->m.noah_satn, satn.data(), sizeof(double) * NE,
+                                           cudaMemcpyHostToDevice, c->stream)) ?:
+                 cuda_fail(cudaMemcpyAsync((void *)c->m.noah_fcr, f.data(), sizeof(double) * NE,
+                                           cudaMemcpyHostToDevice, c->stream)) ?:
+                 cuda_fail(cudaMemcpyAsync((void *)c->m.noah_wtin, wtin.data(), sizeof(int32_t) * NE,
+                                           cudaMemcpyHostToDevice, c->stream)) ?:
+                 cuda_fail(cudaStreamSynchronize(c->stream));
+  if (rc == PIHM_GPU_OK) c->m.noah = 1;
   return rc;
 }
 

@@ -105,6 +105,16 @@ struct DevMesh {
   const uint8_t *active;
   const double *sys_dt;
   unsigned int *err_sys;
+
+  // Flux-PIHM (_NOAH_) right-hand side, when noah != 0: per element, from
+  // Noah's per-step outputs, the transpiration of the layers from the water
+  // table down to the root depth (GwTransp's sum, noah/lsm_func.c:163-185)
+  // and whether the water table is within the root zone, Infil's saturation
+  // from the top layer's moisture (src/vert_flow.c:94-98, unclamped) and the
+  // frozen-soil factor (src/vert_flow.c:16-19)
+  int noah;
+  const double *noah_etgw, *noah_satn, *noah_fcr;
+  const int32_t *noah_wtin;
 };
 
 // Optional per-kernel CUDA-event timing of the right-hand-side launches.
@@ -140,4 +150,5 @@ struct pihm_gpu_ctx {
   int nan_check_deferred;  // 1: pihm_gpu_ode does not synchronise to read the error word
   long long launches;      // kernels launched by this context so far
   pihm::Profiler *prof;    // non-null while profiling is on
+  void *d_noah;            // Flux-PIHM input planes, allocated on first use
 };

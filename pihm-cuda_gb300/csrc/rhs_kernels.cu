@@ -286,11 +286,27 @@ __global__ void __launch_bounds__(256) k_elem_main(DevMesh m, const double *REST
   const double edir = m.edir[i], ett = m.ett[i];
   double edir_surf = 0.0, edir_unsat = 0.0, edir_gw = 0.0, ett_unsat = 0.0, ett_gw = 0.0;
   const bool gw_in_dinf = gw > d_dinf;
-  if (surfh >= kDeprStg) edir_surf = edir;
-  else if (gw_in_dinf) edir_gw = edir;
-  else edir_unsat = edir;
-  if (gw > m.d_rzd[i]) ett_gw = ett;
-  else ett_unsat = ett;
+  if (m.noah) {
+    // Flux-PIHM (src/hydrol.c:43-55,79-83): no ponded-water source, and the
+    // transpiration split by GwTransp (noah/lsm_func.c:163-185) over the
+    // Noah layers from the water table down to the root depth
+    if (gw_in_dinf) edir_gw = edir;
+    else edir_unsat = edir;
+    double gwet = 0.0;
+    if (ett > 0.0 && m.noah_wtin[i]) {
+      gwet = m.noah_etgw[i] / ett;
+      gwet = (gwet > 1.0) ? 1.0 : gwet;
+      gwet = (gwet < 0.0) ? 0.0 : gwet;
+    }
+    ett_unsat = (1.0 - gwet) * ett;
+    ett_gw = gwet * ett;
+  } else {
+    if (surfh >= kDeprStg) edir_surf = edir;
+    else if (gw_in_dinf) edir_gw = edir;
+    else edir_unsat = edir;
+    if (gw > m.d_rzd[i]) ett_gw = ett;
+    else ett_unsat = ett;
+  }
 
   // Infil, src/vert_flow.c:33-130, and Recharge, :132-170, sharing KrFunc and
   // Psi of the same saturation
@@ -312,6 +328,20 @@ __global__ void __launch_bounds__(256) k_elem_main(DevMesh m, const double *REST
     // Psi, src/vert_flow.c:272-278
     psi_u = -pow_fast(pow_fast(1.0 / satn, vm) - 1.0, m.vg_ib[i]) * m.inv_alpha[i];
   }
+  // Infil's saturation: the same one, except in Flux-PIHM, where it is
+  // Noah's top-layer moisture (src/vert_flow.c:94-98) and Recharge keeps
+  // the column's
+  double satn_i = satn, satkfunc_i = satkfunc, psi_i = psi_u;
+  if (m.noah && !gw_in_dinf) {
+    double s = m.noah_satn[i];
+    s = (s > 1.0) ? 1.0 : s;
+    s = (s < kSatMin) ? kSatMin : s;
+    const double vm = m.vg_m[i];
+    const double t = 1.0 - pow_fast(1.0 - pow_fast(s, vm), m.vg_e[i]);
+    satn_i = s;
+    satkfunc_i = sqrt(s) * t * t;
+    psi_i = -pow_fast(pow_fast(1.0 / s, vm) - 1.0, m.vg_ib[i]) * m.inv_alpha[i];
+  }
   // KrFunc(beta, 1) == 1 exactly: pow(1 - pow(1, m), e) == pow(0, e) == 0
   double infil;
   if (unsat + gw > depth) {
@@ -326,12 +356,12 @@ __global__ void __launch_bounds__(256) k_elem_main(DevMesh m, const double *REST
     wetfrac = (wetfrac > 0.0) ? wetfrac : 0.0;
     wetfrac = (wetfrac < 1.0) ? wetfrac : 1.0;
     double dh_by_dz;
-    double esatn = satn;
+    double esatn = satn_i;
     if (gw_in_dinf) {
       dh_by_dz = (surfh + zmax - gwhead) / (0.5 * (surfh + dinf));
       esatn = 1.0;
     } else {
-      const double psi_c = (psi_u > kPsiMin) ? psi_u : kPsiMin;
+      const double psi_c = (psi_i > kPsiMin) ? psi_i : kPsiMin;
       const double h_u = psi_c + zmax - 0.5 * dinf;
       dh_by_dz = (surfh + zmax - h_u) / (0.5 * (surfh + dinf));
     }
@@ -339,17 +369,17 @@ __global__ void __launch_bounds__(256) k_elem_main(DevMesh m, const double *REST
     // EffKinf, src/vert_flow.c:211-270
     double kinf;
     if (areafh == 0.0) {
-      kinf = kinfv * satkfunc;
+      kinf = kinfv * satkfunc_i;
     } else if (surfh > kDeprStg) {
-      kinf = kinf_mat * satkfunc + kmac_a;
-    } else if (applrate <= dh_by_dz * kinfv * satkfunc) {
-      kinf = kinfv * satkfunc;
-    } else if (applrate < dh_by_dz * (kmac_a + kinf_mat * satkfunc)) {
+      kinf = kinf_mat * satkfunc_i + kmac_a;
+    } else if (applrate <= dh_by_dz * kinfv * satkfunc_i) {
+      kinf = kinfv * satkfunc_i;
+    } else if (applrate < dh_by_dz * (kmac_a + kinf_mat * satkfunc_i)) {
       // KrFunc(2, satn): pow(satn, 2) and pow(., 0.5) are a product and sqrt
       const double t2 = 1.0 - sqrt(1.0 - esatn * esatn);
-      kinf = kinf_mat * satkfunc + kmac_a * (sqrt(esatn) * t2 * t2);
+      kinf = kinf_mat * satkfunc_i + kmac_a * (sqrt(esatn) * t2 * t2);
     } else {
-      kinf = kinf_mat * satkfunc + kmac_a;
+      kinf = kinf_mat * satkfunc_i + kmac_a;
     }
     infil = kinf * dh_by_dz;
     if (!gw_in_dinf) infil = (infil > 0.0) ? infil : 0.0;
@@ -359,6 +389,7 @@ __global__ void __launch_bounds__(256) k_elem_main(DevMesh m, const double *REST
     infil = (infil > infil_max) ? infil_max : infil;
     infil *= wetfrac;
   }
+  if (m.noah) infil *= m.noah_fcr[i];  // frozen top soil, src/vert_flow.c:16-19
   double rechg;
   if (gw_in_dinf) {
     rechg = infil;

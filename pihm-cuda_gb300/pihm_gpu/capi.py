@@ -142,6 +142,19 @@ class GpuRhs:
         _check("pihm_gpu_set_river_edge_ovlflow",
                self.lib.pihm_gpu_set_river_edge_ovlflow(self.h, f64p(_c(ovl))))
 
+    def set_noah(self, noah: dict):
+        """Flux-PIHM right-hand side with Noah's per-step inputs (reference
+        order): et [nelem, nlayers], nwtbl, nroot, sh2o0, smcmin, smcmax, fcr."""
+        et = np.ascontiguousarray(noah["et"], np.float64)
+        nl = et.shape[1] if et.ndim == 2 else 0
+        nw = np.ascontiguousarray(noah["nwtbl"], np.int32)
+        nr = np.ascontiguousarray(noah["nroot"], np.int32)
+        f = self.lib.pihm_gpu_set_noah
+        f.argtypes = [_VP, _F64P, ctypes.c_int, _I32P, _I32P, _F64P, _F64P, _F64P, _F64P]
+        f.restype = ctypes.c_int
+        _check("pihm_gpu_set_noah", f(self.h, f64p(et), nl, i32p(nw), i32p(nr),
+                                      *(f64p(_c(noah[k])) for k in ("sh2o0", "smcmin", "smcmax", "fcr"))))
+
     def set_diagnostics(self, on: bool):
         _check("pihm_gpu_set_diagnostics", self.lib.pihm_gpu_set_diagnostics(self.h, int(on)))
 

@@ -569,3 +569,25 @@ def random_forcing(ws: Watershed, seed: int = 3):
     pcpdrp = np.where(rng.uniform(size=ne) < 0.5, rng.gamma(0.7, 3.0, ne), 0.0) / 3.6e6
     pet = rng.uniform(0.0, 0.3, ne) / 3.6e6
     return pcpdrp, 0.3 * pet, 0.7 * pet
+
+
+def noah_inputs(ws: Watershed, seed: int = 4, nlayers: int = 4) -> dict:
+    """Synthetic per-step outputs of the Noah land-surface model that the
+    Flux-PIHM right-hand side reads: transpiration per soil layer et
+    [nelem, nlayers] (m/s), the water-table layer nwtbl (0..nlayers+1) and the
+    root layers nroot (1..nlayers), the top layer's unfrozen moisture sh2o0
+    between the residual and saturated contents smcmin / smcmax (a few outside
+    to reach the saturation clamps; smcmax - smcmin = porosity), and the
+    frozen-soil infiltration factor fcr (1 for unfrozen soil, 0.3..1 for
+    a third of the elements)."""
+    rng = np.random.default_rng(9000 + seed)
+    ne = ws.nelem
+    por = ws.arrays["porosity"]
+    smcmin = rng.uniform(0.02, 0.08, ne)
+    smcmax = smcmin + por
+    et = rng.uniform(0.0, 2e-8, (ne, nlayers)) * (rng.random((ne, nlayers)) < 0.8)
+    nwtbl = rng.integers(0, nlayers + 2, ne).astype(np.int32)
+    nroot = rng.integers(1, nlayers + 1, ne).astype(np.int32)
+    sh2o0 = smcmin + por * rng.uniform(-0.05, 1.05, ne)
+    fcr = np.where(rng.random(ne) < 1.0 / 3.0, rng.uniform(0.3, 1.0, ne), 1.0)
+    return dict(et=et, nwtbl=nwtbl, nroot=nroot, sh2o0=sh2o0, smcmin=smcmin, smcmax=smcmax, fcr=fcr)

@@ -50,7 +50,7 @@ def compare(got, want, scale, rtol=RTOL):
     return bool(worst <= rtol and np.all(np.isfinite(got) == np.isfinite(want))), worst, k
 
 
-def scenario(ws, seed: int, bc: bool = False):
+def scenario(ws, seed: int, bc: bool = False, noah: bool = False):
     """A reproducible single-call scenario: state, forcing, carried values and
     (optionally) Dirichlet / Neumann boundary edges and river inflow BCs.
     Returns (watershed, scenario); with bc=True the watershed is a copy whose
@@ -87,11 +87,18 @@ def scenario(ws, seed: int, bc: bool = False):
         # NaN for inflow, and the reference then exits
         river_bc = np.where(rk == 1, ws.arrays["riv_zbed"] - rng.uniform(0.1, 1.0, nr),
                             np.where(rk == 2, rng.normal(0, 0.01, nr), 0.0))
-    return ws, dict(y=y, pcpdrp=pcpdrp, edir=edir, ett=ett, ws0=ws0, ovl=ovl,
-                    elem_bc=elem_bc, river_bc=river_bc)
+    sc = dict(y=y, pcpdrp=pcpdrp, edir=edir, ett=ett, ws0=ws0, ovl=ovl,
+              elem_bc=elem_bc, river_bc=river_bc)
+    if noah:
+        # Flux-PIHM: Noah's per-step inputs; some elements without transpiration
+        sc["noah"] = W.noah_inputs(ws, seed)
+        sc["ett"] = np.where(rng.random(ne) < 0.15, 0.0, ett)
+    return ws, sc
 
 
 def apply(model, sc):
+    if sc.get("noah") is not None:
+        model.set_noah(sc["noah"])
     model.set_forcing(sc["pcpdrp"], sc["edir"], sc["ett"])
     model.set_ws0_surf(sc["ws0"])
     model.set_river_edge_ovlflow(sc["ovl"])

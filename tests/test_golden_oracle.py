@@ -108,3 +108,38 @@ def test_oracle_bit_exact_with_reference_build():
             fa, fb = o.fluxes(), r.fluxes()
             for key in fa:
                 assert np.array_equal(fa[key], fb[key]), (seed, k, key)
+
+
+def _noah_inputs(z, tag):
+    return {k: z[f"{tag}_noah_{k}"] for k in ("et", "nwtbl", "nroot", "sh2o0", "smcmin", "smcmax", "fcr")}
+
+
+def test_oracle_matches_reference_noah_goldens():
+    """Flux-PIHM (_NOAH_) variant: bit for bit with the reference built with
+    -D_NOAH_ (tests/golden/make_golden_noah.py)."""
+    from oracle import Oracle
+    ws = _load_ws("c0_watershed.npz")
+    z = np.load(os.path.join(GOLD, "c0_noah_calls.npz"))
+    assert bytes(z["digest"]).decode() == ws.digest()
+    for seed in range(3):
+        tag = f"n{seed}"
+        o = Oracle(ws)
+        o.set_noah(_noah_inputs(z, tag))
+        o.set_forcing(z[f"{tag}_pcpdrp"], z[f"{tag}_edir"], z[f"{tag}_ett"])
+        o.set_ws0_surf(z[f"{tag}_ws0"])
+        o.set_river_edge_ovlflow(z[f"{tag}_ovl"])
+        for c in range(3):
+            got, rc = o.rhs(z[f"{tag}_call{c}_y"])
+            assert rc == 0
+            assert np.array_equal(got, z[f"{tag}_call{c}_ydot"]), (tag, c)
+            if c == 0:
+                fx = o.fluxes()
+                for k in ("ovlflow", "subsurf", "infil", "rechg", "et_split", "rivflow"):
+                    assert np.array_equal(fx[k], z[f"{tag}_call0_{k}"]), (tag, k)
+        # the variant is live: the plain right-hand side differs on these inputs
+        o2 = Oracle(ws)
+        o2.set_forcing(z[f"{tag}_pcpdrp"], z[f"{tag}_edir"], z[f"{tag}_ett"])
+        o2.set_ws0_surf(z[f"{tag}_ws0"])
+        o2.set_river_edge_ovlflow(z[f"{tag}_ovl"])
+        plain, _ = o2.rhs(z[f"{tag}_call0_y"])
+        assert not np.array_equal(plain, z[f"{tag}_call0_ydot"])

@@ -131,3 +131,43 @@ def test_nan_reports_error_without_exit():
     want, rc_o = o.rhs(sc["y"])
     got, rc_g = g.rhs_host(sc["y"])
     assert rc_o == 0 and rc_g == 0
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_flux_pihm_noah_variant(seed):
+    """Flux-PIHM right-hand side (Noah's per-step inputs) against the oracle,
+    which is pinned bit for bit to the reference built with _NOAH_."""
+    ws = W.generate(1000, 100, seed=seed)
+    ws, sc = scenario(ws, seed, noah=True)
+    o, g = _pair(ws)
+    apply(o, sc)
+    apply(g, sc)
+    _check_call(o, g, ws, sc, label=f"noah seed {seed}")
+
+
+def test_flux_pihm_noah_reference_goldens():
+    """The GPU Flux-PIHM right-hand side against the reference's own _NOAH_
+    build (tests/golden/c0_noah_calls.npz)."""
+    import os
+    from oracle import Oracle
+    from pihm_gpu.capi import GpuRhs
+    gold = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    ws = W.Watershed.load(os.path.join(gold, "c0_watershed.npz"))
+    z = np.load(os.path.join(gold, "c0_noah_calls.npz"))
+    for seed in range(3):
+        tag = f"n{seed}"
+        noah = {k: z[f"{tag}_noah_{k}"] for k in ("et", "nwtbl", "nroot", "sh2o0", "smcmin", "smcmax", "fcr")}
+        g, o = GpuRhs(ws), Oracle(ws)
+        for m in (g, o):
+            m.set_noah(noah)
+            m.set_forcing(z[f"{tag}_pcpdrp"], z[f"{tag}_edir"], z[f"{tag}_ett"])
+            m.set_ws0_surf(z[f"{tag}_ws0"])
+            m.set_river_edge_ovlflow(z[f"{tag}_ovl"])
+        for c in range(3):
+            y = z[f"{tag}_call{c}_y"]
+            got, rc = g.rhs_host(y)
+            _, _ = o.rhs(y)
+            assert rc == 0
+            scale = row_scales(ws, o.fluxes(), z[f"{tag}_pcpdrp"], z[f"{tag}_edir"], z[f"{tag}_ett"])
+            ok, worst, idx = compare(got, z[f"{tag}_call{c}_ydot"], scale)
+            assert ok, f"{tag} call {c}: worst {worst:.3e} at {idx}"
