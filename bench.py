@@ -243,6 +243,76 @@ def bench_batched():
     }
 
 
+FLUX_NELEM, FLUX_LAYERS, FLUX_STATES, FLUX_STEPS = 200_000, 4, 40, 10
+
+
+def bench_flux_pihm():
+    """Flux-PIHM right-hand side (Noah's per-step inputs fused into the
+    element kernel) on a 200,000-element mesh with 4 soil layers, beside the
+    plain right-hand side on the same states, and a short solve with the Noah
+    inputs renewed every model hour."""
+    import numpy as np
+    import torch
+    import pihm_gpu.watershed as W
+    from pihm_gpu import workloads as WL
+    from pihm_gpu.capi import GpuRhs
+    from pihm_gpu.single import GpuWatershed
+    from pihm_gpu.solver import StepControl, run_steps
+    ws = W.generate(FLUX_NELEM, WL.river_count(FLUX_NELEM), seed=2)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.Stream(device=dev)
+    base = W.reference_state(ws, 3)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(99)
+    res = {}
+    for mode in ("plain", "noah"):
+        g = GpuRhs(ws, stream=stream.cuda_stream)
+        g.set_forcing(*W.random_forcing(ws, 5))
+        g.set_ws0_surf(base[:ws.nelem])
+        if mode == "noah":
+            g.set_noah(W.noah_inputs(ws, 2, nlayers=FLUX_LAYERS))
+        with torch.cuda.stream(stream):
+            b = torch.from_numpy(base).to(dev)
+            ref = torch.stack([b * (0.9 + 0.2 * torch.rand(ws.neq, generator=gen, device=dev, dtype=torch.float64))
+                               for _ in range(FLUX_STATES)])
+            st = torch.empty_like(ref)
+            for k in range(FLUX_STATES):
+                g.to_internal(ref[k].data_ptr(), st[k].data_ptr())
+            yd = torch.empty((1, ws.neq), dtype=torch.float64, device=dev)
+        for k in range(3):
+            g.rhs_device(st[k].data_ptr(), yd[0].data_ptr())
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(FLUX_STATES):
+            g.rhs_device(st[k].data_ptr(), yd[0].data_ptr())
+        e1.record(stream)
+        e1.synchronize()
+        assert g.status() == 0
+        res[mode] = FLUX_NELEM * FLUX_STATES / (e0.elapsed_time(e1) * 1e-3)
+        g.close()
+    # a short solve: Noah's inputs renewed every model hour
+    pcp, edir, ett = WL.step_forcing(ws, FLUX_STEPS, 60.0, seed=8)
+    m = GpuWatershed(ws, W.relax_state(ws), pcp, edir, ett)
+    base_forcing = m.set_forcing
+
+    def forcing(k):
+        if k % 60 == 0:
+            m.g.set_noah(W.noah_inputs(ws, 100 + k // 60, nlayers=FLUX_LAYERS))
+        base_forcing(k)
+    t = time.perf_counter()
+    r = run_steps(m, StepControl(), FLUX_STEPS, forcing, outlet=int(np.where(ws.arrays["down"] < 0)[0][0]))
+    solve_s = time.perf_counter() - t
+    m.close()
+    return {"metric": "Flux-PIHM RHS element-evals/s", "unit": "elem-evals/s", "value": res["noah"],
+            "plain_rhs_value": res["plain"],
+            "workload": f"{FLUX_NELEM} elements, {ws.nriver} segments, {FLUX_LAYERS} Noah soil layers "
+                        f"(synthetic per-step Noah outputs), {FLUX_STATES} jittered states; solve: "
+                        f"{FLUX_STEPS} model steps of 60 s from RelaxIc",
+            "solve_s": solve_s, "solve_steps": int(r["stats"].nst),
+            "note": "Noah (SFLX) itself is not on this path: its per-step outputs are generated"}
+
+
 def bench_serving():
     """Poisson stream of calibration requests at SERVE_LOAD of measured capacity."""
     import numpy as np
@@ -318,6 +388,7 @@ def main():
     ap.add_argument("--nriver", type=int, default=NRIVER)
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-watersheds leg")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving leg")
+    ap.add_argument("--no-flux", action="store_true", help="skip the Flux-PIHM leg")
     args = ap.parse_args()
     globals()["NELEM"], globals()["NRIVER"] = args.nelem, args.nriver
     if args.impl == "reference":
@@ -455,7 +526,7 @@ def main():
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
 
     # ---- batched watersheds and serving (N = 1 only) ----
-    batched = serving = None
+    batched = serving = flux = None
     if rank == 0 and world == 1:
         g.close()
         if not args.no_batched:
@@ -468,6 +539,11 @@ def main():
                 serving = bench_serving()
             except Exception as exc:
                 serving = {"error": repr(exc)}
+        if not args.no_flux:
+            try:
+                flux = bench_flux_pihm()
+            except Exception as exc:
+                flux = {"error": repr(exc)}
 
     if rank == 0:
         line = {
@@ -492,6 +568,7 @@ def main():
             "setup_s": setup_s,
             "batched": batched,
             "serving": serving,
+            "flux_pihm": flux,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

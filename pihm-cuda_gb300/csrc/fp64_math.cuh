@@ -47,6 +47,46 @@ __device__ __forceinline__ double exp_dd_fast(double zh, double zl) {
   return __longlong_as_double(__double_as_longlong(res) + ((long long)q << 52));
 }
 
+// ln x as a double-double (sh + lo) for x positive and normal (the logarithm
+// half of pow_fast); false for anything else.
+__device__ __forceinline__ bool log_dd_fast(double x, double &sh, double &lo) {
+  const long long xb = __double_as_longlong(x);
+  const unsigned top = (unsigned)((unsigned long long)xb >> 52);  // sign and exponent
+  if (top - 1u >= 2046u) return false;  // x <= 0, zero, subnormal, inf or nan
+  const int k = (int)top - 1023;
+  const double m = __longlong_as_double((xb & 0x000FFFFFFFFFFFFFLL) | 0x3FF0000000000000LL);
+  const int i = (int)((xb >> 44) & 0xFF);
+  const double F = __ldg(&kLogF[i]);
+  const double gh = __ldg(&kLogGhi[i]);
+  const double gl = __ldg(&kLogGlo[i]);
+  const double p = m * F;
+  const double pe = fma(m, F, -p);
+  const double rh = p - 1.0;
+  double q = fma(rh, 1.0 / 7.0, -1.0 / 6.0);
+  q = fma(q, rh, 0.2);
+  q = fma(q, rh, -0.25);
+  q = fma(q, rh, 1.0 / 3.0);
+  q = fma(q, rh, -0.5);
+  const double t = (rh * rh) * q;
+  const double kd = (double)k;
+  const double s1 = fma(kd, kLn2Hi, gh);
+  sh = s1 + rh;
+  const double bb = sh - s1;
+  const double se = (s1 - (sh - bb)) + (rh - bb);
+  lo = se + (fma(-pe, rh, pe) + (t + fma(kd, kLn2Lo, gl)));
+  return true;
+}
+
+// x^y from ln x = sh + lo (log_dd_fast), y finite; pow(x, y) is the fallback
+// when y ln x leaves the fast range.  pow_fast(x, y) == pow_from_log(x, sh,
+// lo, y) bit for bit.
+__device__ __forceinline__ double pow_from_log(double x, double sh, double lo, double y) {
+  const double zh = y * sh;
+  const double zl = fma(y, lo, fma(y, sh, -zh));
+  if (!(fabs(zh) < 700.0)) return pow(x, y);
+  return exp_dd_fast(zh, zl);
+}
+
 __device__ __forceinline__ double pow_fast(double x, double y) {
   const long long xb = __double_as_longlong(x);
   const unsigned top = (unsigned)((unsigned long long)xb >> 52);  // sign and exponent

@@ -17,7 +17,7 @@ const double *DevMesh::*const kElemMember[EP_COUNT] = {
     &DevMesh::den_x, &DevMesh::den_y,
     &DevMesh::inv_area, &DevMesh::inv_por, &DevMesh::inv_alpha, &DevMesh::vg_m, &DevMesh::vg_e,
     &DevMesh::vg_ib, &DevMesh::kinf_mat, &DevMesh::kmac_a, &DevMesh::kv2_mac, &DevMesh::d_dinf,
-    &DevMesh::d_rzd, &DevMesh::d_dmac, &DevMesh::kh_k1};
+    &DevMesh::d_rzd, &DevMesh::d_dmac, &DevMesh::kh_k1, &DevMesh::inv_depth};
 const double *DevMesh::*const kEdgeMember[XP_COUNT] = {&DevMesh::edge, &DevMesh::nabrdist, &DevMesh::nabr_x,
                                                        &DevMesh::nabr_y};
 const double *DevMesh::*const kRiverMember[RP_COUNT] = {
@@ -237,6 +237,7 @@ int build_image(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double step
     e[EP_D_RZD][i] = depth - e[EP_RZD][i];
     e[EP_D_DMAC][i] = depth - e[EP_DMAC][i];
     e[EP_KH_K1][i] = e[EP_KMACH][i] * e[EP_AREAFV][i] + e[EP_KSATH][i] * (1.0 - e[EP_AREAFV][i]);
+    e[EP_INV_DEPTH][i] = 1.0 / depth;
   }
   im->nb.resize(3 * (size_t)ne);
   im->bct.resize(3 * (size_t)ne);

@@ -19,7 +19,7 @@ enum ElemPlane {
   EP_POROSITY, EP_DMAC, EP_KMACH, EP_KMACV, EP_AREAFV, EP_AREAFH, EP_ROUGH, EP_RZD,
   EP_DEN_X, EP_DEN_Y,
   EP_INV_AREA, EP_INV_POR, EP_INV_ALPHA, EP_VG_M, EP_VG_E, EP_VG_IB, EP_KINF_MAT, EP_KMAC_A,
-  EP_KV2_MAC, EP_D_DINF, EP_D_RZD, EP_D_DMAC, EP_KH_K1,
+  EP_KV2_MAC, EP_D_DINF, EP_D_RZD, EP_D_DMAC, EP_KH_K1, EP_INV_DEPTH,
   EP_COUNT
 };
 // Edge planes [3][ne] of doubles.

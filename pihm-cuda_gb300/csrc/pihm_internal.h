@@ -59,6 +59,7 @@ struct DevMesh {
   const double *kinf_mat, *kmac_a, *kv2_mac; // kinfv(1-areafh), kmacv areafh, AvgKv k2
   const double *d_dinf, *d_rzd, *d_dmac;     // depth-dinf, depth-rzd, depth-dmac
   const double *kh_k1;                       // EffKh k1 = kmach areafv + ksath (1-areafv)
+  const double *inv_depth;                   // 1/depth (Recharge's denominators sum to depth)
   // interior edges: each pair of neighbouring elements is evaluated once by
   // its owner and read with a sign by the other side
   int32_t nedge;

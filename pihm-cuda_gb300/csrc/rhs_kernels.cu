@@ -117,6 +117,27 @@ __device__ __forceinline__ double riv_perim(int order, double depth, double coef
   return 0.0;
 }
 
+// KrFunc (src/soil.c:8-13) and Psi (src/vert_flow.c:272-278) of one
+// saturation in [SATMIN, 1].  Psi's (1/satn)^m - 1 is evaluated as
+// (1 - satn^m) / satn^m from KrFunc's satn^m: one division in place of a
+// second logarithm-exponential pair (within an ulp of the reference's form,
+// the same cancellation as satn -> 1, and exactly 0 at satn = 1).
+__device__ __forceinline__ void kr_psi(double satn, double vm, double vg_e, double vg_ib, double inv_alpha,
+                                       double &satkfunc, double &psi) {
+  double lh, ll;
+  if (!log_dd_fast(satn, lh, ll)) {  // not positive and normal (NaN state)
+    const double t = 1.0 - pow_fast(1.0 - pow_fast(satn, vm), vg_e);
+    satkfunc = sqrt(satn) * t * t;
+    psi = -pow_fast(pow_fast(1.0 / satn, vm) - 1.0, vg_ib) * inv_alpha;
+    return;
+  }
+  const double x1 = pow_from_log(satn, lh, ll, vm);  // satn^m, as pow_fast(satn, m)
+  const double a = 1.0 - x1;
+  const double t = 1.0 - pow_fast(a, vg_e);
+  satkfunc = sqrt(satn) * t * t;
+  psi = -pow_fast(a / x1, vg_ib) * inv_alpha;
+}
+
 // Batch engine: whether the watershed of item idx sits out this evaluation
 // (a free arena slot, or a watershed that did not ask for one).  Always false
 // in a single-watershed context.
@@ -321,12 +342,7 @@ __global__ void __launch_bounds__(256) k_elem_main(DevMesh m, const double *REST
     satn = unsat / deficit;
     satn = (satn > 1.0) ? 1.0 : satn;
     satn = (satn < kSatMin) ? kSatMin : satn;
-    const double vm = m.vg_m[i];
-    // KrFunc, src/soil.c:8-13
-    const double t = 1.0 - pow_fast(1.0 - pow_fast(satn, vm), m.vg_e[i]);
-    satkfunc = sqrt(satn) * t * t;
-    // Psi, src/vert_flow.c:272-278
-    psi_u = -pow_fast(pow_fast(1.0 / satn, vm) - 1.0, m.vg_ib[i]) * m.inv_alpha[i];
+    kr_psi(satn, m.vg_m[i], m.vg_e[i], m.vg_ib[i], m.inv_alpha[i], satkfunc, psi_u);
   }
   // Infil's saturation: the same one, except in Flux-PIHM, where it is
   // Noah's top-layer moisture (src/vert_flow.c:94-98) and Recharge keeps
@@ -336,11 +352,8 @@ __global__ void __launch_bounds__(256) k_elem_main(DevMesh m, const double *REST
     double s = m.noah_satn[i];
     s = (s > 1.0) ? 1.0 : s;
     s = (s < kSatMin) ? kSatMin : s;
-    const double vm = m.vg_m[i];
-    const double t = 1.0 - pow_fast(1.0 - pow_fast(s, vm), m.vg_e[i]);
     satn_i = s;
-    satkfunc_i = sqrt(s) * t * t;
-    psi_i = -pow_fast(pow_fast(1.0 / s, vm) - 1.0, m.vg_ib[i]) * m.inv_alpha[i];
+    kr_psi(s, m.vg_m[i], m.vg_e[i], m.vg_ib[i], m.inv_alpha[i], satkfunc_i, psi_i);
   }
   // KrFunc(beta, 1) == 1 exactly: pow(1 - pow(1, m), e) == pow(0, e) == 0
   double infil;
@@ -395,7 +408,10 @@ __global__ void __launch_bounds__(256) k_elem_main(DevMesh m, const double *REST
     rechg = infil;
   } else {
     const double deficit = depth - gw;
-    const double dh_by_dz = (0.5 * deficit + psi_u) / (0.5 * (deficit + gw));
+    // the denominators of Recharge add up to depth: (deficit + gw) and the
+    // AvgKv weights d1 + d2 + d3 (to an ulp); multiply by 1/depth instead
+    const double inv_depth = m.inv_depth[i];
+    const double dh_by_dz = (0.5 * deficit + psi_u) * (2.0 * inv_depth);
     // AvgKv, src/vert_flow.c:172-209, arithmetic mean (_ARITH_ is defined at
     // src/include/pihm_func.h:4)
     double k1, k2, k3, d1, d2, d3;
@@ -414,7 +430,7 @@ __global__ void __launch_bounds__(256) k_elem_main(DevMesh m, const double *REST
       k3 = ksatv;
       d3 = gw - (dmac - deficit);
     }
-    const double kavg = (k1 * d1 + k2 * d2 + k3 * d3) / (d1 + d2 + d3);
+    const double kavg = (k1 * d1 + k2 * d2 + k3 * d3) * inv_depth;
     rechg = kavg * dh_by_dz;
     rechg = (rechg > 0.0 && unsat <= 0.0) ? 0.0 : rechg;
     rechg = (rechg < 0.0 && gw <= 0.0) ? 0.0 : rechg;
