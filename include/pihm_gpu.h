@@ -200,6 +200,19 @@ int pihm_gpu_set_noah(pihm_gpu_ctx *ctx, const double *et, int nlayers, const in
  * running sum of out[0] - out[1] - (out[2] - previous out[2]).  Synchronous. */
 int pihm_gpu_water_balance(pihm_gpu_ctx *ctx, const double *y_dev, double dt, double *out);
 
+/* Restart files in the reference's binary .ic format (host only, no GPU):
+ * per element cmc, sneqv, surf, unsat, gw, then per segment stage, gw, as
+ * ReadIc reads them (src/read_ic.c:3-39) and PrintInit writes them
+ * (src/print.c:213-330).  y is the state vector in reference order
+ * [surf | unsat | gw | stage | rivgw]; cmc and sneqv (canopy and snow
+ * storage, not part of y) may be NULL (written as 0 / not returned).
+ * pihm_ic_read returns PIHM_GPU_ERR_MESH when the file size does not match
+ * nelem and nriver, as the reference refuses such a file. */
+int pihm_ic_write(const char *path, int32_t nelem, int32_t nriver, const double *y,
+                  const double *cmc, const double *sneqv);
+int pihm_ic_read(const char *path, int32_t nelem, int32_t nriver, double *y, double *cmc,
+                 double *sneqv);
+
 /* Keep per-element and per-segment fluxes of every later call so that
  * pihm_gpu_get_fluxes can read them (costs extra stores). */
 int pihm_gpu_set_diagnostics(pihm_gpu_ctx *ctx, int on);

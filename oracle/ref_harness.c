@@ -172,6 +172,30 @@ int ref_load_example(const char *workdir, const char *proj, double *y0,
 
 #endif /* !_NOAH_ */
 
+#if !defined(_NOAH_)
+/* Read a restart file with the reference's own ReadIc (src/read_ic.c:3) into
+ * the model built by ref_build, and return what it stored: y in reference
+ * order from ic.surf/unsat/gw and river ic.stage/gw, and ic.cmc, ic.sneqv. */
+int ref_read_ic(const char *path, double *y, double *cmc, double *sneqv)
+{
+    int i;
+    if (!g_pihm) return -1;
+    ReadIc(path, g_pihm->elem, g_pihm->river);
+    for (i = 0; i < nelem; i++) {
+        y[i] = g_pihm->elem[i].ic.surf;
+        y[nelem + i] = g_pihm->elem[i].ic.unsat;
+        y[2 * nelem + i] = g_pihm->elem[i].ic.gw;
+        cmc[i] = g_pihm->elem[i].ic.cmc;
+        sneqv[i] = g_pihm->elem[i].ic.sneqv;
+    }
+    for (i = 0; i < nriver; i++) {
+        y[3 * nelem + i] = g_pihm->river[i].ic.stage;
+        y[3 * nelem + nriver + i] = g_pihm->river[i].ic.gw;
+    }
+    return 0;
+}
+#endif
+
 int ref_sizes(int *ne, int *nr, int *stepsize, int *surf_mode, int *riv_mode)
 {
     if (!g_pihm) return -1;

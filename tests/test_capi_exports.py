@@ -16,7 +16,7 @@ def _declared():
         src = open(h).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
         src = re.sub(r"//[^\n]*", "", src)
-        for m in re.finditer(r"\b(pihm_(?:gpu|bdf|batch|serve)_\w+|N_V\w+_PihmGpu)\s*\(", src):
+        for m in re.finditer(r"\b(pihm_(?:gpu|bdf|batch|serve|ic)_\w+|N_V\w+_PihmGpu)\s*\(", src):
             names.add(m.group(1))
     return names
 
