@@ -219,6 +219,8 @@ int place(pihm_batch *B, Sys *s, const Prepared &job) {
   rc |= h2d((int32_t *)m.sys_bank + bo, own.data(), im.nbank, st);
   const double dt = job.ctrl.stepsize;
   rc |= h2d((double *)m.sys_dt + s->slot, &dt, 1, st);
+  const double inv_dt = 1.0 / dt;
+  rc |= h2d((double *)m.sys_inv_dt + s->slot, &inv_dt, 1, st);
   // initial state, internal order, into vector slot 0
   std::vector<double> y(s->neq);
   for (int p = 0; p < 3; p++)
@@ -623,6 +625,7 @@ int pihm_batch_create(const pihm_batch_limits *lim, int surf_mode, int riv_mode,
   m.sys_edge = sed;
   m.sys_bank = sb;
   m.sys_dt = D(MS);
+  m.sys_inv_dt = D(MS);
   DeviceArena &A = B->A;
   A.vec = D((size_t)kVecSlots * NEQ);
   A.neq_cap = NEQ;

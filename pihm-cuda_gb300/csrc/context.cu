@@ -101,6 +101,7 @@ int pihm_gpu_create(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double 
   m.surf_mode = surf_mode;
   m.riv_mode = riv_mode;
   m.dt = stepsize;
+  m.inv_dt = 1.0 / stepsize;
   for (int k = 0; k < EP_COUNT; k++) m.*kElemMember[k] = put(im.el[k].data(), NE, NE);
   for (int k = 0; k < XP_COUNT; k++) m.*kEdgeMember[k] = put(im.ed[k].data(), 3 * NE, 3 * NE);
   m.nb = put(im.nb.data(), 3 * NE, 3 * NE);

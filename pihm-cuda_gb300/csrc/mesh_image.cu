@@ -14,7 +14,7 @@ const double *DevMesh::*const kElemMember[EP_COUNT] = {
     &DevMesh::area, &DevMesh::zmin, &DevMesh::zmax, &DevMesh::depth, &DevMesh::ksath, &DevMesh::ksatv,
     &DevMesh::kinfv, &DevMesh::dinf, &DevMesh::alpha, &DevMesh::beta, &DevMesh::porosity, &DevMesh::dmac,
     &DevMesh::kmach, &DevMesh::kmacv, &DevMesh::areafv, &DevMesh::areafh, &DevMesh::rough, &DevMesh::rzd,
-    &DevMesh::den_x, &DevMesh::den_y,
+    &DevMesh::inv_den_x, &DevMesh::inv_den_y,
     &DevMesh::inv_area, &DevMesh::inv_por, &DevMesh::inv_alpha, &DevMesh::vg_m, &DevMesh::vg_e,
     &DevMesh::vg_ib, &DevMesh::kinf_mat, &DevMesh::kmac_a, &DevMesh::kv2_mac, &DevMesh::d_dinf,
     &DevMesh::d_rzd, &DevMesh::d_dmac, &DevMesh::kh_k1, &DevMesh::inv_depth};
@@ -210,12 +210,13 @@ int build_image(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double step
   for (int k = EP_DEN_X; k < EP_COUNT; k++) im->el[k].resize(ne);
   const std::vector<double> &nx = im->ed[XP_NABR_X], &ny = im->ed[XP_NABR_Y];
   for (int i = 0; i < ne; i++) {
-    // denominators of DhByDl (src/lat_flow.c:239-246): l2[2](l1[1]-l1[0]) +
-    // l2[1](l1[0]-l1[2]) + l2[0](l1[2]-l1[1]) for (l1,l2) = (y,x) and (x,y)
+    // reciprocals of the denominators of DhByDl (src/lat_flow.c:239-246):
+    // l2[2](l1[1]-l1[0]) + l2[1](l1[0]-l1[2]) + l2[0](l1[2]-l1[1]) for
+    // (l1,l2) = (y,x) and (x,y)
     const double x0 = nx[i], x1 = nx[ne + i], x2 = nx[2 * (size_t)ne + i];
     const double y0 = ny[i], y1 = ny[ne + i], y2 = ny[2 * (size_t)ne + i];
-    im->el[EP_DEN_X][i] = x2 * (y1 - y0) + x1 * (y0 - y2) + x0 * (y2 - y1);
-    im->el[EP_DEN_Y][i] = y2 * (x1 - x0) + y1 * (x0 - x2) + y0 * (x2 - x1);
+    im->el[EP_DEN_X][i] = 1.0 / (x2 * (y1 - y0) + x1 * (y0 - y2) + x0 * (y2 - y1));
+    im->el[EP_DEN_Y][i] = 1.0 / (y2 * (x1 - x0) + y1 * (x0 - x2) + y0 * (x2 - x1));
   }
   // derived element constants (see DevMesh); same expressions as the
   // reference's inline ones, evaluated without contraction

@@ -40,7 +40,7 @@ constexpr int32_t kBoundary = INT32_MIN;
 struct DevMesh {
   int32_t ne, nr, nbank;
   int surf_mode, riv_mode;
-  double dt;  // model step (s), caps infiltration
+  double dt, inv_dt;  // model step (s), caps infiltration; its reciprocal
 
   // element static data [ne]
   const double *area, *zmin, *zmax;
@@ -50,7 +50,7 @@ struct DevMesh {
   const int32_t *nb;        // neighbour (encoded as above)
   const int32_t *bctype;    // boundary condition type (boundary edges)
   const double *edge, *nabrdist, *nabr_x, *nabr_y;
-  const double *den_x, *den_y;  // [ne] geometric denominators of the gradient
+  const double *inv_den_x, *inv_den_y;  // [ne] reciprocals of the gradient's geometric denominators
   // element constants derived once at load: the reference evaluates these
   // sub-expressions inline with the same operation order (bit-identical),
   // except the reciprocals, which replace divisions (<= 1 ulp apart)
@@ -104,7 +104,7 @@ struct DevMesh {
   // and their error words.
   const int32_t *sys_elem, *sys_riv, *sys_edge, *sys_bank;
   const uint8_t *active;
-  const double *sys_dt;
+  const double *sys_dt, *sys_inv_dt;
   unsigned int *err_sys;
 
   // Flux-PIHM (_NOAH_) right-hand side, when noah != 0: per element, from

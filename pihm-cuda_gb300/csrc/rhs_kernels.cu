@@ -193,8 +193,8 @@ __global__ void __launch_bounds__(256) k_elem_grad(DevMesh m, const double *REST
   const double y0 = m.nabr_y[i], y1 = m.nabr_y[ne + i], y2 = m.nabr_y[2 * ne + i];
   const double x0 = m.nabr_x[i], x1 = m.nabr_x[ne + i], x2 = m.nabr_x[2 * ne + i];
   // DhByDl(nabr_y, nabr_x, h) and DhByDl(nabr_x, nabr_y, h)
-  const double dhdx = -1.0 * (y2 * (h[1] - h[0]) + y1 * (h[0] - h[2]) + y0 * (h[2] - h[1])) / m.den_x[i];
-  const double dhdy = -1.0 * (x2 * (h[1] - h[0]) + x1 * (h[0] - h[2]) + x0 * (h[2] - h[1])) / m.den_y[i];
+  const double dhdx = -1.0 * (y2 * (h[1] - h[0]) + y1 * (h[0] - h[2]) + y0 * (h[2] - h[1])) * m.inv_den_x[i];
+  const double dhdy = -1.0 * (x2 * (h[1] - h[0]) + x1 * (h[0] - h[2]) + x0 * (h[2] - h[1])) * m.inv_den_y[i];
   m.gradmag[i] = sqrt(dhdx * dhdx + dhdy * dhdy);
 }
 
@@ -397,8 +397,8 @@ __global__ void __launch_bounds__(256) k_elem_main(DevMesh m, const double *REST
     infil = kinf * dh_by_dz;
     if (!gw_in_dinf) infil = (infil > 0.0) ? infil : 0.0;
     const double ws0 = m.ws0_surf[i];
-    const double dt = m.sys_dt ? m.sys_dt[sy] : m.dt;
-    const double infil_max = applrate + ((ws0 > 0.0) ? ws0 / dt : 0.0);
+    const double inv_dt = m.sys_inv_dt ? m.sys_inv_dt[sy] : m.inv_dt;
+    const double infil_max = applrate + ((ws0 > 0.0) ? ws0 * inv_dt : 0.0);
     infil = (infil > infil_max) ? infil_max : infil;
     infil *= wetfrac;
   }
