@@ -210,6 +210,8 @@ int place(pihm_batch *B, Sys *s, const Prepared &job) {
   // a fresh watershed carries no river-edge flux from an earlier evaluation
   for (int k = 0; k < NUM_RIVFLX; k++)
     if (nr && cudaMemsetAsync(m.rivflow + k * NR + ro, 0, sizeof(double) * nr, st) != cudaSuccess) rc = -1;
+  for (int k = 0; k < 2; k++)
+    if (nr && cudaMemsetAsync(m.carry_ovl + k * NR + ro, 0, sizeof(double) * nr, st) != cudaSuccess) rc = -1;
   // owner tables
   std::vector<int32_t> own(std::max<int64_t>({(int64_t)ne, (int64_t)nr, (int64_t)im.nedge, (int64_t)im.nbank, 1}),
                            s->slot);
@@ -436,7 +438,8 @@ int run_round(pihm_batch *B, bool *any) {
   if (tune) cudaEventRecord(B->tev[1], st);
   if (rhs) {
     if (cudaMemsetAsync(B->err_sys, 0, sizeof(unsigned int) * B->max_sys, st) != cudaSuccess) return -1;
-    if (launch_rhs(B->A.m, B->A.rhs_in, B->A.rhs_out, st, &B->launches, nullptr) != cudaSuccess) return -1;
+    if (launch_rhs(B->A.m, B->A.rhs_in, B->A.rhs_out, st, &B->launches, nullptr, &B->side) != cudaSuccess)
+      return -1;
     B->rhs_rounds++;
   }
   if (B->profiling) cudaEventRecord(B->ev[2], st);
@@ -615,6 +618,7 @@ int pihm_batch_create(const pihm_batch_limits *lim, int surf_mode, int riv_mode,
   m.effk = D(NE);
   m.gradmag = D(NE);
   m.rivflow = D(NUM_RIVFLX * NR);
+  m.carry_ovl = D(2 * NR);
   m.eflux_ovl = D(NED);
   m.eflux_sub = D(NED);
   m.bank_part = D(8 * NE);
@@ -663,9 +667,14 @@ int pihm_batch_create(const pihm_batch_limits *lim, int surf_mode, int riv_mode,
            cudaMemset(A.tickets, 0, sizeof(unsigned int) * MS) == cudaSuccess &&
            cudaMemset(B->d_up, 0, up_bytes) == cudaSuccess &&
            cudaMemset(m.rivflow, 0, sizeof(double) * NUM_RIVFLX * NR) == cudaSuccess &&
+           cudaMemset(m.carry_ovl, 0, sizeof(double) * 2 * NR) == cudaSuccess &&
            cudaMemset(A.rhs_in, 0, sizeof(double) * NEQ) == cudaSuccess &&
            cudaDeviceSynchronize() == cudaSuccess;
   if (!z) return PIHM_GPU_ERR_CUDA;
+  if (cudaStreamCreateWithFlags(&B->side.side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&B->side.fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&B->side.join, cudaEventDisableTiming) != cudaSuccess)
+    return PIHM_GPU_ERR_CUDA;
   for (cudaEvent_t &e : B->tev)
     if (cudaEventCreate(&e) != cudaSuccess) return PIHM_GPU_ERR_CUDA;
   B->update_extents();

@@ -83,7 +83,5 @@ cudaError_t launch_program(const DeviceArena &a, int nrs, int nblocks, int varia
 
 }  // namespace batch
 
-cudaError_t launch_rhs(const DevMesh &m, const double *y, double *ydot, cudaStream_t st,
-                       long long *launches, Profiler *prof);
 
 }  // namespace pihm

@@ -201,6 +201,7 @@ struct pihm_batch {
   double tune_ms_per_block[pihm::batch::kProgramVariants] = {0};
   int tune_n[pihm::batch::kProgramVariants] = {0};
   cudaEvent_t tev[2] = {nullptr, nullptr};
+  pihm::RhsStreams side;  // river kernel beside the element kernels
   // counters and timing (host: building rounds and running the coroutines;
   // wait: blocked on the device; program/rhs: device time, when profiling)
   long long rounds = 0, rhs_rounds = 0, launches = 0;
@@ -216,6 +217,9 @@ struct pihm_batch {
       if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : tev)
       if (e) cudaEventDestroy(e);
+    if (side.fork) cudaEventDestroy(side.fork);
+    if (side.join) cudaEventDestroy(side.join);
+    if (side.side) cudaStreamDestroy(side.side);
     slots.clear();
     for (void *p : owned) cudaFree(p);
     if (h_up) cudaFreeHost(h_up);

@@ -13,8 +13,6 @@
 #include "pihm_internal.h"
 
 namespace pihm {
-cudaError_t launch_rhs(const DevMesh &m, const double *y, double *ydot, cudaStream_t st,
-                       long long *launches, Profiler *prof);
 cudaError_t launch_permute(const double *src, double *dst, const int32_t *perm, int ne, int nr,
                            int to_internal, cudaStream_t st);
 }  // namespace pihm
@@ -141,6 +139,7 @@ int pihm_gpu_create(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double 
   dbytes += carve_size<double>(NR);           // river_bc
   dbytes += 4 * carve_size<double>(NE);       // surfh, head, effk, gradmag
   dbytes += carve_size<double>(11 * NR);      // rivflow
+  dbytes += carve_size<double>(2 * NR);       // carried river-edge overland flux
   dbytes += 2 * carve_size<double>(NED);      // edge fluxes
   dbytes += carve_size<double>(8 * NB);       // bank_part
   dbytes += 2 * carve_size<double>(3 * NE) + 2 * carve_size<double>(NE) + carve_size<double>(5 * NE);
@@ -163,6 +162,7 @@ int pihm_gpu_create(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double 
   m.surfh = carve<double>(dp, NE); m.head = carve<double>(dp, NE); m.effk = carve<double>(dp, NE);
   m.gradmag = carve<double>(dp, NE);
   m.rivflow = carve<double>(dp, 11 * NR);
+  m.carry_ovl = carve<double>(dp, 2 * NR);
   m.eflux_ovl = carve<double>(dp, NED); m.eflux_sub = carve<double>(dp, NED);
   m.bank_part = carve<double>(dp, 8 * NB);
   m.d_ovl = carve<double>(dp, 3 * NE); m.d_sub = carve<double>(dp, 3 * NE);
@@ -171,6 +171,12 @@ int pihm_gpu_create(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double 
   c->d_stage_out = carve<double>(dp, c->neq);
   m.err = carve<unsigned int>(dp, 1);
   m.diag = 0;
+  if (cudaStreamCreateWithFlags(&c->side.side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->side.fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->side.join, cudaEventDisableTiming) != cudaSuccess) {
+    pihm_gpu_destroy(c);
+    return PIHM_GPU_ERR_CUDA;
+  }
   *out = c;
   return PIHM_GPU_OK;
 }
@@ -189,6 +195,9 @@ void pihm_gpu_destroy(pihm_gpu_ctx *c) {
   if (c->d_static) cudaFree(c->d_static);
   if (c->d_dyn) cudaFree(c->d_dyn);
   if (c->d_noah) cudaFree(c->d_noah);
+  if (c->side.fork) cudaEventDestroy(c->side.fork);
+  if (c->side.join) cudaEventDestroy(c->side.join);
+  if (c->side.side) cudaStreamDestroy(c->side.side);
   std::free(c->h_perm);
   std::free(c->h_iperm);
   delete c;
@@ -305,7 +314,8 @@ int pihm_gpu_set_river_edge_ovlflow(pihm_gpu_ctx *c, const double *ovl) {
   if (!c || !ovl) return PIHM_GPU_ERR_ARG;
   if (!c->nr) return PIHM_GPU_OK;
   // the carried value of element e's river edge is -rivflow[LEFT/RIGHT_SURF2CHANL]
-  // of that river (src/river_flow.c:159-182); rebuild those two slots
+  // of that river (src/river_flow.c:159-182); rebuild the carry (and those
+  // two slots)
   std::vector<double> slots(2 * (size_t)c->nr, 0.0);
   const int ne = c->ne;
   std::vector<int32_t> left(c->nr), right(c->nr);
@@ -324,7 +334,9 @@ int pihm_gpu_set_river_edge_ovlflow(pihm_gpu_ctx *c, const double *ovl) {
       }
     }
   double *F = c->m.rivflow;
-  return cuda_fail(cudaMemcpyAsync(F + LEFT_SURF2CHANL * (size_t)c->nr, slots.data(),
+  return cuda_fail(cudaMemcpyAsync(c->m.carry_ovl, slots.data(), sizeof(double) * 2 * c->nr,
+                                   cudaMemcpyHostToDevice, c->stream)) ?:
+         cuda_fail(cudaMemcpyAsync(F + LEFT_SURF2CHANL * (size_t)c->nr, slots.data(),
                                    sizeof(double) * c->nr, cudaMemcpyHostToDevice, c->stream)) ?:
          cuda_fail(cudaMemcpyAsync(F + RIGHT_SURF2CHANL * (size_t)c->nr, slots.data() + c->nr,
                                    sizeof(double) * c->nr, cudaMemcpyHostToDevice, c->stream)) ?:
@@ -335,7 +347,7 @@ int pihm_gpu_rhs(pihm_gpu_ctx *c, double t, const double *y, double *ydot) {
   (void)t;
   if (!c || !y || !ydot) return PIHM_GPU_ERR_ARG;
   c->m.diag = c->diag;
-  return cuda_fail(launch_rhs(c->m, y, ydot, c->stream, &c->launches, c->prof));
+  return cuda_fail(launch_rhs(c->m, y, ydot, c->stream, &c->launches, c->prof, &c->side));
 }
 
 int pihm_gpu_status(pihm_gpu_ctx *c) {
@@ -363,7 +375,7 @@ int pihm_gpu_rhs_host(pihm_gpu_ctx *c, double t, const double *y_host, double *y
   double *y_int = c->d_stage_out, *ydot_int = c->d_stage_in;
   if (e == cudaSuccess) {
     c->m.diag = c->diag;
-    e = launch_rhs(c->m, y_int, ydot_int, c->stream, &c->launches, c->prof);
+    e = launch_rhs(c->m, y_int, ydot_int, c->stream, &c->launches, c->prof, &c->side);
   }
   if (e == cudaSuccess) {
     e = launch_permute(ydot_int, c->d_stage_out, c->d_perm, c->ne, c->nr, 0, c->stream);

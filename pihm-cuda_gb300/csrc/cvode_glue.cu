@@ -8,11 +8,6 @@
 #include "pihm_internal.h"
 #include "pihm_nvector.h"
 
-namespace pihm {
-cudaError_t launch_rhs(const DevMesh &m, const double *y, double *ydot, cudaStream_t st,
-                       long long *launches, Profiler *prof);
-}
-
 namespace {
 
 struct HostContentPrefix {  // SUNDIALS 2.7 serial / OpenMP content layout prefix
@@ -47,7 +42,7 @@ int pihm_gpu_ode(double t, N_Vector y, N_Vector ydot, void *user_data) {
     if (N_VGetLength_PihmGpu(y) != c->neq || N_VGetLength_PihmGpu(ydot) != c->neq) return -1;
     c->m.diag = c->diag;
     if (pihm::launch_rhs(c->m, N_VGetDeviceArrayPointer_PihmGpu(y), N_VGetDeviceArrayPointer_PihmGpu(ydot),
-                         c->stream, &c->launches, c->prof) != cudaSuccess)
+                         c->stream, &c->launches, c->prof, &c->side) != cudaSuccess)
       return -1;
     if (c->nan_check_deferred) return 0;
     return pihm_gpu_status(c) == PIHM_GPU_OK ? 0 : -1;

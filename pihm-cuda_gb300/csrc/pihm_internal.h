@@ -86,7 +86,10 @@ struct DevMesh {
   // scratch written and read inside one evaluation
   double *surfh, *head, *effk, *gradmag;  // [ne]
   double *eflux_ovl, *eflux_sub;          // [nedge]
-  double *rivflow;                        // [11][nr]; slots 2/3 carry over
+  double *rivflow;                        // [11][nr]
+  double *carry_ovl;                      // [2][nr] river-edge overland flux (LEFT, RIGHT
+                                          // SURF2CHANL of the last evaluation) that the
+                                          // next evaluation's Infil reads
   double *bank_part;                      // [8][nbank]
   // diagnostics (optional)
   double *d_ovl, *d_sub, *d_infil, *d_rechg, *d_et;  // [3][ne],[3][ne],[ne],[ne],[5][ne]
@@ -132,6 +135,17 @@ struct Profiler {
 
 enum KernelId { K_PREP = 0, K_GRAD, K_MAIN, K_RIVER, K_FINISH, K_EDGE, K_PERMUTE };
 
+// A second stream on which the river kernel of an evaluation runs beside the
+// element kernels (it needs only k_elem_prep's outputs), joined before
+// k_finish.  Null members: everything on one stream.
+struct RhsStreams {
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+};
+
+cudaError_t launch_rhs(const DevMesh &m, const double *y, double *ydot, cudaStream_t st,
+                       long long *launches, Profiler *prof, const RhsStreams *side = nullptr);
+
 }  // namespace pihm
 
 struct pihm_gpu_ctx {
@@ -152,4 +166,5 @@ struct pihm_gpu_ctx {
   long long launches;      // kernels launched by this context so far
   pihm::Profiler *prof;    // non-null while profiling is on
   void *d_noah;            // Flux-PIHM input planes, allocated on first use
+  pihm::RhsStreams side;   // river kernel beside the element kernels
 };

@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(256) k_edge(DevMesh m, const double *RESTRICT 
 // ---------------------------------------------------------------------------
 // k_elem_main
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_elem_main(DevMesh m, const double *RESTRICT y,
+__global__ void __launch_bounds__(256, 3) k_elem_main(DevMesh m, const double *RESTRICT y,
                                                     double *RESTRICT ydot) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   int sy;
@@ -278,8 +278,7 @@ __global__ void __launch_bounds__(256) k_elem_main(DevMesh m, const double *REST
       if (nb != kBoundary) {
         // river edge: Infil sees the previous evaluation's value
         const int s = -1 - nb;
-        const int slot = (m.left[s] == i) ? LEFT_SURF2CHANL : RIGHT_SURF2CHANL;
-        ovl[j] = -m.rivflow[slot * m.nr + s];
+        ovl[j] = -m.carry_ovl[(m.left[s] == i ? 0 : 1) * m.nr + s];
         sub[j] = 0.0;
         riv[j] = true;
       } else {
@@ -712,6 +711,10 @@ __global__ void __launch_bounds__(128) k_finish(DevMesh m, double *RESTRICT ydot
       m.rivflow[UP_AQUIF2AQUIF * nr + s] = up_a;
     }
     if (isnan(ds) | isnan(dg)) report_err(m, sy);
+    // the next evaluation's Infil reads this evaluation's river-edge
+    // overland flux (src/vert_flow.c:61 before src/river_flow.c:159-182)
+    m.carry_ovl[s] = F[LEFT_SURF2CHANL * nr + s];
+    m.carry_ovl[nr + s] = F[RIGHT_SURF2CHANL * nr + s];
     return;
   }
   const int b = t - m.nr_run;
@@ -810,13 +813,24 @@ static void prof_end(Profiler *p, bool on, cudaStream_t st) {
 }
 
 cudaError_t launch_rhs(const DevMesh &m, const double *y, double *ydot, cudaStream_t st,
-                       long long *launches, Profiler *prof) {
+                       long long *launches, Profiler *prof, const RhsStreams *side) {
   bool on;
+  // the river kernel reads only k_elem_prep's outputs, the state and static
+  // data, so with a side stream it runs beside grad/edge/main (per-kernel
+  // timing keeps one stream)
+  const bool fork = side && side->side && !prof && m.ne_run > 0 && m.nr_run > 0;
   if (m.ne_run > 0) {
     on = prof_begin(prof, K_PREP, st);
     k_elem_prep<<<blocks_for(m.ne_run, 256), 256, 0, st>>>(m, y);
     prof_end(prof, on, st);
     ++*launches;
+    if (fork) {
+      if (cudaEventRecord(side->fork, st) != cudaSuccess) return cudaErrorUnknown;
+      if (cudaStreamWaitEvent(side->side, side->fork, 0) != cudaSuccess) return cudaErrorUnknown;
+      k_river<<<blocks_for(m.nr_run, 128), 128, 0, side->side>>>(m, y);
+      ++*launches;
+      if (cudaEventRecord(side->join, side->side) != cudaSuccess) return cudaErrorUnknown;
+    }
     if (m.surf_mode == kDiffWave) {
       on = prof_begin(prof, K_GRAD, st);
       k_elem_grad<<<blocks_for(m.ne_run, 256), 256, 0, st>>>(m, y);
@@ -834,7 +848,9 @@ cudaError_t launch_rhs(const DevMesh &m, const double *y, double *ydot, cudaStre
     prof_end(prof, on, st);
     ++*launches;
   }
-  if (m.nr_run > 0) {
+  if (fork) {
+    if (cudaStreamWaitEvent(st, side->join, 0) != cudaSuccess) return cudaErrorUnknown;
+  } else if (m.nr_run > 0) {
     on = prof_begin(prof, K_RIVER, st);
     k_river<<<blocks_for(m.nr_run, 128), 128, 0, st>>>(m, y);
     prof_end(prof, on, st);
