@@ -24,6 +24,7 @@
 
 #include <cmath>
 
+#include "fp64_cmp.h"
 #include "fp64_tables.h"
 
 namespace pihm {
@@ -77,14 +78,36 @@ __device__ __forceinline__ bool log_dd_fast(double x, double &sh, double &lo) {
   return true;
 }
 
+// y (sh + lo) as a double-double zh + zl (Dekker's product with an FMA)
+__device__ __forceinline__ void mul_dd(double y, double sh, double lo, double &zh, double &zl) {
+  zh = y * sh;
+  zl = fma(y, lo, fma(y, sh, -zh));
+}
+
+// (ah + al) - (bh + bl) as an unnormalised double-double: Knuth's two-sum of
+// the high parts, its error plus the difference of the low parts
+__device__ __forceinline__ void sub_dd(double ah, double al, double bh, double bl, double &sh,
+                                       double &sl) {
+  sh = ah - bh;
+  const double bb = sh - ah;
+  sl = ((ah - (sh - bb)) - (bh + bb)) + (al - bl);
+}
+
+// exp(zh + zl) through the table path when |zh| < 700 (the range
+// exp_dd_fast covers); false otherwise
+__device__ __forceinline__ bool exp_dd_checked(double zh, double zl, double &r) {
+  if (!cmp::abs_lt_c(zh, 700.0)) return false;
+  r = exp_dd_fast(zh, zl);
+  return true;
+}
+
 // x^y from ln x = sh + lo (log_dd_fast), y finite; pow(x, y) is the fallback
 // when y ln x leaves the fast range.  pow_fast(x, y) == pow_from_log(x, sh,
 // lo, y) bit for bit.
 __device__ __forceinline__ double pow_from_log(double x, double sh, double lo, double y) {
-  const double zh = y * sh;
-  const double zl = fma(y, lo, fma(y, sh, -zh));
-  if (!(fabs(zh) < 700.0)) return pow(x, y);
-  return exp_dd_fast(zh, zl);
+  double zh, zl, r;
+  mul_dd(y, sh, lo, zh, zl);
+  return exp_dd_checked(zh, zl, r) ? r : pow(x, y);
 }
 
 __device__ __forceinline__ double pow_fast(double x, double y) {
@@ -118,10 +141,9 @@ __device__ __forceinline__ double pow_fast(double x, double y) {
   // tail, k ln2_lo + G_lo
   const double lo = se + (fma(-pe, rh, pe) + (t + fma(kd, kLn2Lo, gl)));
   // z = y (sh + lo) as a double-double
-  const double zh = y * sh;
-  const double zl = fma(y, lo, fma(y, sh, -zh));
-  if (!(fabs(zh) < 700.0)) return pow(x, y);
-  return exp_dd_fast(zh, zl);
+  double zh, zl, res;
+  mul_dd(y, sh, lo, zh, zl);
+  return exp_dd_checked(zh, zl, res) ? res : pow(x, y);
 }
 
 }  // namespace pihm

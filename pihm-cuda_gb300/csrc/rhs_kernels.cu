@@ -45,12 +45,14 @@ namespace pihm {
 
 #define RESTRICT __restrict__
 
-__device__ __forceinline__ double clamp0(double v) { return (v >= 0.0) ? v : 0.0; }
+// Comparisons go through fp64_cmp.h: the same results as the C operators,
+// evaluated on the integer pipe instead of the FP64 pipe.
+__device__ __forceinline__ double clamp0(double v) { return cmp::ge0(v) ? v : 0.0; }
 
 // SurfH, src/hydrol.c:100-134
 __device__ __forceinline__ double surf_h(double surfeqv) {
-  if (surfeqv < 0.0) return 0.0;
-  if (surfeqv <= 0.5 * kDeprStg) return sqrt(2.0 * kDeprStg * surfeqv);
+  if (cmp::lt0(surfeqv)) return 0.0;
+  if (cmp::le_c(surfeqv, 0.5 * kDeprStg)) return sqrt(2.0 * kDeprStg * surfeqv);
   return kDeprStg + (surfeqv - 0.5 * kDeprStg);
 }
 
@@ -58,9 +60,9 @@ __device__ __forceinline__ double surf_h(double surfeqv) {
 // (the reference evaluates both inline with the same operations)
 __device__ __forceinline__ double eff_kh_pre(double k1, double ksath, double depth, double dmac,
                                              double d_dmac, double gw) {
-  gw = (gw > 0.0) ? gw : 0.0;
-  if (gw > d_dmac) {
-    const double d1 = (gw > depth) ? dmac : gw - d_dmac;
+  gw = cmp::gt0(gw) ? gw : 0.0;
+  if (cmp::gt_v(gw, d_dmac)) {
+    const double d1 = cmp::gt_v(gw, depth) ? dmac : gw - d_dmac;
     return (k1 * d1 + ksath * d_dmac) / (d1 + d_dmac);
   }
   return ksath;
@@ -68,14 +70,14 @@ __device__ __forceinline__ double eff_kh_pre(double k1, double ksath, double dep
 
 // AvgH, src/lat_flow.c:217-237
 __device__ __forceinline__ double avg_h_sub(double diff, double hsub, double hnabr) {
-  if (diff > 0.0) return (hsub > 0.0) ? hsub : 0.0;
-  return (hnabr > 0.0) ? hnabr : 0.0;
+  if (cmp::gt0(diff)) return cmp::gt0(hsub) ? hsub : 0.0;
+  return cmp::gt0(hnabr) ? hnabr : 0.0;
 }
 
 // AvgHsurf, src/lat_flow.c:187-215
 __device__ __forceinline__ double avg_h_surf(double diff, double hsurf, double hnabr) {
-  if (diff > 0.0) return (hsurf > kDeprStg) ? 1.0 * (hsurf - kDeprStg) : 0.0;
-  return (hnabr > kDeprStg) ? 1.0 * (hnabr - kDeprStg) : 0.0;
+  if (cmp::gt0(diff)) return cmp::gt_c(hsurf, kDeprStg) ? 1.0 * (hsurf - kDeprStg) : 0.0;
+  return cmp::gt_c(hnabr, kDeprStg) ? 1.0 * (hnabr - kDeprStg) : 0.0;
 }
 
 // OverLandFlow, src/lat_flow.c:279-283
@@ -118,10 +120,15 @@ __device__ __forceinline__ double riv_perim(int order, double depth, double coef
 }
 
 // KrFunc (src/soil.c:8-13) and Psi (src/vert_flow.c:272-278) of one
-// saturation in [SATMIN, 1].  Psi's (1/satn)^m - 1 is evaluated as
-// (1 - satn^m) / satn^m from KrFunc's satn^m: one division in place of a
-// second logarithm-exponential pair (within an ulp of the reference's form,
-// the same cancellation as satn -> 1, and exactly 0 at satn = 1).
+// saturation in [SATMIN, 1], sharing one logarithm of satn:
+//   x1 = satn^m = exp(z), z = m ln satn (a double-double), a = 1 - x1,
+//   KrFunc = sqrt(satn) (1 - a^e)^2,
+//   Psi = -((1/satn)^m - 1)^ib / alpha = -(a / x1)^ib / alpha
+//       = -exp(ib (ln a - z)) / alpha.
+// The last form takes ln a, which a^e needs anyway, in place of a division
+// and a third logarithm; the difference ln a - z is carried as a
+// double-double, so Psi stays within an ulp of the reference's form (the
+// same cancellation in a as satn -> 1, exactly 0 at satn = 1).
 __device__ __forceinline__ void kr_psi(double satn, double vm, double vg_e, double vg_ib, double inv_alpha,
                                        double &satkfunc, double &psi) {
   double lh, ll;
@@ -133,9 +140,22 @@ __device__ __forceinline__ void kr_psi(double satn, double vm, double vg_e, doub
   }
   const double x1 = pow_from_log(satn, lh, ll, vm);  // satn^m, as pow_fast(satn, m)
   const double a = 1.0 - x1;
-  const double t = 1.0 - pow_fast(a, vg_e);
+  double zh, zl, ah, al;
+  mul_dd(vm, lh, ll, zh, zl);  // the z pow_from_log formed
+  if (!cmp::abs_lt_c(zh, 700.0) || !log_dd_fast(a, ah, al)) {
+    // a == 0 (satn == 1), or outside the table path's ranges
+    const double t = 1.0 - pow_fast(a, vg_e);
+    satkfunc = sqrt(satn) * t * t;
+    psi = -pow_fast(a / x1, vg_ib) * inv_alpha;
+    return;
+  }
+  const double t = 1.0 - pow_from_log(a, ah, al, vg_e);  // as pow_fast(a, e)
   satkfunc = sqrt(satn) * t * t;
-  psi = -pow_fast(a / x1, vg_ib) * inv_alpha;
+  double dh, dl, qh, ql, p;
+  sub_dd(ah, al, zh, zl, dh, dl);  // ln(a / x1)
+  mul_dd(vg_ib, dh, dl, qh, ql);
+  if (!exp_dd_checked(qh, ql, p)) p = pow(a / x1, vg_ib);
+  psi = -p * inv_alpha;
 }
 
 // Batch engine: whether the watershed of item idx sits out this evaluation
@@ -185,7 +205,7 @@ __global__ void __launch_bounds__(256) k_elem_grad(DevMesh m, const double *REST
     } else if (nb != kBoundary) {
       const int s = -1 - nb;
       const double stage = clamp0(y[3 * ne + s]);
-      h[j] = (stage > m.r_depth[s]) ? m.r_zbed[s] + stage : m.r_zmax[s];
+      h[j] = cmp::gt_v(stage, m.r_depth[s]) ? m.r_zbed[s] + stage : m.r_zmax[s];
     } else {
       h[j] = (m.bctype[j * ne + i] == 0) ? hself : m.elem_bc[j * ne + i];
     }
@@ -229,16 +249,16 @@ __global__ void __launch_bounds__(256) k_edge(DevMesh m, const double *RESTRICT 
     diff_h = m.zmax[i] - m.zmax[k];
     avg_h = avg_h_surf(diff_h, s_i, s_k);
     grad_h = diff_h * invdist;
-    avg_sf = (grad_h > 0.0) ? grad_h : kGradMin;
+    avg_sf = cmp::gt0(grad_h) ? grad_h : kGradMin;
   } else {
     diff_h = m.head[i] - m.head[k];
     avg_h = avg_h_surf(diff_h, s_i, s_k);
     grad_h = diff_h * invdist;
     avg_sf = 0.5 * (m.gradmag[i] + m.gradmag[k]);
-    avg_sf = (avg_sf > kGradMin) ? avg_sf : kGradMin;
+    avg_sf = cmp::gt_c(avg_sf, kGradMin) ? avg_sf : kGradMin;
   }
   double ovl = 0.0;
-  if (avg_h > 0.0) {  // avg_h == 0 gives crossa == 0: the flux is zero
+  if (cmp::gt0(avg_h)) {  // avg_h == 0 gives crossa == 0: the flux is zero
     const double crossa = avg_h * len;
     ovl = crossa * pow_fast(avg_h, 0.6666667) * grad_h * rsqrt(avg_sf) * m.e_invrough[e];
   }
@@ -305,7 +325,7 @@ __global__ void __launch_bounds__(256, 3) k_elem_main(DevMesh m, const double *R
   const double d_dinf = m.d_dinf[i];
   const double edir = m.edir[i], ett = m.ett[i];
   double edir_surf = 0.0, edir_unsat = 0.0, edir_gw = 0.0, ett_unsat = 0.0, ett_gw = 0.0;
-  const bool gw_in_dinf = gw > d_dinf;
+  const bool gw_in_dinf = cmp::gt_v(gw, d_dinf);
   if (m.noah) {
     // Flux-PIHM (src/hydrol.c:43-55,79-83): no ponded-water source, and the
     // transpiration split by GwTransp (noah/lsm_func.c:163-185) over the
@@ -313,18 +333,18 @@ __global__ void __launch_bounds__(256, 3) k_elem_main(DevMesh m, const double *R
     if (gw_in_dinf) edir_gw = edir;
     else edir_unsat = edir;
     double gwet = 0.0;
-    if (ett > 0.0 && m.noah_wtin[i]) {
+    if (cmp::gt0(ett) && m.noah_wtin[i]) {
       gwet = m.noah_etgw[i] / ett;
-      gwet = (gwet > 1.0) ? 1.0 : gwet;
-      gwet = (gwet < 0.0) ? 0.0 : gwet;
+      gwet = cmp::gt_c(gwet, 1.0) ? 1.0 : gwet;
+      gwet = cmp::lt0(gwet) ? 0.0 : gwet;
     }
     ett_unsat = (1.0 - gwet) * ett;
     ett_gw = gwet * ett;
   } else {
-    if (surfh >= kDeprStg) edir_surf = edir;
+    if (cmp::ge_c(surfh, kDeprStg)) edir_surf = edir;
     else if (gw_in_dinf) edir_gw = edir;
     else edir_unsat = edir;
-    if (gw > m.d_rzd[i]) ett_gw = ett;
+    if (cmp::gt_v(gw, m.d_rzd[i])) ett_gw = ett;
     else ett_unsat = ett;
   }
 
@@ -339,8 +359,8 @@ __global__ void __launch_bounds__(256, 3) k_elem_main(DevMesh m, const double *R
   if (!gw_in_dinf) {
     const double deficit = depth - gw;
     satn = unsat / deficit;
-    satn = (satn > 1.0) ? 1.0 : satn;
-    satn = (satn < kSatMin) ? kSatMin : satn;
+    satn = cmp::gt_c(satn, 1.0) ? 1.0 : satn;
+    satn = cmp::lt_c(satn, kSatMin) ? kSatMin : satn;
     kr_psi(satn, m.vg_m[i], m.vg_e[i], m.vg_ib[i], m.inv_alpha[i], satkfunc, psi_u);
   }
   // Infil's saturation: the same one, except in Flux-PIHM, where it is
@@ -349,44 +369,44 @@ __global__ void __launch_bounds__(256, 3) k_elem_main(DevMesh m, const double *R
   double satn_i = satn, satkfunc_i = satkfunc, psi_i = psi_u;
   if (m.noah && !gw_in_dinf) {
     double s = m.noah_satn[i];
-    s = (s > 1.0) ? 1.0 : s;
-    s = (s < kSatMin) ? kSatMin : s;
+    s = cmp::gt_c(s, 1.0) ? 1.0 : s;
+    s = cmp::lt_c(s, kSatMin) ? kSatMin : s;
     satn_i = s;
     kr_psi(s, m.vg_m[i], m.vg_e[i], m.vg_ib[i], m.inv_alpha[i], satkfunc_i, psi_i);
   }
   // KrFunc(beta, 1) == 1 exactly: pow(1 - pow(1, m), e) == pow(0, e) == 0
   double infil;
-  if (unsat + gw > depth) {
+  if (cmp::gt_v(unsat + gw, depth)) {
     infil = 0.0;
   } else {
     double applrate = 0.0;
 #pragma unroll
     for (int j = 0; j < 3; j++) applrate += -ovl[j] * inv_area;
-    applrate = (applrate > 0.0) ? applrate : 0.0;
+    applrate = cmp::gt0(applrate) ? applrate : 0.0;
     applrate += pcpdrp;
     double wetfrac = surfh * (1.0 / kDeprStg);
-    wetfrac = (wetfrac > 0.0) ? wetfrac : 0.0;
-    wetfrac = (wetfrac < 1.0) ? wetfrac : 1.0;
+    wetfrac = cmp::gt0(wetfrac) ? wetfrac : 0.0;
+    wetfrac = cmp::lt_c(wetfrac, 1.0) ? wetfrac : 1.0;
     double dh_by_dz;
     double esatn = satn_i;
     if (gw_in_dinf) {
       dh_by_dz = (surfh + zmax - gwhead) / (0.5 * (surfh + dinf));
       esatn = 1.0;
     } else {
-      const double psi_c = (psi_i > kPsiMin) ? psi_i : kPsiMin;
+      const double psi_c = cmp::gt_nc(psi_i, kPsiMin) ? psi_i : kPsiMin;
       const double h_u = psi_c + zmax - 0.5 * dinf;
       dh_by_dz = (surfh + zmax - h_u) / (0.5 * (surfh + dinf));
     }
-    dh_by_dz = (surfh <= 0.0 && dh_by_dz > 0.0) ? 0.0 : dh_by_dz;
+    dh_by_dz = (cmp::le0(surfh) && cmp::gt0(dh_by_dz)) ? 0.0 : dh_by_dz;
     // EffKinf, src/vert_flow.c:211-270
     double kinf;
-    if (areafh == 0.0) {
+    if (cmp::eq0(areafh)) {
       kinf = kinfv * satkfunc_i;
-    } else if (surfh > kDeprStg) {
+    } else if (cmp::gt_c(surfh, kDeprStg)) {
       kinf = kinf_mat * satkfunc_i + kmac_a;
-    } else if (applrate <= dh_by_dz * kinfv * satkfunc_i) {
+    } else if (cmp::le_v(applrate, dh_by_dz * kinfv * satkfunc_i)) {
       kinf = kinfv * satkfunc_i;
-    } else if (applrate < dh_by_dz * (kmac_a + kinf_mat * satkfunc_i)) {
+    } else if (cmp::lt_v(applrate, dh_by_dz * (kmac_a + kinf_mat * satkfunc_i))) {
       // KrFunc(2, satn): pow(satn, 2) and pow(., 0.5) are a product and sqrt
       const double t2 = 1.0 - sqrt(1.0 - esatn * esatn);
       kinf = kinf_mat * satkfunc_i + kmac_a * (sqrt(esatn) * t2 * t2);
@@ -394,11 +414,11 @@ __global__ void __launch_bounds__(256, 3) k_elem_main(DevMesh m, const double *R
       kinf = kinf_mat * satkfunc_i + kmac_a;
     }
     infil = kinf * dh_by_dz;
-    if (!gw_in_dinf) infil = (infil > 0.0) ? infil : 0.0;
+    if (!gw_in_dinf) infil = cmp::gt0(infil) ? infil : 0.0;
     const double ws0 = m.ws0_surf[i];
     const double inv_dt = m.sys_inv_dt ? m.sys_inv_dt[sy] : m.inv_dt;
-    const double infil_max = applrate + ((ws0 > 0.0) ? ws0 * inv_dt : 0.0);
-    infil = (infil > infil_max) ? infil_max : infil;
+    const double infil_max = applrate + (cmp::gt0(ws0) ? ws0 * inv_dt : 0.0);
+    infil = cmp::gt_v(infil, infil_max) ? infil_max : infil;
     infil *= wetfrac;
   }
   if (m.noah) infil *= m.noah_fcr[i];  // frozen top soil, src/vert_flow.c:16-19
@@ -414,7 +434,7 @@ __global__ void __launch_bounds__(256, 3) k_elem_main(DevMesh m, const double *R
     // AvgKv, src/vert_flow.c:172-209, arithmetic mean (_ARITH_ is defined at
     // src/include/pihm_func.h:4)
     double k1, k2, k3, d1, d2, d3;
-    if (deficit > dmac) {
+    if (cmp::gt_v(deficit, dmac)) {
       k1 = satkfunc * ksatv;
       d1 = dmac;
       k2 = satkfunc * ksatv;
@@ -431,8 +451,8 @@ __global__ void __launch_bounds__(256, 3) k_elem_main(DevMesh m, const double *R
     }
     const double kavg = (k1 * d1 + k2 * d2 + k3 * d3) * inv_depth;
     rechg = kavg * dh_by_dz;
-    rechg = (rechg > 0.0 && unsat <= 0.0) ? 0.0 : rechg;
-    rechg = (rechg < 0.0 && gw <= 0.0) ? 0.0 : rechg;
+    rechg = (cmp::gt0(rechg) && cmp::le0(unsat)) ? 0.0 : rechg;
+    rechg = (cmp::lt0(rechg) && cmp::le0(gw)) ? 0.0 : rechg;
   }
 
   if (m.diag) {
@@ -458,7 +478,7 @@ __global__ void __launch_bounds__(256, 3) k_elem_main(DevMesh m, const double *R
   const double base_gw = rechg - edir_gw - ett_gw;
   const double du = (infil - rechg - edir_unsat - ett_unsat) * inv_por;
   ydot[ne + i] = du;
-  unsigned int bad = isnan(du);
+  unsigned int bad = cmp::isnan_(du);
   if (riv[0] || riv[1] || riv[2]) {
     const int b = m.bank_slot[i];
     const int nbk = m.nbank;
@@ -480,7 +500,7 @@ __global__ void __launch_bounds__(256, 3) k_elem_main(DevMesh m, const double *R
     dg *= inv_por;
     ydot[i] = ds;
     ydot[2 * ne + i] = dg;
-    bad |= isnan(ds) | isnan(dg);
+    bad |= cmp::isnan_(ds) | cmp::isnan_(dg);
   }
   if (bad) report_err(m, sy);
 }

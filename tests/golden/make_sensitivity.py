@@ -13,7 +13,9 @@ expected to land; the GPU end-to-end test is held to it.
     python tests/golden/make_sensitivity.py [--runs 4]
 
 writes tests/golden/c0_sensitivity.npz: final states [runs, neq], outlet
-flux series [runs, nsteps], step counts [runs], seeds.
+flux series [runs, nsteps], step counts [runs], the water-balance sums of
+PrintWaterBal (src/print.c:337-542) per model step [runs, nsteps, 3],
+seeds.
 """
 import argparse
 import ctypes
@@ -53,7 +55,7 @@ def noisy_run(ws, z, ctrl, seed):
     b.rhs = ctypes.cast(b._cb, ctypes.c_void_p)
     try:
         return run_steps(b, ctrl, z["outlet_q"].shape[0], b.set_forcing, record_every=int(z["every"]),
-                         outlet=int(z["outlet"]))
+                         outlet=int(z["outlet"]), water_balance=True)
     finally:
         b.close()
 
@@ -68,15 +70,16 @@ def main():
     ctrl = StepControl(**{str(k): (int(v) if str(k) == "stepsize" else float(v))
                           for k, v in zip(z["ctrl_names"], z["ctrl"])})
     seeds = list(range(args.runs))
-    finals, outs, nst = [], [], []
+    finals, outs, nst, wbs = [], [], [], []
     for s in seeds:
         r = noisy_run(ws, z, ctrl, s)
         finals.append(r["states"][-1])
         outs.append(r["outlet"])
         nst.append(r["stats"].nst)
+        wbs.append(r["wb"])
         print("seed", s, "nst", r["stats"].nst)
     np.savez_compressed(args.out, final=np.array(finals), outlet=np.array(outs), nst=np.array(nst),
-                        seeds=np.array(seeds))
+                        wb=np.array(wbs), seeds=np.array(seeds))
 
 
 if __name__ == "__main__":
