@@ -57,7 +57,9 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi samples during the timed region."""
+    """nvidia-smi samples during the timed region: the sampler starts, its
+    first sample is awaited, and only the samples stamped between entering
+    and leaving the block are kept."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -65,27 +67,42 @@ class ClockSampler:
     def __init__(self, gpu: int):
         self.gpu = gpu
         self.proc = None
+        self.stamped = []
+        self.lines = []
+        self.t0 = self.t1 = 0.0
+
+    def _read(self):
+        for line in self.proc.stdout:
+            if line.strip():
+                self.stamped.append((time.monotonic(), line))
 
     def __enter__(self):
+        import threading
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.reader = threading.Thread(target=self._read, daemon=True)
+            self.reader.start()
+            deadline = time.monotonic() + 10.0
+            while not self.stamped and time.monotonic() < deadline and self.proc.poll() is None:
+                time.sleep(0.02)
         except Exception:
             self.proc = None
+        self.t0 = time.monotonic()
         return self
 
     def __exit__(self, *a):
-        self.lines = []
+        self.t1 = time.monotonic()
         if self.proc is not None:
             self.proc.terminate()
             try:
-                out, _ = self.proc.communicate(timeout=5)
+                self.proc.wait(timeout=5)
             except Exception:
                 self.proc.kill()
-                out = ""
-            self.lines = [l for l in out.splitlines() if l.strip()]
+            self.reader.join(timeout=5)
+        self.lines = [l for t, l in self.stamped if self.t0 <= t <= self.t1]
 
     def summary(self):
         sm, mx, reasons = [], None, set()
@@ -103,7 +120,8 @@ class ClockSampler:
                 if v.lower().startswith("active"):
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm),
+                "window_s": round(self.t1 - self.t0, 3)}
 
 
 def cpu_time_oracle(ws, states_host, threads, max_seconds=12.0, min_evals=2):
@@ -380,7 +398,7 @@ def bench_serving():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")

@@ -253,6 +253,12 @@ int pihm_gpu_kernel_times(pihm_gpu_ctx *ctx, double *ms, int64_t *calls, int n);
  * tests to measure the error of the fast path. */
 int pihm_gpu_selftest_pow(const double *x, const double *y, double *fast,
                           double *cuda_pow, int64_t n, void *stream);
+/* Diagnostic: the Manning-exponent power of the right-hand-side kernels,
+ * out[i] = x[i]^0.6666667 (river == 0, overland flow) or x[i]^(2.0/3.0)
+ * (river != 0, channel flow); device arrays of length n, asynchronous on
+ * `stream`. */
+int pihm_gpu_selftest_pow_manning(const double *x, int river, double *out, int64_t n,
+                                  void *stream);
 
 #ifdef __cplusplus
 }

@@ -83,7 +83,8 @@ __device__ __forceinline__ double avg_h_surf(double diff, double hsurf, double h
 // OverLandFlow, src/lat_flow.c:279-283
 __device__ __forceinline__ double overland_flow(double avg_h, double grad_h, double avg_sf,
                                                 double crossa, double avg_rough) {
-  return crossa * pow_fast(avg_h, 0.6666667) * grad_h / (sqrt(avg_sf) * avg_rough);
+  return crossa * pow_manning(avg_h, kManningSurf, kManningSurfDelta) * grad_h /
+         (sqrt(avg_sf) * avg_rough);
 }
 
 // ---------------------------------------------------------------------------
@@ -260,7 +261,8 @@ __global__ void __launch_bounds__(256) k_edge(DevMesh m, const double *RESTRICT 
   double ovl = 0.0;
   if (cmp::gt0(avg_h)) {  // avg_h == 0 gives crossa == 0: the flux is zero
     const double crossa = avg_h * len;
-    ovl = crossa * pow_fast(avg_h, 0.6666667) * grad_h * rsqrt(avg_sf) * m.e_invrough[e];
+    ovl = crossa * pow_manning(avg_h, kManningSurf, kManningSurfDelta) * grad_h * rsqrt(avg_sf) *
+          m.e_invrough[e];
   }
   m.eflux_ovl[e] = ovl;
 }
@@ -666,7 +668,9 @@ __global__ void __launch_bounds__(128) k_river(DevMesh m, const double *RESTRICT
       const double grad_h = (r.zbed - (m.r_node_zmax[s] - depth)) / distance;
       const double avg_perim = riv_perim(r.order, r.stage, r.coeff);
       const double crossa = riv_cs_area(r.order, r.stage, r.coeff);
-      q = sqrt(grad_h) * crossa * ((avg_perim > 0.0) ? pow_fast(crossa / avg_perim, 2.0 / 3.0) : 0.0) / r.rough;
+      q = sqrt(grad_h) * crossa *
+          ((avg_perim > 0.0) ? pow_manning(crossa / avg_perim, kManningRiv, kManningRivDelta) : 0.0) /
+          r.rough;
     } else {  // kCritDpth (other values are rejected at load)
       const double crossa = riv_cs_area(r.order, r.stage, r.coeff);
       q = crossa * sqrt(kGrav * r.stage);

@@ -1,5 +1,6 @@
-// Diagnostic entry point: the table-driven pow of the right-hand-side kernels
-// next to CUDA's pow, element by element, so tests can measure its error.
+// Diagnostic entry points: the table-driven pow of the right-hand-side kernels
+// next to CUDA's pow, and the Manning-exponent power, element by element, so
+// tests can measure their error.
 #include <cstdint>
 
 #include "fp64_math.cuh"
@@ -11,11 +12,25 @@ __global__ void k_pow_pair(const double *x, const double *y, double *fast, doubl
   fast[i] = pihm::pow_fast(x[i], y[i]);
   if (ref) ref[i] = pow(x[i], y[i]);
 }
+
+__global__ void k_pow_manning(const double *x, int river, double *out, long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = river ? pihm::pow_manning(x[i], pihm::kManningRiv, pihm::kManningRivDelta)
+                 : pihm::pow_manning(x[i], pihm::kManningSurf, pihm::kManningSurfDelta);
+}
 }  // namespace
 
 extern "C" int pihm_gpu_selftest_pow(const double *x, const double *y, double *fast, double *cuda_pow,
                                      int64_t n, void *stream) {
   if (n <= 0 || !x || !y || !fast) return -1;
   k_pow_pair<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(x, y, fast, cuda_pow, n);
+  return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
+
+extern "C" int pihm_gpu_selftest_pow_manning(const double *x, int river, double *out, int64_t n,
+                                             void *stream) {
+  if (n <= 0 || !x || !out) return -1;
+  k_pow_manning<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(x, river, out, n);
   return cudaGetLastError() == cudaSuccess ? 0 : -2;
 }
