@@ -18,8 +18,9 @@
 //
 // Error: about 0.51 ulp for the arguments the model produces (checked against
 // 60-digit references and CUDA's pow in tests/test_fp64_math_gpu.py).  The
-// fast path needs x positive and normal and |y ln x| < 700; everything else
-// (x <= 0, zero, subnormal, inf, nan, overflow, underflow) goes to pow().
+// fast path needs x positive and normal and |y ln x| < 700; +0 to a positive
+// power is +0, and everything else (x < 0, -0, subnormal, inf, nan, other
+// powers of +0, overflow, underflow) goes to pow().
 #pragma once
 
 #include <cmath>
@@ -113,7 +114,12 @@ __device__ __forceinline__ double pow_from_log(double x, double sh, double lo, d
 __device__ __forceinline__ double pow_fast(double x, double y) {
   const long long xb = __double_as_longlong(x);
   const unsigned top = (unsigned)((unsigned long long)xb >> 52);  // sign and exponent
-  if (top - 1u >= 2046u) return pow(x, y);  // x <= 0, zero, subnormal, inf or nan
+  if (top - 1u >= 2046u) {  // x <= 0, zero, subnormal, inf or nan
+    // +0 to a positive power is +0 (C99 F.9.4.4): a full soil column makes
+    // 1 - satn^m exactly 0, so this case is common enough to skip the call
+    if (xb == 0 && cmp::gt0(y)) return 0.0;
+    return pow(x, y);
+  }
   const int k = (int)top - 1023;
   const double m = __longlong_as_double((xb & 0x000FFFFFFFFFFFFFLL) | 0x3FF0000000000000LL);
   const int i = (int)((xb >> 44) & 0xFF);

@@ -67,8 +67,10 @@ def test_pow_fast_special_values():
     lib = capi.load()
     f = lib.pihm_gpu_selftest_pow
     f.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_int64, ctypes.c_void_p]
-    x = np.array([0.0, 1.0, 2.0, 4.0, 1e-310, np.inf, 0.5, 1e-300, 1e300, 1.0])
-    y = np.array([0.6666667, 3.7, 0.5, 0.5, 0.5, 0.5, 2000.0, 2.0, 0.5, 0.0])
+    x = np.array([0.0, 1.0, 2.0, 4.0, 1e-310, np.inf, 0.5, 1e-300, 1e300, 1.0,
+                  0.0, 0.0, 0.0, 0.0, -0.0, -0.0, 0.0])
+    y = np.array([0.6666667, 3.7, 0.5, 0.5, 0.5, 0.5, 2000.0, 2.0, 0.5, 0.0,
+                  3.0, 0.0, -1.0, np.nan, 3.0, 0.5, 5e-324])
     tx, ty = torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()
     fast, ref = torch.empty_like(tx), torch.empty_like(tx)
     assert f(tx.data_ptr(), ty.data_ptr(), fast.data_ptr(), ref.data_ptr(), x.size, None) == 0
@@ -78,8 +80,9 @@ def test_pow_fast_special_values():
     for k in range(x.size):
         if np.isfinite(cu[k]) and cu[k] != 0:
             assert abs(fa[k] - cu[k]) <= 2 * math.ulp(cu[k]), (k, fa[k], cu[k])
-        else:
-            assert fa[k] == cu[k] or (np.isnan(fa[k]) and np.isnan(cu[k])), (k, fa[k], cu[k])
+        else:  # zeros (with their sign), infinities and NaNs exactly as CUDA's pow
+            assert (fa[k:k + 1].view(np.int64) == cu[k:k + 1].view(np.int64)).all() or (
+                np.isnan(fa[k]) and np.isnan(cu[k])), (k, fa[k], cu[k])
 
 
 def _manning(x, river):
