@@ -671,10 +671,7 @@ int pihm_batch_create(const pihm_batch_limits *lim, int surf_mode, int riv_mode,
            cudaMemset(A.rhs_in, 0, sizeof(double) * NEQ) == cudaSuccess &&
            cudaDeviceSynchronize() == cudaSuccess;
   if (!z) return PIHM_GPU_ERR_CUDA;
-  if (cudaStreamCreateWithFlags(&B->side.side, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreateWithFlags(&B->side.fork, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&B->side.join, cudaEventDisableTiming) != cudaSuccess)
-    return PIHM_GPU_ERR_CUDA;
+  if (pihm::create_rhs_streams(&B->side) != cudaSuccess) return PIHM_GPU_ERR_CUDA;
   for (cudaEvent_t &e : B->tev)
     if (cudaEventCreate(&e) != cudaSuccess) return PIHM_GPU_ERR_CUDA;
   B->update_extents();

@@ -171,9 +171,7 @@ int pihm_gpu_create(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double 
   c->d_stage_out = carve<double>(dp, c->neq);
   m.err = carve<unsigned int>(dp, 1);
   m.diag = 0;
-  if (cudaStreamCreateWithFlags(&c->side.side, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->side.fork, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->side.join, cudaEventDisableTiming) != cudaSuccess) {
+  if (pihm::create_rhs_streams(&c->side) != cudaSuccess) {
     pihm_gpu_destroy(c);
     return PIHM_GPU_ERR_CUDA;
   }

@@ -1,6 +1,7 @@
 // Host image of one watershed (mesh_image.h): validation, renumbering,
 // edge ownership, bank elements, upstream lists and derived constants.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <numeric>
 #include <queue>
@@ -24,7 +25,8 @@ const double *DevMesh::*const kRiverMember[RP_COUNT] = {
     &DevMesh::r_area, &DevMesh::r_zmin, &DevMesh::r_zmax, &DevMesh::r_zbed, &DevMesh::r_node_zmax,
     &DevMesh::r_dist_left, &DevMesh::r_dist_right, &DevMesh::r_depth, &DevMesh::r_coeff, &DevMesh::r_length,
     &DevMesh::r_width, &DevMesh::r_rough, &DevMesh::r_cwr, &DevMesh::r_ksath, &DevMesh::r_ksatv,
-    &DevMesh::r_bedthick, &DevMesh::r_porosity};
+    &DevMesh::r_bedthick, &DevMesh::r_porosity, &DevMesh::r_inv_half_len, &DevMesh::r_inv_dist_down,
+    &DevMesh::r_inv_dist_left, &DevMesh::r_inv_dist_right, &DevMesh::r_inv_bedthick, &DevMesh::r_ovl_coef};
 
 namespace {
 
@@ -266,7 +268,20 @@ int build_image(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double step
                                   g->riv_dist_left, g->riv_dist_right, g->riv_depth, g->riv_coeff,
                                   g->riv_length, g->riv_width, g->riv_rough, g->riv_cwr, g->riv_ksath,
                                   g->riv_ksatv, g->riv_bedthick, g->riv_porosity};
-  for (int k = 0; k < RP_COUNT; k++) im->rv[k].assign(rsrc[k], rsrc[k] + nr);
+  for (int k = 0; k < RP_INV_HALF_LEN; k++) im->rv[k].assign(rsrc[k], rsrc[k] + nr);
+  // reciprocals of the static distances the river fluxes divide by, and the
+  // weir coefficient of OvlFlowElemToRiver, cwr 2 sqrt(2 g) length / 3
+  // (src/river_flow.c:185-255, 257-331, 333-390, 429-518)
+  for (int k = RP_INV_HALF_LEN; k < RP_COUNT; k++) im->rv[k].assign(nr, 0.0);
+  for (int s = 0; s < nr; s++) {
+    const double len = g->riv_length[s];
+    im->rv[RP_INV_HALF_LEN][s] = 1.0 / (0.5 * len);
+    if (g->down[s] > 0) im->rv[RP_INV_DIST_DOWN][s] = 1.0 / (0.5 * (len + g->riv_length[g->down[s] - 1]));
+    im->rv[RP_INV_DIST_LEFT][s] = 1.0 / g->riv_dist_left[s];
+    im->rv[RP_INV_DIST_RIGHT][s] = 1.0 / g->riv_dist_right[s];
+    im->rv[RP_INV_BEDTHICK][s] = 1.0 / g->riv_bedthick[s];
+    im->rv[RP_OVL_COEF][s] = g->riv_cwr[s] * 2.0 * std::sqrt(2.0 * kGrav) * len / 3.0;
+  }
   return PIHM_GPU_OK;
 }
 

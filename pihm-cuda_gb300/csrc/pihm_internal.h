@@ -74,6 +74,10 @@ struct DevMesh {
   const double *r_area, *r_zmin, *r_zmax, *r_zbed, *r_node_zmax, *r_dist_left,
       *r_dist_right, *r_depth, *r_coeff, *r_length, *r_width, *r_rough, *r_cwr,
       *r_ksath, *r_ksatv, *r_bedthick, *r_porosity;
+  // derived at load: 1/(length/2), 1/((length + downstream length)/2) (0 at
+  // an outlet), 1/dist_left, 1/dist_right, 1/bedthick, cwr 2 sqrt(2g) length/3
+  const double *r_inv_half_len, *r_inv_dist_down, *r_inv_dist_left, *r_inv_dist_right,
+      *r_inv_bedthick, *r_ovl_coef;
   const int32_t *up_ptr, *up_idx;  // CSR of upstream segments, reference order
   const int32_t *up_end;           // [nr] end of each upstream list (up_ptr + 1 in a
                                    // single-watershed context)
@@ -142,6 +146,19 @@ struct RhsStreams {
   cudaStream_t side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
 };
+
+// The river kernel's stream and events.  The stream has the highest
+// priority the device offers, so that the few, long-running river blocks are
+// dispatched ahead of the element kernels' many short ones and finish under
+// them instead of after them.
+inline cudaError_t create_rhs_streams(RhsStreams *s) {
+  int least = 0, greatest = 0;
+  cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+  if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s->side, cudaStreamNonBlocking, greatest);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming);
+  return e;
+}
 
 cudaError_t launch_rhs(const DevMesh &m, const double *y, double *ydot, cudaStream_t st,
                        long long *launches, Profiler *prof, const RhsStreams *side = nullptr);

@@ -91,7 +91,7 @@ __device__ __forceinline__ double overland_flow(double avg_h, double grad_h, dou
 // river geometry, src/river_flow.c:520-583
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double riv_cs_area(int order, double depth, double coeff) {
-  depth = (depth > 0.0) ? depth : 0.0;
+  depth = cmp::gt0(depth) ? depth : 0.0;
   switch (order) {
     case kRectangle: return depth * coeff;
     case kTriangle: return depth * depth / coeff;
@@ -102,7 +102,7 @@ __device__ __forceinline__ double riv_cs_area(int order, double depth, double co
 }
 
 __device__ __forceinline__ double riv_perim(int order, double depth, double coeff) {
-  depth = (depth > 0.0) ? depth : 0.0;
+  depth = cmp::gt0(depth) ? depth : 0.0;
   switch (order) {
     case kRectangle: return 2.0 * depth + coeff;
     case kTriangle: return 2.0 * depth * sqrt(1.0 + coeff * coeff) / coeff;
@@ -530,24 +530,21 @@ __device__ __forceinline__ RivState load_riv(const DevMesh &m, const double *y, 
   return r;
 }
 
-// OvlFlowElemToRiver, src/river_flow.c:185-255
+// OvlFlowElemToRiver, src/river_flow.c:185-255, with the weir coefficient
+// cwr 2 sqrt(2 g) length / 3 formed at load (coef)
 __device__ __forceinline__ double ovl_elem_to_river(double e_zmax, double e_surfh, const RivState &r,
-                                                    double cwr) {
-  const double zbank = (r.zmax > e_zmax) ? r.zmax : e_zmax;
+                                                    double coef) {
+  const double zbank = cmp::gt_v(r.zmax, e_zmax) ? r.zmax : e_zmax;
   const double elem_h = e_zmax + e_surfh;
   const double rivseg_h = r.zbed + r.stage;
-  if (rivseg_h > elem_h) {
-    if (elem_h > zbank)
-      return cwr * 2.0 * sqrt(2.0 * kGrav) * r.length * sqrt(rivseg_h - elem_h) * (rivseg_h - zbank) / 3.0;
-    if (zbank < rivseg_h)
-      return cwr * 2.0 * sqrt(2.0 * kGrav) * r.length * sqrt(rivseg_h - zbank) * (rivseg_h - zbank) / 3.0;
+  if (cmp::gt_v(rivseg_h, elem_h)) {
+    if (cmp::gt_v(elem_h, zbank)) return coef * sqrt(rivseg_h - elem_h) * (rivseg_h - zbank);
+    if (cmp::lt_v(zbank, rivseg_h)) return coef * sqrt(rivseg_h - zbank) * (rivseg_h - zbank);
     return 0.0;
   }
-  if (e_surfh > kDeprStg) {
-    if (rivseg_h > zbank)
-      return -cwr * 2.0 * sqrt(2.0 * kGrav) * r.length * sqrt(elem_h - rivseg_h) * (elem_h - zbank) / 3.0;
-    if (zbank < elem_h)
-      return -cwr * 2.0 * sqrt(2.0 * kGrav) * r.length * sqrt(elem_h - zbank) * (elem_h - zbank) / 3.0;
+  if (cmp::gt_c(e_surfh, kDeprStg)) {
+    if (cmp::gt_v(rivseg_h, zbank)) return -coef * sqrt(elem_h - rivseg_h) * (elem_h - zbank);
+    if (cmp::lt_v(zbank, elem_h)) return -coef * sqrt(elem_h - zbank) * (elem_h - zbank);
     return 0.0;
   }
   return 0.0;
@@ -556,14 +553,14 @@ __device__ __forceinline__ double ovl_elem_to_river(double e_zmax, double e_surf
 // ChanFlowElemToRiver, src/river_flow.c:429-460
 __device__ __forceinline__ double chan_elem_to_river(double e_gw, double e_zmin, double effk,
                                                      const RivState &r, double r_ksath,
-                                                     double distance) {
+                                                     double inv_distance) {
   const double diff_h = (r.stage + r.zbed) - (e_gw + e_zmin);
   double avg_h;
-  if (e_zmin > r.zbed) avg_h = e_gw;
-  else if (e_zmin + e_gw > r.zbed) avg_h = e_zmin + e_gw - r.zbed;
+  if (cmp::gt_v(e_zmin, r.zbed)) avg_h = e_gw;
+  else if (cmp::gt_v(e_zmin + e_gw, r.zbed)) avg_h = e_zmin + e_gw - r.zbed;
   else avg_h = 0.0;
   avg_h = avg_h_sub(diff_h, r.stage, avg_h);
-  const double grad_h = diff_h / distance;
+  const double grad_h = diff_h * inv_distance;
   const double avg_ksat = 0.5 * (effk + r_ksath);
   return r.length * avg_ksat * grad_h * avg_h;
 }
@@ -571,15 +568,15 @@ __device__ __forceinline__ double chan_elem_to_river(double e_gw, double e_zmin,
 // SubFlowElemToRiver, src/river_flow.c:462-498 (arithmetic mean)
 __device__ __forceinline__ double sub_elem_to_river(double e_gw, double e_zmin, double effk,
                                                     const RivState &r, double effk_riv,
-                                                    double distance) {
+                                                    double inv_distance) {
   const double diff_h = (r.gw + r.zmin) - (e_gw + e_zmin);
   double avg_h;
-  if (e_zmin > r.zbed) avg_h = 0.0;
-  else if (e_zmin + e_gw > r.zbed) avg_h = r.zbed - e_zmin;
+  if (cmp::gt_v(e_zmin, r.zbed)) avg_h = 0.0;
+  else if (cmp::gt_v(e_zmin + e_gw, r.zbed)) avg_h = r.zbed - e_zmin;
   else avg_h = e_gw;
   avg_h = avg_h_sub(diff_h, r.gw, avg_h);
   const double avg_ksat = 0.5 * (effk + effk_riv);
-  const double grad_h = diff_h / distance;
+  const double grad_h = diff_h * inv_distance;
   return r.length * avg_ksat * grad_h * avg_h;
 }
 
@@ -603,11 +600,10 @@ __global__ void __launch_bounds__(128) k_river(DevMesh m, const double *RESTRICT
       const double bc = m.river_bc[s];
       if (bct > 0) {
         const double total_h = r.stage + r.zbed;
-        const double distance = 0.5 * r.length;
-        const double grad_h = (total_h - bc) / distance;
+        const double grad_h = (total_h - bc) * m.r_inv_half_len[s];
         const double avg_perim = riv_perim(r.order, r.stage, r.coeff);
         const double crossa = riv_cs_area(r.order, r.stage, r.coeff);
-        const double avg_h = (avg_perim == 0.0) ? 0.0 : (crossa / avg_perim);
+        const double avg_h = cmp::eq0(avg_perim) ? 0.0 : (crossa / avg_perim);
         flux = overland_flow(avg_h, grad_h, grad_h, crossa, r.rough);
       } else {
         flux = -bc;
@@ -616,6 +612,7 @@ __global__ void __launch_bounds__(128) k_river(DevMesh m, const double *RESTRICT
     }
     const int d = down - 1;
     const RivState dn = load_riv(m, y, d);
+    const double inv_dist_down = m.r_inv_dist_down[s];
     // ChanFlowRiverToRiver, src/river_flow.c:257-300
     {
       const double total_h = r.stage + r.zbed;
@@ -624,14 +621,13 @@ __global__ void __launch_bounds__(128) k_river(DevMesh m, const double *RESTRICT
       const double perim_down = riv_perim(dn.order, dn.stage, dn.coeff);
       const double avg_perim = (perim + perim_down) / 2.0;
       const double avg_rough = (r.rough + dn.rough) / 2.0;
-      const double distance = 0.5 * (r.length + dn.length);
       const double diff_h = (m.riv_mode == kKinematic) ? (r.zbed - dn.zbed) : (total_h - total_h_down);
-      const double grad_h = diff_h / distance;
-      const double avg_sf = (grad_h > 0.0) ? grad_h : kRivGradMin;
+      const double grad_h = diff_h * inv_dist_down;
+      const double avg_sf = cmp::gt0(grad_h) ? grad_h : kRivGradMin;
       const double crossa = riv_cs_area(r.order, r.stage, r.coeff);
       const double crossa_down = riv_cs_area(dn.order, dn.stage, dn.coeff);
       const double avg_crossa = 0.5 * (crossa + crossa_down);
-      const double avg_h = (avg_perim == 0.0) ? 0.0 : (avg_crossa / avg_perim);
+      const double avg_h = cmp::eq0(avg_perim) ? 0.0 : (avg_crossa / avg_perim);
       f[DOWN_CHANL2CHANL] = overland_flow(avg_h, grad_h, avg_sf, crossa, avg_rough);
     }
     // SubFlowRiverToRiver, src/river_flow.c:302-331 (arithmetic mean)
@@ -643,8 +639,7 @@ __global__ void __launch_bounds__(128) k_river(DevMesh m, const double *RESTRICT
       const double avg_wid = (r.width + dn.width) / 2.0;
       const double diff_h = total_h - total_h_down;
       const double avg_h = avg_h_sub(diff_h, r.gw, dn.gw);
-      const double distance = 0.5 * (r.length + dn.length);
-      const double grad_h = diff_h / distance;
+      const double grad_h = diff_h * inv_dist_down;
       const double avg_ksat = 0.5 * (effk + effk_nabr);
       f[DOWN_AQUIF2AQUIF] = avg_ksat * grad_h * avg_h * avg_wid;
     }
@@ -655,21 +650,19 @@ __global__ void __launch_bounds__(128) k_river(DevMesh m, const double *RESTRICT
     double q = 0.0;
     if (down == kDirichlet) {
       const double total_h = r.stage + r.zbed;
-      const double distance = 0.5 * r.length;
-      const double grad_h = (total_h - bc) / distance;
+      const double grad_h = (total_h - bc) * m.r_inv_half_len[s];
       const double avg_perim = riv_perim(r.order, r.stage, r.coeff);
       const double crossa = riv_cs_area(r.order, r.stage, r.coeff);
-      const double avg_h = (avg_perim == 0.0) ? 0.0 : (crossa / avg_perim);
+      const double avg_h = cmp::eq0(avg_perim) ? 0.0 : (crossa / avg_perim);
       q = overland_flow(avg_h, grad_h, grad_h, crossa, r.rough);
     } else if (down == kNeumann) {
       q = -bc;
     } else if (down == kZeroDpthGrad) {
-      const double distance = 0.5 * r.length;
-      const double grad_h = (r.zbed - (m.r_node_zmax[s] - depth)) / distance;
+      const double grad_h = (r.zbed - (m.r_node_zmax[s] - depth)) * m.r_inv_half_len[s];
       const double avg_perim = riv_perim(r.order, r.stage, r.coeff);
       const double crossa = riv_cs_area(r.order, r.stage, r.coeff);
       q = sqrt(grad_h) * crossa *
-          ((avg_perim > 0.0) ? pow_manning(crossa / avg_perim, kManningRiv, kManningRivDelta) : 0.0) /
+          (cmp::gt0(avg_perim) ? pow_manning(crossa / avg_perim, kManningRiv, kManningRivDelta) : 0.0) /
           r.rough;
     } else {  // kCritDpth (other values are rejected at load)
       const double crossa = riv_cs_area(r.order, r.stage, r.coeff);
@@ -679,23 +672,24 @@ __global__ void __launch_bounds__(128) k_river(DevMesh m, const double *RESTRICT
     f[DOWN_AQUIF2AQUIF] = 0.0;
   }
   // RiverToElem, src/river_flow.c:113-183
-  const double cwr = m.r_cwr[s];
+  const double coef = m.r_ovl_coef[s];
   const double gw_l = clamp0(y[2 * ne + L]), gw_r = clamp0(y[2 * ne + R]);
   const double zmin_l = m.zmin[L], zmin_r = m.zmin[R];
-  f[LEFT_SURF2CHANL] = ovl_elem_to_river(m.zmax[L], m.surfh[L], r, cwr);
-  f[RIGHT_SURF2CHANL] = ovl_elem_to_river(m.zmax[R], m.surfh[R], r, cwr);
+  f[LEFT_SURF2CHANL] = ovl_elem_to_river(m.zmax[L], m.surfh[L], r, coef);
+  f[RIGHT_SURF2CHANL] = ovl_elem_to_river(m.zmax[R], m.surfh[R], r, coef);
   const double r_ksath = m.r_ksath[s];
-  f[LEFT_AQUIF2CHANL] = chan_elem_to_river(gw_l, zmin_l, effk_l, r, r_ksath, m.r_dist_left[s]);
-  f[RIGHT_AQUIF2CHANL] = chan_elem_to_river(gw_r, zmin_r, effk_r, r, r_ksath, m.r_dist_right[s]);
+  const double inv_dl = m.r_inv_dist_left[s], inv_dr = m.r_inv_dist_right[s];
+  f[LEFT_AQUIF2CHANL] = chan_elem_to_river(gw_l, zmin_l, effk_l, r, r_ksath, inv_dl);
+  f[RIGHT_AQUIF2CHANL] = chan_elem_to_river(gw_r, zmin_r, effk_r, r, r_ksath, inv_dr);
   const double effk_avg = 0.5 * (effk_l + effk_r);
-  f[LEFT_AQUIF2AQUIF] = sub_elem_to_river(gw_l, zmin_l, effk_l, r, effk_avg, m.r_dist_left[s]);
-  f[RIGHT_AQUIF2AQUIF] = sub_elem_to_river(gw_r, zmin_r, effk_r, r, effk_avg, m.r_dist_right[s]);
+  f[LEFT_AQUIF2AQUIF] = sub_elem_to_river(gw_l, zmin_l, effk_l, r, effk_avg, inv_dl);
+  f[RIGHT_AQUIF2AQUIF] = sub_elem_to_river(gw_r, zmin_r, effk_r, r, effk_avg, inv_dr);
   // ChanLeak, src/river_flow.c:500-518
   {
     double diff_h;
-    if (r.zbed - (r.gw + r.zmin) > 0.0) diff_h = r.stage;
+    if (cmp::gt0(r.zbed - (r.gw + r.zmin))) diff_h = r.stage;
     else diff_h = r.stage + r.zbed - (r.gw + r.zmin);
-    const double grad_h = diff_h / m.r_bedthick[s];
+    const double grad_h = diff_h * m.r_inv_bedthick[s];
     f[CHANL_LKG] = m.r_ksatv[s] * r.width * r.length * grad_h;
   }
 #pragma unroll
@@ -734,7 +728,7 @@ __global__ void __launch_bounds__(128) k_finish(DevMesh m, double *RESTRICT ydot
       m.rivflow[UP_CHANL2CHANL * nr + s] = up_c;
       m.rivflow[UP_AQUIF2AQUIF * nr + s] = up_a;
     }
-    if (isnan(ds) | isnan(dg)) report_err(m, sy);
+    if (cmp::isnan_(ds) | cmp::isnan_(dg)) report_err(m, sy);
     // the next evaluation's Infil reads this evaluation's river-edge
     // overland flux (src/vert_flow.c:61 before src/river_flow.c:159-182)
     m.carry_ovl[s] = F[LEFT_SURF2CHANL * nr + s];
@@ -775,7 +769,7 @@ __global__ void __launch_bounds__(128) k_finish(DevMesh m, double *RESTRICT ydot
   dg *= m.inv_por[i];
   ydot[i] = ds;
   ydot[2 * ne + i] = dg;
-  if (isnan(ds) | isnan(dg)) report_err(m, sy);
+  if (cmp::isnan_(ds) | cmp::isnan_(dg)) report_err(m, sy);
 }
 
 // ---------------------------------------------------------------------------
