@@ -130,12 +130,14 @@ __device__ __forceinline__ double riv_perim(int order, double depth, double coef
 // and a third logarithm; the difference ln a - z is carried as a
 // double-double, so Psi stays within an ulp of the reference's form (the
 // same cancellation in a as satn -> 1, exactly 0 at satn = 1).
+// sq returns sqrt(satn), which EffKinf's macropore branch needs too.
 __device__ __forceinline__ void kr_psi(double satn, double vm, double vg_e, double vg_ib, double inv_alpha,
-                                       double &satkfunc, double &psi) {
+                                       double &satkfunc, double &psi, double &sq) {
   double lh, ll;
   if (!log_dd_fast(satn, lh, ll)) {  // not positive and normal (NaN state)
     const double t = 1.0 - pow_fast(1.0 - pow_fast(satn, vm), vg_e);
-    satkfunc = sqrt(satn) * t * t;
+    sq = sqrt(satn);
+    satkfunc = sq * t * t;
     psi = -pow_fast(pow_fast(1.0 / satn, vm) - 1.0, vg_ib) * inv_alpha;
     return;
   }
@@ -146,12 +148,14 @@ __device__ __forceinline__ void kr_psi(double satn, double vm, double vg_e, doub
   if (!cmp::abs_lt_c(zh, 700.0) || !log_dd_fast(a, ah, al)) {
     // a == 0 (satn == 1), or outside the table path's ranges
     const double t = 1.0 - pow_fast(a, vg_e);
-    satkfunc = sqrt(satn) * t * t;
+    sq = sqrt(satn);
+    satkfunc = sq * t * t;
     psi = -pow_fast(a / x1, vg_ib) * inv_alpha;
     return;
   }
   const double t = 1.0 - pow_from_log(a, ah, al, vg_e);  // as pow_fast(a, e)
-  satkfunc = sqrt(satn) * t * t;
+  sq = sqrt(satn);
+  satkfunc = sq * t * t;
   double dh, dl, qh, ql, p;
   sub_dd(ah, al, zh, zl, dh, dl);  // ln(a / x1)
   mul_dd(vg_ib, dh, dl, qh, ql);
@@ -357,24 +361,24 @@ __global__ void __launch_bounds__(256, 3) k_elem_main(DevMesh m, const double *R
   const double pcpdrp = m.pcpdrp[i];
   const double zmax = m.zmax[i];
   const double dinf = m.dinf[i];
-  double satn = 1.0, satkfunc = 1.0, psi_u = 0.0;
+  double satn = 1.0, satkfunc = 1.0, psi_u = 0.0, sq = 1.0;
   if (!gw_in_dinf) {
     const double deficit = depth - gw;
     satn = unsat / deficit;
     satn = cmp::gt_c(satn, 1.0) ? 1.0 : satn;
     satn = cmp::lt_c(satn, kSatMin) ? kSatMin : satn;
-    kr_psi(satn, m.vg_m[i], m.vg_e[i], m.vg_ib[i], m.inv_alpha[i], satkfunc, psi_u);
+    kr_psi(satn, m.vg_m[i], m.vg_e[i], m.vg_ib[i], m.inv_alpha[i], satkfunc, psi_u, sq);
   }
   // Infil's saturation: the same one, except in Flux-PIHM, where it is
   // Noah's top-layer moisture (src/vert_flow.c:94-98) and Recharge keeps
   // the column's
-  double satn_i = satn, satkfunc_i = satkfunc, psi_i = psi_u;
+  double satn_i = satn, satkfunc_i = satkfunc, psi_i = psi_u, sq_i = sq;
   if (m.noah && !gw_in_dinf) {
     double s = m.noah_satn[i];
     s = cmp::gt_c(s, 1.0) ? 1.0 : s;
     s = cmp::lt_c(s, kSatMin) ? kSatMin : s;
     satn_i = s;
-    kr_psi(s, m.vg_m[i], m.vg_e[i], m.vg_ib[i], m.inv_alpha[i], satkfunc_i, psi_i);
+    kr_psi(s, m.vg_m[i], m.vg_e[i], m.vg_ib[i], m.inv_alpha[i], satkfunc_i, psi_i, sq_i);
   }
   // KrFunc(beta, 1) == 1 exactly: pow(1 - pow(1, m), e) == pow(0, e) == 0
   double infil;
@@ -389,16 +393,18 @@ __global__ void __launch_bounds__(256, 3) k_elem_main(DevMesh m, const double *R
     double wetfrac = surfh * (1.0 / kDeprStg);
     wetfrac = cmp::gt0(wetfrac) ? wetfrac : 0.0;
     wetfrac = cmp::lt_c(wetfrac, 1.0) ? wetfrac : 1.0;
-    double dh_by_dz;
-    double esatn = satn_i;
-    if (gw_in_dinf) {
-      dh_by_dz = (surfh + zmax - gwhead) / (0.5 * (surfh + dinf));
-      esatn = 1.0;
-    } else {
+    // the head below the infiltration front: the water table when it lies
+    // within dinf of the surface, else the unsaturated zone's; both
+    // reference branches divide (surfh + zmax - head) by the same
+    // denominator, so one division serves a warp whose lanes take both
+    double h_u = gwhead;
+    double esatn = 1.0;
+    if (!gw_in_dinf) {
       const double psi_c = cmp::gt_nc(psi_i, kPsiMin) ? psi_i : kPsiMin;
-      const double h_u = psi_c + zmax - 0.5 * dinf;
-      dh_by_dz = (surfh + zmax - h_u) / (0.5 * (surfh + dinf));
+      h_u = psi_c + zmax - 0.5 * dinf;
+      esatn = satn_i;
     }
+    double dh_by_dz = (surfh + zmax - h_u) / (0.5 * (surfh + dinf));
     dh_by_dz = (cmp::le0(surfh) && cmp::gt0(dh_by_dz)) ? 0.0 : dh_by_dz;
     // EffKinf, src/vert_flow.c:211-270
     double kinf;
@@ -409,9 +415,10 @@ __global__ void __launch_bounds__(256, 3) k_elem_main(DevMesh m, const double *R
     } else if (cmp::le_v(applrate, dh_by_dz * kinfv * satkfunc_i)) {
       kinf = kinfv * satkfunc_i;
     } else if (cmp::lt_v(applrate, dh_by_dz * (kmac_a + kinf_mat * satkfunc_i))) {
-      // KrFunc(2, satn): pow(satn, 2) and pow(., 0.5) are a product and sqrt
+      // KrFunc(2, satn): pow(satn, 2) and pow(., 0.5) are a product and
+      // sqrt; sqrt(esatn) is kr_psi's (1 when esatn is 1)
       const double t2 = 1.0 - sqrt(1.0 - esatn * esatn);
-      kinf = kinf_mat * satkfunc_i + kmac_a * (sqrt(esatn) * t2 * t2);
+      kinf = kinf_mat * satkfunc_i + kmac_a * (sq_i * t2 * t2);
     } else {
       kinf = kinf_mat * satkfunc_i + kmac_a;
     }
