@@ -133,33 +133,40 @@ __device__ __forceinline__ double riv_perim(int order, double depth, double coef
 // sq returns sqrt(satn), which EffKinf's macropore branch needs too.
 __device__ __forceinline__ void kr_psi(double satn, double vm, double vg_e, double vg_ib, double inv_alpha,
                                        double &satkfunc, double &psi, double &sq) {
+  sq = sqrt(satn);
   double lh, ll;
   if (!log_dd_fast(satn, lh, ll)) {  // not positive and normal (NaN state)
     const double t = 1.0 - pow_fast(1.0 - pow_fast(satn, vm), vg_e);
-    sq = sqrt(satn);
     satkfunc = sq * t * t;
     psi = -pow_fast(pow_fast(1.0 / satn, vm) - 1.0, vg_ib) * inv_alpha;
     return;
   }
   const double x1 = pow_from_log(satn, lh, ll, vm);  // satn^m, as pow_fast(satn, m)
   const double a = 1.0 - x1;
+  // a == 0 (satn^m == 1: a full column, where x1 == 1 and a / x1 == a) runs
+  // the table path on a stand-in argument, and its powers of +0 replace the
+  // results below, so that such lanes do not split the warp
+  const bool a0 = cmp::eq0(a);
   double zh, zl, ah, al;
   mul_dd(vm, lh, ll, zh, zl);  // the z pow_from_log formed
-  if (!cmp::abs_lt_c(zh, 700.0) || !log_dd_fast(a, ah, al)) {
-    // a == 0 (satn == 1), or outside the table path's ranges
+  if (!cmp::abs_lt_c(zh, 700.0) || !log_dd_fast(a0 ? 0.5 : a, ah, al)) {
+    // outside the table path's ranges
     const double t = 1.0 - pow_fast(a, vg_e);
-    sq = sqrt(satn);
     satkfunc = sq * t * t;
     psi = -pow_fast(a / x1, vg_ib) * inv_alpha;
     return;
   }
-  const double t = 1.0 - pow_from_log(a, ah, al, vg_e);  // as pow_fast(a, e)
-  sq = sqrt(satn);
-  satkfunc = sq * t * t;
+  double pe = pow_from_log(a, ah, al, vg_e);  // as pow_fast(a, e)
   double dh, dl, qh, ql, p;
   sub_dd(ah, al, zh, zl, dh, dl);  // ln(a / x1)
   mul_dd(vg_ib, dh, dl, qh, ql);
   if (!exp_dd_checked(qh, ql, p)) p = pow(a / x1, vg_ib);
+  if (a0) {
+    pe = pow_fast(a, vg_e);
+    p = pow_fast(a, vg_ib);
+  }
+  const double t = 1.0 - pe;
+  satkfunc = sq * t * t;
   psi = -p * inv_alpha;
 }
 
