@@ -619,6 +619,8 @@ int pihm_batch_create(const pihm_batch_limits *lim, int surf_mode, int riv_mode,
   m.gradmag = D(NE);
   m.rivflow = D(NUM_RIVFLX * NR);
   m.carry_ovl = D(2 * NR);
+  m.r_perim = D(NR);
+  m.r_crossa = D(NR);
   m.eflux_ovl = D(NED);
   m.eflux_sub = D(NED);
   m.bank_part = D(8 * NE);

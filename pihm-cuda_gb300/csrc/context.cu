@@ -140,6 +140,7 @@ int pihm_gpu_create(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double 
   dbytes += 4 * carve_size<double>(NE);       // surfh, head, effk, gradmag
   dbytes += carve_size<double>(11 * NR);      // rivflow
   dbytes += carve_size<double>(2 * NR);       // carried river-edge overland flux
+  dbytes += 2 * carve_size<double>(NR);       // channel perimeter and area
   dbytes += 2 * carve_size<double>(NED);      // edge fluxes
   dbytes += carve_size<double>(8 * NB);       // bank_part
   dbytes += 2 * carve_size<double>(3 * NE) + 2 * carve_size<double>(NE) + carve_size<double>(5 * NE);
@@ -163,6 +164,7 @@ int pihm_gpu_create(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double 
   m.gradmag = carve<double>(dp, NE);
   m.rivflow = carve<double>(dp, 11 * NR);
   m.carry_ovl = carve<double>(dp, 2 * NR);
+  m.r_perim = carve<double>(dp, NR); m.r_crossa = carve<double>(dp, NR);
   m.eflux_ovl = carve<double>(dp, NED); m.eflux_sub = carve<double>(dp, NED);
   m.bank_part = carve<double>(dp, 8 * NB);
   m.d_ovl = carve<double>(dp, 3 * NE); m.d_sub = carve<double>(dp, 3 * NE);

@@ -26,7 +26,8 @@ const double *DevMesh::*const kRiverMember[RP_COUNT] = {
     &DevMesh::r_dist_left, &DevMesh::r_dist_right, &DevMesh::r_depth, &DevMesh::r_coeff, &DevMesh::r_length,
     &DevMesh::r_width, &DevMesh::r_rough, &DevMesh::r_cwr, &DevMesh::r_ksath, &DevMesh::r_ksatv,
     &DevMesh::r_bedthick, &DevMesh::r_porosity, &DevMesh::r_inv_half_len, &DevMesh::r_inv_dist_down,
-    &DevMesh::r_inv_dist_left, &DevMesh::r_inv_dist_right, &DevMesh::r_inv_bedthick, &DevMesh::r_ovl_coef};
+    &DevMesh::r_inv_dist_left, &DevMesh::r_inv_dist_right, &DevMesh::r_inv_bedthick, &DevMesh::r_ovl_coef,
+    &DevMesh::r_geo0, &DevMesh::r_geo1, &DevMesh::r_geo2, &DevMesh::r_geo3, &DevMesh::r_geo4};
 
 namespace {
 
@@ -281,6 +282,37 @@ int build_image(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double step
     im->rv[RP_INV_DIST_RIGHT][s] = 1.0 / g->riv_dist_right[s];
     im->rv[RP_INV_BEDTHICK][s] = 1.0 / g->riv_bedthick[s];
     im->rv[RP_OVL_COEF][s] = g->riv_cwr[s] * 2.0 * std::sqrt(2.0 * kGrav) * len / 3.0;
+    // the coefficient-only factors of RivCsArea / RivPerim
+    // (src/river_flow.c:520-583) for the segment's shape
+    const double c = g->riv_coeff[s];
+    double *geo[5] = {&im->rv[RP_GEO0][s], &im->rv[RP_GEO1][s], &im->rv[RP_GEO2][s],
+                      &im->rv[RP_GEO3][s], &im->rv[RP_GEO4][s]};
+    switch (g->intrpl_ord[s]) {
+      case kRectangle:  // area d c, perimeter 2 d + c
+        *geo[0] = c;
+        break;
+      case kTriangle:  // area d^2 / c, perimeter 2 d sqrt(1 + c^2) / c
+        *geo[0] = 1.0 / c;
+        *geo[1] = 2.0 * std::sqrt(1.0 + c * c) / c;
+        break;
+      case kQuadratic:  // area 4 d^1.5 / (3 sqrt c), perimeter
+                        // sqrt(d (1 + 4 c d) / c) + ln(2 sqrt(c d) + sqrt(1 + 4 c d)) / (2 c)
+        *geo[0] = 4.0 / (3.0 * std::sqrt(c));
+        *geo[1] = 4.0 * c;
+        *geo[2] = 1.0 / c;
+        *geo[3] = 1.0 / (2.0 * c);
+        *geo[4] = 2.0 * std::sqrt(c);
+        break;
+      case kCubic: {  // area 3 d^(4/3) / (2 c^(1/3)), perimeter
+                      // 2 (sqrt(d (1 + 9 c^(2/3) d)) / 3 + ln(3 c^(1/3) sqrt(d) + sqrt(1 + 9 c^(2/3) d)) / (9 c^(1/3)))
+        const double c13 = std::pow(c, 1.0 / 3.0), c23 = std::pow(c, 2.0 / 3.0);
+        *geo[0] = 3.0 / (2.0 * c13);
+        *geo[1] = 9.0 * c23;
+        *geo[2] = 3.0 * c13;
+        *geo[3] = 1.0 / (9.0 * c13);
+        break;
+      }
+    }
   }
   return PIHM_GPU_OK;
 }

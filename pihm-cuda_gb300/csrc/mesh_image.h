@@ -29,6 +29,7 @@ enum RiverPlane {
   RP_AREA = 0, RP_ZMIN, RP_ZMAX, RP_ZBED, RP_NODE_ZMAX, RP_DIST_LEFT, RP_DIST_RIGHT, RP_DEPTH,
   RP_COEFF, RP_LENGTH, RP_WIDTH, RP_ROUGH, RP_CWR, RP_KSATH, RP_KSATV, RP_BEDTHICK, RP_POROSITY,
   RP_INV_HALF_LEN, RP_INV_DIST_DOWN, RP_INV_DIST_LEFT, RP_INV_DIST_RIGHT, RP_INV_BEDTHICK, RP_OVL_COEF,
+  RP_GEO0, RP_GEO1, RP_GEO2, RP_GEO3, RP_GEO4,
   RP_COUNT
 };
 

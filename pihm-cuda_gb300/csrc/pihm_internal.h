@@ -78,6 +78,9 @@ struct DevMesh {
   // an outlet), 1/dist_left, 1/dist_right, 1/bedthick, cwr 2 sqrt(2g) length/3
   const double *r_inv_half_len, *r_inv_dist_down, *r_inv_dist_left, *r_inv_dist_right,
       *r_inv_bedthick, *r_ovl_coef;
+  // coefficient-only factors of the channel area and wetted perimeter, by
+  // shape (k_riv_geom)
+  const double *r_geo0, *r_geo1, *r_geo2, *r_geo3, *r_geo4;
   const int32_t *up_ptr, *up_idx;  // CSR of upstream segments, reference order
   const int32_t *up_end;           // [nr] end of each upstream list (up_ptr + 1 in a
                                    // single-watershed context)
@@ -91,6 +94,7 @@ struct DevMesh {
   double *surfh, *head, *effk, *gradmag;  // [ne]
   double *eflux_ovl, *eflux_sub;          // [nedge]
   double *rivflow;                        // [11][nr]
+  double *r_perim, *r_crossa;             // [nr] wetted perimeter and area at the stage
   double *carry_ovl;                      // [2][nr] river-edge overland flux (LEFT, RIGHT
                                           // SURF2CHANL of the last evaluation) that the
                                           // next evaluation's Infil reads

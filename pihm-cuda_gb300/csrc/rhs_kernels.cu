@@ -1,9 +1,10 @@
 // FP64 right-hand-side kernels of the PIHM hydrologic model for sm_103a.
 //
 // One evaluation of f(t, y) (the reference ODE(), src/ode.c:4-399) runs as
-// six stream-ordered launches with no host synchronisation (k_edge is listed
-// at its definition: each interior edge is evaluated once and read with a
-// sign by both elements).  GB300 issues ~2 FP64 instructions per clock per SM,
+// seven launches with no host synchronisation, the two river kernels on a
+// second stream beside k_elem_grad/k_edge/k_elem_main (k_edge is listed at
+// its definition: each interior edge is evaluated once and read with a sign
+// by both elements).  GB300 issues ~2 FP64 instructions per clock per SM,
 // so the kernels are FP64-issue bound: powers go through the table-driven
 // pow_fast (fp64_math.cuh), divisions by static quantities are multiplications
 // by reciprocals computed at load, and sub-expressions the reference
@@ -25,6 +26,8 @@
 //                 (src/ode.c:111-209).  Elements with river edges hand their
 //                 partial sums to k_finish, because their river-edge fluxes are
 //                 written by the river kernel of the same evaluation.
+//   k_riv_geom    per segment: channel area and wetted perimeter at the
+//                 stage (src/river_flow.c:520-583), once per segment.
 //   k_river       per segment: RiverFlow (src/river_flow.c:3-94) and
 //                 RiverToElem (:113-183), ChanLeak, OutletFlux, BoundFluxRiver.
 //   k_finish      per segment: upstream accumulation in reference order
@@ -34,8 +37,9 @@
 //
 // Infil reads the river-edge overland flux of the previous evaluation
 // (src/vert_flow.c:61 runs before src/river_flow.c:159-182 rewrites it); that
-// value is the previous evaluation's rivflow slot LEFT/RIGHT_SURF2CHANL, which
-// k_elem_main reads before k_river of this evaluation overwrites it.
+// value is the previous evaluation's LEFT/RIGHT_SURF2CHANL, which k_finish
+// copies to carry_ovl, so k_elem_main can read it while this evaluation's
+// k_river runs.
 #include <cmath>
 
 #include "fp64_math.cuh"
@@ -85,39 +89,6 @@ __device__ __forceinline__ double overland_flow(double avg_h, double grad_h, dou
                                                 double crossa, double avg_rough) {
   return crossa * pow_manning(avg_h, kManningSurf, kManningSurfDelta) * grad_h /
          (sqrt(avg_sf) * avg_rough);
-}
-
-// ---------------------------------------------------------------------------
-// river geometry, src/river_flow.c:520-583
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ double riv_cs_area(int order, double depth, double coeff) {
-  depth = cmp::gt0(depth) ? depth : 0.0;
-  switch (order) {
-    case kRectangle: return depth * coeff;
-    case kTriangle: return depth * depth / coeff;
-    case kQuadratic: return 4.0 * depth * sqrt(depth) / (3.0 * sqrt(coeff));
-    case kCubic: return 3.0 * pow_fast(depth, 4.0 / 3.0) / (2.0 * pow_fast(coeff, 1.0 / 3.0));
-  }
-  return 0.0;
-}
-
-__device__ __forceinline__ double riv_perim(int order, double depth, double coeff) {
-  depth = cmp::gt0(depth) ? depth : 0.0;
-  switch (order) {
-    case kRectangle: return 2.0 * depth + coeff;
-    case kTriangle: return 2.0 * depth * sqrt(1.0 + coeff * coeff) / coeff;
-    case kQuadratic:
-      return sqrt(depth * (1.0 + 4.0 * coeff * depth) / coeff) +
-             log(2.0 * sqrt(coeff * depth) + sqrt(1.0 + 4.0 * coeff * depth)) / (2.0 * coeff);
-    case kCubic: {
-      const double c23 = pow_fast(coeff, 2.0 / 3.0);
-      const double c13 = pow_fast(coeff, 1.0 / 3.0);
-      return 2.0 * ((pow_fast(depth * (1.0 + 9.0 * c23 * depth), 0.5) / 3.0) +
-                    (log(3.0 * c13 * sqrt(depth) + pow_fast(1.0 + 9.0 * c23 * depth, 0.5)) /
-                     (9.0 * c13)));
-    }
-  }
-  return 0.0;
 }
 
 // KrFunc (src/soil.c:8-13) and Psi (src/vert_flow.c:272-278) of one
@@ -522,22 +493,73 @@ __global__ void __launch_bounds__(256, 3) k_elem_main(DevMesh m, const double *R
 }
 
 // ---------------------------------------------------------------------------
+// k_riv_geom: wetted perimeter and cross-section area of every segment at its
+// stage (RivPerim / RivCsArea, src/river_flow.c:520-583), once per segment
+// and evaluation (k_river needs them for the segment and for its downstream
+// neighbour), with the coefficient-only factors formed at load (r_geo*, in
+// the order the shape's formula uses them):
+//   rectangle  area d c,           perimeter 2 d + c
+//   triangle   area d^2 / c,       perimeter 2 d sqrt(1 + c^2) / c
+//   quadratic  area 4 d^1.5 / (3 sqrt c),
+//              perimeter sqrt(d (1 + 4 c d) / c) + ln(2 sqrt(c d) + sqrt(1 + 4 c d)) / (2 c)
+//   cubic      area 3 d^(4/3) / (2 c^(1/3)),
+//              perimeter 2 (sqrt(d (1 + 9 c^(2/3) d)) / 3
+//                           + ln(3 c^(1/3) sqrt(d) + sqrt(1 + 9 c^(2/3) d)) / (9 c^(1/3)))
+// The reference's pow(x, 0.5) is sqrt(x).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double log_of(double x) {
+  double sh, lo;
+  return log_dd_fast(x, sh, lo) ? sh + lo : log(x);
+}
+
+__global__ void __launch_bounds__(128) k_riv_geom(DevMesh m, const double *RESTRICT y) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  int sy;
+  if (s >= m.nr_run || skip_item(m, m.sys_riv, s, &sy)) return;
+  double d = y[3 * m.ne + s];
+  d = cmp::gt0(d) ? d : 0.0;
+  const double g0 = m.r_geo0[s];
+  double area = 0.0, perim = 0.0;
+  switch (m.intrpl_ord[s]) {
+    case kRectangle:
+      area = d * g0;
+      perim = 2.0 * d + g0;
+      break;
+    case kTriangle:
+      area = d * d * g0;
+      perim = d * m.r_geo1[s];
+      break;
+    case kQuadratic: {
+      const double sd = sqrt(d), w = 1.0 + m.r_geo1[s] * d;
+      area = g0 * d * sd;
+      perim = sqrt(d * w * m.r_geo2[s]) + log_of(m.r_geo4[s] * sd + sqrt(w)) * m.r_geo3[s];
+      break;
+    }
+    case kCubic: {
+      const double sd = sqrt(d), w = 1.0 + m.r_geo1[s] * d;
+      area = g0 * pow_fast(d, 4.0 / 3.0);
+      perim = 2.0 * (sqrt(d * w) * (1.0 / 3.0) + log_of(m.r_geo2[s] * sd + sqrt(w)) * m.r_geo3[s]);
+      break;
+    }
+  }
+  m.r_perim[s] = perim;
+  m.r_crossa[s] = area;
+}
+
+// ---------------------------------------------------------------------------
 // k_river
 // ---------------------------------------------------------------------------
 struct RivState {
-  int order;
-  double stage, gw, zbed, zmin, zmax, coeff, length, width, rough;
+  double stage, gw, zbed, zmin, zmax, length, width, rough;
 };
 
 __device__ __forceinline__ RivState load_riv(const DevMesh &m, const double *y, int s) {
   RivState r;
-  r.order = m.intrpl_ord[s];
   r.stage = clamp0(y[3 * m.ne + s]);
   r.gw = clamp0(y[3 * m.ne + m.nr + s]);
   r.zbed = m.r_zbed[s];
   r.zmin = m.r_zmin[s];
   r.zmax = m.r_zmax[s];
-  r.coeff = m.r_coeff[s];
   r.length = m.r_length[s];
   r.width = m.r_width[s];
   r.rough = m.r_rough[s];
@@ -615,8 +637,8 @@ __global__ void __launch_bounds__(128) k_river(DevMesh m, const double *RESTRICT
       if (bct > 0) {
         const double total_h = r.stage + r.zbed;
         const double grad_h = (total_h - bc) * m.r_inv_half_len[s];
-        const double avg_perim = riv_perim(r.order, r.stage, r.coeff);
-        const double crossa = riv_cs_area(r.order, r.stage, r.coeff);
+        const double avg_perim = m.r_perim[s];
+        const double crossa = m.r_crossa[s];
         const double avg_h = cmp::eq0(avg_perim) ? 0.0 : (crossa / avg_perim);
         flux = overland_flow(avg_h, grad_h, grad_h, crossa, r.rough);
       } else {
@@ -630,16 +652,16 @@ __global__ void __launch_bounds__(128) k_river(DevMesh m, const double *RESTRICT
     // ChanFlowRiverToRiver, src/river_flow.c:257-300
     {
       const double total_h = r.stage + r.zbed;
-      const double perim = riv_perim(r.order, r.stage, r.coeff);
+      const double perim = m.r_perim[s];
       const double total_h_down = dn.stage + dn.zbed;
-      const double perim_down = riv_perim(dn.order, dn.stage, dn.coeff);
+      const double perim_down = m.r_perim[d];
       const double avg_perim = (perim + perim_down) / 2.0;
       const double avg_rough = (r.rough + dn.rough) / 2.0;
       const double diff_h = (m.riv_mode == kKinematic) ? (r.zbed - dn.zbed) : (total_h - total_h_down);
       const double grad_h = diff_h * inv_dist_down;
       const double avg_sf = cmp::gt0(grad_h) ? grad_h : kRivGradMin;
-      const double crossa = riv_cs_area(r.order, r.stage, r.coeff);
-      const double crossa_down = riv_cs_area(dn.order, dn.stage, dn.coeff);
+      const double crossa = m.r_crossa[s];
+      const double crossa_down = m.r_crossa[d];
       const double avg_crossa = 0.5 * (crossa + crossa_down);
       const double avg_h = cmp::eq0(avg_perim) ? 0.0 : (avg_crossa / avg_perim);
       f[DOWN_CHANL2CHANL] = overland_flow(avg_h, grad_h, avg_sf, crossa, avg_rough);
@@ -665,21 +687,21 @@ __global__ void __launch_bounds__(128) k_river(DevMesh m, const double *RESTRICT
     if (down == kDirichlet) {
       const double total_h = r.stage + r.zbed;
       const double grad_h = (total_h - bc) * m.r_inv_half_len[s];
-      const double avg_perim = riv_perim(r.order, r.stage, r.coeff);
-      const double crossa = riv_cs_area(r.order, r.stage, r.coeff);
+      const double avg_perim = m.r_perim[s];
+      const double crossa = m.r_crossa[s];
       const double avg_h = cmp::eq0(avg_perim) ? 0.0 : (crossa / avg_perim);
       q = overland_flow(avg_h, grad_h, grad_h, crossa, r.rough);
     } else if (down == kNeumann) {
       q = -bc;
     } else if (down == kZeroDpthGrad) {
       const double grad_h = (r.zbed - (m.r_node_zmax[s] - depth)) * m.r_inv_half_len[s];
-      const double avg_perim = riv_perim(r.order, r.stage, r.coeff);
-      const double crossa = riv_cs_area(r.order, r.stage, r.coeff);
+      const double avg_perim = m.r_perim[s];
+      const double crossa = m.r_crossa[s];
       q = sqrt(grad_h) * crossa *
           (cmp::gt0(avg_perim) ? pow_manning(crossa / avg_perim, kManningRiv, kManningRivDelta) : 0.0) /
           r.rough;
     } else {  // kCritDpth (other values are rejected at load)
-      const double crossa = riv_cs_area(r.order, r.stage, r.coeff);
+      const double crossa = m.r_crossa[s];
       q = crossa * sqrt(kGrav * r.stage);
     }
     f[DOWN_CHANL2CHANL] = q;
@@ -859,8 +881,9 @@ cudaError_t launch_rhs(const DevMesh &m, const double *y, double *ydot, cudaStre
     if (fork) {
       if (cudaEventRecord(side->fork, st) != cudaSuccess) return cudaErrorUnknown;
       if (cudaStreamWaitEvent(side->side, side->fork, 0) != cudaSuccess) return cudaErrorUnknown;
+      k_riv_geom<<<blocks_for(m.nr_run, 128), 128, 0, side->side>>>(m, y);
       k_river<<<blocks_for(m.nr_run, 128), 128, 0, side->side>>>(m, y);
-      ++*launches;
+      *launches += 2;
       if (cudaEventRecord(side->join, side->side) != cudaSuccess) return cudaErrorUnknown;
     }
     if (m.surf_mode == kDiffWave) {
@@ -883,10 +906,11 @@ cudaError_t launch_rhs(const DevMesh &m, const double *y, double *ydot, cudaStre
   if (fork) {
     if (cudaStreamWaitEvent(st, side->join, 0) != cudaSuccess) return cudaErrorUnknown;
   } else if (m.nr_run > 0) {
-    on = prof_begin(prof, K_RIVER, st);
+    on = prof_begin(prof, K_RIVER, st);  // both river kernels
+    k_riv_geom<<<blocks_for(m.nr_run, 128), 128, 0, st>>>(m, y);
     k_river<<<blocks_for(m.nr_run, 128), 128, 0, st>>>(m, y);
     prof_end(prof, on, st);
-    ++*launches;
+    *launches += 2;
   }
   if (m.nr_run + m.nbank_run > 0) {
     on = prof_begin(prof, K_FINISH, st);
