@@ -173,8 +173,8 @@ int place(pihm_batch *B, Sys *s, const Prepared &job) {
   rc |= h2d((int32_t *)m.e_i + edo, ei.data(), im.nedge, st);
   rc |= h2d((int32_t *)m.e_k + edo, ek.data(), im.nedge, st);
   rc |= h2d((double *)m.e_invdist + edo, im.e_invdist.data(), im.nedge, st);
-  rc |= h2d((double *)m.e_len + edo, im.e_len.data(), im.nedge, st);
-  rc |= h2d((double *)m.e_invrough + edo, im.e_invrough.data(), im.nedge, st);
+  rc |= h2d((double *)m.e_subk + edo, im.e_subk.data(), im.nedge, st);
+  rc |= h2d((double *)m.e_ovlk + edo, im.e_ovlk.data(), im.nedge, st);
   std::vector<int32_t> bs(ne), be(im.nbank);
   for (int i = 0; i < ne; i++) bs[i] = im.bank_slot[i] >= 0 ? (int32_t)(im.bank_slot[i] + bo) : -1;
   for (int b = 0; b < im.nbank; b++) be[b] = (int32_t)(im.bank_elem[b] + eo);
@@ -594,8 +594,8 @@ int pihm_batch_create(const pihm_batch_limits *lim, int surf_mode, int riv_mode,
   m.e_i = I(NED);
   m.e_k = I(NED);
   m.e_invdist = D(NED);
-  m.e_len = D(NED);
-  m.e_invrough = D(NED);
+  m.e_subk = D(NED);
+  m.e_ovlk = D(NED);
   m.bank_slot = I(NE);
   m.bank_elem = I(NE);
   m.down = I(NR);

@@ -108,8 +108,8 @@ int pihm_gpu_create(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double 
   m.e_i = put(im.e_i.data(), nedge, NED);
   m.e_k = put(im.e_k.data(), nedge, NED);
   m.e_invdist = put(im.e_invdist.data(), nedge, NED);
-  m.e_len = put(im.e_len.data(), nedge, NED);
-  m.e_invrough = put(im.e_invrough.data(), nedge, NED);
+  m.e_subk = put(im.e_subk.data(), nedge, NED);
+  m.e_ovlk = put(im.e_ovlk.data(), nedge, NED);
   m.bank_slot = put(im.bank_slot.data(), NE, NE);
   m.bank_elem = put(im.bank_elem.data(), nbank, NB);
   m.down = put(im.down.data(), nr, NR);

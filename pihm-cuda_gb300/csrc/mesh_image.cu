@@ -166,8 +166,8 @@ int build_image(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double step
   im->e_i.clear();
   im->e_k.clear();
   im->e_invdist.clear();
-  im->e_len.clear();
-  im->e_invrough.clear();
+  im->e_subk.clear();
+  im->e_ovlk.clear();
   for (int i = 0; i < ne; i++) {
     const int ri = perm[i];
     for (int j = 0; j < 3; j++) {
@@ -187,9 +187,15 @@ int build_image(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double step
       const int e = (int)im->e_i.size();
       im->e_i.push_back(i);
       im->e_k.push_back(k);
-      im->e_invdist.push_back(1.0 / g->nabrdist[3 * ri + j]);
-      im->e_len.push_back(g->edge[3 * ri + j]);
-      im->e_invrough.push_back(1.0 / (0.5 * (g->rough[ri] + g->rough[rk])));
+      // the edge's constant factors: 1/distance, and the products the two
+      // flux formulas multiply by, edge/(2 distance) for the Darcy flux
+      // (avg_ksat grad_h avg_h edge with avg_ksat a mean and grad_h a
+      // difference over the distance) and edge/(distance avg_rough) for the
+      // Manning flux (src/lat_flow.c:279-338)
+      const double invdist = 1.0 / g->nabrdist[3 * ri + j], len = g->edge[3 * ri + j];
+      im->e_invdist.push_back(invdist);
+      im->e_subk.push_back(0.5 * len * invdist);
+      im->e_ovlk.push_back(len * invdist / (0.5 * (g->rough[ri] + g->rough[rk])));
       im->emap[(size_t)j * ne + i] = e + 1;
       if (sym) im->emap[(size_t)jr * ne + k] = -(e + 1);
     }

@@ -45,7 +45,7 @@ struct SystemImage {
   std::vector<int32_t> nb, bct, emap;          // [3*ne]; nb: >= 0 element, -1-s river, kBoundary
   std::vector<int32_t> bank_slot, bank_elem;   // [ne] (-1: no river edge), [nbank]
   std::vector<int32_t> e_i, e_k;               // [nedge]
-  std::vector<double> e_invdist, e_len, e_invrough;
+  std::vector<double> e_invdist, e_subk, e_ovlk;
   std::vector<int32_t> down, left, right, ord, rbct;  // [nr]; down as in the reference (1-based or BC code)
   std::vector<double> rv[RP_COUNT];            // [nr]
   std::vector<int32_t> up_ptr, up_idx;         // [nr+1], [up_ptr[nr]]

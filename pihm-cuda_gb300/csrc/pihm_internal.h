@@ -64,7 +64,7 @@ struct DevMesh {
   // its owner and read with a sign by the other side
   int32_t nedge;
   const int32_t *e_i, *e_k;                  // owner, neighbour (internal)
-  const double *e_invdist, *e_len, *e_invrough;
+  const double *e_invdist, *e_subk, *e_ovlk;  // 1/dist, edge/(2 dist), edge/(dist avg_rough)
   const int32_t *emap;                       // [3][ne] +(e+1) owner, -(e+1) other, 0 none
   const int32_t *bank_slot;     // [ne] slot of an element with river edges
   const int32_t *bank_elem;     // [nbank]

@@ -217,34 +217,31 @@ __global__ void __launch_bounds__(256) k_edge(DevMesh m, const double *RESTRICT 
   if (e >= m.nedge_run || skip_item(m, m.sys_edge, e, &sy)) return;
   const int ne = m.ne;
   const int i = m.e_i[e], k = m.e_k[e];
-  const double invdist = m.e_invdist[e], len = m.e_len[e];
-  // Darcy flux between the two groundwater columns
+  // Darcy flux between the two groundwater columns,
+  // avg_ksat grad_h avg_h edge = (effk_i + effk_k) diff_h avg_h edge/(2 dist)
   const double gw_i = clamp0(y[2 * ne + i]), gw_k = clamp0(y[2 * ne + k]);
   double diff_h = (gw_i + m.zmin[i]) - (gw_k + m.zmin[k]);
   double avg_h = avg_h_sub(diff_h, gw_i, gw_k);
-  double grad_h = diff_h * invdist;
-  const double avg_ksat = 0.5 * (m.effk[i] + m.effk[k]);
-  m.eflux_sub[e] = avg_ksat * grad_h * avg_h * len;
-  // Manning overland flux
+  m.eflux_sub[e] = (m.effk[i] + m.effk[k]) * diff_h * avg_h * m.e_subk[e];
+  // Manning overland flux, crossa h^p grad_h / (sqrt(avg_sf) avg_rough) =
+  // avg_h h^p diff_h / sqrt(avg_sf) edge/(dist avg_rough)
   const double s_i = m.surfh[i], s_k = m.surfh[k];
   double avg_sf;
   if (m.surf_mode == kKinematic) {
     diff_h = m.zmax[i] - m.zmax[k];
     avg_h = avg_h_surf(diff_h, s_i, s_k);
-    grad_h = diff_h * invdist;
+    const double grad_h = diff_h * m.e_invdist[e];
     avg_sf = cmp::gt0(grad_h) ? grad_h : kGradMin;
   } else {
     diff_h = m.head[i] - m.head[k];
     avg_h = avg_h_surf(diff_h, s_i, s_k);
-    grad_h = diff_h * invdist;
     avg_sf = 0.5 * (m.gradmag[i] + m.gradmag[k]);
     avg_sf = cmp::gt_c(avg_sf, kGradMin) ? avg_sf : kGradMin;
   }
   double ovl = 0.0;
   if (cmp::gt0(avg_h)) {  // avg_h == 0 gives crossa == 0: the flux is zero
-    const double crossa = avg_h * len;
-    ovl = crossa * pow_manning(avg_h, kManningSurf, kManningSurfDelta) * grad_h * rsqrt(avg_sf) *
-          m.e_invrough[e];
+    ovl = avg_h * pow_manning(avg_h, kManningSurf, kManningSurfDelta) * diff_h * rsqrt(avg_sf) *
+          m.e_ovlk[e];
   }
   m.eflux_ovl[e] = ovl;
 }
