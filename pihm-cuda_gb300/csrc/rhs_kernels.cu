@@ -210,40 +210,76 @@ __global__ void __launch_bounds__(256) k_elem_grad(DevMesh m, const double *REST
 // neighbour reads the negated value.  Kinematic overland flow is not
 // antisymmetric (avg_sf depends on the sign of the gradient): there every
 // element side is its own one-sided edge.
+//
+// The Manning flux costs about 35 FP64 operations and only edges whose
+// upwind element holds water above the depression storage have one (about
+// half of them, spread over nearly every warp).  So each thread computes its
+// Darcy flux and the Manning flux's inputs, the edges with water are queued
+// in shared memory (warp-aggregated slots), and after one barrier the block
+// evaluates the queue densely: ceil(n/32) warps instead of all eight carry
+// the powers.  Each flux depends on its edge alone, so which thread computes
+// it changes no bit.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_edge(DevMesh m, const double *RESTRICT y) {
+constexpr int kEdgeBlock = 256;
+
+__global__ void __launch_bounds__(kEdgeBlock) k_edge(DevMesh m, const double *RESTRICT y) {
+  __shared__ int q_e[kEdgeBlock];
+  __shared__ double q_h[kEdgeBlock], q_d[kEdgeBlock], q_sf[kEdgeBlock];
+  __shared__ int q_n;
+  if (threadIdx.x == 0) q_n = 0;
+  __syncthreads();
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   int sy;
-  if (e >= m.nedge_run || skip_item(m, m.sys_edge, e, &sy)) return;
-  const int ne = m.ne;
-  const int i = m.e_i[e], k = m.e_k[e];
-  // Darcy flux between the two groundwater columns,
-  // avg_ksat grad_h avg_h edge = (effk_i + effk_k) diff_h avg_h edge/(2 dist)
-  const double gw_i = clamp0(y[2 * ne + i]), gw_k = clamp0(y[2 * ne + k]);
-  double diff_h = (gw_i + m.zmin[i]) - (gw_k + m.zmin[k]);
-  double avg_h = avg_h_sub(diff_h, gw_i, gw_k);
-  m.eflux_sub[e] = (m.effk[i] + m.effk[k]) * diff_h * avg_h * m.e_subk[e];
-  // Manning overland flux, crossa h^p grad_h / (sqrt(avg_sf) avg_rough) =
-  // avg_h h^p diff_h / sqrt(avg_sf) edge/(dist avg_rough)
-  const double s_i = m.surfh[i], s_k = m.surfh[k];
-  double avg_sf;
-  if (m.surf_mode == kKinematic) {
-    diff_h = m.zmax[i] - m.zmax[k];
-    avg_h = avg_h_surf(diff_h, s_i, s_k);
-    const double grad_h = diff_h * m.e_invdist[e];
-    avg_sf = cmp::gt0(grad_h) ? grad_h : kGradMin;
-  } else {
-    diff_h = m.head[i] - m.head[k];
-    avg_h = avg_h_surf(diff_h, s_i, s_k);
-    avg_sf = 0.5 * (m.gradmag[i] + m.gradmag[k]);
-    avg_sf = cmp::gt_c(avg_sf, kGradMin) ? avg_sf : kGradMin;
+  bool wet = false;
+  double avg_h = 0.0, diff_h = 0.0, avg_sf = 0.0;
+  if (e < m.nedge_run && !skip_item(m, m.sys_edge, e, &sy)) {
+    const int ne = m.ne;
+    const int i = m.e_i[e], k = m.e_k[e];
+    // Darcy flux between the two groundwater columns,
+    // avg_ksat grad_h avg_h edge = (effk_i + effk_k) diff_h avg_h edge/(2 dist)
+    const double gw_i = clamp0(y[2 * ne + i]), gw_k = clamp0(y[2 * ne + k]);
+    diff_h = (gw_i + m.zmin[i]) - (gw_k + m.zmin[k]);
+    avg_h = avg_h_sub(diff_h, gw_i, gw_k);
+    m.eflux_sub[e] = (m.effk[i] + m.effk[k]) * diff_h * avg_h * m.e_subk[e];
+    // Manning overland flux, crossa h^p grad_h / (sqrt(avg_sf) avg_rough) =
+    // avg_h h^p diff_h / sqrt(avg_sf) edge/(dist avg_rough)
+    const double s_i = m.surfh[i], s_k = m.surfh[k];
+    if (m.surf_mode == kKinematic) {
+      diff_h = m.zmax[i] - m.zmax[k];
+      avg_h = avg_h_surf(diff_h, s_i, s_k);
+      const double grad_h = diff_h * m.e_invdist[e];
+      avg_sf = cmp::gt0(grad_h) ? grad_h : kGradMin;
+    } else {
+      diff_h = m.head[i] - m.head[k];
+      avg_h = avg_h_surf(diff_h, s_i, s_k);
+      avg_sf = 0.5 * (m.gradmag[i] + m.gradmag[k]);
+      avg_sf = cmp::gt_c(avg_sf, kGradMin) ? avg_sf : kGradMin;
+    }
+    // avg_h == 0 gives crossa == 0: the flux is zero
+    wet = cmp::gt0(avg_h);
+    if (!wet) m.eflux_ovl[e] = 0.0;
   }
-  double ovl = 0.0;
-  if (cmp::gt0(avg_h)) {  // avg_h == 0 gives crossa == 0: the flux is zero
-    ovl = avg_h * pow_manning(avg_h, kManningSurf, kManningSurfDelta) * diff_h * rsqrt(avg_sf) *
-          m.e_ovlk[e];
+  // queue the wet edges: one shared atomic per warp
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned mask = __ballot_sync(0xffffffffu, wet);
+  int base = 0;
+  if (lane == 0 && mask) base = atomicAdd(&q_n, __popc(mask));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (wet) {
+    const int slot = base + __popc(mask & ((1u << lane) - 1u));
+    q_e[slot] = e;
+    q_h[slot] = avg_h;
+    q_d[slot] = diff_h;
+    q_sf[slot] = avg_sf;
   }
-  m.eflux_ovl[e] = ovl;
+  __syncthreads();
+  const int t = threadIdx.x;
+  if (t < q_n) {
+    const int qe = q_e[t];
+    const double h = q_h[t];
+    m.eflux_ovl[qe] = h * pow_manning(h, kManningSurf, kManningSurfDelta) * q_d[t] * rsqrt(q_sf[t]) *
+                      m.e_ovlk[qe];
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -891,7 +927,7 @@ cudaError_t launch_rhs(const DevMesh &m, const double *y, double *ydot, cudaStre
     }
     if (m.nedge_run > 0) {
       on = prof_begin(prof, K_EDGE, st);
-      k_edge<<<blocks_for(m.nedge_run, 256), 256, 0, st>>>(m, y);
+      k_edge<<<blocks_for(m.nedge_run, kEdgeBlock), kEdgeBlock, 0, st>>>(m, y);
       prof_end(prof, on, st);
       ++*launches;
     }
