@@ -10,12 +10,14 @@ how far any right-hand side that differs from the reference's in the last
 bit (another libm, fused multiply-adds, another reduction order) can be
 expected to land; the GPU end-to-end test is held to it.
 
-    python tests/golden/make_sensitivity.py [--runs 4]
+    python tests/golden/make_sensitivity.py [--runs 24]
 
 writes tests/golden/c0_sensitivity.npz: final states [runs, neq], outlet
-flux series [runs, nsteps], step counts [runs], the water-balance sums of
-PrintWaterBal (src/print.c:337-542) per model step [runs, nsteps, 3],
-seeds.
+flux series [runs, nsteps], step counts [runs], the largest cumulative
+water-balance residual of PrintWaterBal (src/print.c:337-542) over the run
+[runs], seeds.  The residual is heavy-tailed under this noise (six runs
+spread from 13 to 96 m3 around the unperturbed 35 m3), so the default is
+24 runs.
 """
 import argparse
 import ctypes
@@ -62,7 +64,7 @@ def noisy_run(ws, z, ctrl, seed):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--runs", type=int, default=4)
+    ap.add_argument("--runs", type=int, default=24)
     ap.add_argument("--out", default=os.path.join(HERE, "c0_sensitivity.npz"))
     args = ap.parse_args()
     z = np.load(os.path.join(HERE, "c0_solve.npz"))
@@ -76,10 +78,12 @@ def main():
         finals.append(r["states"][-1])
         outs.append(r["outlet"])
         nst.append(r["stats"].nst)
-        wbs.append(r["wb"])
-        print("seed", s, "nst", r["stats"].nst)
+        wb = r["wb"]
+        resid = np.cumsum(wb[1:, 0] - wb[1:, 1] - (wb[1:, 2] - wb[:-1, 2]))
+        wbs.append(np.abs(resid).max())
+        print("seed", s, "nst", r["stats"].nst, "water-balance residual", wbs[-1])
     np.savez_compressed(args.out, final=np.array(finals), outlet=np.array(outs), nst=np.array(nst),
-                        wb=np.array(wbs), seeds=np.array(seeds))
+                        wb_resid=np.array(wbs), seeds=np.array(seeds))
 
 
 if __name__ == "__main__":
