@@ -5,16 +5,17 @@
 // side.  pow_fast(x, y) = exp(y ln x) follows P. T. P. Tang's table-driven
 // algorithms ("Table-driven implementation of the exponential function in
 // IEEE floating-point arithmetic", ACM TOMS 15(2) 1989; "... of the logarithm
-// function ...", ACM TOMS 16(4) 1990) with 256-entry tables generated by
+// function ...", ACM TOMS 16(4) 1990) with 1024-entry tables generated by
 // gen_fp64_tables.py:
 //
-//   ln x:  x = 2^k m, m in [1,2); i = top 8 fraction bits; r = m F_i - 1 is
+//   ln x:  x = 2^k m, m in [1,2); i = top 10 fraction bits; r = m F_i - 1 is
 //          formed exactly (two-product, Sterbenz); ln x = k ln2 + G_i +
-//          log1p(r), log1p by its Taylor series to r^7 (|r| < 2^-8.9),
-//          carried as a double-double;
+//          log1p(r), log1p by its Taylor series to r^5 (|r| <= 2^-11, the
+//          next term below 2^-68), carried as a double-double;
 //   y ln x: double-double product;
-//   exp:   z = (256 q + j) ln2/256 + r, |r| <= ln2/512;
-//          exp z = 2^q T_j (1 + expm1 r), expm1 by its Taylor series to r^5.
+//   exp:   z = (1024 q + j) ln2/1024 + r, |r| <= ln2/2048;
+//          exp z = 2^q T_j (1 + expm1 r), expm1 by its Taylor series to r^4
+//          (the next term below 2^-64 relative).
 //
 // Error: about 0.51 ulp for the arguments the model produces (checked against
 // 60-digit references and CUDA's pow in tests/test_fp64_math_gpu.py).  The
@@ -32,17 +33,16 @@ namespace pihm {
 
 __device__ __forceinline__ double exp_dd_fast(double zh, double zl) {
   const double shifter = 0x1.8p52;  // 1.5 * 2^52: rounds to an integer in the low bits
-  const double u = fma(zh, k256ByLn2, shifter);
+  const double u = fma(zh, kNByLn2, shifter);
   const int kk = __double2loint(u);
   const double nd = u - shifter;
-  double r = fma(-nd, kLn2By256Hi, zh);
-  r = fma(-nd, kLn2By256Lo, r) + zl;
-  double p = fma(r, 1.0 / 120.0, 1.0 / 24.0);
-  p = fma(p, r, 1.0 / 6.0);
+  double r = fma(-nd, kLn2ByNHi, zh);
+  r = fma(-nd, kLn2ByNLo, r) + zl;
+  double p = fma(r, 1.0 / 24.0, 1.0 / 6.0);
   p = fma(p, r, 0.5);
   p = fma(p, r * r, r);  // expm1(r)
-  const int j = kk & 255;
-  const int q = kk >> 8;
+  const int j = kk & ((1 << kTableBits) - 1);
+  const int q = kk >> kTableBits;
   const double th = __ldg(&kExpThi[j]);
   const double tl = __ldg(&kExpTlo[j]);
   const double res = th + fma(th, p, tl);
@@ -57,16 +57,14 @@ __device__ __forceinline__ bool log_dd_fast(double x, double &sh, double &lo) {
   if (top - 1u >= 2046u) return false;  // x <= 0, zero, subnormal, inf or nan
   const int k = (int)top - 1023;
   const double m = __longlong_as_double((xb & 0x000FFFFFFFFFFFFFLL) | 0x3FF0000000000000LL);
-  const int i = (int)((xb >> 44) & 0xFF);
+  const int i = (int)((xb >> (52 - kTableBits)) & ((1 << kTableBits) - 1));
   const double F = __ldg(&kLogF[i]);
   const double gh = __ldg(&kLogGhi[i]);
   const double gl = __ldg(&kLogGlo[i]);
   const double p = m * F;
   const double pe = fma(m, F, -p);
   const double rh = p - 1.0;
-  double q = fma(rh, 1.0 / 7.0, -1.0 / 6.0);
-  q = fma(q, rh, 0.2);
-  q = fma(q, rh, -0.25);
+  double q = fma(rh, 0.2, -0.25);
   q = fma(q, rh, 1.0 / 3.0);
   q = fma(q, rh, -0.5);
   const double t = (rh * rh) * q;
@@ -122,7 +120,7 @@ __device__ __forceinline__ double pow_fast(double x, double y) {
   }
   const int k = (int)top - 1023;
   const double m = __longlong_as_double((xb & 0x000FFFFFFFFFFFFFLL) | 0x3FF0000000000000LL);
-  const int i = (int)((xb >> 44) & 0xFF);
+  const int i = (int)((xb >> (52 - kTableBits)) & ((1 << kTableBits) - 1));
   const double F = __ldg(&kLogF[i]);
   const double gh = __ldg(&kLogGhi[i]);
   const double gl = __ldg(&kLogGlo[i]);
@@ -130,10 +128,8 @@ __device__ __forceinline__ double pow_fast(double x, double y) {
   const double p = m * F;
   const double pe = fma(m, F, -p);
   const double rh = p - 1.0;
-  // log1p(rh) - rh = rh^2 (-1/2 + rh (1/3 + rh (-1/4 + rh (1/5 + rh (-1/6 + rh/7)))))
-  double q = fma(rh, 1.0 / 7.0, -1.0 / 6.0);
-  q = fma(q, rh, 0.2);
-  q = fma(q, rh, -0.25);
+  // log1p(rh) - rh = rh^2 (-1/2 + rh (1/3 + rh (-1/4 + rh/5)))
+  double q = fma(rh, 0.2, -0.25);
   q = fma(q, rh, 1.0 / 3.0);
   q = fma(q, rh, -0.5);
   const double t = (rh * rh) * q;
@@ -186,8 +182,8 @@ __device__ __forceinline__ float ex2_approx(float x) {
 //     below 2^-60;
 //   exp(delta ln x) = 1 + v, v = u + u^2/2 + u^3/6, u = delta ln x,
 //     |u| < 2^-17 over the range below (the next term is below 2^-72); ln x
-//     from the 256-entry log table (|r| <= 2^-9) and log1p(r) to r^3,
-//     absolute error below 4e-12, which moves u by less than 2^-62;
+//     from the 1024-entry log table (|r| <= 2^-11) and log1p(r) to r^3,
+//     absolute error below 2e-14, which moves u by less than 2^-69;
 //   x r0 = ph + pl exactly, and everything else goes into one correction
 //     term: x^p = ph + (pl + ph w), w = (1 + c)(1 + v) - 1.
 //
@@ -219,7 +215,7 @@ __device__ __forceinline__ double pow_manning(double x, double p, double delta) 
   const double c = e * fma(e, 2.0 / 9.0, 1.0 / 3.0);
   // ln x = k ln 2 + G_i + log1p(r), r = m F_i - 1
   const double m = __longlong_as_double((xb & 0x000FFFFFFFFFFFFFLL) | 0x3FF0000000000000LL);
-  const int i = (int)((xb >> 44) & 0xFF);
+  const int i = (int)((xb >> (52 - kTableBits)) & ((1 << kTableBits) - 1));
   const double r = fma(m, __ldg(&kLogF[i]), -1.0);
   const double lp = fma(fma(r, 1.0 / 3.0, -0.5), r * r, r);
   const double lnx = fma((double)k, kLn2Hi, __ldg(&kLogGhi[i])) + lp;
