@@ -53,25 +53,6 @@ namespace pihm {
 // evaluated on the integer pipe instead of the FP64 pipe.
 __device__ __forceinline__ double clamp0(double v) { return cmp::ge0(v) ? v : 0.0; }
 
-// SurfH, src/hydrol.c:100-134
-__device__ __forceinline__ double surf_h(double surfeqv) {
-  if (cmp::lt0(surfeqv)) return 0.0;
-  if (cmp::le_c(surfeqv, 0.5 * kDeprStg)) return sqrt(2.0 * kDeprStg * surfeqv);
-  return kDeprStg + (surfeqv - 0.5 * kDeprStg);
-}
-
-// EffKh with k1 = kmach*areafv + ksath*(1-areafv) and depth-dmac precomputed
-// (the reference evaluates both inline with the same operations)
-__device__ __forceinline__ double eff_kh_pre(double k1, double ksath, double depth, double dmac,
-                                             double d_dmac, double gw) {
-  gw = cmp::gt0(gw) ? gw : 0.0;
-  if (cmp::gt_v(gw, d_dmac)) {
-    const double d1 = cmp::gt_v(gw, depth) ? dmac : gw - d_dmac;
-    return (k1 * d1 + ksath * d_dmac) / (d1 + d_dmac);
-  }
-  return ksath;
-}
-
 // AvgH, src/lat_flow.c:217-237
 __device__ __forceinline__ double avg_h_sub(double diff, double hsub, double hnabr) {
   if (cmp::gt0(diff)) return cmp::gt0(hsub) ? hsub : 0.0;
@@ -156,18 +137,89 @@ __device__ __forceinline__ void report_err(const DevMesh &m, int sy) {
   atomicOr(m.err_sys ? &m.err_sys[sy] : m.err, 1u);
 }
 
+// Slot of the calling thread in a block's shared-memory work queue when take
+// is true (one shared atomic per warp); every thread of the warp calls it.
+// Queued work is evaluated densely after a barrier, so a few lanes that need
+// an expensive branch do not hold a whole warp on the FP64 pipe.
+__device__ __forceinline__ int queue_slot(int *count, bool take) {
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned mask = __ballot_sync(0xffffffffu, take);
+  int base = 0;
+  if (lane == 0 && mask) base = atomicAdd(count, __popc(mask));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  return base + __popc(mask & ((1u << lane) - 1u));
+}
+
 // ---------------------------------------------------------------------------
-// k_elem_prep
+// k_elem_prep.  Thin surface films (SurfH's square root, about half the
+// elements) and water tables inside the macropore zone (EffKh's division,
+// about a third) are spread over every warp, so both are queued and
+// evaluated densely.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_elem_prep(DevMesh m, const double *RESTRICT y) {
+constexpr int kPrepBlock = 256;
+
+__global__ void __launch_bounds__(kPrepBlock) k_elem_prep(DevMesh m, const double *RESTRICT y) {
+  __shared__ int qs_i[kPrepBlock], qd_i[kPrepBlock];
+  __shared__ double qs_x[kPrepBlock], qd_num[kPrepBlock], qd_den[kPrepBlock];
+  __shared__ int qs_n, qd_n;
+  if (threadIdx.x == 0) {
+    qs_n = 0;
+    qd_n = 0;
+  }
+  __syncthreads();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   int sy;
-  if (i >= m.ne_run || skip_item(m, m.sys_elem, i, &sy)) return;
-  const double surfh = surf_h(clamp0(y[i]));
-  const double gw = clamp0(y[2 * m.ne + i]);
-  m.surfh[i] = surfh;
-  m.head[i] = surfh + m.zmax[i];
-  m.effk[i] = eff_kh_pre(m.kh_k1[i], m.ksath[i], m.depth[i], m.dmac[i], m.d_dmac[i], gw);
+  bool thin = false, mix = false;
+  double sx = 0.0, num = 0.0, den = 0.0;
+  if (i < m.ne_run && !skip_item(m, m.sys_elem, i, &sy)) {
+    // SurfH, src/hydrol.c:100-134
+    const double surfeqv = clamp0(y[i]);
+    if (cmp::lt0(surfeqv)) {
+      m.surfh[i] = 0.0;
+      m.head[i] = 0.0 + m.zmax[i];
+    } else if (cmp::le_c(surfeqv, 0.5 * kDeprStg)) {
+      thin = true;
+      sx = 2.0 * kDeprStg * surfeqv;
+    } else {
+      const double sh = kDeprStg + (surfeqv - 0.5 * kDeprStg);
+      m.surfh[i] = sh;
+      m.head[i] = sh + m.zmax[i];
+    }
+    // EffKh, src/lat_flow.c:248-277, with k1 = kmach*areafv + ksath*(1-areafv)
+    // and depth - dmac formed at load (the reference evaluates both inline
+    // with the same operations)
+    double gw = clamp0(y[2 * m.ne + i]);
+    gw = cmp::gt0(gw) ? gw : 0.0;
+    const double d_dmac = m.d_dmac[i];
+    if (cmp::gt_v(gw, d_dmac)) {
+      const double d1 = cmp::gt_v(gw, m.depth[i]) ? m.dmac[i] : gw - d_dmac;
+      num = m.kh_k1[i] * d1 + m.ksath[i] * d_dmac;
+      den = d1 + d_dmac;
+      mix = true;
+    } else {
+      m.effk[i] = m.ksath[i];
+    }
+  }
+  const int ss = queue_slot(&qs_n, thin);
+  if (thin) {
+    qs_i[ss] = i;
+    qs_x[ss] = sx;
+  }
+  const int sd = queue_slot(&qd_n, mix);
+  if (mix) {
+    qd_i[sd] = i;
+    qd_num[sd] = num;
+    qd_den[sd] = den;
+  }
+  __syncthreads();
+  const int t = threadIdx.x;
+  if (t < qs_n) {
+    const int e = qs_i[t];
+    const double sh = sqrt(qs_x[t]);
+    m.surfh[e] = sh;
+    m.head[e] = sh + m.zmax[e];
+  }
+  if (t < qd_n) m.effk[qd_i[t]] = qd_num[t] / qd_den[t];
 }
 
 // ---------------------------------------------------------------------------
@@ -259,14 +311,8 @@ __global__ void __launch_bounds__(kEdgeBlock) k_edge(DevMesh m, const double *RE
     wet = cmp::gt0(avg_h);
     if (!wet) m.eflux_ovl[e] = 0.0;
   }
-  // queue the wet edges: one shared atomic per warp
-  const unsigned lane = threadIdx.x & 31u;
-  const unsigned mask = __ballot_sync(0xffffffffu, wet);
-  int base = 0;
-  if (lane == 0 && mask) base = atomicAdd(&q_n, __popc(mask));
-  base = __shfl_sync(0xffffffffu, base, 0);
+  const int slot = queue_slot(&q_n, wet);
   if (wet) {
-    const int slot = base + __popc(mask & ((1u << lane) - 1u));
     q_e[slot] = e;
     q_h[slot] = avg_h;
     q_d[slot] = diff_h;
@@ -908,7 +954,7 @@ cudaError_t launch_rhs(const DevMesh &m, const double *y, double *ydot, cudaStre
   const bool fork = side && side->side && !prof && m.ne_run > 0 && m.nr_run > 0;
   if (m.ne_run > 0) {
     on = prof_begin(prof, K_PREP, st);
-    k_elem_prep<<<blocks_for(m.ne_run, 256), 256, 0, st>>>(m, y);
+    k_elem_prep<<<blocks_for(m.ne_run, kPrepBlock), kPrepBlock, 0, st>>>(m, y);
     prof_end(prof, on, st);
     ++*launches;
     if (fork) {
