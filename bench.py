@@ -500,23 +500,33 @@ def main():
         rc = lib.pihm_gpu_rhs_host(g.h, 0.0, ctypes.cast(y_host[k].data_ptr(), f64p),
                                    ctypes.cast(yd_host[k].data_ptr(), f64p))
         assert rc == 0, rc
-    for k in range(2):
-        e2e_one(k)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    barrier()
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for k in range(e2e_evals):
-        e2e_one(k % STATES_PER_STEP)
-    e1.record(stream)
-    e1.synchronize()
-    e2e_ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = world * NELEM * e2e_evals / (e2e_ms * 1e-3)
+    def time_e2e(mode):
+        # mode 0: the library default (direct host access where possible),
+        # 1: copies through device staging
+        g.set_host_path(mode)
+        for k in range(2):
+            e2e_one(k)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for k in range(e2e_evals):
+            e2e_one(k % STATES_PER_STEP)
+        e1.record(stream)
+        e1.synchronize()
+        ms_ = e0.elapsed_time(e1)
+        if world > 1:
+            t = torch.tensor([ms_], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms_ = float(t.item())
+        return world * NELEM * e2e_evals / (ms_ * 1e-3)
+    e2e_copy_value = time_e2e(1)
+    e2e_value = time_e2e(0)
+    direct, pageable = g.host_path_info()
+    host_path = ("direct: the reordering kernels read y from and write ydot to pinned host memory"
+                 if direct else "copy through device staging") + (
+                 "; the device can access pageable host memory" if pageable else "")
     bytes_state = ws.neq * 8
 
     # ---- roofline of one right-hand-side evaluation ----
@@ -579,7 +589,8 @@ def main():
                          "alg_bytes_per_eval": alg_bytes, "ms_per_eval": ms_per_eval},
             "kernels": kernels, "dominant_kernel": dominant,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": bytes_state * STATES_PER_STEP,
-                    "d2h_bytes_per_step": bytes_state * STATES_PER_STEP, "evals": e2e_evals},
+                    "d2h_bytes_per_step": bytes_state * STATES_PER_STEP, "evals": e2e_evals,
+                    "host_path": host_path, "copy_path_value": e2e_copy_value},
             "gpu_launches": launches,
             "clocks": clk.summary(),
             "cpu_baseline": cpu,

@@ -165,11 +165,22 @@ int pihm_gpu_rhs(pihm_gpu_ctx *ctx, double t, const double *y_dev,
  * 0 or PIHM_GPU_ERR_NAN / PIHM_GPU_ERR_CUDA. */
 int pihm_gpu_status(pihm_gpu_ctx *ctx);
 
-/* Same evaluation from host arrays in reference order: copy y in, run, copy
- * ydot out, synchronise.  This is the call a CPU-side integrator makes in
- * place of the serial ODE() (src/ode.c:4-399). */
+/* Same evaluation from host arrays in reference order: y in, run, ydot out,
+ * synchronise.  This is the call a CPU-side integrator makes in place of the
+ * serial ODE() (src/ode.c:4-399).  When the device can address both arrays
+ * (pinned or registered host memory, or any host memory on a device with
+ * pageable-memory access, as Grace-based GB300 systems over NVLink-C2C), the
+ * reordering kernels read y from and write ydot to host memory directly;
+ * otherwise the arrays are copied through device staging.  Both paths give
+ * the same bits. */
 int pihm_gpu_rhs_host(pihm_gpu_ctx *ctx, double t, const double *y_host,
                       double *ydot_host);
+/* pihm_gpu_rhs_host's path: mode 0 (default) reads and writes host arrays
+ * directly where the device can address them, 1 always copies. */
+int pihm_gpu_set_host_path(pihm_gpu_ctx *ctx, int mode);
+/* Whether the last pihm_gpu_rhs_host call accessed host memory directly, and
+ * whether the device can access pageable host memory (either may be NULL). */
+int pihm_gpu_host_path_info(const pihm_gpu_ctx *ctx, int *last_direct, int *pageable_access);
 
 /* pihm_gpu_ode on device vectors synchronises after each evaluation to read
  * the NaN error word (the reference checks every call).  deferred = 1 skips

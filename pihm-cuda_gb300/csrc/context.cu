@@ -15,11 +15,35 @@
 namespace pihm {
 cudaError_t launch_permute(const double *src, double *dst, const int32_t *perm, int ne, int nr,
                            int to_internal, cudaStream_t st);
+cudaError_t launch_permute_ref(const double *src, double *dst, const int32_t *iperm, int ne, int nr,
+                               int to_internal, cudaStream_t st);
 }  // namespace pihm
 
 using namespace pihm;
 
 namespace {
+
+// An address through which kernels may read or write the host range
+// [p, p + bytes), or nullptr: any host address on a device with
+// pageable-memory access, else pinned or registered memory, whose first and
+// last bytes must map to one contiguous device range.
+const void *host_view(const pihm_gpu_ctx *c, const void *p, size_t bytes) {
+  if (c->host_pageable) return p;
+  cudaPointerAttributes a{}, b{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+  const char *last = (const char *)p + bytes - 1;
+  if (cudaPointerGetAttributes(&b, last) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (b.type != cudaMemoryTypeHost || !b.devicePointer) return nullptr;
+  if ((const char *)b.devicePointer - (const char *)a.devicePointer != (ptrdiff_t)(bytes - 1)) return nullptr;
+  return a.devicePointer;
+}
 
 template <class T>
 T *carve(char *&p, size_t n) {
@@ -59,6 +83,16 @@ int pihm_gpu_create(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double 
   c->nan_check_deferred = 0;
   c->prof = nullptr;
   c->d_noah = nullptr;
+  c->host_path = 0;
+  c->last_direct = 0;
+  {
+    int dev = 0, pageable = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess)
+      c->host_pageable = pageable;
+    else
+      c->host_pageable = 0;
+  }
   c->h_perm = (int32_t *)std::malloc(sizeof(int32_t) * ne);
   c->h_iperm = (int32_t *)std::malloc(sizeof(int32_t) * ne);
   std::memcpy(c->h_perm, im.perm.data(), sizeof(int32_t) * ne);
@@ -75,7 +109,7 @@ int pihm_gpu_create(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double 
   sbytes += carve_size<int32_t>(NE) + carve_size<int32_t>(NB); // bank_slot, bank_elem
   sbytes += 5 * carve_size<int32_t>(NR) + RP_COUNT * carve_size<double>(NR);
   sbytes += carve_size<int32_t>(NR + 1) + carve_size<int32_t>(NUP);
-  sbytes += carve_size<int32_t>(NE);                           // perm
+  sbytes += 2 * carve_size<int32_t>(NE);                       // perm, iperm
   std::vector<char> host(sbytes, 0);
   char *hp = host.data();
   if (cudaMalloc(&c->d_static, sbytes) != cudaSuccess) {
@@ -121,6 +155,7 @@ int pihm_gpu_create(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double 
   m.up_ptr = put(im.up_ptr.data(), nr + 1, NR + 1);
   m.up_idx = put(im.up_idx.data(), im.up_idx.size(), NUP);
   c->d_perm = put(im.perm.data(), NE, NE);
+  c->d_iperm = put(im.iperm.data(), NE, NE);
   if (cudaMemcpy(c->d_static, host.data(), sbytes, cudaMemcpyHostToDevice) != cudaSuccess) {
     pihm_gpu_destroy(c);
     return PIHM_GPU_ERR_CUDA;
@@ -367,6 +402,26 @@ int pihm_gpu_status(pihm_gpu_ctx *c) {
 int pihm_gpu_rhs_host(pihm_gpu_ctx *c, double t, const double *y_host, double *ydot_host) {
   if (!c || !y_host || !ydot_host) return PIHM_GPU_ERR_ARG;
   const size_t bytes = sizeof(double) * c->neq;
+  // direct: the reordering kernels read y from and write ydot to host memory
+  // over the host link, in reference order (contiguous on the host side)
+  const double *y_dev = c->host_path == 0 ? (const double *)host_view(c, y_host, bytes) : nullptr;
+  double *yd_dev = y_dev ? (double *)host_view(c, ydot_host, bytes) : nullptr;
+  c->last_direct = yd_dev != nullptr;
+  if (yd_dev) {
+    double *y_int = c->d_stage_out, *ydot_int = c->d_stage_in;
+    cudaError_t e = launch_permute_ref(y_dev, y_int, c->d_iperm, c->ne, c->nr, 1, c->stream);
+    c->launches++;
+    if (e == cudaSuccess) {
+      c->m.diag = c->diag;
+      e = launch_rhs(c->m, y_int, ydot_int, c->stream, &c->launches, c->prof, &c->side);
+    }
+    if (e == cudaSuccess) {
+      e = launch_permute_ref(ydot_int, yd_dev, c->d_iperm, c->ne, c->nr, 0, c->stream);
+      c->launches++;
+    }
+    if (e != cudaSuccess) return PIHM_GPU_ERR_CUDA;
+    return pihm_gpu_status(c);
+  }
   cudaError_t e = cudaMemcpyAsync(c->d_stage_in, y_host, bytes, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) {
     e = launch_permute(c->d_stage_in, c->d_stage_out, c->d_perm, c->ne, c->nr, 1, c->stream);
@@ -385,6 +440,19 @@ int pihm_gpu_rhs_host(pihm_gpu_ctx *c, double t, const double *y_host, double *y
     e = cudaMemcpyAsync(ydot_host, c->d_stage_out, bytes, cudaMemcpyDeviceToHost, c->stream);
   if (e != cudaSuccess) return PIHM_GPU_ERR_CUDA;
   return pihm_gpu_status(c);
+}
+
+int pihm_gpu_set_host_path(pihm_gpu_ctx *c, int mode) {
+  if (!c || (mode != 0 && mode != 1)) return PIHM_GPU_ERR_ARG;
+  c->host_path = mode;
+  return PIHM_GPU_OK;
+}
+
+int pihm_gpu_host_path_info(const pihm_gpu_ctx *c, int *last_direct, int *pageable_access) {
+  if (!c) return PIHM_GPU_ERR_ARG;
+  if (last_direct) *last_direct = c->last_direct;
+  if (pageable_access) *pageable_access = c->host_pageable;
+  return PIHM_GPU_OK;
 }
 
 int pihm_gpu_set_diagnostics(pihm_gpu_ctx *c, int on) {

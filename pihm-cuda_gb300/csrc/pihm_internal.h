@@ -181,6 +181,10 @@ struct pihm_gpu_ctx {
   size_t dyn_bytes;
   double *d_stage_in, *d_stage_out;   // host-path staging [neq]
   int32_t *d_perm;                    // internal -> reference element index
+  int32_t *d_iperm;                   // reference -> internal element index
+  int host_pageable;                  // the device can access pageable host memory
+  int host_path;                      // 0 direct where possible, 1 always copy
+  int last_direct;                    // the last rhs_host accessed host memory directly
   int32_t *h_perm, *h_iperm;          // host copies (perm, inverse)
   int diag;
   int nan_check_deferred;  // 1: pihm_gpu_ode does not synchronise to read the error word

@@ -905,6 +905,25 @@ __global__ void k_permute(const double *RESTRICT src, double *RESTRICT dst, cons
   }
 }
 
+// The same reordering walked in reference order (iperm: reference ->
+// internal element index): the reference-order side is read or written
+// contiguously, which is the side in host memory when the host-buffer
+// evaluation accesses it directly.
+__global__ void k_permute_ref(const double *RESTRICT src, double *RESTRICT dst,
+                              const int32_t *RESTRICT iperm, int ne, int nr, int to_internal) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long n_el = 3LL * ne;
+  if (t < n_el) {
+    const int blk = (int)(t / ne);
+    const int r = (int)(t - (long long)blk * ne);
+    const long long in = (long long)blk * ne + iperm[r];
+    if (to_internal) dst[in] = src[t];
+    else dst[t] = src[in];
+  } else if (t < n_el + 2LL * nr) {
+    dst[t] = src[t];
+  }
+}
+
 }  // namespace pihm
 
 // ---------------------------------------------------------------------------
@@ -1005,6 +1024,14 @@ cudaError_t launch_permute(const double *src, double *dst, const int32_t *perm, 
   const long long n = 3LL * ne + 2LL * nr;
   if (n == 0) return cudaSuccess;
   k_permute<<<blocks_for(n, 256), 256, 0, st>>>(src, dst, perm, ne, nr, to_internal);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_permute_ref(const double *src, double *dst, const int32_t *iperm, int ne, int nr,
+                               int to_internal, cudaStream_t st) {
+  const long long n = 3LL * ne + 2LL * nr;
+  if (n == 0) return cudaSuccess;
+  k_permute_ref<<<blocks_for(n, 256), 256, 0, st>>>(src, dst, iperm, ne, nr, to_internal);
   return cudaGetLastError();
 }
 

@@ -59,6 +59,8 @@ def load() -> ctypes.CDLL:
         "pihm_gpu_status": ([_VP], ctypes.c_int),
         "pihm_gpu_rhs_host": ([_VP, ctypes.c_double, _F64P, _F64P], ctypes.c_int),
         "pihm_gpu_set_diagnostics": ([_VP, ctypes.c_int], ctypes.c_int),
+        "pihm_gpu_set_host_path": ([_VP, ctypes.c_int], ctypes.c_int),
+        "pihm_gpu_host_path_info": ([_VP, _I32P, _I32P], ctypes.c_int),
         "pihm_gpu_get_fluxes": ([_VP] + [_F64P] * 6, ctypes.c_int),
         "pihm_gpu_to_internal": ([_VP, _VP, _VP], ctypes.c_int),
         "pihm_gpu_to_reference": ([_VP, _VP, _VP], ctypes.c_int),
@@ -158,8 +160,25 @@ class GpuRhs:
     def set_diagnostics(self, on: bool):
         _check("pihm_gpu_set_diagnostics", self.lib.pihm_gpu_set_diagnostics(self.h, int(on)))
 
+    def set_host_path(self, mode: int):
+        """0: rhs_host reads and writes host arrays directly where the device
+        can address them; 1: it always copies through device staging."""
+        _check("pihm_gpu_set_host_path", self.lib.pihm_gpu_set_host_path(self.h, int(mode)))
+
+    def host_path_info(self):
+        """(the last rhs_host accessed host memory directly, the device can
+        access pageable host memory)."""
+        d, p = ctypes.c_int32(), ctypes.c_int32()
+        _check("pihm_gpu_host_path_info",
+               self.lib.pihm_gpu_host_path_info(self.h, ctypes.byref(d), ctypes.byref(p)))
+        return bool(d.value), bool(p.value)
+
+    def rhs_host_ptr(self, y_ptr: int, ydot_ptr: int, t: float = 0.0) -> int:
+        """pihm_gpu_rhs_host on raw host addresses (reference order)."""
+        return self.lib.pihm_gpu_rhs_host(self.h, t, ctypes.cast(y_ptr, _F64P), ctypes.cast(ydot_ptr, _F64P))
+
     def rhs_host(self, y, t: float = 0.0):
-        """Host arrays in reference order (copy in, evaluate, copy out)."""
+        """Host arrays in reference order (in, evaluate, out; synchronous)."""
         y = _c(y)
         out = np.empty_like(y)
         rc = self.lib.pihm_gpu_rhs_host(self.h, t, f64p(y), f64p(out))

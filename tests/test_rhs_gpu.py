@@ -171,3 +171,35 @@ def test_flux_pihm_noah_reference_goldens():
             scale = row_scales(ws, o.fluxes(), z[f"{tag}_pcpdrp"], z[f"{tag}_edir"], z[f"{tag}_ett"])
             ok, worst, idx = compare(got, z[f"{tag}_call{c}_ydot"], scale)
             assert ok, f"{tag} call {c}: worst {worst:.3e} at {idx}"
+
+
+def test_host_path_direct_equals_copy():
+    """pihm_gpu_rhs_host on pinned host buffers: the reordering kernels read y
+    from and write ydot to host memory directly, and the result is the copy
+    path's bit for bit and meets the oracle.  Pageable arrays take the direct
+    path only on a device with pageable-memory access, with the same bits."""
+    import torch
+    ws = W.generate(1000, 100, seed=4)
+    ws, sc = scenario(ws, 4)
+    o, g = _pair(ws)
+    y = torch.from_numpy(sc["y"]).pin_memory()
+    out = {}
+    for mode in (0, 1):
+        apply(g, sc)  # the same carried river-edge flux before each call
+        res = torch.empty_like(y).pin_memory()
+        g.set_host_path(mode)
+        assert g.rhs_host_ptr(y.data_ptr(), res.data_ptr()) == 0
+        direct, pageable = g.host_path_info()
+        assert direct == (mode == 0)  # pinned buffers are always addressable
+        out[mode] = res.numpy().copy()
+    assert np.array_equal(out[0], out[1])
+    apply(o, sc)
+    want, rc = o.rhs(sc["y"])
+    assert rc == 0
+    ok, worst, idx = compare(out[0], want, row_scales(ws, o.fluxes(), sc["pcpdrp"], sc["edir"], sc["ett"]))
+    assert ok, (worst, idx)
+    apply(g, sc)
+    g.set_host_path(0)
+    got, rc = g.rhs_host(sc["y"])  # pageable numpy arrays
+    assert rc == 0 and g.host_path_info()[0] == pageable
+    assert np.array_equal(got, out[1])
