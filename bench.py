@@ -540,6 +540,25 @@ def main():
             traffic = json.load(open(tp)).get("dram_bytes_per_eval")
         except Exception:
             traffic = None
+    # The FP64 pipe, not HBM, bounds these kernels: GB300 retires 2 FP64
+    # lanes per clock per SM, so one warp-wide FP64 instruction holds it for
+    # 16 cycles.  The per-evaluation FP64 instruction counts come from an ncu
+    # capture (profiles/rhs_fp64.json); the time and clock are this run's.
+    fp64 = None
+    fp = os.path.join(ROOT, "profiles", "rhs_fp64.json")
+    if os.path.exists(fp) and NELEM == 1_000_000 and NRIVER == 30_000:
+        try:
+            cnt = json.load(open(fp))
+            sm_mhz = clk.summary().get("sm_mhz") or 2070.0
+            peak_slots = torch.cuda.get_device_properties(dev).multi_processor_count * 2 * sm_mhz * 1e6
+            slots = cnt["fp64_warp_instr_per_eval"] * 32 / (ms_per_eval * 1e-3)
+            lanes = cnt["fp64_lane_ops_per_eval"] / (ms_per_eval * 1e-3)
+            fp64 = {"achieved": slots / 1e9, "peak": peak_slots / 1e9, "unit": "G FP64 lane slots/s",
+                    "frac": slots / peak_slots, "useful_frac": lanes / peak_slots,
+                    "sm_mhz": sm_mhz, "counts": "profiles/rhs_fp64.json",
+                    "note": "frac: FP64 pipe busy over the evaluation; useful_frac: predicated-on lanes only"}
+        except Exception as exc:
+            fp64 = {"error": repr(exc)}
 
     # ---- CPU baseline (rank 0, N = 1 only) ----
     cpu = None
@@ -586,7 +605,8 @@ def main():
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "peak_kind": peak_kind, "scope": "one RHS evaluation (all its kernels)",
-                         "alg_bytes_per_eval": alg_bytes, "ms_per_eval": ms_per_eval},
+                         "alg_bytes_per_eval": alg_bytes, "ms_per_eval": ms_per_eval,
+                         "limit": "FP64 pipe (see fp64_pipe), not HBM", "fp64_pipe": fp64},
             "kernels": kernels, "dominant_kernel": dominant,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": bytes_state * STATES_PER_STEP,
                     "d2h_bytes_per_step": bytes_state * STATES_PER_STEP, "evals": e2e_evals,
