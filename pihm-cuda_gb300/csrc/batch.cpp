@@ -137,49 +137,78 @@ int h2d(T *dst, const T *src, size_t n, cudaStream_t st) {
   return cudaMemcpyAsync(dst, src, sizeof(T) * n, cudaMemcpyHostToDevice, st) == cudaSuccess ? 0 : -1;
 }
 
+// A watershed's uploads: on a device that can access pageable host memory,
+// descriptors for one gather kernel that reads the host arrays directly
+// (one launch instead of about a hundred staged copies); else staged copies.
+// Either way every source must stay valid until flush() has synchronised.
+struct Uploader {
+  bool direct;
+  cudaStream_t st;
+  std::vector<CopyDesc> desc;
+  uint64_t max_bytes = 0;
+  int rc = 0;
+  template <class T>
+  void operator()(T *dst, const T *src, size_t n) {
+    if (n == 0) return;
+    if (direct) {
+      desc.push_back({(const void *)src, (void *)dst, (uint64_t)(sizeof(T) * n)});
+      max_bytes = std::max<uint64_t>(max_bytes, sizeof(T) * n);
+    } else {
+      rc |= h2d(dst, src, n, st);
+    }
+  }
+  int flush() {
+    if (direct && !desc.empty() && launch_gather_host(desc.data(), (int)desc.size(), max_bytes, st) != cudaSuccess)
+      rc = -1;
+    if (cudaStreamSynchronize(st) != cudaSuccess) rc = -1;
+    return rc;
+  }
+};
+
 // Translate a watershed image's indices to its arena ranges and upload it.
 int place(pihm_batch *B, Sys *s, const Prepared &job) {
   const SystemImage &im = job.im;
   DevMesh &m = B->A.m;
   cudaStream_t st = B->st;
+  Uploader up{B->host_pageable != 0, st, {}};
   const int ne = im.ne, nr = im.nr;
   const int64_t NE = B->ne_cap, NR = B->nr_cap;
   const int64_t eo = s->eoff, ro = s->roff, edo = s->edoff, bo = s->boff, uo = s->upoff;
   int rc = 0;
-  for (int k = 0; k < EP_COUNT; k++) rc |= h2d((double *)(m.*kElemMember[k]) + eo, im.el[k].data(), ne, st);
+  for (int k = 0; k < EP_COUNT; k++) up((double *)(m.*kElemMember[k]) + eo, im.el[k].data(), ne);
   for (int k = 0; k < XP_COUNT; k++)
     for (int j = 0; j < 3; j++)
-      rc |= h2d((double *)(m.*kEdgeMember[k]) + j * NE + eo, im.ed[k].data() + (size_t)j * ne, ne, st);
+      up((double *)(m.*kEdgeMember[k]) + j * NE + eo, im.ed[k].data() + (size_t)j * ne, ne);
   std::vector<int32_t> t(3 * (size_t)ne);
   for (size_t q = 0; q < t.size(); q++) {
     const int32_t v = im.nb[q];
     t[q] = v >= 0 ? (int32_t)(v + eo) : (v == kBoundary ? v : (int32_t)(-1 - ((-1 - v) + ro)));
   }
-  for (int j = 0; j < 3; j++) rc |= h2d((int32_t *)m.nb + j * NE + eo, t.data() + (size_t)j * ne, ne, st);
+  for (int j = 0; j < 3; j++) up((int32_t *)m.nb + j * NE + eo, t.data() + (size_t)j * ne, ne);
   std::vector<int32_t> t2(3 * (size_t)ne);
   for (size_t q = 0; q < t2.size(); q++) {
     const int32_t v = im.emap[q];
     t2[q] = v > 0 ? (int32_t)(v + edo) : (v < 0 ? (int32_t)(v - edo) : 0);
   }
   for (int j = 0; j < 3; j++) {
-    rc |= h2d((int32_t *)m.emap + j * NE + eo, t2.data() + (size_t)j * ne, ne, st);
-    rc |= h2d((int32_t *)m.bctype + j * NE + eo, im.bct.data() + (size_t)j * ne, ne, st);
+    up((int32_t *)m.emap + j * NE + eo, t2.data() + (size_t)j * ne, ne);
+    up((int32_t *)m.bctype + j * NE + eo, im.bct.data() + (size_t)j * ne, ne);
   }
   std::vector<int32_t> ei(im.nedge), ek(im.nedge);
   for (int e = 0; e < im.nedge; e++) {
     ei[e] = (int32_t)(im.e_i[e] + eo);
     ek[e] = (int32_t)(im.e_k[e] + eo);
   }
-  rc |= h2d((int32_t *)m.e_i + edo, ei.data(), im.nedge, st);
-  rc |= h2d((int32_t *)m.e_k + edo, ek.data(), im.nedge, st);
-  rc |= h2d((double *)m.e_invdist + edo, im.e_invdist.data(), im.nedge, st);
-  rc |= h2d((double *)m.e_subk + edo, im.e_subk.data(), im.nedge, st);
-  rc |= h2d((double *)m.e_ovlk + edo, im.e_ovlk.data(), im.nedge, st);
+  up((int32_t *)m.e_i + edo, ei.data(), im.nedge);
+  up((int32_t *)m.e_k + edo, ek.data(), im.nedge);
+  up((double *)m.e_invdist + edo, im.e_invdist.data(), im.nedge);
+  up((double *)m.e_subk + edo, im.e_subk.data(), im.nedge);
+  up((double *)m.e_ovlk + edo, im.e_ovlk.data(), im.nedge);
   std::vector<int32_t> bs(ne), be(im.nbank);
   for (int i = 0; i < ne; i++) bs[i] = im.bank_slot[i] >= 0 ? (int32_t)(im.bank_slot[i] + bo) : -1;
   for (int b = 0; b < im.nbank; b++) be[b] = (int32_t)(im.bank_elem[b] + eo);
-  rc |= h2d((int32_t *)m.bank_slot + eo, bs.data(), ne, st);
-  rc |= h2d((int32_t *)m.bank_elem + bo, be.data(), im.nbank, st);
+  up((int32_t *)m.bank_slot + eo, bs.data(), ne);
+  up((int32_t *)m.bank_elem + bo, be.data(), im.nbank);
   std::vector<int32_t> dn(nr), lf(nr), rt(nr), ub(nr), ue(nr), ui(im.up_idx.size());
   for (int r = 0; r < nr; r++) {
     dn[r] = im.down[r] > 0 ? (int32_t)(im.down[r] + ro) : im.down[r];
@@ -189,24 +218,24 @@ int place(pihm_batch *B, Sys *s, const Prepared &job) {
     ue[r] = (int32_t)(im.up_ptr[r + 1] + uo);
   }
   for (size_t q = 0; q < ui.size(); q++) ui[q] = (int32_t)(im.up_idx[q] + ro);
-  rc |= h2d((int32_t *)m.down + ro, dn.data(), nr, st);
-  rc |= h2d((int32_t *)m.left + ro, lf.data(), nr, st);
-  rc |= h2d((int32_t *)m.right + ro, rt.data(), nr, st);
-  rc |= h2d((int32_t *)m.intrpl_ord + ro, im.ord.data(), nr, st);
-  rc |= h2d((int32_t *)m.bctype_riv + ro, im.rbct.data(), nr, st);
-  rc |= h2d((int32_t *)m.up_ptr + ro, ub.data(), nr, st);
-  rc |= h2d((int32_t *)m.up_end + ro, ue.data(), nr, st);
-  rc |= h2d((int32_t *)m.up_idx + uo, ui.data(), ui.size(), st);
-  for (int k = 0; k < RP_COUNT; k++) rc |= h2d((double *)(m.*kRiverMember[k]) + ro, im.rv[k].data(), nr, st);
+  up((int32_t *)m.down + ro, dn.data(), nr);
+  up((int32_t *)m.left + ro, lf.data(), nr);
+  up((int32_t *)m.right + ro, rt.data(), nr);
+  up((int32_t *)m.intrpl_ord + ro, im.ord.data(), nr);
+  up((int32_t *)m.bctype_riv + ro, im.rbct.data(), nr);
+  up((int32_t *)m.up_ptr + ro, ub.data(), nr);
+  up((int32_t *)m.up_end + ro, ue.data(), nr);
+  up((int32_t *)m.up_idx + uo, ui.data(), ui.size());
+  for (int k = 0; k < RP_COUNT; k++) up((double *)(m.*kRiverMember[k]) + ro, im.rv[k].data(), nr);
   // boundary conditions (reference order in the job)
   std::vector<double> bc(3 * (size_t)ne, 0.0);
   if (!job.elem_bc.empty())
     for (int j = 0; j < 3; j++)
       for (int i = 0; i < ne; i++) bc[(size_t)j * ne + i] = job.elem_bc[3 * (size_t)im.perm[i] + j];
-  for (int j = 0; j < 3; j++) rc |= h2d((double *)m.elem_bc + j * NE + eo, bc.data() + (size_t)j * ne, ne, st);
+  for (int j = 0; j < 3; j++) up((double *)m.elem_bc + j * NE + eo, bc.data() + (size_t)j * ne, ne);
   std::vector<double> rbc(nr, 0.0);
   if (!job.river_bc.empty()) std::copy(job.river_bc.begin(), job.river_bc.end(), rbc.begin());
-  rc |= h2d((double *)m.river_bc + ro, rbc.data(), nr, st);
+  up((double *)m.river_bc + ro, rbc.data(), nr);
   // a fresh watershed carries no river-edge flux from an earlier evaluation
   for (int k = 0; k < NUM_RIVFLX; k++)
     if (nr && cudaMemsetAsync(m.rivflow + k * NR + ro, 0, sizeof(double) * nr, st) != cudaSuccess) rc = -1;
@@ -215,20 +244,20 @@ int place(pihm_batch *B, Sys *s, const Prepared &job) {
   // owner tables
   std::vector<int32_t> own(std::max<int64_t>({(int64_t)ne, (int64_t)nr, (int64_t)im.nedge, (int64_t)im.nbank, 1}),
                            s->slot);
-  rc |= h2d((int32_t *)m.sys_elem + eo, own.data(), ne, st);
-  rc |= h2d((int32_t *)m.sys_riv + ro, own.data(), nr, st);
-  rc |= h2d((int32_t *)m.sys_edge + edo, own.data(), im.nedge, st);
-  rc |= h2d((int32_t *)m.sys_bank + bo, own.data(), im.nbank, st);
+  up((int32_t *)m.sys_elem + eo, own.data(), ne);
+  up((int32_t *)m.sys_riv + ro, own.data(), nr);
+  up((int32_t *)m.sys_edge + edo, own.data(), im.nedge);
+  up((int32_t *)m.sys_bank + bo, own.data(), im.nbank);
   const double dt = job.ctrl.stepsize;
-  rc |= h2d((double *)m.sys_dt + s->slot, &dt, 1, st);
+  up((double *)m.sys_dt + s->slot, &dt, 1);
   const double inv_dt = 1.0 / dt;
-  rc |= h2d((double *)m.sys_inv_dt + s->slot, &inv_dt, 1, st);
+  up((double *)m.sys_inv_dt + s->slot, &inv_dt, 1);
   // initial state, internal order, into vector slot 0
   std::vector<double> y(s->neq);
   for (int p = 0; p < 3; p++)
     for (int i = 0; i < ne; i++) y[(size_t)p * ne + i] = job.y0[(size_t)p * ne + im.perm[i]];
   for (int64_t q = 3LL * ne; q < s->neq; q++) y[q] = job.y0[q];
-  rc |= h2d(B->A.vec + s->soff, y.data(), s->neq, st);
+  up(B->A.vec + s->soff, y.data(), s->neq);
   SysInfo info{};
   info.off = s->soff;
   info.neq = (int32_t)s->neq;
@@ -238,8 +267,8 @@ int place(pihm_batch *B, Sys *s, const Prepared &job) {
   info.roff = (int32_t)ro;
   info.nblk = (int32_t)pihm_nv::red_grid_for(s->neq);
   info.rec_off = s->recoff;
-  rc |= h2d(B->A.sysinfo + s->slot, &info, 1, st);
-  if (cudaStreamSynchronize(st) != cudaSuccess) rc = -1;
+  up(B->A.sysinfo + s->slot, &info, 1);
+  rc |= up.flush();
   return rc ? PIHM_GPU_ERR_CUDA : PIHM_GPU_OK;
 }
 
@@ -674,6 +703,12 @@ int pihm_batch_create(const pihm_batch_limits *lim, int surf_mode, int riv_mode,
            cudaDeviceSynchronize() == cudaSuccess;
   if (!z) return PIHM_GPU_ERR_CUDA;
   if (pihm::create_rhs_streams(&B->side) != cudaSuccess) return PIHM_GPU_ERR_CUDA;
+  {
+    int dev = 0, pageable = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess)
+      B->host_pageable = pageable;
+  }
   for (cudaEvent_t &e : B->tev)
     if (cudaEventCreate(&e) != cudaSuccess) return PIHM_GPU_ERR_CUDA;
   B->update_extents();

@@ -81,6 +81,20 @@ struct DeviceArena {
 constexpr int kProgramVariants = 3;
 cudaError_t launch_program(const DeviceArena &a, int nrs, int nblocks, int variant, cudaStream_t st);
 
+// One host-to-device copy of a watershed's upload: bytes from src (host
+// memory) to dst (arena).
+struct CopyDesc {
+  const void *src;
+  void *dst;
+  uint64_t bytes;
+};
+// Copies every descriptor with one kernel that reads the host memory
+// directly.  Only for a device that can access pageable host memory
+// (cudaDevAttrPageableMemoryAccess): desc and every src may be ordinary
+// host allocations, and they must stay valid until the stream has passed
+// the kernel.
+cudaError_t launch_gather_host(const CopyDesc *desc, int n, uint64_t max_bytes, cudaStream_t st);
+
 }  // namespace batch
 
 

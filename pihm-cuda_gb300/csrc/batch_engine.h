@@ -202,6 +202,7 @@ struct pihm_batch {
   int tune_n[pihm::batch::kProgramVariants] = {0};
   cudaEvent_t tev[2] = {nullptr, nullptr};
   pihm::RhsStreams side;  // river kernel beside the element kernels
+  int host_pageable = 0;  // the device can access pageable host memory (uploads by one gather kernel)
   // counters and timing (host: building rounds and running the coroutines;
   // wait: blocked on the device; program/rhs: device time, when profiling)
   long long rounds = 0, rhs_rounds = 0, launches = 0;

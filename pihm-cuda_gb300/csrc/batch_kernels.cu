@@ -223,6 +223,38 @@ __global__ void __launch_bounds__(kThreads, (kU == 1 ? 6 : (kU == 2 ? 5 : 3))) k
 
 static_assert(sizeof(Op) == 40 && sizeof(Op) % sizeof(double) == 0, "Op is staged as doubles");
 
+// blockIdx.y picks the descriptor, blockIdx.x a kGatherChunk-byte chunk of
+// it; 8-byte words where source, destination and size allow, else 4-byte
+// words, else bytes
+constexpr uint64_t kGatherChunk = 64 * 1024;
+
+__global__ void __launch_bounds__(256) k_gather_host(const CopyDesc *desc, int n) {
+  const CopyDesc d = desc[blockIdx.y];
+  const uint64_t lo = (uint64_t)blockIdx.x * kGatherChunk;
+  if (lo >= d.bytes) return;
+  const uint64_t hi = min(d.bytes, lo + kGatherChunk);
+  const uintptr_t align = (uintptr_t)d.src | (uintptr_t)d.dst | (uintptr_t)d.bytes;
+  const char *src = (const char *)d.src;
+  char *dst = (char *)d.dst;
+  if ((align & 7) == 0) {
+    for (uint64_t b = lo + 8 * (uint64_t)threadIdx.x; b < hi; b += 8 * (uint64_t)blockDim.x)
+      *(uint64_t *)(dst + b) = *(const uint64_t *)(src + b);
+  } else if ((align & 3) == 0) {
+    for (uint64_t b = lo + 4 * (uint64_t)threadIdx.x; b < hi; b += 4 * (uint64_t)blockDim.x)
+      *(uint32_t *)(dst + b) = *(const uint32_t *)(src + b);
+  } else {
+    for (uint64_t b = lo + threadIdx.x; b < hi; b += blockDim.x) dst[b] = src[b];
+  }
+}
+
+cudaError_t launch_gather_host(const CopyDesc *desc, int n, uint64_t max_bytes, cudaStream_t st) {
+  if (n <= 0 || max_bytes == 0) return cudaSuccess;
+  if (n > 65535) return cudaErrorInvalidValue;
+  const dim3 grid((unsigned)((max_bytes + kGatherChunk - 1) / kGatherChunk), (unsigned)n);
+  k_gather_host<<<grid, 256, 0, st>>>(desc, n);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_program(const DeviceArena &a, int nrs, int nblocks, int variant, cudaStream_t st) {
   if (nrs <= 0 || nblocks <= 0) return cudaSuccess;
   const size_t smem = sizeof(Op) * kMaxProgOps + sizeof(int32_t) * (size_t)nrs;
