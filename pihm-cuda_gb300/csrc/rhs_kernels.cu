@@ -72,6 +72,9 @@ __device__ __forceinline__ double overland_flow(double avg_h, double grad_h, dou
          (sqrt(avg_sf) * avg_rough);
 }
 
+// Below this 1 - satn^m, Psi follows the reference's operations (kr_psi).
+constexpr double kPsiNearSat = 1e-3;
+
 // KrFunc (src/soil.c:8-13) and Psi (src/vert_flow.c:272-278) of one
 // saturation in [SATMIN, 1], sharing one logarithm of satn:
 //   x1 = satn^m = exp(z), z = m ln satn (a double-double), a = 1 - x1,
@@ -80,8 +83,10 @@ __device__ __forceinline__ double overland_flow(double avg_h, double grad_h, dou
 //       = -exp(ib (ln a - z)) / alpha.
 // The last form takes ln a, which a^e needs anyway, in place of a division
 // and a third logarithm; the difference ln a - z is carried as a
-// double-double, so Psi stays within an ulp of the reference's form (the
-// same cancellation in a as satn -> 1, exactly 0 at satn = 1).
+// double-double, so Psi stays within an ulp of the reference's form while
+// 1 - satn^m >= kPsiNearSat.  Closer to saturation both forms cancel to a
+// few ulps of 1, each with its own rounding, and Psi takes the reference's
+// form pow(pow(1/satn, m) - 1, ib); exactly 0 at satn = 1.
 // sq returns sqrt(satn), which EffKinf's macropore branch needs too.
 __device__ __forceinline__ void kr_psi(double satn, double vm, double vg_e, double vg_ib, double inv_alpha,
                                        double &satkfunc, double &psi, double &sq) {
@@ -116,6 +121,10 @@ __device__ __forceinline__ void kr_psi(double satn, double vm, double vg_e, doub
   if (a0) {
     pe = pow_fast(a, vg_e);
     p = pow_fast(a, vg_ib);
+  } else if (cmp::lt_c(a, kPsiNearSat)) {
+    // near saturation (1/satn)^m - 1 is a few ulps of 1, so its value is set
+    // by the rounding of the reference's own operations: take them
+    p = pow_fast(pow_fast(1.0 / satn, vm) - 1.0, vg_ib);
   }
   const double t = 1.0 - pe;
   satkfunc = sq * t * t;

@@ -79,6 +79,11 @@ class Watershed:
     seed: int = 0
     x: np.ndarray | None = None   # element centroids (not read by the RHS)
     y: np.ndarray | None = None
+    # the node mesh a generated watershed was built from (what an input deck
+    # stores, pihm_gpu.deck.write_deck): node x, y, zmin, zmax, the element
+    # node ids `tri` [nelem, 3] and the segment end nodes `from_n`, `to_n`,
+    # all 0-based
+    nodes: dict | None = None
 
     @property
     def neq(self) -> int:
@@ -241,12 +246,14 @@ def _drainage(z, px, py, interior, outlet, u, v, start):
 # ----------------------------------------------------------------------------
 
 def _river_eq_wid(order, depth, coeff):
-    """RiverEqWid, src/init_river.c:99-124."""
+    """RiverEqWid, src/init_river.c:99-124, with the C library's pow as the
+    reference calls it (numpy's vectorised power can differ from it in the
+    last bit, and differently on different processors)."""
     depth = np.maximum(depth, 0.0)
     out = np.where(order == RECTANGLE, coeff, 0.0)
-    m = order != RECTANGLE
-    e = 1.0 / (order[m].astype(np.float64) - 1.0)
-    out[m] = 2.0 * np.power(depth[m] + RIVDPTHMIN, e) / np.power(coeff[m], e)
+    for k in np.nonzero(order != RECTANGLE)[0]:
+        e = 1.0 / (float(order[k]) - 1.0)
+        out[k] = 2.0 * math.pow(float(depth[k]) + RIVDPTHMIN, e) / math.pow(float(coeff[k]), e)
     return out
 
 
@@ -495,7 +502,9 @@ def generate(nelem: int = 1000, nriver: int = 100, seed: int = 0,
         "riv_ksath": f64(rksath), "riv_ksatv": f64(rksatv),
         "riv_bedthick": f64(rbed), "riv_porosity": f64(rpor),
     }
-    return Watershed(ne, nr, arrays, seed=seed, x=cx, y=cy)
+    nodes = {"x": px, "y": py, "zmin": zmin_n, "zmax": zmax_n, "tri": tri,
+             "from_n": np.asarray(from_n), "to_n": np.asarray(to_n)}
+    return Watershed(ne, nr, arrays, seed=seed, x=cx, y=cy, nodes=nodes)
 
 
 # ----------------------------------------------------------------------------
