@@ -16,7 +16,7 @@ def _declared():
         src = open(h).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
         src = re.sub(r"//[^\n]*", "", src)
-        for m in re.finditer(r"\b(pihm_(?:gpu|bdf|batch|serve|ic)_\w+|N_V\w+_PihmGpu)\s*\(", src):
+        for m in re.finditer(r"\b(pihm_(?:gpu|bdf|batch|serve|ic|deck)_\w+|N_V\w+_PihmGpu)\s*\(", src):
             names.add(m.group(1))
     return names
 
@@ -25,6 +25,7 @@ def test_header_declares_entry_points():
     names = _declared()
     assert "pihm_gpu_create" in names and "pihm_gpu_rhs" in names
     assert {"pihm_bdf_solve", "pihm_batch_add", "pihm_batch_step", "pihm_serve_run"} <= names
+    assert {"pihm_deck_read", "pihm_deck_mesh", "pihm_deck_bc", "pihm_deck_free"} <= names
 
 
 def test_library_exports_declared_symbols():

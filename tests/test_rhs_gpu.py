@@ -203,3 +203,40 @@ def test_host_path_direct_equals_copy():
     got, rc = g.rhs_host(sc["y"])  # pageable numpy arrays
     assert rc == 0 and g.host_path_info()[0] == pageable
     assert np.array_equal(got, out[1])
+
+
+def test_deck_mesh_straight_to_gpu(tmp_path):
+    """A deck read by the library, its pihm_gpu_mesh handed straight to
+    pihm_gpu_create as a C caller does, evaluated at the deck's initial
+    state: the oracle's result on the same arrays, within the parity bar."""
+    import ctypes
+    from oracle import Oracle
+    from pihm_gpu import capi, deck
+    from pihm_gpu.meshdesc import MeshDesc, f64p
+    d = tmp_path / "input" / "gen"
+    deck.write_deck(W.generate(1000, 100, seed=9), str(d), "gen")
+    dk = deck.Deck.read(str(d), "gen")
+    ws = dk.watershed()
+    y0 = dk.initial_state()
+    pcpdrp, edir, ett = W.random_forcing(ws, 9)
+    ws0 = np.ascontiguousarray(y0[:ws.nelem])
+    lib = capi.load()
+    m = MeshDesc()
+    assert dk.lib.pihm_deck_mesh(dk.h, ctypes.byref(m)) == 0
+    h = ctypes.c_void_p()
+    assert lib.pihm_gpu_create(ctypes.byref(m), ws.surf_mode, ws.riv_mode, ws.stepsize, capi.ORDER_RCM,
+                               ctypes.byref(h)) == 0
+    try:
+        assert lib.pihm_gpu_set_forcing(h, f64p(pcpdrp), f64p(edir), f64p(ett)) == 0
+        assert lib.pihm_gpu_set_ws0_surf(h, f64p(ws0)) == 0
+        got = np.empty_like(y0)
+        assert lib.pihm_gpu_rhs_host(h, 0.0, f64p(y0), f64p(got)) == 0
+    finally:
+        lib.pihm_gpu_destroy(h)
+    o = Oracle(ws)
+    o.set_forcing(pcpdrp, edir, ett)
+    o.set_ws0_surf(ws0)
+    want, rc = o.rhs(y0)
+    assert rc == 0
+    ok, worst, idx = compare(got, want, row_scales(ws, o.fluxes(), pcpdrp, edir, ett))
+    assert ok, (worst, idx)
