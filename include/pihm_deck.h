@@ -2,15 +2,15 @@
  * the host, so that the same watershed on disk feeds this library, the
  * reference and its CPU restatement.
  *
- * A deck is <dir>/<proj>.{riv,mesh,att,soil,para,bc} with <dir>/<project>.calib
- * (and <dir>/<project>.ic for a hot start), where <proj> is <project> up to
- * its first '.', plus the land-cover table (the reference reads
+ * A deck is <dir>/<proj>.{riv,mesh,att,soil,para,meteo,bc} (and .lai when
+ * an element names an LAI series) with <dir>/<project>.calib (and
+ * <dir>/<project>.ic for a hot start), where <proj> is <project> up to its
+ * first '.', plus the land-cover table (the reference reads
  * input/vegprmt.tbl).  Reading follows ReadAlloc (src/read_alloc.c:3-162:
- * ReadRiver, ReadMesh, ReadAtt, ReadSoil, ReadLc, ReadPara, ReadCalib,
- * ReadBc; the meteorological and LAI files are forcing, not read here) and
- * initialisation follows Initialize (src/initialize.c:9-222: InitMesh,
- * InitTopo, InitSoil, InitLc, InitRiver, CorrElev when asked, InitSurfL,
- * then RelaxIc or ReadIc).  Unlike the reference, a malformed deck returns
+ * ReadRiver, ReadMesh, ReadAtt, ReadSoil, ReadLc, ReadForc, ReadLai,
+ * ReadPara, ReadCalib, ReadBc) and initialisation follows Initialize
+ * (src/initialize.c:9-222: InitMesh, InitTopo, InitSoil, InitLc, InitForc,
+ * InitRiver, CorrElev when asked, InitSurfL, then RelaxIc or ReadIc).  Unlike the reference, a malformed deck returns
  * an error code with a message instead of exiting the process.
  *
  * Host only; nothing here touches the GPU. */
@@ -21,6 +21,7 @@
 
 #include "pihm_batch.h"
 #include "pihm_gpu.h"
+#include "pihm_land.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -63,6 +64,15 @@ int pihm_deck_control_get(const pihm_deck *deck, pihm_deck_control *ctrl);
 /* Initial state [3*nelem + 2*nriver] in reference order: RelaxIc
  * (src/initialize.c:496-575) or the .ic restart file (src/read_ic.c:3-39). */
 int pihm_deck_initial_state(const pihm_deck *deck, double *y0);
+
+/* The land-surface model of the deck for pihm_gpu_land_init: the element
+ * parameters InitSoil, InitLc and InitForc leave (src/init_soil.c:34-54 with
+ * FieldCapacity and WiltingPoint of the soil table, src/soil.c:16-81;
+ * src/init_lc.c:19-38; the station's wind height, src/init_forc.c:81-85)
+ * and the .meteo and .lai series (src/read_forc.c, src/read_lai.c) with the
+ * calibration's climate scenario applied.  The pointers stay valid until
+ * pihm_deck_free. */
+int pihm_deck_land(const pihm_deck *deck, pihm_land_params *params, pihm_forcing_series *series);
 
 /* Boundary values at time t (seconds since 1970-01-01 UTC) as ApplyBc sets
  * them (src/forcing.c:24-249): elem_bc [3*nelem] (element-major, edge j of

@@ -204,10 +204,11 @@ int pihm_gpu_set_noah(pihm_gpu_ctx *ctx, const double *et, int nlayers, const in
                       const double *smcmax, const double *fcr);
 /* The watershed water balance of a model step of dt seconds, from the state
  * y_dev (device, internal order) and the current forcing and river fluxes:
- * out[0] sources (prcp area dt), out[1] sinks ((edir + ett) area dt plus the
- * outlet segments' discharge dt), out[2] storage (surface, pore water and
- * river water volume), the three sums of PrintWaterBal (src/print.c:337-542)
- * with no canopy or snow stores.  The reference's cumulative error is the
+ * out[0] sources (prcp area dt), out[1] sinks ((edir + ett + ec) area dt
+ * plus the outlet segments' discharge dt), out[2] storage (canopy, snow,
+ * surface, pore water and river water volume), the three sums of
+ * PrintWaterBal (src/print.c:337-542).  Without the land-surface model
+ * (include/pihm_land.h) prcp is pcpdrp and there is no canopy or snow.  The reference's cumulative error is the
  * running sum of out[0] - out[1] - (out[2] - previous out[2]).  Synchronous. */
 int pihm_gpu_water_balance(pihm_gpu_ctx *ctx, const double *y_dev, double dt, double *out);
 

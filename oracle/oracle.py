@@ -2,6 +2,8 @@
 
 `Oracle`    -- the C restatement of the reference right-hand side
                (oracle/pihm_oracle.c), serial or OpenMP build.
+`OracleLand`-- the C restatement of the land-surface step (ApplyForc +
+               IntcpSnowEt, oracle/land_oracle.c).
 `Reference` -- the reference's own serial/OpenMP code compiled from its
                sources (oracle/ref_harness.c + oracle/Makefile target `ref`);
                present only where the reference sources were available at
@@ -151,6 +153,10 @@ class Reference:
                                              _F64P, ctypes.c_int]
             lib.ref_apply_forcing.argtypes = [ctypes.c_int]
             lib.ref_model_times.argtypes = [ctypes.POINTER(ctypes.c_int)] * 4
+            lib.ref_land_step.argtypes = [ctypes.c_int, ctypes.c_double]
+            lib.ref_land_set_state.argtypes = [_F64P] * 4
+            lib.ref_monthly.argtypes = [ctypes.c_int, ctypes.c_int, _F64P]
+            lib.ref_monthly.restype = None
         self.lib = lib
         self.ne = self.nr = 0
 
@@ -205,6 +211,22 @@ class Reference:
     def set_noah(self, noah: dict):
         _set_noah(self.lib.ref_set_noah, noah)
 
+    # land-surface step of a loaded deck (ApplyForc + IntcpSnowEt)
+    def land_set_state(self, unsat=None, gw=None, cmc=None, sneqv=None):
+        keep = [_c(a) for a in (unsat, gw, cmc, sneqv)]
+        assert self.lib.ref_land_set_state(*(f64p(a) for a in keep)) == 0
+
+    def land_step(self, t: int, stepsize: float):
+        assert self.lib.ref_land_step(int(t), float(stepsize)) == 0
+
+    def land_fields(self) -> dict:
+        return {k: self.export(k, self.ne) for k in ("prcp", "pcpdrp", "edir", "ett", "ec", "drip", "cmc", "sneqv")}
+
+    def monthly(self, t: int, lc: int) -> np.ndarray:
+        out = np.zeros(3)
+        self.lib.ref_monthly(int(t), int(lc), f64p(out))
+        return out
+
     def fluxes(self):
         ne, nr = self.ne, self.nr
         out = dict(ovlflow=np.zeros(3 * ne), subsurf=np.zeros(3 * ne),
@@ -212,6 +234,57 @@ class Reference:
                    et_split=np.zeros(5 * ne), rivflow=np.zeros(11 * nr))
         self.lib.ref_get_fluxes(*(f64p(out[k]) for k in (
             "ovlflow", "subsurf", "infil", "rechg", "et_split", "rivflow")))
+        return out
+
+
+class OracleLand:
+    """The land-surface restatement (oracle/land_oracle.c) for a land.Land
+    and the watershed's zmax, depth, porosity, rzd."""
+
+    FIELDS = ("prcp", "pcpdrp", "edir", "ett", "ec", "drip", "cmc", "sneqv")
+
+    def __init__(self, land, ws, omp: bool = False):
+        from pihm_gpu import land as L
+        name = "liboracle_omp.so" if omp else "liboracle.so"
+        lib = _lib(os.path.join(HERE, "_build", name))
+        lib.oracle_land_create.restype = ctypes.c_void_p
+        lib.oracle_land_create.argtypes = [ctypes.POINTER(L.LandParamsC), ctypes.POINTER(L.ForcingSeriesC)] + \
+            [_F64P] * 4
+        lib.oracle_land_destroy.argtypes = [ctypes.c_void_p]
+        lib.oracle_land_set_state.argtypes = [ctypes.c_void_p, _F64P, _F64P]
+        lib.oracle_land_step.argtypes = [ctypes.c_void_p, ctypes.c_longlong, ctypes.c_double, _F64P, _F64P]
+        lib.oracle_land_step.restype = ctypes.c_int
+        lib.oracle_land_get.argtypes = [ctypes.c_void_p, ctypes.c_int, _F64P]
+        lib.oracle_land_monthly.argtypes = [ctypes.c_longlong, ctypes.c_int, _F64P]
+        self.lib, self.ne = lib, land.nelem
+        p, s = land.structs()
+        mesh = [_c(ws.arrays[k]) for k in ("zmax", "depth", "porosity", "rzd")]
+        self.h = lib.oracle_land_create(ctypes.byref(p), ctypes.byref(s), *(f64p(a) for a in mesh))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.oracle_land_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def set_state(self, cmc=None, sneqv=None):
+        self.lib.oracle_land_set_state(self.h, f64p(_c(cmc)), f64p(_c(sneqv)))
+
+    def step(self, t: int, stepsize: float, unsat, gw) -> int:
+        return self.lib.oracle_land_step(self.h, int(t), float(stepsize), f64p(_c(unsat)), f64p(_c(gw)))
+
+    def get(self, field: str) -> np.ndarray:
+        out = np.zeros(self.ne)
+        self.lib.oracle_land_get(self.h, self.FIELDS.index(field), f64p(out))
+        return out
+
+    def fields(self) -> dict:
+        return {k: self.get(k) for k in self.FIELDS}
+
+    def monthly(self, t: int, lc: int) -> np.ndarray:
+        out = np.zeros(3)
+        self.lib.oracle_land_monthly(int(t), int(lc), f64p(out))
         return out
 
 

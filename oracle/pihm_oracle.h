@@ -15,6 +15,7 @@
 #define PIHM_ORACLE_H
 
 #include "pihm_gpu.h"
+#include "pihm_land.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -47,6 +48,20 @@ void oracle_get_fluxes(const oracle_model *m, double *ovlflow, double *subsurf,
 void oracle_post_step(oracle_model *m, const double *y);
 /* CVRhsFn over SUNDIALS serial N_Vectors, user_data = oracle_model. */
 int oracle_cvrhs(double t, void *y, void *ydot, void *user_data);
+/* Land-surface step (land_oracle.c): ApplyForc + IntcpSnowEt of the
+ * non-Noah model, elements in reference order.  zmax, depth, porosity, rzd
+ * are the mesh's planes. */
+typedef struct oracle_land oracle_land;
+oracle_land *oracle_land_create(const pihm_land_params *p, const pihm_forcing_series *s, const double *zmax,
+                                const double *depth, const double *porosity, const double *rzd);
+void oracle_land_destroy(oracle_land *l);
+void oracle_land_set_state(oracle_land *l, const double *cmc, const double *sneqv);
+/* one step at time t (seconds since 1970 UTC) over stepsize seconds with the
+ * soil state unsat, gw [nelem]; 0, or -1 when t lies outside a series */
+int oracle_land_step(oracle_land *l, long long t, double stepsize, const double *unsat, const double *gw);
+void oracle_land_get(const oracle_land *l, int field, double *out);
+void oracle_land_monthly(long long t, int lc, double *out3);
+
 /* Number of OpenMP threads the oracle runs with (1 without OpenMP). */
 int oracle_num_threads(void);
 void oracle_set_num_threads(int n);

@@ -244,6 +244,16 @@ int ref_export_double(const char *name, double *out)
     EF("ws0_surf", ws0.surf) EF3("bc", bc.head)
     EF3("ovlflow", wf.ovlflow) EF3("subsurf", wf.subsurf)
     EF("infil", wf.infil) EF("rechg", wf.rechg)
+    /* land-surface model: parameters Initialize leaves and the step's
+       state and fluxes (src/init_soil.c, src/init_lc.c, src/init_forc.c,
+       src/is_sm_et.c) */
+    EF("cmc", ws.cmc) EF("sneqv", ws.sneqv) EF("prcp", wf.prcp) EF("ec", wf.ec)
+    EF("drip", wf.drip) EF("albedomin", lc.albedomin) EF("albedomax", lc.albedomax)
+    EF("shdfac", lc.shdfac) EF("cmcfactr", lc.cmcfactr) EF("cfactr", lc.cfactr)
+    EF("rgl", epc.rgl) EF("rsmin", epc.rsmin) EF("rsmax", epc.rsmax) EF("topt", epc.topt)
+    EF("smcmin", soil.smcmin) EF("smcwlt", soil.smcwlt) EF("smcref", soil.smcref)
+    EF("zlvl_wind", ps.zlvl_wind) EF("sfctmp", es.sfctmp) EF("proj_lai", ps.proj_lai)
+    EF("unsat", ws.unsat) EF("gw", ws.gw) EF("surf", ws.surf)
     RF("riv_area", topo.area) RF("riv_zmin", topo.zmin)
     RF("riv_zmax", topo.zmax) RF("riv_zbed", topo.zbed)
     RF("riv_node_zmax", topo.node_zmax) RF("riv_dist_left", topo.dist_left)
@@ -266,6 +276,13 @@ int ref_export_int(const char *name, int *out)
     if (strcmp(name, "nabr") == 0) {
         for (i = 0; i < nelem; i++)
             for (j = 0; j < NUM_EDGE; j++) out[3 * i + j] = g_pihm->elem[i].nabr[j];
+        return 0;
+    }
+    if (strcmp(name, "lc_type") == 0 || strcmp(name, "meteo_type") == 0 || strcmp(name, "lai_type") == 0) {
+        for (i = 0; i < nelem; i++)
+            out[i] = name[1] == 'c' ? g_pihm->elem[i].attrib.lc_type
+                     : name[1] == 'e' ? g_pihm->elem[i].attrib.meteo_type
+                                      : g_pihm->elem[i].attrib.lai_type;
         return 0;
     }
     if (strcmp(name, "bc_type") == 0) {
@@ -403,6 +420,39 @@ int ref_apply_forcing(int t)
     ApplyForc(&g_pihm->forc, g_pihm->elem, t);
     IntcpSnowEt(t, (realtype)g_pihm->ctrl.etstep, g_pihm->elem, &g_pihm->cal);
     return 0;
+}
+
+/* The land-surface part of that step alone: ApplyForc and IntcpSnowEt
+ * (src/pihm.c:30-66) at time t over `stepsize` seconds. */
+int ref_land_step(int t, double stepsize)
+{
+    if (!g_pihm || !g_have_tables) return -1;
+    ApplyForc(&g_pihm->forc, g_pihm->elem, t);
+    IntcpSnowEt(t, (realtype)stepsize, g_pihm->elem, &g_pihm->cal);
+    return 0;
+}
+
+/* Set the element state the land-surface step reads and carries (ws.unsat,
+ * ws.gw, ws.cmc, ws.sneqv); a null array leaves that field. */
+int ref_land_set_state(const double *unsat, const double *gw, const double *cmc, const double *sneqv)
+{
+    int i;
+    if (!g_pihm) return -1;
+    for (i = 0; i < nelem; i++) {
+        if (unsat) g_pihm->elem[i].ws.unsat = unsat[i];
+        if (gw) g_pihm->elem[i].ws.gw = gw[i];
+        if (cmc) g_pihm->elem[i].ws.cmc = cmc[i];
+        if (sneqv) g_pihm->elem[i].ws.sneqv = sneqv[i];
+    }
+    return 0;
+}
+
+/* MonthlyLai, MonthlyRl, MonthlyMf (src/forcing.c:532-798) at t for type lc */
+void ref_monthly(int t, int lc, double *out3)
+{
+    out3[0] = MonthlyLai(t, lc);
+    out3[1] = MonthlyRl(t, lc);
+    out3[2] = MonthlyMf(t);
 }
 
 int ref_model_times(int *starttime, int *endtime, int *etstep, int *nstep)

@@ -83,6 +83,7 @@ int pihm_gpu_create(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double 
   c->nan_check_deferred = 0;
   c->prof = nullptr;
   c->d_noah = nullptr;
+  c->d_land = nullptr;
   c->host_path = 0;
   c->last_direct = 0;
   {
@@ -230,6 +231,7 @@ void pihm_gpu_destroy(pihm_gpu_ctx *c) {
   if (c->d_static) cudaFree(c->d_static);
   if (c->d_dyn) cudaFree(c->d_dyn);
   if (c->d_noah) cudaFree(c->d_noah);
+  if (c->d_land) cudaFree(c->d_land);
   if (c->side.fork) cudaEventDestroy(c->side.fork);
   if (c->side.join) cudaEventDestroy(c->side.join);
   if (c->side.side) cudaStreamDestroy(c->side.side);

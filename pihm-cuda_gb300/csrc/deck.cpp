@@ -10,6 +10,8 @@
 // same order (the reference's pow(x, 2) is x * x; the C library's pow is
 // called where the reference calls it), so a deck gives the reference's
 // values bit for bit.
+#include <algorithm>
+#include <array>
 #include <cctype>
 #include <cmath>
 #include <cstdarg>
@@ -21,6 +23,7 @@
 #include <vector>
 
 #include "pihm_deck.h"
+#include "pihm_land.h"
 
 namespace {
 
@@ -29,6 +32,7 @@ thread_local std::string g_error;
 constexpr int kEdges = 3;
 constexpr double kRivDpthMin = 0.05;  // RIVDPTHMIN, src/include/pihm_const.h:78
 constexpr double kSatMin = 0.1;
+constexpr double kCmcFactr = 2E-4;    // CMCFACTR, canopy water capacity per LAI (m), src/include/pihm_const.h:80
 enum { kRectangle = 1, kTriangle = 2, kQuadratic = 3, kCubic = 4 };
 
 struct DeckError {
@@ -154,35 +158,45 @@ int64_t keyword_time(LineFile &f, const char *key) {
   return t;
 }
 
-// A time series: knots and values (tsdata_struct with one variable).
+// A time series: knots and nvar values per knot (tsdata_struct).
 struct Series {
+  int nvar = 1;
   std::vector<int64_t> t;
-  std::vector<double> v;
+  std::vector<double> v;  // [knot][nvar]
 };
 
 // Read the data lines of a series block until a line whose first token is
 // one of the stop words, or the end of the file; returns that line (or "").
-std::string read_series(LineFile &f, Series *s, const std::vector<const char *> &stop) {
+// A data line is a time stamp and nvar numbers (ReadTS, src/read_func.c:3-37).
+std::string read_series(LineFile &f, Series *s, const std::vector<const char *> &stop, int nvar = 1) {
   std::string line;
+  s->nvar = nvar;
   while (f.next(line)) {
     const std::string tok = first_token(line);
     for (const char *w : stop)
       if (same_word(tok, w)) return line;
     char t1[256], t2[256];
-    double v;
-    int n = 0;
-    if (std::sscanf(line.c_str(), "%255s %255s %lf%n", t1, t2, &v, &n) != 3) f.bad("expected YYYY-MM-DD hh:mm value");
+    int used = 0;
+    if (std::sscanf(line.c_str(), "%255s %255s%n", t1, t2, &used) != 2) f.bad("expected YYYY-MM-DD hh:mm values");
+    const char *p = line.c_str() + used;
+    for (int k = 0; k < nvar; k++) {
+      double v;
+      int n = 0;
+      if (std::sscanf(p, "%lf%n", &v, &n) != 1) f.bad("expected YYYY-MM-DD hh:mm values");
+      s->v.push_back(v);
+      p += n;
+    }
     bool ok;
     const int64_t t = parse_time(t1, t2, &ok);
     if (!ok) f.bad("bad time stamp");
     s->t.push_back(t);
-    s->v.push_back(v);
   }
   return "";
 }
 
 // IntrplForc (src/forcing.c:482-531): the reference's bisection for the
-// interval that holds t, then linear interpolation between its knots.
+// interval that holds t, then linear interpolation between its knots, for
+// every variable of the series.
 bool interpolate(const Series &s, int64_t t, double *out) {
   const int64_t n = (int64_t)s.t.size();
   if (n < 2 || t < s.t[0] || t > s.t[n - 1]) return false;
@@ -190,8 +204,10 @@ bool interpolate(const Series &s, int64_t t, double *out) {
   while (first <= last) {
     const int64_t middle = (first + last) / 2;
     if (t >= s.t[middle - 1] && t <= s.t[middle]) {
-      *out = ((double)(s.t[middle] - t) * s.v[middle - 1] + (double)(t - s.t[middle - 1]) * s.v[middle]) /
-             (double)(s.t[middle] - s.t[middle - 1]);
+      const double *a = &s.v[(size_t)(middle - 1) * s.nvar], *b = &s.v[(size_t)middle * s.nvar];
+      for (int k = 0; k < s.nvar; k++)
+        out[k] = ((double)(s.t[middle] - t) * a[k] + (double)(t - s.t[middle - 1]) * b[k]) /
+                 (double)(s.t[middle] - s.t[middle - 1]);
       return true;
     }
     if (s.t[middle] > t)
@@ -238,6 +254,41 @@ double ptf_beta(double silt, double clay, double om, double bd, int top) {
                         0.02264 * bd * clay + 0.0896 * bd * om + 0.00718 * ts * clay);
 }
 
+// KrFunc (src/soil.c:8-13): the Mualem-van Genuchten relative conductivity
+double kr_func(double beta, double satn) {
+  const double a = 1.0 - std::pow(1.0 - std::pow(satn, beta / (beta - 1.0)), (beta - 1.0) / beta);
+  return std::sqrt(satn) * a * a;
+}
+
+// FieldCapacity (src/soil.c:16-73): the moisture where the conductivity falls
+// to 5.79e-9 m s-1 (Chen and Dudhia 2001, with van Genuchten in place of
+// Campbell), found by at most 10 Newton steps on the saturation.
+double field_capacity(double beta, double kv, double smcmax, double smcmin) {
+  const double kfc = 5.79E-9, tol = 1.0E-3;
+  const double mx = 1.0 - 1.0 / beta;
+  double satn = 0.75, dsatn = 999.0;
+  for (int n = 0; n < 10 && dsatn > tol; n++) {
+    const double df = kr_func(beta, satn) - kfc / kv;
+    const double ftheta = 1.0 - std::pow(satn, 1.0 / mx);
+    const double denom = 0.5 * std::pow(satn, -0.5) * std::pow(1.0 - std::pow(ftheta, mx), 2.0) +
+                         2.0 * std::pow(satn, 1.0 / mx - 0.5) *
+                             (std::pow(ftheta, mx - 1.0) - std::pow(ftheta, 2.0 * mx - 1.0));
+    double satnk = satn - df / denom;
+    satnk = (satnk > 1.0 - 1.0E-3) ? 1.0 - 1.0E-3 : satnk;
+    satnk = (satnk < kSatMin) ? kSatMin : satnk;
+    dsatn = std::fabs(satnk - satn);
+    satn = satnk;
+  }
+  if (dsatn > tol) satn = 0.75;
+  return (1.0 / 3.0 + 2.0 / 3.0 * satn) * (smcmax - smcmin) + smcmin;
+}
+
+// WiltingPoint (src/soil.c:75-81): the moisture at a suction head of 200 m
+double wilting_point(double smcmax, double smcmin, double alpha, double beta) {
+  const double psiw = 200.0;
+  return 0.5 * (smcmax - smcmin) * std::pow(1.0 / (1.0 + std::pow(psiw * alpha, beta)), 1.0 - 1.0 / beta) + smcmin;
+}
+
 // RiverEqWid (src/init_river.c:98-124)
 double river_eq_width(int order, double depth, double coeff) {
   depth = (depth > 0.0) ? depth : 0.0;
@@ -263,6 +314,16 @@ struct pihm_deck {
   pihm_deck_control ctrl{};
   std::vector<double> y0;
   std::vector<Series> bc, riverbc;
+  // land-surface model (include/pihm_land.h): element parameters as
+  // InitSoil / InitLc / InitForc leave them, and the forcing series
+  std::vector<int32_t> lc_type, meteo_type, lai_type;
+  std::vector<double> albedomin, albedomax, shdfac, cmcfactr, cfactr, rgl, rsmin, rsmax, topt, smcmin, smcwlt,
+      smcref, zlvl_wind;
+  double cal_edir = 1.0, cal_ec = 1.0, cal_ett = 1.0;
+  std::vector<Series> meteo, lai;
+  std::vector<int32_t> meteo_len, lai_len;  // flattened for pihm_deck_land
+  std::vector<int64_t> meteo_time, lai_time;
+  std::vector<double> meteo_data, lai_data;
 };
 
 namespace {
@@ -475,16 +536,16 @@ void build(const std::string &dir, const std::string &project, const std::string
     }
 
   // ---- .att (src/read_att.c) ----
-  std::vector<int> att_soil(ne), att_lc(ne), att_bc(3 * (size_t)ne);
+  std::vector<int> att_soil(ne), att_lc(ne), att_meteo(ne), att_lai(ne), att_bc(3 * (size_t)ne);
   {
     LineFile f(base + ".att");
     f.need("header");
     for (int i = 0; i < ne; i++) {
       const std::string line = f.need("an attribute line");
-      int index, geol, meteo, lai, source;
+      int index, geol, source;
       int *b = &att_bc[3 * (size_t)i];
       if (std::sscanf(line.c_str(), "%d %d %d %d %d %d %d %d %d %d", &index, &att_soil[i], &geol, &att_lc[i],
-                      &meteo, &lai, &source, &b[0], &b[1], &b[2]) != 10)
+                      &att_meteo[i], &att_lai[i], &source, &b[0], &b[1], &b[2]) != 10)
         f.bad("bad attribute line");
     }
   }
@@ -492,6 +553,7 @@ void build(const std::string &dir, const std::string &project, const std::string
   // ---- .soil (src/read_soil.c) ----
   struct SoilRow {
     double silt, clay, om, bd, kinfv, ksatv, ksath, smcmax, smcmin, alpha, beta, areafh, areafv, dmac, qtz;
+    double smcref, smcwlt;  // FieldCapacity and WiltingPoint of the row (src/read_soil.c:118-122)
   };
   std::vector<SoilRow> soil;
   double s_dinf, s_kmacv_ro, s_kmach_ro;
@@ -518,6 +580,8 @@ void build(const std::string &dir, const std::string &project, const std::string
       if (r.smcmin < 0.0) r.smcmin = ptf_thetar(r.silt, r.clay);
       if (r.alpha < 0.0) r.alpha = ptf_alpha(r.silt, r.clay, r.om, r.bd, 0);
       if (r.beta < 0.0) r.beta = ptf_beta(r.silt, r.clay, r.om, r.bd, 0);
+      r.smcref = field_capacity(r.beta, r.ksatv, r.smcmax, r.smcmin);
+      r.smcwlt = wilting_point(r.smcmax, r.smcmin, r.alpha, r.beta);
     }
     s_dinf = keyword_double(f, "DINF");
     s_kmacv_ro = keyword_double(f, "KMACV_RO");
@@ -526,6 +590,10 @@ void build(const std::string &dir, const std::string &project, const std::string
 
   // ---- land-cover table (src/read_lc.c) ----
   std::vector<double> lc_rzd, lc_rough;
+  std::vector<std::array<double, 15>> lc_row;  // vegfrac rzd rsmin rgl hs snup laimin laimax emissmin emissmax
+                                               // albedomin albedomax z0min z0max rough
+  double lc_topt, lc_cfactr, lc_rsmax;
+  int lc_bare;
   {
     LineFile f(lc_path);
     const int n = keyword_int(f, "NUMLC");
@@ -541,12 +609,60 @@ void build(const std::string &dir, const std::string &project, const std::string
         f.bad("bad land-cover line");
       lc_rzd.push_back(v[1]);     // vegfrac, rzd, rsmin, ...
       lc_rough.push_back(v[14]);  // ..., z0max, rough
+      std::array<double, 15> row;
+      std::copy(v, v + 15, row.begin());
+      lc_row.push_back(row);
     }
-    keyword_double(f, "TOPT_DATA");
-    keyword_double(f, "CFACTR_DATA");
-    keyword_double(f, "RSMAX_DATA");
-    keyword_int(f, "BARE");
+    lc_topt = keyword_double(f, "TOPT_DATA");
+    lc_cfactr = keyword_double(f, "CFACTR_DATA");
+    lc_rsmax = keyword_double(f, "RSMAX_DATA");
+    lc_bare = keyword_int(f, "BARE");
     keyword_int(f, "NATURAL");
+  }
+
+  // ---- .meteo (src/read_forc.c): one block per station, "METEO_TS <k>
+  // WIND_LVL <m>", two header lines, then time-stamped records of the seven
+  // variables; .lai (src/read_lai.c), read when an element names an LAI series ----
+  std::vector<double> station_wind;
+  {
+    LineFile f(base + ".meteo");
+    std::string line;
+    bool have = f.next(line);
+    for (int k = 0; have; k++) {
+      int index;
+      double zlvl;
+      char tok[1024], tok2[1024];
+      if (std::sscanf(line.c_str(), "%1023s %d %1023s %lf", tok, &index, tok2, &zlvl) != 4 ||
+          !same_word(tok, "METEO_TS") || index != k + 1)
+        f.bad("expected METEO_TS <index> WIND_LVL <height>");
+      f.need("header");
+      f.need("header");
+      Series s;
+      line = read_series(f, &s, {"METEO_TS"}, PIHM_METEO_NVAR);
+      d->meteo.push_back(std::move(s));
+      station_wind.push_back(zlvl);
+      have = !line.empty();
+    }
+    if (d->meteo.empty()) f.bad("no METEO_TS block");
+  }
+  bool any_lai = false;
+  for (int v : att_lai) any_lai |= v > 0;
+  if (any_lai) {
+    LineFile f(base + ".lai");
+    std::string line;
+    bool have = f.next(line);
+    for (int k = 0; have; k++) {
+      int index;
+      char tok[1024];
+      if (std::sscanf(line.c_str(), "%1023s %d", tok, &index) != 2 || !same_word(tok, "LAI_TS") || index != k + 1)
+        f.bad("expected LAI_TS <index>");
+      f.need("header");
+      f.need("header");
+      Series s;
+      line = read_series(f, &s, {"LAI_TS"}, 1);
+      d->lai.push_back(std::move(s));
+      have = !line.empty();
+    }
   }
 
   read_para(base + ".para", &d->ctrl);
@@ -592,8 +708,13 @@ void build(const std::string &dir, const std::string &project, const std::string
   auto sized = [](std::vector<double> &v, size_t n) { v.assign(n, 0.0); };
   for (auto *v : {&d->area, &d->x, &d->y, &d->zmin, &d->zmax, &d->depth, &d->ksath, &d->ksatv, &d->kinfv,
                   &d->dinf, &d->alpha, &d->beta, &d->porosity, &d->dmac, &d->kmach, &d->kmacv, &d->areafv,
-                  &d->areafh, &d->rough, &d->rzd})
+                  &d->areafh, &d->rough, &d->rzd, &d->albedomin, &d->albedomax, &d->shdfac, &d->cmcfactr,
+                  &d->cfactr, &d->rgl, &d->rsmin, &d->rsmax, &d->topt, &d->smcmin, &d->smcwlt, &d->smcref,
+                  &d->zlvl_wind})
     sized(*v, ne);
+  d->lc_type.assign(ne, 0);
+  d->meteo_type.assign(ne, 0);
+  d->lai_type.assign(ne, 0);
   for (auto *v : {&d->edge, &d->nabrdist, &d->nabr_x, &d->nabr_y}) sized(*v, 3 * (size_t)ne);
   d->nabr.assign(nabr0.begin(), nabr0.end());
   d->bc_type.assign(att_bc.begin(), att_bc.end());
@@ -647,7 +768,50 @@ void build(const std::string &dir, const std::string &project, const std::string
     d->kmach[i] = cal.kmach * s_kmach_ro * r.ksath;
     d->rzd[i] = cal.rzd * lc_rzd[lt];
     d->rough[i] = cal.rough * lc_rough[lt];
+    // the land-surface model's soil and land-cover parameters
+    // (src/init_soil.c:34-54, src/init_lc.c:19-38 without the Noah factors)
+    d->smcmin[i] = smcmin;
+    d->smcwlt[i] = cal.porosity * r.smcwlt;
+    d->smcref[i] = cal.porosity * r.smcref;
+    const std::array<double, 15> &row = lc_row[lt];
+    d->rsmin[i] = row[2];
+    d->rgl[i] = row[3];
+    d->rsmax[i] = lc_rsmax;
+    d->topt[i] = lc_topt;
+    d->shdfac[i] = cal.vegfrac * row[0];
+    d->albedomin[i] = cal.albedo * row[10];
+    d->albedomax[i] = cal.albedo * row[11];
+    d->cmcfactr[i] = kCmcFactr;
+    d->cfactr[i] = lc_cfactr;
+    if (lc_bare == att_lc[i]) d->shdfac[i] = 0.0;
+    d->lc_type[i] = att_lc[i];
+    d->meteo_type[i] = att_meteo[i];
+    d->lai_type[i] = att_lai[i];
+    if (att_meteo[i] < 1 || att_meteo[i] > (int)d->meteo.size())
+      fail(PIHM_DECK_ERR_VALUE, "element %d: meteorological station %d is not in the .meteo file", i + 1, att_meteo[i]);
+    if (att_lai[i] < 0 || att_lai[i] > (int)d->lai.size())
+      fail(PIHM_DECK_ERR_VALUE, "element %d: LAI series %d is not in the .lai file", i + 1, att_lai[i]);
+    d->zlvl_wind[i] = station_wind[att_meteo[i] - 1];
   }
+  // InitForc's climate scenario (src/init_forc.c:8-17)
+  for (Series &s : d->meteo)
+    for (size_t j = 0; j < s.t.size(); j++) {
+      s.v[j * PIHM_METEO_NVAR + PIHM_METEO_PRCP] *= cal.prcp;
+      s.v[j * PIHM_METEO_NVAR + PIHM_METEO_SFCTMP] += cal.sfctmp;
+    }
+  d->cal_edir = cal.edir;
+  d->cal_ec = cal.ec;
+  d->cal_ett = cal.ett;
+  auto flatten = [](const std::vector<Series> &ss, std::vector<int32_t> *len, std::vector<int64_t> *tt,
+                    std::vector<double> *vv) {
+    for (const Series &s : ss) {
+      len->push_back((int32_t)s.t.size());
+      tt->insert(tt->end(), s.t.begin(), s.t.end());
+      vv->insert(vv->end(), s.v.begin(), s.v.end());
+    }
+  };
+  flatten(d->meteo, &d->meteo_len, &d->meteo_time, &d->meteo_data);
+  flatten(d->lai, &d->lai_len, &d->lai_time, &d->lai_data);
 
   // ---- InitRiver (src/init_river.c:6-96) ----
   for (auto *v : {&d->riv_x, &d->riv_y, &d->riv_area, &d->riv_zmin, &d->riv_zmax, &d->riv_zbed, &d->riv_node_zmax,
@@ -867,6 +1031,41 @@ int pihm_deck_control_get(const pihm_deck *d, pihm_deck_control *c) {
 int pihm_deck_initial_state(const pihm_deck *d, double *y0) {
   if (!d || !y0) return PIHM_GPU_ERR_ARG;
   std::memcpy(y0, d->y0.data(), sizeof(double) * d->y0.size());
+  return PIHM_GPU_OK;
+}
+
+int pihm_deck_land(const pihm_deck *d, pihm_land_params *p, pihm_forcing_series *s) {
+  if (!d || !p || !s) return PIHM_GPU_ERR_ARG;
+  *p = pihm_land_params{};
+  p->nelem = d->ne;
+  p->lc_type = d->lc_type.data();
+  p->meteo_type = d->meteo_type.data();
+  p->lai_type = d->lai_type.data();
+  p->albedomin = d->albedomin.data();
+  p->albedomax = d->albedomax.data();
+  p->shdfac = d->shdfac.data();
+  p->cmcfactr = d->cmcfactr.data();
+  p->cfactr = d->cfactr.data();
+  p->rgl = d->rgl.data();
+  p->rsmin = d->rsmin.data();
+  p->rsmax = d->rsmax.data();
+  p->topt = d->topt.data();
+  p->smcmin = d->smcmin.data();
+  p->smcwlt = d->smcwlt.data();
+  p->smcref = d->smcref.data();
+  p->zlvl_wind = d->zlvl_wind.data();
+  p->cal_edir = d->cal_edir;
+  p->cal_ec = d->cal_ec;
+  p->cal_ett = d->cal_ett;
+  *s = pihm_forcing_series{};
+  s->nmeteo = (int32_t)d->meteo.size();
+  s->meteo_len = d->meteo_len.data();
+  s->meteo_time = d->meteo_time.data();
+  s->meteo_data = d->meteo_data.data();
+  s->nlai = (int32_t)d->lai.size();
+  s->lai_len = d->lai_len.data();
+  s->lai_time = d->lai_time.data();
+  s->lai_data = d->lai_data.data();
   return PIHM_GPU_OK;
 }
 

@@ -127,6 +127,32 @@ struct DevMesh {
   int noah;
   const double *noah_etgw, *noah_satn, *noah_fcr;
   const int32_t *noah_wtin;
+
+  // Land-surface model outputs the water balance reads when the model is
+  // attached (include/pihm_land.h; null otherwise): precipitation, canopy
+  // evaporation, canopy storage, snow water equivalent [ne]
+  const double *land_prcp, *land_ec, *land_cmc, *land_sneqv;
+};
+
+// Device view of the land-surface model (include/pihm_land.h), internal
+// element order.  Derived planes are the reference's own sub-expressions
+// evaluated once on the host with the same operations (bit-identical):
+// albedo = 0.5 (albedomin + albedomax), rs_ratio = rsmin / rsmax,
+// topt_c = topt - 273.15, dsmc = smcref - smcwlt, and the surface pressure
+// pres = 101.325e3 ((293 - 0.0065 zmax) / 293)^5.26 (src/is_sm_et.c:47-58,
+// 134-137, 148-150).
+struct LandDev {
+  const int32_t *lc, *meteo, *lai_type;  // [ne], 1-based
+  const double *albedo, *shdfac, *cmcfactr, *cfactr, *rgl, *rsmin, *rs_ratio, *rsmax, *topt_c, *smcmin,
+      *smcwlt, *dsmc, *zlvl, *pres;
+  const double *depth, *porosity, *rzd, *d_rzd;  // the mesh's planes (d_rzd = depth - rzd)
+  double cal_edir, cal_ec, cal_ett;
+  const int32_t *meteo_off, *meteo_len, *lai_off, *lai_len;  // first knot, knots per series
+  const int64_t *meteo_time, *lai_time;
+  const double *meteo_data, *lai_data;  // [knot][7], [knot]
+  double *cmc, *sneqv;                  // state carried between steps
+  double *prcp, *ec, *drip;             // outputs besides the forcing planes
+  double *pcpdrp, *edir, *ett;          // the right-hand side's forcing planes
 };
 
 // Optional per-kernel CUDA-event timing of the right-hand-side launches.
@@ -191,5 +217,8 @@ struct pihm_gpu_ctx {
   long long launches;      // kernels launched by this context so far
   pihm::Profiler *prof;    // non-null while profiling is on
   void *d_noah;            // Flux-PIHM input planes, allocated on first use
+  void *d_land;            // land-surface model (pihm_gpu_land_init), or null
+  pihm::LandDev land;
+  int64_t land_t_lo, land_t_hi;  // model times every forcing series covers
   pihm::RhsStreams side;   // river kernel beside the element kernels
 };

@@ -1,11 +1,13 @@
 // Watershed water balance of one model step on the device: the three sums of
 // PrintWaterBal (src/print.c:337-542) over the current state and fluxes --
-//   sources  sum over elements of prcp area dt (prcp = pcpdrp: no canopy),
-//   sinks    sum over elements of (edir + ett + ec) area dt (ec = 0) plus the
-//            outlet segments' DOWN_CHANL2CHANL flux times dt,
+//   sources  sum over elements of prcp area dt,
+//   sinks    sum over elements of (edir + ett + ec) area dt plus the outlet
+//            segments' DOWN_CHANL2CHANL flux times dt,
 //   storage  sum over elements of (cmc + sneqv + surf + (unsat + gw) porosity)
-//            area (cmc = sneqv = 0: no canopy or snow on this path) plus the
-//            segments' (stage + gw porosity) area.
+//            area plus the segments' (stage + gw porosity) area.
+// With the land-surface model attached (include/pihm_land.h) prcp, ec, cmc
+// and sneqv are its planes; without it the forcing is given directly, so
+// prcp = pcpdrp and ec = cmc = sneqv = 0 (no canopy or snow).
 // The caller accumulates src - snk - (storage - previous storage) as the
 // reference's cumulative error.  Sums are deterministic (fixed block tree and
 // a fixed-order final pass).
@@ -29,9 +31,15 @@ __global__ void __launch_bounds__(kWbThreads) k_water_balance(DevMesh m, const d
     if (t < ne) {
       const int i = (int)t;
       const double area = m.area[i];
-      src += m.pcpdrp[i] * area * dt;
-      snk += (m.edir[i] + m.ett[i]) * area * dt;
-      strg += (y[i] + (y[ne + i] + y[2 * ne + i]) * m.porosity[i]) * area;
+      if (m.land_prcp) {
+        src += m.land_prcp[i] * area * dt;
+        snk += (m.edir[i] + m.ett[i] + m.land_ec[i]) * area * dt;
+        strg += (m.land_cmc[i] + m.land_sneqv[i] + y[i] + (y[ne + i] + y[2 * ne + i]) * m.porosity[i]) * area;
+      } else {
+        src += m.pcpdrp[i] * area * dt;
+        snk += (m.edir[i] + m.ett[i]) * area * dt;
+        strg += (y[i] + (y[ne + i] + y[2 * ne + i]) * m.porosity[i]) * area;
+      }
     } else {
       const int s = (int)(t - ne);
       strg += (y[3 * ne + s] + y[3 * ne + nr + s] * m.r_porosity[s]) * m.r_area[s];

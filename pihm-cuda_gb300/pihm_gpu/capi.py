@@ -137,6 +137,31 @@ class GpuRhs:
         _check("pihm_gpu_water_balance", self.lib.pihm_gpu_water_balance(self.h, _VP(y_ptr), float(dt), f64p(out)))
         return tuple(out)
 
+    # ---- land-surface model (include/pihm_land.h) ----
+    def land_init(self, land):
+        """Attach a land.Land (forcing series and parameters) to the context."""
+        from . import land as L
+        lib = L._lib()
+        p, s = land.structs()
+        self._land = (land, p, s)  # the arrays stay referenced while the context lives
+        _check("pihm_gpu_land_init", lib.pihm_gpu_land_init(self.h, ctypes.byref(p), ctypes.byref(s)))
+
+    def land_set_state(self, cmc=None, sneqv=None):
+        from . import land as L
+        _check("pihm_gpu_land_set_state", L._lib().pihm_gpu_land_set_state(self.h, f64p(_c(cmc)), f64p(_c(sneqv))))
+
+    def land_step(self, t: int, stepsize: float, y_ptr: int):
+        """One land-surface step at model time t (s since 1970 UTC); y_ptr: the
+        device state in internal order."""
+        from . import land as L
+        _check("pihm_gpu_land_step", L._lib().pihm_gpu_land_step(self.h, int(t), float(stepsize), _VP(y_ptr)))
+
+    def land_get(self, field: str) -> np.ndarray:
+        from . import land as L
+        out = np.zeros(self.ws.nelem)
+        _check("pihm_gpu_land_get", L._lib().pihm_gpu_land_get(self.h, L.FIELDS[field], f64p(out)))
+        return out
+
     def set_ws0_surf(self, ws0):
         _check("pihm_gpu_set_ws0_surf", self.lib.pihm_gpu_set_ws0_surf(self.h, f64p(_c(ws0))))
 

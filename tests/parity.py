@@ -104,3 +104,42 @@ def apply(model, sc):
     model.set_river_edge_ovlflow(sc["ovl"])
     if sc["elem_bc"] is not None or sc["river_bc"] is not None:
         model.set_bc(sc["elem_bc"], sc["river_bc"])
+
+
+def land_states(depth, seed: int, nsteps: int):
+    """Soil states (unsat, gw) for a sequence of land-surface steps: the water
+    table anywhere in the column, the unsaturated store from slightly negative
+    to above the column's capacity, so that every branch of the soil
+    saturation in IntcpSnowEt (src/is_sm_et.c:103-118) is taken."""
+    depth = np.asarray(depth, np.float64)
+    rng = np.random.default_rng(seed)
+    for _ in range(nsteps):
+        gw = depth * rng.uniform(0.0, 1.0, depth.size)
+        unsat = (depth - gw) * rng.uniform(-0.1, 1.2, depth.size)
+        yield unsat, gw
+
+
+def land_deck(directory: str, seed: int = 11, land_seed: int = 5, hours: int = 96):
+    """Write a generated 1,000-element deck with a seeded land-surface model
+    (pihm_gpu.land.synthetic_land, per-type canopy parameters, hourly forcing
+    with snow, rain and melt, LSM_STEP 900 s) to <directory>/input/gen; returns
+    that path."""
+    import datetime
+    import os
+
+    import pihm_gpu.land as L
+    import pihm_gpu.watershed as W
+    from pihm_gpu import deck as D
+    ws = W.generate(1000, 100, seed=seed)
+    land = L.synthetic_land(ws, seed=land_seed, hours=hours, per_type=True)
+    rng = np.random.default_rng(0)
+    lc = land.params["lc_type"]
+    rough_t = np.round(rng.uniform(0.02, 0.3, L.NLC), 3)
+    rzd_t = np.round(rng.uniform(0.3, 1.5, L.NLC), 2)
+    ws.arrays["rough"] = rough_t[lc - 1]
+    ws.arrays["rzd"] = rzd_t[lc - 1]
+    path = os.path.join(directory, "input", "gen")
+    end = L.epoch("2009-01-01 00:00") + 3600 * hours
+    end_s = datetime.datetime.fromtimestamp(end, datetime.timezone.utc).strftime("%Y-%m-%d %H:%M")
+    D.write_deck(ws, path, "gen", land=land, lsm_step=900, start="2009-01-01 00:00", end=end_s)
+    return path
