@@ -580,4 +580,83 @@ int ref_run_pihm(double *y, int nsteps, int stepsize, double reltol, double abst
     N_VDestroy(cv_y);
     return 0;
 }
+
+/* The reference's main loop on a deck loaded by ref_load_example, with its
+ * own forcing: from the deck's START, every model step ApplyBc, every
+ * LSM_STEP ApplyForc and IntcpSnowEt (src/pihm.c:15-66), then SolveCVode,
+ * Summary, AdjCVodeMaxStep (src/pihm.c:86-99, src/main.c:217-254), with the
+ * solver controls of the .para file.  y: the initial state (in, reference
+ * order) and the final state (out).  Records the state every `every` steps,
+ * the outlet segment's DOWN_CHANL2CHANL flux after every step, PrintWaterBal's
+ * three sums at full precision after every step (wb_out [nsteps][3], may be
+ * null) and CVODE's counters. */
+int ref_run_deck(double *y, int nsteps, int outlet, int every, double *y_out, double *q_out, double *wb_out,
+                 long *stats)
+{
+    int n = NumStateVar();
+    int i, s;
+    N_Vector cv_y;
+    void *cvode_mem;
+    pihm_struct p = g_pihm;
+    if (!p || !g_have_tables) return -1;
+    cv_y = N_VMake_Serial(n, y);
+    cvode_mem = CVodeCreate(CV_BDF, CV_NEWTON);
+    for (i = 0; i < nelem; i++) {
+        p->elem[i].ws0.surf = y[i];
+        p->elem[i].ws0.unsat = y[i + nelem];
+        p->elem[i].ws0.gw = y[i + 2 * nelem];
+        p->elem[i].ws.surf = y[i];
+        p->elem[i].ws.unsat = y[i + nelem];
+        p->elem[i].ws.gw = y[i + 2 * nelem];
+    }
+    SetCVodeParam(p, cvode_mem, cv_y);
+    for (s = 0; s < nsteps; s++) {
+        const int t = p->ctrl.starttime + s * p->ctrl.stepsize;
+        int tret = t;
+        ApplyBc(&p->forc, p->elem, p->river, t);
+        if ((t - p->ctrl.starttime) % p->ctrl.etstep == 0) {
+            ApplyForc(&p->forc, p->elem, t);
+            IntcpSnowEt(t, (realtype)p->ctrl.etstep, p->elem, &p->cal);
+        }
+        SolveCVode(p->ctrl.starttime, &tret, t + p->ctrl.stepsize, 0.0, cvode_mem, cv_y);
+        Summary(p->elem, p->river, cv_y, (realtype)p->ctrl.stepsize);
+        AdjCVodeMaxStep(cvode_mem, &p->ctrl);
+        if (q_out) q_out[s] = p->river[outlet].wf.rivflow[DOWN_CHANL2CHANL];
+        if (wb_out) {
+            /* PrintWaterBal's sums (src/print.c:337-542) in its order */
+            double src = 0.0, snk = 0.0, strg = 0.0;
+            const double dt = (double)p->ctrl.stepsize;
+            for (i = 0; i < nelem; i++) {
+                const elem_struct *e = &p->elem[i];
+                src += e->wf.prcp * e->topo.area * dt;
+                snk += (e->wf.edir + e->wf.ett + e->wf.ec) * e->topo.area * dt;
+                strg += (e->ws.cmc + e->ws.sneqv + e->ws.surf + (e->ws.unsat + e->ws.gw) * e->soil.porosity) *
+                        e->topo.area;
+            }
+            for (i = 0; i < nriver; i++) {
+                const river_struct *r = &p->river[i];
+                strg += (r->ws.stage + r->ws.gw * r->matl.porosity) * r->topo.area;
+                if (r->down < 0) snk += r->wf.rivflow[DOWN_CHANL2CHANL] * dt;
+            }
+            wb_out[3 * s] = src;
+            wb_out[3 * s + 1] = snk;
+            wb_out[3 * s + 2] = strg;
+        }
+        if (y_out && every > 0 && (s + 1) % every == 0)
+            memcpy(y_out + (size_t)((s + 1) / every - 1) * n, y, sizeof(double) * n);
+    }
+    if (stats) {
+        long v;
+        CVodeGetNumSteps(cvode_mem, &v); stats[0] = v;
+        CVodeGetNumRhsEvals(cvode_mem, &v); stats[1] = v;
+        CVodeGetNumNonlinSolvIters(cvode_mem, &v); stats[2] = v;
+        CVodeGetNumNonlinSolvConvFails(cvode_mem, &v); stats[3] = v;
+        CVodeGetNumErrTestFails(cvode_mem, &v); stats[4] = v;
+        CVSpilsGetNumLinIters(cvode_mem, &v); stats[5] = v;
+        CVSpilsGetNumRhsEvals(cvode_mem, &v); stats[6] = v;
+    }
+    CVodeFree(&cvode_mem);
+    N_VDestroy(cv_y);
+    return 0;
+}
 #endif /* _NOAH_ */

@@ -188,7 +188,9 @@ def synthetic_land(ws, *, start: str = "2009-01-01 00:00", hours: int = 72, nsta
     params = {
         "lc_type": lc, "meteo_type": (block + 1).astype(np.int32), "lai_type": lai_type,
         "albedomin": albmin, "albedomax": albmin + rng.uniform(0.0, 0.1, ne),
-        "shdfac": np.where(rng.random(ne) < 0.05, 0.0, rng.uniform(0.3, 0.95, ne)),
+        # (no bare soil: with shdfac 0 and a positive LAI the canopy capacity is
+        # 0 and the reference's canopy evaporation is 0/0, src/is_sm_et.c:128)
+        "shdfac": rng.uniform(0.3, 0.95, ne),
         "cmcfactr": np.full(ne, 2e-4), "cfactr": np.full(ne, 0.5),
         "rgl": rng.uniform(30.0, 100.0, ne), "rsmin": rng.uniform(40.0, 300.0, ne), "rsmax": np.full(ne, 5000.0),
         "topt": np.full(ne, 298.0), "smcmin": smcmin, "smcwlt": smcwlt, "smcref": smcref,

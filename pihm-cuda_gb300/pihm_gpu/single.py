@@ -1,7 +1,13 @@
 """The single-watershed GPU path as a model-step backend (pihm_gpu.solver.run_steps):
 device N_Vectors (N_VNew_PihmGpu), the drop-in right-hand side pihm_gpu_ode,
 the post-step update on the device.  This is the plain path one watershed at
-a time; the batch engine (pihm_gpu.batch) reproduces it bit for bit."""
+a time; the batch engine (pihm_gpu.batch) reproduces it bit for bit.
+
+`DeckWatershed` / `run_deck` run an input deck the way the reference's main
+loop does (src/main.c:217-254, src/pihm.c:7-187): the deck's boundary series
+every model step, the land-surface step on the device (forcing interpolation,
+interception, snow, evapotranspiration; include/pihm_land.h) every LSM_STEP,
+then the integration to the end of the step, Summary and AdjCVodeMaxStep."""
 from __future__ import annotations
 
 import ctypes
@@ -41,6 +47,10 @@ class GpuWatershed:
         ne = self.ws.nelem
         self.g.set_forcing(np.full(ne, self.pcp[k]), np.full(ne, self.edir[k]), np.full(ne, self.ett[k]))
 
+    def device_state(self) -> int:
+        """Device pointer of the state (internal order)."""
+        return self.lib.N_VGetDeviceArrayPointer_PihmGpu(self.y)
+
     def post_step(self):
         assert self.lib.pihm_gpu_summary(self.g.h, self.y) == 0
 
@@ -75,3 +85,57 @@ def solve_alone(case: dict):
     finally:
         b.close()
     return dict(y=r["states"][-1], outlet=r["outlet"], stats=r["stats"])
+
+
+class DeckWatershed(GpuWatershed):
+    """An input deck (pihm_gpu.deck.Deck) as a model-step backend: its mesh,
+    initial state, boundary series and land-surface model on the GPU."""
+
+    def __init__(self, deck, order=1):
+        self.deck = deck
+        self.ctrl = deck.control()
+        ws = deck.watershed()
+        super().__init__(ws, deck.initial_state(), None, None, None, order=order)
+        self.g.land_init(deck.land())
+        self.has_bc = bool(np.any(ws.arrays["bc_type"]) or np.any(ws.arrays["riverbc_type"]))
+        self.start = int(self.ctrl.start)
+        self.stepsize = int(self.ctrl.step["stepsize"])
+        self.lsm_step = int(self.ctrl.lsm_step)
+
+    def set_forcing(self, k):
+        """The forcing of model step k (src/pihm.c:15-66): ApplyBc at t, and at
+        every LSM_STEP the land-surface step over LSM_STEP seconds."""
+        t = self.start + k * self.stepsize
+        if self.has_bc:
+            e, r = self.deck.bc(t)
+            self.g.set_bc(e, r)
+        if (t - self.start) % self.lsm_step == 0:
+            self.g.land_step(t, float(self.lsm_step), self.device_state())
+
+    def land(self, field: str) -> np.ndarray:
+        return self.g.land_get(field)
+
+
+def step_control(ctrl):
+    """solver.StepControl from a deck's control block."""
+    from .solver import StepControl
+    sc = StepControl()
+    for k in ("stepsize", "reltol", "abstol", "initstep", "nncfn", "nnimax", "nnimin", "decr", "incr", "stmin",
+              "mxstep"):
+        setattr(sc, k, type(getattr(sc, k))(ctrl.step[k]))
+    return sc
+
+
+def run_deck(deck, nsteps: int | None = None, record_every: int = 0, outlet: int | None = None,
+             water_balance: bool = False, order: int = 1):
+    """Run a deck on the GPU for nsteps model steps (default: START to END).
+    Returns run_steps' dict (states in reference order, outlet flux series,
+    integrator counters, water-balance sums)."""
+    from .solver import run_steps
+    b = DeckWatershed(deck, order=order)
+    try:
+        n = nsteps if nsteps is not None else (int(b.ctrl.end) - b.start) // b.stepsize
+        return run_steps(b, step_control(b.ctrl), n, b.set_forcing, record_every=record_every, outlet=outlet,
+                         water_balance=water_balance)
+    finally:
+        b.close()

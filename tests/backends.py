@@ -82,3 +82,53 @@ class OracleBackend:
 # the product's single-watershed path (device N_Vector, pihm_gpu_ode, the
 # post-step update on the device)
 from pihm_gpu.single import GpuWatershed as GpuBackend  # noqa: E402,F401
+
+
+class OracleDeckBackend(OracleBackend):
+    """An input deck on the CPU restatements: the right-hand side
+    (oracle/pihm_oracle.c) and the land-surface step (oracle/land_oracle.c),
+    driven the way the reference's main loop drives them
+    (src/pihm.c:15-99)."""
+
+    def __init__(self, deck):
+        from oracle import OracleLand
+        self.deck = deck
+        self.ctrl = deck.control()
+        ws = deck.watershed()
+        super().__init__(ws, deck.initial_state(), None, None, None)
+        self.land = OracleLand(deck.land(), ws)
+        self.land.set_state(None, None)
+        self.has_bc = bool(np.any(ws.arrays["bc_type"]) or np.any(ws.arrays["riverbc_type"]))
+        self.start = int(self.ctrl.start)
+        self.stepsize = int(self.ctrl.step["stepsize"])
+        self.lsm_step = int(self.ctrl.lsm_step)
+
+    def set_forcing(self, k):
+        ne = self.ws.nelem
+        t = self.start + k * self.stepsize
+        self.k = k
+        if self.has_bc:
+            e, r = self.deck.bc(t)
+            self.model.set_bc(e, r)
+        if (t - self.start) % self.lsm_step == 0:
+            y = self.yarr
+            assert self.land.step(t, float(self.lsm_step), y[ne:2 * ne], y[2 * ne:3 * ne]) == 0
+            self.model.set_forcing(self.land.get("pcpdrp"), self.land.get("edir"), self.land.get("ett"))
+
+    def water_balance(self, dt):
+        """PrintWaterBal's sums (src/print.c:337-542) in its summation order,
+        with the land-surface model's precipitation, canopy evaporation,
+        canopy storage and snow."""
+        a, ne, nr = self.ws.arrays, self.ws.nelem, self.ws.nriver
+        y = self.yarr
+        area = a["area"]
+        f = {k: self.land.get(k) for k in ("prcp", "edir", "ett", "ec", "cmc", "sneqv")}
+        src = np.cumsum(f["prcp"] * area * dt)[-1]
+        e_snk = (f["edir"] + f["ett"] + f["ec"]) * area * dt
+        rivflow = self.model.fluxes()["rivflow"].reshape(nr, 11)[:, 1]
+        r_snk = (rivflow * dt)[a["down"] < 0]
+        snk = np.cumsum(np.concatenate([e_snk, r_snk]))[-1]
+        e_strg = ((f["cmc"] + f["sneqv"] + y[:ne]) + (y[ne:2 * ne] + y[2 * ne:3 * ne]) * a["porosity"]) * area
+        r_strg = (y[3 * ne:3 * ne + nr] + y[3 * ne + nr:] * a["riv_porosity"]) * a["riv_area"]
+        strg = np.cumsum(np.concatenate([e_strg, r_strg]))[-1]
+        return float(src), float(snk), float(strg)

@@ -50,6 +50,7 @@ def _state_on_device(g, ws, unsat, gw):
 
 def _check(got, want, label, stats):
     got, want = np.asarray(got), np.asarray(want)
+    assert np.all(np.isfinite(want)), f"{label}: the expected values hold NaN or infinity"
     floor = LAND_FLOOR * np.max(np.abs(want)) if want.size else 0.0
     err = np.abs(got - want)
     lim = LAND_RTOL * np.maximum(np.abs(want), floor)
