@@ -331,6 +331,76 @@ def bench_flux_pihm():
             "note": "Noah (SFLX) itself is not on this path: its per-step outputs are generated"}
 
 
+LAND_STEPS = 96            # one day of 900 s land-surface steps
+LAND_BYTES_PER_ELEM = 252  # algorithmic: 188 B read, 64 B written per element and step
+
+
+def bench_land(ws):
+    """The land-surface step (forcing interpolation, snow, interception,
+    evapotranspiration; include/pihm_land.h) on the headline mesh: 64
+    stations, 8 LAI series, a day of 900 s steps, timed with CUDA events on
+    the launching stream; the OpenMP restatement on the host cores on a
+    bounded sample of the same steps."""
+    import numpy as np
+    import torch
+    import pihm_gpu.land as L
+    from pihm_gpu.capi import GpuRhs
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.Stream(device=dev)
+    land = L.synthetic_land(ws, hours=LAND_STEPS // 4 + 2, nstations=64, nlai=8, seed=21)
+    g = GpuRhs(ws, stream=stream.cuda_stream)
+    g.land_init(land)
+    # a soil state with the water table anywhere in the column
+    rng = np.random.default_rng(5)
+    depth = np.asarray(ws.arrays["depth"])
+    gw = depth * rng.uniform(0.0, 1.0, depth.size)
+    unsat = (depth - gw) * rng.uniform(-0.1, 1.2, depth.size)
+    y = np.zeros(ws.neq)
+    ne = ws.nelem
+    y[ne:2 * ne], y[2 * ne:3 * ne] = unsat, gw
+    with torch.cuda.stream(stream):
+        yr = torch.from_numpy(y).to(dev)
+        yi = torch.empty_like(yr)
+        g.to_internal(yr.data_ptr(), yi.data_ptr())
+    t0 = L.epoch("2009-01-01 00:00")
+    for k in range(3):
+        g.land_step(t0 + 900 * k, 900.0, yi.data_ptr())
+    stream.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(LAND_STEPS):
+        g.land_step(t0 + 900 * k, 900.0, yi.data_ptr())
+    e1.record(stream)
+    e1.synchronize()
+    assert g.status() == 0
+    ms = e0.elapsed_time(e1) / LAND_STEPS
+    value = ne / (ms * 1e-3)
+    g.close()
+    cpu = None
+    try:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        o = oracle.OracleLand(land, ws, omp=True)
+        n, t = 0, time.perf_counter()
+        while n < 3 or (time.perf_counter() - t < 10.0 and n < LAND_STEPS):
+            assert o.step(t0 + 900 * n, 900.0, unsat, gw) == 0
+            n += 1
+        cpu_s = time.perf_counter() - t
+        cpu = {"value": ne * n / cpu_s, "unit": "element-steps/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{n} land-surface steps of the {ne}-element mesh (OpenMP restatement)"}
+        o.close()
+    except Exception as exc:
+        cpu = {"error": repr(exc)}
+    peak, _ = peaks()
+    achieved = LAND_BYTES_PER_ELEM * ne / (ms * 1e-3) / 1e9
+    return {"metric": "land-surface element-steps/s", "unit": "element-steps/s", "value": value,
+            "ms_per_step": ms,
+            "workload": f"{ne} elements, 64 meteorological stations, 8 LAI series, {LAND_STEPS} steps of 900 s",
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "alg_bytes_per_elem": LAND_BYTES_PER_ELEM},
+            "cpu_baseline": cpu}
+
+
 def bench_serving():
     """Poisson stream of calibration requests at SERVE_LOAD of measured capacity."""
     import numpy as np
@@ -407,6 +477,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-watersheds leg")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving leg")
     ap.add_argument("--no-flux", action="store_true", help="skip the Flux-PIHM leg")
+    ap.add_argument("--no-land", action="store_true", help="skip the land-surface leg")
     args = ap.parse_args()
     globals()["NELEM"], globals()["NRIVER"] = args.nelem, args.nriver
     if args.impl == "reference":
@@ -573,9 +644,14 @@ def main():
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
 
     # ---- batched watersheds and serving (N = 1 only) ----
-    batched = serving = flux = None
+    batched = serving = flux = land = None
     if rank == 0 and world == 1:
         g.close()
+        if not args.no_land:
+            try:
+                land = bench_land(ws)
+            except Exception as exc:
+                land = {"error": repr(exc)}
         if not args.no_batched:
             try:
                 batched = bench_batched()
@@ -618,6 +694,7 @@ def main():
             "batched": batched,
             "serving": serving,
             "flux_pihm": flux,
+            "land_surface": land,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
