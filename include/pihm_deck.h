@@ -65,6 +65,12 @@ int pihm_deck_control_get(const pihm_deck *deck, pihm_deck_control *ctrl);
  * (src/initialize.c:496-575) or the .ic restart file (src/read_ic.c:3-39). */
 int pihm_deck_initial_state(const pihm_deck *deck, double *y0);
 
+/* Canopy storage and snow water equivalent at the start [nelem], for
+ * pihm_gpu_land_set_state: 0 after RelaxIc (src/initialize.c:509-510), the
+ * restart file's ic.cmc and ic.sneqv otherwise (src/read_ic.c:3-39,
+ * src/initialize.c:594-595); either may be NULL. */
+int pihm_deck_initial_storage(const pihm_deck *deck, double *cmc, double *sneqv);
+
 /* The land-surface model of the deck for pihm_gpu_land_init: the element
  * parameters InitSoil, InitLc and InitForc leave (src/init_soil.c:34-54 with
  * FieldCapacity and WiltingPoint of the soil table, src/soil.c:16-81;

@@ -313,6 +313,7 @@ struct pihm_deck {
       riv_ksatv, riv_bedthick, riv_porosity;
   pihm_deck_control ctrl{};
   std::vector<double> y0;
+  std::vector<double> ic_cmc, ic_sneqv;  // canopy and snow storage at the start
   std::vector<Series> bc, riverbc;
   // land-surface model (include/pihm_land.h): element parameters as
   // InitSoil / InitLc / InitForc leave them, and the forcing series
@@ -921,6 +922,8 @@ void build(const std::string &dir, const std::string &project, const std::string
 
   // ---- initial state: RelaxIc (src/initialize.c:496-575) or the restart file ----
   d->y0.assign(3 * (size_t)ne + 2 * (size_t)nr, 0.0);
+  d->ic_cmc.assign(ne, 0.0);  // RelaxIc (src/initialize.c:509-510)
+  d->ic_sneqv.assign(ne, 0.0);
   if (d->ctrl.init_mode == 0) {
     const double kInitUnsat = 0.1;
     for (int i = 0; i < ne; i++) {
@@ -934,7 +937,7 @@ void build(const std::string &dir, const std::string &project, const std::string
     }
   } else {
     const std::string ic = dir + "/" + project + ".ic";
-    const int rc = pihm_ic_read(ic.c_str(), ne, nr, d->y0.data(), nullptr, nullptr);
+    const int rc = pihm_ic_read(ic.c_str(), ne, nr, d->y0.data(), d->ic_cmc.data(), d->ic_sneqv.data());
     if (rc != 0) fail(rc == PIHM_DECK_ERR_IO ? rc : PIHM_DECK_ERR_IO, "cannot read restart file %s", ic.c_str());
   }
 }
@@ -1031,6 +1034,13 @@ int pihm_deck_control_get(const pihm_deck *d, pihm_deck_control *c) {
 int pihm_deck_initial_state(const pihm_deck *d, double *y0) {
   if (!d || !y0) return PIHM_GPU_ERR_ARG;
   std::memcpy(y0, d->y0.data(), sizeof(double) * d->y0.size());
+  return PIHM_GPU_OK;
+}
+
+int pihm_deck_initial_storage(const pihm_deck *d, double *cmc, double *sneqv) {
+  if (!d) return PIHM_GPU_ERR_ARG;
+  if (cmc) std::memcpy(cmc, d->ic_cmc.data(), sizeof(double) * d->ic_cmc.size());
+  if (sneqv) std::memcpy(sneqv, d->ic_sneqv.data(), sizeof(double) * d->ic_sneqv.size());
   return PIHM_GPU_OK;
 }
 

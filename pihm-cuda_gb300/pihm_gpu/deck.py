@@ -60,6 +60,9 @@ def _lib():
         lib.pihm_deck_land.argtypes = [_VP, ctypes.POINTER(land_mod.LandParamsC),
                                        ctypes.POINTER(land_mod.ForcingSeriesC)]
         lib.pihm_deck_land.restype = ctypes.c_int
+        lib.pihm_deck_initial_storage.argtypes = [_VP, ctypes.POINTER(ctypes.c_double),
+                                                  ctypes.POINTER(ctypes.c_double)]
+        lib.pihm_deck_initial_storage.restype = ctypes.c_int
         lib._deck_sigs = True
     return lib
 
@@ -143,6 +146,17 @@ class Deck:
         capi._check("pihm_deck_initial_state",
                     self.lib.pihm_deck_initial_state(self.h, y.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
         return y
+
+    def initial_storage(self):
+        """(cmc, sneqv) at the start: zeros after RelaxIc, the .ic file's values
+        on a hot start."""
+        m = MeshDesc()
+        capi._check("pihm_deck_mesh", self.lib.pihm_deck_mesh(self.h, ctypes.byref(m)))
+        cmc, sneqv = np.zeros(m.nelem), np.zeros(m.nelem)
+        P = ctypes.POINTER(ctypes.c_double)
+        capi._check("pihm_deck_initial_storage",
+                    self.lib.pihm_deck_initial_storage(self.h, cmc.ctypes.data_as(P), sneqv.ctypes.data_as(P)))
+        return cmc, sneqv
 
     def land(self) -> "land_mod.Land":
         """The land-surface model (parameters and forcing series, copies)."""

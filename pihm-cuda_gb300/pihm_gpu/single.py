@@ -97,6 +97,7 @@ class DeckWatershed(GpuWatershed):
         ws = deck.watershed()
         super().__init__(ws, deck.initial_state(), None, None, None, order=order)
         self.g.land_init(deck.land())
+        self.g.land_set_state(*deck.initial_storage())
         self.has_bc = bool(np.any(ws.arrays["bc_type"]) or np.any(ws.arrays["riverbc_type"]))
         self.start = int(self.ctrl.start)
         self.stepsize = int(self.ctrl.step["stepsize"])

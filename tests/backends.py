@@ -97,7 +97,7 @@ class OracleDeckBackend(OracleBackend):
         ws = deck.watershed()
         super().__init__(ws, deck.initial_state(), None, None, None)
         self.land = OracleLand(deck.land(), ws)
-        self.land.set_state(None, None)
+        self.land.set_state(*deck.initial_storage())
         self.has_bc = bool(np.any(ws.arrays["bc_type"]) or np.any(ws.arrays["riverbc_type"]))
         self.start = int(self.ctrl.start)
         self.stepsize = int(self.ctrl.step["stepsize"])

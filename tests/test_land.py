@@ -176,3 +176,34 @@ def test_written_forcing_reads_back(tmp_path):
         assert np.array_equal(got.params[k], want.params[k]), k
     assert got.cal == (1.0, 1.0, 1.0)
     assert d.control().lsm_step == 900
+
+
+def test_hot_start_restores_canopy_and_snow(tmp_path):
+    """INIT_MODE 1: the restart file's state, canopy storage and snow, as the
+    reference's ReadIc + InitVar leave them (ws.cmc, ws.sneqv)."""
+    import ctypes
+    _have_lib()
+    ref = _ref()
+    from pihm_gpu import capi, deck as D
+    path = land_deck(str(tmp_path))
+    d0 = D.Deck.read(path, "gen")
+    ws = d0.watershed()
+    ne, nr = ws.nelem, ws.nriver
+    rng = np.random.default_rng(4)
+    y = d0.initial_state() * rng.uniform(0.5, 1.5, ws.neq)
+    cmc, sneqv = rng.uniform(0.0, 5e-4, ne), rng.uniform(0.0, 2e-2, ne)
+    lib = capi.load()
+    P = ctypes.POINTER(ctypes.c_double)
+    lib.pihm_ic_write.argtypes = [ctypes.c_char_p, ctypes.c_int32, ctypes.c_int32, P, P, P]
+    assert lib.pihm_ic_write(os.path.join(path, "gen.ic").encode(), ne, nr, y.ctypes.data_as(P),
+                             cmc.ctypes.data_as(P), sneqv.ctypes.data_as(P)) == 0
+    para = os.path.join(path, "gen.para")
+    text = open(para).read()
+    open(para, "w").write(text.replace("INIT_MODE 0", "INIT_MODE 1"))
+    d = D.Deck.read(path, "gen")
+    got_c, got_s = d.initial_storage()
+    assert np.array_equal(d.initial_state(), y)
+    y_ref = ref.load_deck(str(tmp_path), "gen")
+    assert np.array_equal(y_ref, y)
+    assert np.array_equal(got_c, ref.export("cmc", ne)) and np.array_equal(got_c, cmc)
+    assert np.array_equal(got_s, ref.export("sneqv", ne)) and np.array_equal(got_s, sneqv)
