@@ -12,9 +12,13 @@
 // step reproduces the reference's values to the last bit on nearly every
 // element, and within a few ulps of the affected terms elsewhere.
 //
-// Cost: about 60 FP64 operations and six transcendental evaluations per
-// element, and about 30 8-byte loads and stores (coalesced planes; the
-// forcing series are read through the cache by every element of a station).
+// Work is split by what it depends on: k_land_station interpolates each
+// station's record and forms everything that depends on it alone (vapour
+// pressure, snow fraction, melt, the temperature powers) once per station;
+// k_land_month forms the aerodynamic term log(z/z0) log(10 z/z0) of every
+// element when the month changes; k_land_step does the per-element rest,
+// each value formed with the reference's operations in its order, so the
+// split changes no result.
 #include <cstdio>
 #include <cstring>
 #include <ctime>
@@ -75,54 +79,109 @@ __device__ __forceinline__ double lerp(const int64_t *__restrict__ T, const doub
   return ((double)(t1 - t) * d0 + (double)(t - t0) * d1) / (double)(t1 - t0);
 }
 
-__global__ void __launch_bounds__(kLandBlock) k_land_step(LandDev L, const double *__restrict__ y, int ne,
-                                                          int64_t t, int month, double dt) {
+// Station values (ApplyMeteoForc's record, src/forcing.c:343-356, and the
+// parts of IntcpSnowEt that depend on it alone), per station and step.
+enum StationVal {
+  SV_PRCP = 0,   // prcp / 1000 (m s-1)
+  SV_TC,         // air temperature - 273.15 (C)
+  SV_RH,         // relative humidity / 100
+  SV_WIND016,    // wind speed * 0.16
+  SV_SOLDN,      // solar radiation, negative as 0
+  SV_VP,         // vapour pressure 611.2 exp(17.67 T / (T + 243.5)) rh
+  SV_VPRH,       // vp / rh
+  SV_GAMMAS,     // 1 / (1 + 0.00025 (vp / rh - vp)), at least 0.01
+  SV_FRAC_SNOW,  // snow fraction of precipitation
+  SV_MELT,       // degree-day melt rate before the snow store limits it
+  SV_CGAMMA,     // 4 0.7 SIGMA RD / CP (T + 273.15)^4
+  SV_CDELTA,     // LVH2O^2 0.622 / RV / CP / (T + 273.15)^2
+  kStationVals
+};
+
+// One thread per station (then one per LAI series): the interpolation of
+// IntrplForc and the station-only sub-expressions of IntcpSnowEt
+// (src/is_sm_et.c:49-56, 70-77, 97-100, 149-150), in the reference's order.
+__global__ void k_land_station(LandDev L, int64_t t, int month) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const double nan = __longlong_as_double(0x7ff8000000000000LL);
+  if (k < L.nmeteo) {
+    const int off = L.meteo_off[k];
+    const int64_t *mt = L.meteo_time + off;
+    const double *md = L.meteo_data + (size_t)off * PIHM_METEO_NVAR;
+    const int km = bracket(mt, L.meteo_len[k], t);
+    double prcp = nan, tk_in = nan, rh_pct = nan, wind = nan, soldn = nan;
+    if (km > 0) {
+      prcp = lerp(mt, md, PIHM_METEO_NVAR, km, PIHM_METEO_PRCP, t) / 1000.0;
+      tk_in = lerp(mt, md, PIHM_METEO_NVAR, km, PIHM_METEO_SFCTMP, t);
+      rh_pct = lerp(mt, md, PIHM_METEO_NVAR, km, PIHM_METEO_RH, t);
+      wind = lerp(mt, md, PIHM_METEO_NVAR, km, PIHM_METEO_SFCSPD, t);
+      soldn = lerp(mt, md, PIHM_METEO_NVAR, km, PIHM_METEO_SOLAR, t);
+    }
+    soldn = (soldn > 0.0) ? soldn : 0.0;
+    const double sfctmp = tk_in - 273.15;
+    const double rh = rh_pct / 100.0;
+    const double vp = 611.2 * exp_l(17.67 * sfctmp / (sfctmp + 243.5)) * rh;
+    const double vprh = vp / rh;
+    double gammas = 1.0 / (1.0 + 0.00025 * (vp / rh - vp));
+    gammas = (gammas < 0.01) ? 0.01 : gammas;
+    const double frac_snow =
+        (sfctmp < kTSnow) ? 1.0 : ((sfctmp > kTRain) ? 0.0 : (kTRain - sfctmp) / (kTRain - kTSnow));
+    const double melt = (sfctmp > kT0) ? (sfctmp - kT0) * g_melt_factor[month] : 0.0;
+    const double tk = sfctmp + 273.15;
+    double *o = L.station + (size_t)k * kStationVals;
+    o[SV_PRCP] = prcp;
+    o[SV_TC] = sfctmp;
+    o[SV_RH] = rh;
+    o[SV_WIND016] = wind * 0.16;
+    o[SV_SOLDN] = soldn;
+    o[SV_VP] = vp;
+    o[SV_VPRH] = vprh;
+    o[SV_GAMMAS] = gammas;
+    o[SV_FRAC_SNOW] = frac_snow;
+    o[SV_MELT] = melt;
+    o[SV_CGAMMA] = 4.0 * 0.7 * kSigma * kRd / kCp * pow_fast(tk, 4.0);
+    o[SV_CDELTA] = kLvH2O * kLvH2O * 0.622 / kRv / kCp / (tk * tk);
+  } else if (k < L.nmeteo + L.nlai) {
+    const int s = k - L.nmeteo;
+    const int off = L.lai_off[s];
+    const int kl = bracket(L.lai_time + off, L.lai_len[s], t);
+    L.lai_value[s] = kl > 0 ? lerp(L.lai_time + off, L.lai_data + off, 1, kl, 0, t) : nan;
+  }
+}
+
+// log(zlvl / z0) log(10 zlvl / z0) of every element for a month (z0 from the
+// monthly roughness table), the numerator of the aerodynamic resistance
+// (src/is_sm_et.c:93-96); recomputed when the month changes.
+__global__ void __launch_bounds__(kLandBlock) k_land_month(LandDev L, int ne, int month) {
   const int i = blockIdx.x * kLandBlock + threadIdx.x;
   if (i >= ne) return;
-  const double nan = __longlong_as_double(0x7ff8000000000000LL);
+  const double z0 = g_monthly_rl[(__ldg(&L.lc[i]) - 1) * 12 + month];
+  const double zlvl = __ldg(&L.zlvl[i]);
+  L.ra_num[i] = log_l(zlvl / z0) * log_l(10.0 * zlvl / z0);
+}
 
-  // ---- ApplyMeteoForc (src/forcing.c:343-356) and ApplyLai (:466-477) ----
-  const int st = __ldg(&L.meteo[i]) - 1;
-  const int moff = __ldg(&L.meteo_off[st]);
-  const int64_t *mt = L.meteo_time + moff;
-  const double *md = L.meteo_data + (size_t)moff * PIHM_METEO_NVAR;
-  const int km = bracket(mt, __ldg(&L.meteo_len[st]), t);
-  double prcp = nan, sfctmp_k = nan, rh_pct = nan, wind = nan, soldn = nan;
-  if (km > 0) {
-    prcp = lerp(mt, md, PIHM_METEO_NVAR, km, PIHM_METEO_PRCP, t) / 1000.0;
-    sfctmp_k = lerp(mt, md, PIHM_METEO_NVAR, km, PIHM_METEO_SFCTMP, t);
-    rh_pct = lerp(mt, md, PIHM_METEO_NVAR, km, PIHM_METEO_RH, t);
-    wind = lerp(mt, md, PIHM_METEO_NVAR, km, PIHM_METEO_SFCSPD, t);
-    soldn = lerp(mt, md, PIHM_METEO_NVAR, km, PIHM_METEO_SOLAR, t);
-  }
-  soldn = (soldn > 0.0) ? soldn : 0.0;
+__global__ void __launch_bounds__(kLandBlock) k_land_step(LandDev L, const double *__restrict__ y, int ne,
+                                                          int month, double dt) {
+  const int i = blockIdx.x * kLandBlock + threadIdx.x;
+  if (i >= ne) return;
+  const double *sv = L.station + (size_t)(__ldg(&L.meteo[i]) - 1) * kStationVals;
   const int lc = __ldg(&L.lc[i]) - 1;
   const int lt = __ldg(&L.lai_type[i]);
-  double lai;
-  if (lt > 0) {
-    const int loff = __ldg(&L.lai_off[lt - 1]);
-    const int kl = bracket(L.lai_time + loff, __ldg(&L.lai_len[lt - 1]), t);
-    lai = kl > 0 ? lerp(L.lai_time + loff, L.lai_data + loff, 1, kl, 0, t) : nan;
-  } else {
-    lai = g_monthly_lai[lc * 12 + month];
-  }
+  const double lai = lt > 0 ? L.lai_value[lt - 1] : g_monthly_lai[lc * 12 + month];
 
   // ---- IntcpSnowEt (src/is_sm_et.c:46-224) ----
-  const double radnet = soldn * (1.0 - __ldg(&L.albedo[i]));
-  const double sfctmp = sfctmp_k - 273.15;
-  const double rh = rh_pct / 100.0;
-  const double vp = 611.2 * exp_l(17.67 * sfctmp / (sfctmp + 243.5)) * rh;
+  const double prcp = sv[SV_PRCP];
+  const double sfctmp = sv[SV_TC];
+  const double radnet = sv[SV_SOLDN] * (1.0 - __ldg(&L.albedo[i]));
+  const double vp = sv[SV_VP];
   const double pres = __ldg(&L.pres[i]);
   const double qv = 0.622 * vp / pres;
-  const double qvsat = 0.622 * (vp / rh) / pres;
-  const double meltf = g_melt_factor[month];
+  const double qvsat = 0.622 * sv[SV_VPRH] / pres;
 
   // snow accumulation and melt
-  const double frac_snow = (sfctmp < kTSnow) ? 1.0 : ((sfctmp > kTRain) ? 0.0 : (kTRain - sfctmp) / (kTRain - kTSnow));
-  const double snow_rate = frac_snow * prcp;
+  const double frac_snow = sv[SV_FRAC_SNOW];
   double sneqv = L.sneqv[i];
-  sneqv += snow_rate * dt;
-  double melt_rate = (sfctmp > kT0) ? (sfctmp - kT0) * meltf : 0.0;
+  sneqv += frac_snow * prcp * dt;
+  double melt_rate = sv[SV_MELT];
   if (sneqv > melt_rate * dt) {
     sneqv -= melt_rate * dt;
   } else {
@@ -133,12 +192,9 @@ __global__ void __launch_bounds__(kLandBlock) k_land_step(LandDev L, const doubl
   // potential evaporation (Penman-Monteith)
   const double shdfac = __ldg(&L.shdfac[i]);
   const double intcp_max = __ldg(&L.cmcfactr[i]) * lai * shdfac;
-  const double z0 = g_monthly_rl[lc * 12 + month];
-  const double zlvl = __ldg(&L.zlvl[i]);
-  const double ra = log_l(zlvl / z0) * log_l(10.0 * zlvl / z0) / (wind * 0.16);
-  const double tk = sfctmp + 273.15;
-  const double gamma = 4.0 * 0.7 * kSigma * kRd / kCp * pow_fast(tk, 4.0) / (pres / ra) + 1.0;
-  const double delta = kLvH2O * kLvH2O * 0.622 / kRv / kCp / (tk * tk) * qvsat;
+  const double ra = L.ra_num[i] / sv[SV_WIND016];
+  const double gamma = sv[SV_CGAMMA] / (pres / ra) + 1.0;
+  const double delta = sv[SV_CDELTA] * qvsat;
   const double etp =
       (radnet * delta + gamma * (1.2 * kLvH2O * (qvsat - qv) / ra)) / (1000.0 * kLvH2O * (delta + gamma));
 
@@ -182,12 +238,12 @@ __global__ void __launch_bounds__(kLandBlock) k_land_step(LandDev L, const doubl
     const double dtopt = __ldg(&L.topt_c[i]) - sfctmp;
     double etas = 1.0 - 0.0016 * (dtopt * dtopt);
     etas = (etas < 0.0001) ? 0.0001 : etas;
-    double gammas = 1.0 / (1.0 + 0.00025 * (vp / rh - vp));
-    gammas = (gammas < 0.01) ? 0.01 : gammas;
+    const double gammas = sv[SV_GAMMAS];
     const double rsmax = __ldg(&L.rsmax[i]);
     double rs = __ldg(&L.rsmin[i]) * alphar / (betas * lai * etas * gammas);
     rs = (rs > rsmax) ? rsmax : rs;
-    const double pc = (1.0 + delta / gamma) / (1.0 + rs / ra + delta / gamma);
+    const double dg = delta / gamma;  // the reference forms it twice
+    const double pc = (1.0 + dg) / (1.0 + rs / ra + dg);
     ett = shdfac * pc * (1.0 - pw_ett) * etp;
     ett *= L.cal_ett;
     ett = (ett < 0.0) ? 0.0 : ett;
@@ -319,7 +375,8 @@ int pihm_gpu_land_init(pihm_gpu_ctx *c, const pihm_land_params *p, const pihm_fo
   const size_t nm = (size_t)s->nmeteo, nl = (size_t)(s->nlai > 0 ? s->nlai : 1);
   const size_t bytes = 14 * align256(NE * 8) + 3 * align256(NE * 4) + 2 * align256(nm * 4) + 2 * align256(nl * 4) +
                        align256(nmk * 8) + align256(nmk * 8 * PIHM_METEO_NVAR) + align256((nlk ? nlk : 1) * 8) +
-                       align256((nlk ? nlk : 1) * 8) + 5 * align256(NE * 8);
+                       align256((nlk ? nlk : 1) * 8) + 5 * align256(NE * 8) + align256(nm * 8 * kStationVals) +
+                       align256(nl * 8) + align256(NE * 8);
   if (c->d_land) {
     cudaFree(c->d_land);
     c->d_land = nullptr;
@@ -348,6 +405,9 @@ int pihm_gpu_land_init(pihm_gpu_ctx *c, const pihm_land_params *p, const pihm_fo
   double *d_ld = (double *)take((nlk ? nlk : 1) * 8);
   double *state[5];
   for (int k = 0; k < 5; k++) state[k] = (double *)take(NE * 8);
+  double *d_station = (double *)take(nm * 8 * kStationVals);
+  double *d_laival = (double *)take(nl * 8);
+  double *d_ranum = (double *)take(NE * 8);
 
   cudaError_t e = cudaSuccess;
   for (int k = 0; k < 14 && e == cudaSuccess; k++) e = cudaMemcpy(dd[k], hd[k].data(), NE * 8, cudaMemcpyHostToDevice);
@@ -405,12 +465,18 @@ int pihm_gpu_land_init(pihm_gpu_ctx *c, const pihm_land_params *p, const pihm_fo
   L.prcp = state[2];
   L.ec = state[3];
   L.drip = state[4];
+  L.station = d_station;
+  L.lai_value = d_laival;
+  L.ra_num = d_ranum;
+  L.nmeteo = s->nmeteo;
+  L.nlai = s->nlai;
   L.pcpdrp = const_cast<double *>(c->m.pcpdrp);
   L.edir = const_cast<double *>(c->m.edir);
   L.ett = const_cast<double *>(c->m.ett);
   c->land = L;
   c->land_t_lo = lo;
   c->land_t_hi = hi;
+  c->land_month = -1;
   c->m.land_prcp = L.prcp;
   c->m.land_ec = L.ec;
   c->m.land_cmc = L.cmc;
@@ -441,9 +507,16 @@ int pihm_gpu_land_step(pihm_gpu_ctx *c, int64_t t, double stepsize, const double
   if (!gmtime_r(&raw, &tm)) return PIHM_GPU_ERR_ARG;
   const int ne = c->ne;
   if (ne == 0) return PIHM_GPU_OK;
-  k_land_step<<<(ne + kLandBlock - 1) / kLandBlock, kLandBlock, 0, c->stream>>>(c->land, y_dev, ne, t, tm.tm_mon,
-                                                                                stepsize);
-  c->launches++;
+  const unsigned grid = (unsigned)((ne + kLandBlock - 1) / kLandBlock);
+  if (tm.tm_mon != c->land_month) {
+    k_land_month<<<grid, kLandBlock, 0, c->stream>>>(c->land, ne, tm.tm_mon);
+    c->launches++;
+    c->land_month = tm.tm_mon;
+  }
+  const int nser = c->land.nmeteo + c->land.nlai;
+  k_land_station<<<(nser + 127) / 128, 128, 0, c->stream>>>(c->land, t, tm.tm_mon);
+  k_land_step<<<grid, kLandBlock, 0, c->stream>>>(c->land, y_dev, ne, tm.tm_mon, stepsize);
+  c->launches += 2;
   return cuda_rc(cudaGetLastError());
 }
 

@@ -153,6 +153,11 @@ struct LandDev {
   double *cmc, *sneqv;                  // state carried between steps
   double *prcp, *ec, *drip;             // outputs besides the forcing planes
   double *pcpdrp, *edir, *ett;          // the right-hand side's forcing planes
+  // per step: each station's record and the values that depend on it alone
+  // ([nmeteo][kStationVals], k_land_station) and each LAI series' value
+  // [nlai]; per month: each element's log(z/z0) log(10 z/z0) [ne]
+  double *station, *lai_value, *ra_num;
+  int32_t nmeteo, nlai;
 };
 
 // Optional per-kernel CUDA-event timing of the right-hand-side launches.
@@ -220,5 +225,6 @@ struct pihm_gpu_ctx {
   void *d_land;            // land-surface model (pihm_gpu_land_init), or null
   pihm::LandDev land;
   int64_t land_t_lo, land_t_hi;  // model times every forcing series covers
+  int land_month;                // month ra_num holds (-1: none yet)
   pihm::RhsStreams side;   // river kernel beside the element kernels
 };
