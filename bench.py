@@ -401,6 +401,41 @@ def bench_land(ws):
             "cpu_baseline": cpu}
 
 
+def bench_solve(ws, hours):
+    """A solve on the headline 1M-element mesh (the c1 configuration's solve):
+    from RelaxIc, 60 s model steps with hourly synthetic forcing, the
+    integrator over device N_Vectors with the right-hand side on the device
+    (pihm_gpu.single.GpuWatershed through pihm_gpu.solver.run_steps, the
+    reference's model-step loop).  Wall time on the host clock around the
+    whole solve."""
+    import numpy as np
+    import torch
+    import pihm_gpu.watershed as W
+    from pihm_gpu import workloads as WL
+    from pihm_gpu.single import GpuWatershed
+    from pihm_gpu.solver import StepControl, run_steps
+    nsteps = int(hours * 60)
+    pcp, edir, ett = WL.step_forcing(ws, nsteps, 60.0, seed=8)
+    m = GpuWatershed(ws, W.relax_state(ws), pcp, edir, ett)
+    m.g.set_diagnostics(False)
+    outlet = int(np.where(np.asarray(ws.arrays["down"]) < 0)[0][0])
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    r = run_steps(m, StepControl(), nsteps, m.set_forcing, outlet=outlet)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t
+    m.close()
+    st = r["stats"]
+    evals = int(st.nfe + st.nfes)
+    return {"metric": "solve: RHS element-evals/s inside the solve", "unit": "elem-evals/s",
+            "value": ws.nelem * evals / wall,
+            "workload": f"{ws.nelem} elements, {ws.nriver} segments, {nsteps} model steps of 60 s "
+                        f"({hours} simulated hours) from RelaxIc, hourly synthetic forcing, reltol 1e-4",
+            "wall_s": wall, "simulated_hours_per_wall_hour": hours * 3600.0 / wall,
+            "integrator_steps": int(st.nst), "rhs_evals": evals, "newton_iters": int(st.nni),
+            "linear_iters": int(st.nli), "final_outlet_flux": float(r["outlet"][-1])}
+
+
 def bench_serving():
     """Poisson stream of calibration requests at SERVE_LOAD of measured capacity."""
     import numpy as np
@@ -478,6 +513,8 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving leg")
     ap.add_argument("--no-flux", action="store_true", help="skip the Flux-PIHM leg")
     ap.add_argument("--no-land", action="store_true", help="skip the land-surface leg")
+    ap.add_argument("--solve-hours", type=float, default=6.0,
+                    help="simulated hours of the 1M-element solve leg (0 skips it)")
     args = ap.parse_args()
     globals()["NELEM"], globals()["NRIVER"] = args.nelem, args.nriver
     if args.impl == "reference":
@@ -644,9 +681,14 @@ def main():
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
 
     # ---- batched watersheds and serving (N = 1 only) ----
-    batched = serving = flux = land = None
+    batched = serving = flux = land = solve = None
     if rank == 0 and world == 1:
         g.close()
+        if args.solve_hours > 0:
+            try:
+                solve = bench_solve(ws, args.solve_hours)
+            except Exception as exc:
+                solve = {"error": repr(exc)}
         if not args.no_land:
             try:
                 land = bench_land(ws)
@@ -695,6 +737,7 @@ def main():
             "serving": serving,
             "flux_pihm": flux,
             "land_surface": land,
+            "solve": solve,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
