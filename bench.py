@@ -513,7 +513,7 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving leg")
     ap.add_argument("--no-flux", action="store_true", help="skip the Flux-PIHM leg")
     ap.add_argument("--no-land", action="store_true", help="skip the land-surface leg")
-    ap.add_argument("--solve-hours", type=float, default=6.0,
+    ap.add_argument("--solve-hours", type=float, default=0.5,
                     help="simulated hours of the 1M-element solve leg (0 skips it)")
     args = ap.parse_args()
     globals()["NELEM"], globals()["NRIVER"] = args.nelem, args.nriver
