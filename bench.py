@@ -421,14 +421,33 @@ def bench_solve(ws, hours):
     outlet = int(np.where(np.asarray(ws.arrays["down"]) < 0)[0][0])
     torch.cuda.synchronize()
     t = time.perf_counter()
-    r = run_steps(m, StepControl(), nsteps, m.set_forcing, outlet=outlet)
+    r = run_steps(m, StepControl(), nsteps, m.set_forcing, outlet=outlet, record_every=nsteps)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t
     m.close()
     st = r["stats"]
     evals = int(st.nfe + st.nfes)
+    # the same solve as a batch of one in the batch engine (each round's
+    # vector operations fused per watershed, bit-identical to the plain path)
+    engine = None
+    try:
+        from pihm_gpu.batch import Batch, limits_for
+        b = Batch(limits_for([ws], nsteps))
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        i = b.add(ws, W.relax_state(ws), StepControl(), pcp, edir, ett, outlet=outlet)
+        b.step()
+        res = b.result(i)
+        torch.cuda.synchronize()
+        ewall = time.perf_counter() - t
+        b.close()
+        engine = {"wall_s": ewall, "value": ws.nelem * evals / ewall,
+                  "bit_identical_to_plain_path": bool(np.array_equal(res["y"], r["states"][-1]) and
+                                                      np.array_equal(res["outlet"], r["outlet"]))}
+    except Exception as exc:
+        engine = {"error": repr(exc)}
     return {"metric": "solve: RHS element-evals/s inside the solve", "unit": "elem-evals/s",
-            "value": ws.nelem * evals / wall,
+            "value": ws.nelem * evals / wall, "batch_engine": engine,
             "workload": f"{ws.nelem} elements, {ws.nriver} segments, {nsteps} model steps of 60 s "
                         f"({hours} simulated hours) from RelaxIc, hourly synthetic forcing, reltol 1e-4",
             "wall_s": wall, "simulated_hours_per_wall_hour": hours * 3600.0 / wall,
