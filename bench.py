@@ -424,6 +424,21 @@ def bench_solve(ws, hours):
     r = run_steps(m, StepControl(), nsteps, m.set_forcing, outlet=outlet, record_every=nsteps)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t
+    # the right-hand side's own device time in a repeat of the first model
+    # steps with per-kernel events (not part of the timed solve)
+    rhs_ms = None
+    try:
+        m2 = GpuWatershed(ws, W.relax_state(ws), pcp, edir, ett)
+        m2.g.set_diagnostics(False)
+        m2.g.set_profiling(True)
+        k2 = min(nsteps, 10)
+        r2 = run_steps(m2, StepControl(), k2, m2.set_forcing)
+        kt = m2.g.kernel_times()
+        rhs_ms = {"model_steps": k2, "rhs_evals": int(r2["stats"].nfe + r2["stats"].nfes),
+                  "kernel_ms": {k: v[0] for k, v in kt.items()}}
+        m2.close()
+    except Exception as exc:
+        rhs_ms = {"error": repr(exc)}
     m.close()
     st = r["stats"]
     evals = int(st.nfe + st.nfes)
@@ -447,7 +462,7 @@ def bench_solve(ws, hours):
     except Exception as exc:
         engine = {"error": repr(exc)}
     return {"metric": "solve: RHS element-evals/s inside the solve", "unit": "elem-evals/s",
-            "value": ws.nelem * evals / wall, "batch_engine": engine,
+            "value": ws.nelem * evals / wall, "batch_engine": engine, "rhs_device_time": rhs_ms,
             "workload": f"{ws.nelem} elements, {ws.nriver} segments, {nsteps} model steps of 60 s "
                         f"({hours} simulated hours) from RelaxIc, hourly synthetic forcing, reltol 1e-4",
             "wall_s": wall, "simulated_hours_per_wall_hour": hours * 3600.0 / wall,
