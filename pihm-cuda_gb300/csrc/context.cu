@@ -404,19 +404,19 @@ int pihm_gpu_status(pihm_gpu_ctx *c) {
 int pihm_gpu_rhs_host(pihm_gpu_ctx *c, double t, const double *y_host, double *ydot_host) {
   if (!c || !y_host || !ydot_host) return PIHM_GPU_ERR_ARG;
   const size_t bytes = sizeof(double) * c->neq;
-  // direct: the reordering kernels read y from and write ydot to host memory
-  // over the host link, in reference order (contiguous on the host side)
+  // direct: k_elem_prep reads y from and the reordering kernel writes ydot to
+  // host memory over the host link, in reference order (contiguous on the
+  // host side)
   const double *y_dev = c->host_path == 0 ? (const double *)host_view(c, y_host, bytes) : nullptr;
   double *yd_dev = y_dev ? (double *)host_view(c, ydot_host, bytes) : nullptr;
   c->last_direct = yd_dev != nullptr;
   if (yd_dev) {
+    // k_elem_prep reads the state from host memory in reference order and
+    // fills y_int itself
     double *y_int = c->d_stage_out, *ydot_int = c->d_stage_in;
-    cudaError_t e = launch_permute_ref(y_dev, y_int, c->d_iperm, c->ne, c->nr, 1, c->stream);
-    c->launches++;
-    if (e == cudaSuccess) {
-      c->m.diag = c->diag;
-      e = launch_rhs(c->m, y_int, ydot_int, c->stream, &c->launches, c->prof, &c->side);
-    }
+    c->m.diag = c->diag;
+    cudaError_t e = launch_rhs(c->m, y_int, ydot_int, c->stream, &c->launches, c->prof, &c->side, y_dev,
+                               c->d_iperm);
     if (e == cudaSuccess) {
       e = launch_permute_ref(ydot_int, yd_dev, c->d_iperm, c->ne, c->nr, 0, c->stream);
       c->launches++;
@@ -424,15 +424,14 @@ int pihm_gpu_rhs_host(pihm_gpu_ctx *c, double t, const double *y_host, double *y
     if (e != cudaSuccess) return PIHM_GPU_ERR_CUDA;
     return pihm_gpu_status(c);
   }
+  // copy, then k_elem_prep reorders while preparing (the right-hand side
+  // writes ydot over the reference-order copy once it has been read)
   cudaError_t e = cudaMemcpyAsync(c->d_stage_in, y_host, bytes, cudaMemcpyHostToDevice, c->stream);
-  if (e == cudaSuccess) {
-    e = launch_permute(c->d_stage_in, c->d_stage_out, c->d_perm, c->ne, c->nr, 1, c->stream);
-    c->launches++;
-  }
   double *y_int = c->d_stage_out, *ydot_int = c->d_stage_in;
   if (e == cudaSuccess) {
     c->m.diag = c->diag;
-    e = launch_rhs(c->m, y_int, ydot_int, c->stream, &c->launches, c->prof, &c->side);
+    e = launch_rhs(c->m, y_int, ydot_int, c->stream, &c->launches, c->prof, &c->side, c->d_stage_in,
+                   c->d_iperm);
   }
   if (e == cudaSuccess) {
     e = launch_permute(ydot_int, c->d_stage_out, c->d_perm, c->ne, c->nr, 0, c->stream);

@@ -195,8 +195,11 @@ inline cudaError_t create_rhs_streams(RhsStreams *s) {
   return e;
 }
 
+// y_ref, iperm (host-buffer evaluation of a single watershed): the state in
+// reference order, read by k_elem_prep, which fills y (internal order) from it.
 cudaError_t launch_rhs(const DevMesh &m, const double *y, double *ydot, cudaStream_t st,
-                       long long *launches, Profiler *prof, const RhsStreams *side = nullptr);
+                       long long *launches, Profiler *prof, const RhsStreams *side = nullptr,
+                       const double *y_ref = nullptr, const int32_t *iperm = nullptr);
 
 }  // namespace pihm
 

@@ -167,7 +167,17 @@ __device__ __forceinline__ int queue_slot(int *count, bool take) {
 // ---------------------------------------------------------------------------
 constexpr int kPrepBlock = 256;
 
-__global__ void __launch_bounds__(kPrepBlock) k_elem_prep(DevMesh m, const double *RESTRICT y) {
+//
+// kFromRef: the host-buffer evaluation, where the state arrives in reference
+// order in memory the device reads over the host link.  Thread r then takes
+// reference element r (the link read is contiguous), stores its three values
+// at the element's internal position in y_int and prepares that element; the
+// threads past the elements copy the river values.  This replaces a separate
+// reordering pass, and the preparation runs under the transfer.
+template <bool kFromRef>
+__global__ void __launch_bounds__(kPrepBlock) k_elem_prep(DevMesh m, const double *RESTRICT y,
+                                                          const double *RESTRICT y_ref, double *RESTRICT y_int,
+                                                          const int32_t *RESTRICT iperm) {
   __shared__ int qs_i[kPrepBlock], qd_i[kPrepBlock];
   __shared__ double qs_x[kPrepBlock], qd_num[kPrepBlock], qd_den[kPrepBlock];
   __shared__ int qs_n, qd_n;
@@ -176,13 +186,37 @@ __global__ void __launch_bounds__(kPrepBlock) k_elem_prep(DevMesh m, const doubl
     qd_n = 0;
   }
   __syncthreads();
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  int sy;
+  const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = t0;
+  double y_surf = 0.0, y_gw = 0.0;
+  bool elem;
+  int sy = 0;
+  if (kFromRef) {
+    const int ne = m.ne;
+    elem = t0 < ne;
+    if (elem) {
+      i = iperm[t0];
+      y_surf = y_ref[t0];
+      const double u = y_ref[ne + t0];
+      y_gw = y_ref[2 * ne + t0];
+      y_int[i] = y_surf;
+      y_int[ne + i] = u;
+      y_int[2 * ne + i] = y_gw;
+    } else if (t0 < ne + 2 * m.nr) {
+      y_int[2 * ne + t0] = y_ref[2 * ne + t0];  // stage and river gw, same order
+    }
+  } else {
+    elem = i < m.ne_run && !skip_item(m, m.sys_elem, i, &sy);
+    if (elem) {
+      y_surf = y[i];
+      y_gw = y[2 * m.ne + i];
+    }
+  }
   bool thin = false, mix = false;
   double sx = 0.0, num = 0.0, den = 0.0;
-  if (i < m.ne_run && !skip_item(m, m.sys_elem, i, &sy)) {
+  if (elem) {
     // SurfH, src/hydrol.c:100-134
-    const double surfeqv = clamp0(y[i]);
+    const double surfeqv = clamp0(y_surf);
     if (cmp::lt0(surfeqv)) {
       m.surfh[i] = 0.0;
       m.head[i] = 0.0 + m.zmax[i];
@@ -197,7 +231,7 @@ __global__ void __launch_bounds__(kPrepBlock) k_elem_prep(DevMesh m, const doubl
     // EffKh, src/lat_flow.c:248-277, with k1 = kmach*areafv + ksath*(1-areafv)
     // and depth - dmac formed at load (the reference evaluates both inline
     // with the same operations)
-    double gw = clamp0(y[2 * m.ne + i]);
+    double gw = clamp0(y_gw);
     gw = cmp::gt0(gw) ? gw : 0.0;
     const double d_dmac = m.d_dmac[i];
     if (cmp::gt_v(gw, d_dmac)) {
@@ -974,7 +1008,8 @@ static void prof_end(Profiler *p, bool on, cudaStream_t st) {
 }
 
 cudaError_t launch_rhs(const DevMesh &m, const double *y, double *ydot, cudaStream_t st,
-                       long long *launches, Profiler *prof, const RhsStreams *side) {
+                       long long *launches, Profiler *prof, const RhsStreams *side, const double *y_ref,
+                       const int32_t *iperm) {
   bool on;
   // the river kernel reads only k_elem_prep's outputs, the state and static
   // data, so with a side stream it runs beside grad/edge/main (per-kernel
@@ -982,7 +1017,11 @@ cudaError_t launch_rhs(const DevMesh &m, const double *y, double *ydot, cudaStre
   const bool fork = side && side->side && !prof && m.ne_run > 0 && m.nr_run > 0;
   if (m.ne_run > 0) {
     on = prof_begin(prof, K_PREP, st);
-    k_elem_prep<<<blocks_for(m.ne_run, kPrepBlock), kPrepBlock, 0, st>>>(m, y);
+    if (y_ref)  // y is the internal-order buffer the kernel fills
+      k_elem_prep<true><<<blocks_for((long long)m.ne + 2LL * m.nr, kPrepBlock), kPrepBlock, 0, st>>>(
+          m, nullptr, y_ref, const_cast<double *>(y), iperm);
+    else
+      k_elem_prep<false><<<blocks_for(m.ne_run, kPrepBlock), kPrepBlock, 0, st>>>(m, y, nullptr, nullptr, nullptr);
     prof_end(prof, on, st);
     ++*launches;
     if (fork) {
