@@ -666,7 +666,7 @@ def main():
     e2e_copy_value = time_e2e(1)
     e2e_value = time_e2e(0)
     direct, pageable = g.host_path_info()
-    host_path = ("direct: the reordering kernels read y from and write ydot to pinned host memory"
+    host_path = ("direct: k_elem_prep reads y from and the reordering kernel writes ydot to pinned host memory"
                  if direct else "copy through device staging") + (
                  "; the device can access pageable host memory" if pageable else "")
     bytes_state = ws.neq * 8
