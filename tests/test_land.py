@@ -207,3 +207,34 @@ def test_hot_start_restores_canopy_and_snow(tmp_path):
     assert np.array_equal(y_ref, y)
     assert np.array_equal(got_c, ref.export("cmc", ne)) and np.array_equal(got_c, cmc)
     assert np.array_equal(got_s, ref.export("sneqv", ne)) and np.array_equal(got_s, sneqv)
+
+
+def test_malformed_forcing_files(tmp_path):
+    """A missing .meteo, a record cut short and an element naming a station
+    the file does not hold come back as errors naming the file (the reference
+    exits there)."""
+    _have_lib()
+    from pihm_gpu import deck as D
+    path = land_deck(str(tmp_path))
+    meteo = os.path.join(path, "gen.meteo")
+    text = open(meteo).read()
+    os.remove(meteo)
+    with pytest.raises(D.DeckError) as e:
+        D.Deck.read(path, "gen")
+    assert e.value.code == -20 and "gen.meteo" in str(e.value)
+    lines = text.splitlines()
+    lines[5] = " ".join(lines[5].split()[:5])  # a record with three of its seven values
+    open(meteo, "w").write("\n".join(lines) + "\n")
+    with pytest.raises(D.DeckError) as e:
+        D.Deck.read(path, "gen")
+    assert e.value.code == -21 and "gen.meteo" in str(e.value) and "line 6" in str(e.value)
+    open(meteo, "w").write(text)
+    att = os.path.join(path, "gen.att")
+    rows = open(att).read().splitlines()
+    f = rows[1].split()
+    f[4] = "99"  # METEO column: a station the file does not hold
+    rows[1] = " ".join(f)
+    open(att, "w").write("\n".join(rows) + "\n")
+    with pytest.raises(D.DeckError) as e:
+        D.Deck.read(path, "gen")
+    assert e.value.code == -22 and "station 99" in str(e.value)
