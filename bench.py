@@ -461,8 +461,36 @@ def bench_solve(ws, hours):
                                                       np.array_equal(res["outlet"], r["outlet"]))}
     except Exception as exc:
         engine = {"error": repr(exc)}
+    # the CPU restatements on the host cores (OpenMP right-hand side, the same
+    # integrator over host vectors) on the first model step of the same solve
+    cpu = None
+    try:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        from backends import OracleBackend
+        k1 = 1
+        m1 = GpuWatershed(ws, W.relax_state(ws), pcp, edir, ett)
+        m1.g.set_diagnostics(False)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        r1 = run_steps(m1, StepControl(), k1, m1.set_forcing)
+        torch.cuda.synchronize()
+        g1 = time.perf_counter() - t
+        m1.close()
+        ob = OracleBackend(ws, W.relax_state(ws), pcp, edir, ett, omp=True)
+        t = time.perf_counter()
+        rc1 = run_steps(ob, StepControl(), k1, ob.set_forcing)
+        c1 = time.perf_counter() - t
+        ob.close()
+        cpu = {"sample": f"the first model step ({int(rc1['stats'].nst)} integrator steps, "
+                         f"{int(rc1['stats'].nfe + rc1['stats'].nfes)} evaluations)",
+               "cpu_s": c1, "gpu_s": g1, "speedup": c1 / g1, "cores": os.cpu_count(), "kind": "port",
+               "same_step_count": int(rc1["stats"].nst) == int(r1["stats"].nst)}
+    except Exception as exc:
+        cpu = {"error": repr(exc)}
     return {"metric": "solve: RHS element-evals/s inside the solve", "unit": "elem-evals/s",
             "value": ws.nelem * evals / wall, "batch_engine": engine, "rhs_device_time": rhs_ms,
+            "cpu_baseline": cpu,
             "workload": f"{ws.nelem} elements, {ws.nriver} segments, {nsteps} model steps of 60 s "
                         f"({hours} simulated hours) from RelaxIc, hourly synthetic forcing, reltol 1e-4",
             "wall_s": wall, "simulated_hours_per_wall_hour": hours * 3600.0 / wall,

@@ -26,9 +26,9 @@ def step_forcing(ws, nsteps, stepsize=60, seed=2):
 
 
 class OracleBackend:
-    def __init__(self, ws, y0, pcp, edir, ett):
+    def __init__(self, ws, y0, pcp, edir, ett, omp: bool = False):
         from oracle import Oracle
-        self.model = Oracle(ws)
+        self.model = Oracle(ws, omp=omp)
         lib = self.model.lib
         lib.oracle_nv_make.restype = _VP
         lib.oracle_nv_make.argtypes = [ctypes.c_long, _VP]
