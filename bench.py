@@ -47,6 +47,24 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x: float, world: int, device=None) -> float:
+    """The largest x over the ranks (the slowest rank's time); x itself on one
+    rank.  `device`: where the collective's tensor lives (the GPU under NCCL,
+    the host under gloo)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device or "cpu")
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world: int, units_per_rank: float, ms: float) -> float:
+    """Whole-job throughput of `world` replicas that each processed
+    units_per_rank in at most ms milliseconds (the slowest rank's time)."""
+    return world * units_per_rank / (ms * 1e-3)
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -638,13 +656,9 @@ def main():
     barrier()
     torch.cuda.synchronize()
     launches = g.launch_count() - launches0
-    ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1), world, dev)
     evals = args.steps * STATES_PER_STEP
-    value = world * NELEM * evals / (ms * 1e-3)
+    value = replica_throughput(world, NELEM * evals, ms)
     ms_per_eval = ms / evals
     assert g.status() == 0, "NaN in timed evaluations"
 
@@ -685,12 +699,8 @@ def main():
             e2e_one(k % STATES_PER_STEP)
         e1.record(stream)
         e1.synchronize()
-        ms_ = e0.elapsed_time(e1)
-        if world > 1:
-            t = torch.tensor([ms_], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms_ = float(t.item())
-        return world * NELEM * e2e_evals / (ms_ * 1e-3)
+        ms_ = max_over_ranks(e0.elapsed_time(e1), world, dev)
+        return replica_throughput(world, NELEM * e2e_evals, ms_)
     e2e_copy_value = time_e2e(1)
     e2e_value = time_e2e(0)
     direct, pageable = g.host_path_info()
