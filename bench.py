@@ -3,10 +3,11 @@
 Workload (the configuration the headline metric is quoted on): one synthetic
 watershed of 1,000,000 triangular elements and 30,000 river segments (the
 generator of pihm_gpu.watershed, seed 0), evaluated on 100 perturbed states
-(a wet reference state with every storage jittered x U(0.9, 1.1)).  One
-"step" evaluates the right-hand side on STATES_PER_STEP consecutive states of
-that set; 10 states are 245 MB of y alone, more than the 129 MB L2, so no L2
-flush is needed between evaluations.
+(a wet reference state with every storage jittered x U(0.9, 1.1), seeded per
+state: pihm_gpu.workloads.rhs_state, shared with the reference arm and the
+parity tests).  One "step" evaluates the right-hand side once on every state
+of the set, in order; 100 states are 2.4 GB of y, far more than the 129 MB
+L2, so no L2 flush is needed between evaluations.
 
 Printed (one JSON line, rank 0):
   value     element-evals/s with the states resident in HBM (device pointers,
@@ -17,9 +18,11 @@ Printed (one JSON line, rank 0):
             bandwidth: algorithmic bytes (332 B per element + 184 B per
             segment) / device time of one evaluation
   cpu_baseline  the CPU restatement of the reference ODE() (oracle/, OpenMP
-            build, all host cores) on a bounded sample of the same states
+            build on all host cores, and the 1-thread build) on a bounded
+            sample of the same states
 
-`--impl reference` times that CPU implementation alone as the reference arm.
+`--impl reference` times that CPU implementation alone as the reference arm,
+on the same states in the same order.
 """
 import argparse
 import json
@@ -34,7 +37,8 @@ sys.path.insert(0, os.path.join(ROOT, "pihm-cuda_gb300"))
 
 NELEM, NRIVER = 1_000_000, 30_000
 NSTATES = 100
-STATES_PER_STEP = 10
+STATES_PER_STEP = 100      # a step is one pass over the whole state set
+YDOT_RING = 10             # derivative buffers cycled through
 BYTES_PER_ELEM, BYTES_PER_SEG = 332, 184
 METRIC = "RHS element-evals/s"
 UNIT = "elem-evals/s"
@@ -142,80 +146,109 @@ class ClockSampler:
                 "window_s": round(self.t1 - self.t0, 3)}
 
 
-def cpu_time_oracle(ws, states_host, threads, max_seconds=12.0, min_evals=2):
-    """Time the CPU restatement (test infrastructure) on a bounded sample."""
+def workload_config(world: int) -> dict:
+    """The `config` both arms print (the same workload, so the same dict)."""
+    return {"workload": f"rhs_{NELEM}elem_{NRIVER}seg", "nelem": NELEM, "nriver": NRIVER,
+            "states": NSTATES, "evals_per_step": STATES_PER_STEP,
+            "states_source": "pihm_gpu.workloads.rhs_state(base, k), k = 0..states-1, in order",
+            "l2": "inputs larger than L2 (100 states x 24.5 MB per step)",
+            "parallelism": "replicas" if world > 1 else "single"}
+
+
+def host_cores() -> dict:
+    n = os.cpu_count() or 1
+    try:
+        avail = len(os.sched_getaffinity(0))
+    except Exception:
+        avail = n
+    return {"host_cores": n, "host_cores_available": avail}
+
+
+def cpu_time_oracle(ws, state_of, threads, omp=True, max_seconds=12.0, min_evals=2, max_evals=200):
+    """Time the CPU restatement (test infrastructure) on a bounded sample of
+    the benchmark's states, in order; returns (evaluations, seconds, threads)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import numpy as np
     from oracle import Oracle
-    import pihm_gpu.watershed as W
-    o = Oracle(ws, omp=True, threads=threads)
-    pcpdrp, edir, ett = W.random_forcing(ws, 3)
-    o.set_forcing(pcpdrp, edir, ett)
-    o.set_ws0_surf(states_host[0][:ws.nelem])
-    o.rhs(states_host[0])  # warm
+    from pihm_gpu import workloads as WL
+    o = Oracle(ws, omp=omp, threads=threads if omp else None)
+    o.set_forcing(*WL.rhs_forcing(ws))
+    base = WL.rhs_base_state(ws)
+    o.set_ws0_surf(base[:ws.nelem])
+    pre = [state_of(k) for k in range(min(NSTATES, 4))]
+    o.rhs(pre[0])  # warm
     n = 0
     t0 = time.perf_counter()
     while True:
-        o.rhs(states_host[n % len(states_host)])
+        o.rhs(pre[n % len(pre)])
         n += 1
         el = time.perf_counter() - t0
-        if (el >= max_seconds and n >= min_evals) or n >= 200:
+        if (el >= max_seconds and n >= min_evals) or n >= max_evals:
             break
-    return n, el, o.threads
-
-
-def make_states(ws, n, device):
-    """n jittered copies of the reference state on the device (reference
-    order), x U(0.9, 1.1) per storage, seeded."""
-    import numpy as np
-    import torch
-    import pihm_gpu.watershed as W
-    base = torch.from_numpy(W.reference_state(ws, 1)).to(device)
-    g = torch.Generator(device=device)
-    g.manual_seed(1234)
-    out = torch.empty((n, ws.neq), dtype=torch.float64, device=device)
-    for k in range(n):
-        out[k] = base * (0.9 + 0.2 * torch.rand(ws.neq, generator=g, device=device, dtype=torch.float64))
-    return out
+    thr = o.threads if omp else 1
+    o.close()
+    return n, el, thr
 
 
 def run_reference_arm(args):
-    """CPU implementation of the path on the host cores (bounded sample per
-    step), same workload and metric."""
+    """CPU implementation of the path (the OpenMP restatement of the
+    reference ODE() on all host cores) on the same workload: each step
+    evaluates the same states in the same order as the GPU arm's step (a
+    fixed subsample of them when the whole run would not end within a few
+    minutes), same metric."""
     world, rank, _ = dist_env()
     if rank != 0:
         return
-    import numpy as np
     import pihm_gpu.watershed as W
+    from pihm_gpu import workloads as WL
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
-    ws = W.generate(NELEM, NRIVER, seed=0)
-    base = W.reference_state(ws, 1)
-    states = [W.jitter(base, 100 + k) for k in range(4)]
+    ws = W.generate(NELEM, NRIVER, seed=WL.RHS_SEED)
+    base = WL.rhs_base_state(ws)
+    states = [WL.rhs_state(base, k) for k in range(NSTATES)]
     threads = os.cpu_count() or 1
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     from oracle import Oracle
     o = Oracle(ws, omp=True, threads=threads)
-    pcpdrp, edir, ett = W.random_forcing(ws, 3)
-    o.set_forcing(pcpdrp, edir, ett)
+    o.set_forcing(*WL.rhs_forcing(ws))
     o.set_ws0_surf(base[:ws.nelem])
-    evals_per_step = 2
-    for w in range(args.warmup):
-        o.rhs(states[w % len(states)])
+    # warm-up: one evaluation per warm-up step; it also sizes the sample
+    t0 = time.perf_counter()
+    for w in range(max(1, args.warmup)):
+        o.rhs(states[w % NSTATES])
+    per_eval = (time.perf_counter() - t0) / max(1, args.warmup)
+    budget_s = 180.0
+    stride = 1
+    while args.steps * (STATES_PER_STEP // stride) * per_eval > budget_s and stride < STATES_PER_STEP:
+        stride += 1
+    picked = list(range(0, STATES_PER_STEP, stride))
     t0 = time.perf_counter()
     for s in range(args.steps):
-        for e in range(evals_per_step):
-            o.rhs(states[(s * evals_per_step + e) % len(states)])
+        for e in picked:
+            o.rhs(states[(s * STATES_PER_STEP + e) % NSTATES])
     el = time.perf_counter() - t0
-    value = NELEM * evals_per_step * args.steps / el
+    n_evals = len(picked) * args.steps
+    value = NELEM * n_evals / el
+    cores = o.threads
+    sample = (f"every state of each step ({len(picked)} evaluations of the {NELEM}-element mesh)"
+              if stride == 1 else
+              f"{len(picked)} of each step's {STATES_PER_STEP} states (every {stride}th, in order)")
+    o.close()
+    # the 1-thread build on a bounded sample of the same states
+    serial = None
+    try:
+        n1, el1, _ = cpu_time_oracle(ws, lambda k: states[k], 1, omp=False, max_seconds=8.0, min_evals=2)
+        serial = {"value": NELEM * n1 / el1, "unit": UNIT, "cores": 1, "kind": "port",
+                  "sample": f"{n1} evaluations, {el1:.1f} s, 1-thread build"}
+    except Exception as exc:
+        serial = {"error": repr(exc)}
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": el / args.steps * 1e3 * (STATES_PER_STEP / len(picked)),
+        "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"rhs_{NELEM}elem_{NRIVER}seg", "evals_per_step": evals_per_step,
-                   "nelem": NELEM, "nriver": NRIVER},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": o.threads, "kind": "port",
-                         "sample": f"{evals_per_step} RHS evaluations of the {NELEM}-element mesh per step"},
+        "config": workload_config(1),
+        "cpu_baseline": dict({"value": value, "unit": UNIT, "cores": cores,
+                              "kind": "port", "sample": sample, "serial": serial}, **host_cores()),
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -500,7 +533,8 @@ def bench_solve(ws, hours):
         rc1 = run_steps(ob, StepControl(), k1, ob.set_forcing)
         c1 = time.perf_counter() - t
         ob.close()
-        cpu = {"sample": f"the first model step ({int(rc1['stats'].nst)} integrator steps, "
+        cpu = {"scope": "a sample: the first model step of the solve on both paths, not the whole solve",
+               "sample": f"the first model step ({int(rc1['stats'].nst)} integrator steps, "
                          f"{int(rc1['stats'].nfe + rc1['stats'].nfes)} evaluations)",
                "cpu_s": c1, "gpu_s": g1, "speedup": c1 / g1, "cores": os.cpu_count(), "kind": "port",
                "same_step_count": int(rc1["stats"].nst) == int(r1["stats"].nst)}
@@ -610,28 +644,32 @@ def main():
     dev = torch.device("cuda", local)
 
     import pihm_gpu.watershed as W
+    from pihm_gpu import workloads as WL
     from pihm_gpu.capi import GpuRhs
     t_setup = time.perf_counter()
-    ws = W.generate(NELEM, NRIVER, seed=0)
+    ws = W.generate(NELEM, NRIVER, seed=WL.RHS_SEED)
     stream = torch.cuda.Stream(device=dev)
     g = GpuRhs(ws, stream=stream.cuda_stream)
-    pcpdrp, edir, ett = W.random_forcing(ws, 3)
-    g.set_forcing(pcpdrp, edir, ett)
-    base = W.reference_state(ws, 1)
+    g.set_forcing(*WL.rhs_forcing(ws))
+    base = WL.rhs_base_state(ws)
     g.set_ws0_surf(base[:ws.nelem])
+    # the state set, made on the host (the reference arm evaluates the same
+    # arrays) and moved once into HBM in internal order
     with torch.cuda.stream(stream):
-        ref_states = make_states(ws, NSTATES, dev)            # reference order
-        states = torch.empty_like(ref_states)                  # internal order
+        states = torch.empty((NSTATES, ws.neq), dtype=torch.float64, device=dev)
+        stage = torch.empty(ws.neq, dtype=torch.float64, device=dev)
         for k in range(NSTATES):
-            g.to_internal(ref_states[k].data_ptr(), states[k].data_ptr())
-        ydot = torch.empty((STATES_PER_STEP, ws.neq), dtype=torch.float64, device=dev)
+            stage.copy_(torch.from_numpy(WL.rhs_state(base, k)))
+            g.to_internal(stage.data_ptr(), states[k].data_ptr())
+        ydot = torch.empty((YDOT_RING, ws.neq), dtype=torch.float64, device=dev)
+        del stage
     stream.synchronize()
     setup_s = time.perf_counter() - t_setup
 
     def step(s):
         for e in range(STATES_PER_STEP):
             k = (s * STATES_PER_STEP + e) % NSTATES
-            g.rhs_device(states[k].data_ptr(), ydot[e].data_ptr())
+            g.rhs_device(states[k].data_ptr(), ydot[e % YDOT_RING].data_ptr())
 
     def barrier():
         if world > 1:
@@ -664,8 +702,7 @@ def main():
 
     # ---- per-kernel device time (separate pass, events around each kernel) ----
     g.set_profiling(True)
-    for s in range(2):
-        step(s)
+    step(0)
     kt = g.kernel_times()
     g.set_profiling(False)
     tot = sum(v[0] for v in kt.values())
@@ -673,16 +710,19 @@ def main():
     dominant = max(kernels, key=lambda k: kernels[k]["share"])
 
     # ---- end to end through the host-buffer C-ABI call ----
-    e2e_evals = min(evals, 3 * STATES_PER_STEP)
-    y_host = torch.empty((STATES_PER_STEP, ws.neq), dtype=torch.float64, pin_memory=True)
-    yd_host = torch.empty((STATES_PER_STEP, ws.neq), dtype=torch.float64, pin_memory=True)
-    y_host.copy_(ref_states[:STATES_PER_STEP].cpu())
+    # one step (every state once) per host path; the states in pinned host
+    # memory in reference order, the derivatives into a ring of pinned buffers
+    e2e_evals = STATES_PER_STEP
+    y_host = torch.empty((NSTATES, ws.neq), dtype=torch.float64, pin_memory=True)
+    for k in range(NSTATES):
+        y_host[k].copy_(torch.from_numpy(WL.rhs_state(base, k)))
+    yd_host = torch.empty((YDOT_RING, ws.neq), dtype=torch.float64, pin_memory=True)
     import ctypes
     f64p = ctypes.POINTER(ctypes.c_double)
     lib = g.lib
     def e2e_one(k):
         rc = lib.pihm_gpu_rhs_host(g.h, 0.0, ctypes.cast(y_host[k].data_ptr(), f64p),
-                                   ctypes.cast(yd_host[k].data_ptr(), f64p))
+                                   ctypes.cast(yd_host[k % YDOT_RING].data_ptr(), f64p))
         assert rc == 0, rc
     def time_e2e(mode):
         # mode 0: the library default (direct host access where possible),
@@ -696,7 +736,7 @@ def main():
         torch.cuda.synchronize()
         e0.record(stream)
         for k in range(e2e_evals):
-            e2e_one(k % STATES_PER_STEP)
+            e2e_one(k % NSTATES)
         e1.record(stream)
         e1.synchronize()
         ms_ = max_over_ranks(e0.elapsed_time(e1), world, dev)
@@ -743,14 +783,21 @@ def main():
     # ---- CPU baseline (rank 0, N = 1 only) ----
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        host_states = [ref_states[k].cpu().numpy() for k in range(2)]
+        state_of = lambda k: WL.rhs_state(base, k)  # noqa: E731
         try:
-            n, el, thr = cpu_time_oracle(ws, host_states, os.cpu_count() or 1)
-            cpu = {"value": NELEM * n / el, "unit": UNIT, "cores": thr, "kind": "port",
-                   "sample": f"{n} RHS evaluations of the {NELEM}-element mesh, "
-                             f"{el:.1f} s wall, OpenMP restatement of the reference ODE()"}
+            n, el, thr = cpu_time_oracle(ws, state_of, os.cpu_count() or 1)
+            cpu = dict({"value": NELEM * n / el, "unit": UNIT, "cores": thr, "kind": "port",
+                        "sample": f"{n} RHS evaluations of the {NELEM}-element mesh (the benchmark's first "
+                                  f"states, in order), {el:.1f} s wall, OpenMP restatement of the reference ODE()"},
+                       **host_cores())
         except Exception as exc:  # the baseline is reported, never required
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
+        try:
+            n1, el1, _ = cpu_time_oracle(ws, state_of, 1, omp=False, max_seconds=8.0)
+            cpu["serial"] = {"value": NELEM * n1 / el1, "unit": UNIT, "cores": 1, "kind": "port",
+                             "sample": f"{n1} RHS evaluations, {el1:.1f} s wall, 1-thread build of the restatement"}
+        except Exception as exc:
+            cpu["serial"] = {"error": repr(exc)}
 
     # ---- batched watersheds and serving (N = 1 only) ----
     batched = serving = flux = land = solve = None
@@ -788,10 +835,7 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"rhs_{NELEM}elem_{NRIVER}seg", "nelem": NELEM, "nriver": NRIVER,
-                       "states": NSTATES, "evals_per_step": STATES_PER_STEP,
-                       "l2": "inputs larger than L2 (10 states x 24.5 MB per step)",
-                       "parallelism": "replicas" if world > 1 else "single"},
+            "config": workload_config(world),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "peak_kind": peak_kind, "scope": "one RHS evaluation (all its kernels)",

@@ -1,4 +1,9 @@
 /*
+ * Derived from SUNDIALS 2.7.0 (nvector_serial.c). Copyright (c) 2002-2016,
+ * Lawrence Livermore National Security; produced at the Lawrence Livermore
+ * National Laboratory. Redistributed under the SUNDIALS BSD-3 licence: its
+ * full text, conditions and disclaimer are in pihm-cuda_gb300/NOTICE.SUNDIALS.
+ *
  * nvector_host.c -- host N_Vector restating the SUNDIALS 2.7 serial N_Vector
  * (cvode/src/nvec_ser/nvector_serial.c:421-1060 of the reference tree):
  * the same case analysis in N_VLinearSum and N_VScale and left-to-right

@@ -43,6 +43,20 @@ def ref_available() -> bool:
     return os.path.exists(os.path.join(HERE, "_ref", "libpihm_ref.so"))
 
 
+def reference_src() -> str | None:
+    """The reference checkout: $PIHM_REFERENCE_SRC, else the one the
+    reference harness was built from (_ref/REFERENCE_SRC, written by
+    `make ref`); None when neither names an existing directory."""
+    cand = os.environ.get("PIHM_REFERENCE_SRC")
+    if not cand:
+        try:
+            with open(os.path.join(HERE, "_ref", "REFERENCE_SRC")) as f:
+                cand = f.read().strip()
+        except OSError:
+            cand = None
+    return cand if cand and os.path.isdir(cand) else None
+
+
 def _lib(path: str) -> ctypes.CDLL:
     if not os.path.exists(path):
         build()
@@ -77,10 +91,12 @@ class Oracle:
         self.h = lib.oracle_create(ctypes.byref(self.desc), ws.surf_mode,
                                    ws.riv_mode, ws.stepsize)
 
-    def __del__(self):
+    def close(self):
         if getattr(self, "h", None):
             self.lib.oracle_destroy(self.h)
             self.h = None
+
+    __del__ = close
 
     @property
     def threads(self) -> int:

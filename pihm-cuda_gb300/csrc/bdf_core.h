@@ -1,3 +1,9 @@
+// Derived from SUNDIALS 2.7.0 (CVODE 2.9.0). Copyright (c) 2002-2016,
+// Lawrence Livermore National Security; produced at the Lawrence Livermore
+// National Laboratory (UCRL-CODE-155951). Redistributed under the SUNDIALS
+// BSD-3 licence: its full text, conditions and disclaimer are in
+// pihm-cuda_gb300/NOTICE.SUNDIALS.
+//
 // Variable-order BDF integrator with Newton iteration and unpreconditioned
 // GMRES, restating the algorithm of CVODE 2.9.0 (SUNDIALS 2.7.0) as PIHM
 // configures it (src/ode.c:413-529: CV_BDF, CV_NEWTON, scalar tolerances,

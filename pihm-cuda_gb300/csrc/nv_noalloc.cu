@@ -119,6 +119,15 @@ extern "C" int pihm_gpu_nv_wrms_norm_noalloc(const double *x, const double *w, i
   // the ticket must start at zero (a call that failed midway may have left it set)
   if (cudaMemsetAsync(ws + kNoAllocMaxBlocks, 0, sizeof(unsigned int), st) != cudaSuccess) return -2;
   const unsigned grid = (unsigned)((n + kNoAllocChunk - 1) / kNoAllocChunk);
-  k_wrms_static<<<grid, kThreads, 0, st>>>(n, x, w, ws, result_dev);
-  return cudaGetLastError() == cudaSuccess ? 0 : -2;
+  // cudaLaunchKernel returns this launch's own status, so an error left on
+  // the thread by some earlier, unrelated call is neither blamed on this one
+  // nor taken from its owner; only an error of this launch is cleared.
+  long long n_arg = n;
+  void *args[] = {&n_arg, (void *)&x, (void *)&w, &ws, &result_dev};
+  const cudaError_t e = cudaLaunchKernel((const void *)k_wrms_static, dim3(grid), dim3(kThreads), args, 0, st);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    return -2;
+  }
+  return 0;
 }

@@ -1,3 +1,9 @@
+// Derived from SUNDIALS 2.7.0 (CVODE 2.9.0). Copyright (c) 2002-2016,
+// Lawrence Livermore National Security; produced at the Lawrence Livermore
+// National Laboratory (UCRL-CODE-155951). Redistributed under the SUNDIALS
+// BSD-3 licence: its full text, conditions and disclaimer are in
+// pihm-cuda_gb300/NOTICE.SUNDIALS.
+//
 // Host- and device-side description of the N_Vector operations shared by the
 // single-vector kernels (nvector.cu) and the batch engine (batch.cpp,
 // batch_kernels.cu): operation codes, reduction sizes and the serial

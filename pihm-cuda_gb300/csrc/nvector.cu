@@ -1,3 +1,9 @@
+// Derived from SUNDIALS 2.7.0 (CVODE 2.9.0). Copyright (c) 2002-2016,
+// Lawrence Livermore National Security; produced at the Lawrence Livermore
+// National Laboratory (UCRL-CODE-155951). Redistributed under the SUNDIALS
+// BSD-3 licence: its full text, conditions and disclaimer are in
+// pihm-cuda_gb300/NOTICE.SUNDIALS.
+//
 // Device-resident N_Vector (SUNDIALS 2.7 / CVODE 2.9 operations table) for
 // sm_103a.  See include/pihm_nvector.h for the contract.
 //

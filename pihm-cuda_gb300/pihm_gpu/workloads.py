@@ -29,6 +29,28 @@ def river_count(nelem: int) -> int:
     return max(4, int(round(100 * (nelem / 1000.0) ** 0.826)))
 
 
+# The right-hand-side benchmark: one 1,000,000-element / 30,000-segment
+# watershed (generator seed 0) evaluated on 100 perturbed states.
+RHS_NELEM, RHS_NRIVER, RHS_SEED, RHS_NSTATES = 1_000_000, 30_000, 0, 100
+
+
+def rhs_base_state(ws) -> np.ndarray:
+    """The wet reference state the benchmark's states perturb (reference order)."""
+    return W.reference_state(ws, 1)
+
+
+def rhs_state(base: np.ndarray, k: int) -> np.ndarray:
+    """State k of the benchmark set: every storage of `base` x U(0.9, 1.1),
+    seeded by k, so every user of the set (both benchmark arms, the parity
+    tests) evaluates the same numbers."""
+    return W.jitter(base, 100 + int(k))
+
+
+def rhs_forcing(ws):
+    """The benchmark's forcing (pcpdrp, edir, ett) and ws0.surf."""
+    return W.random_forcing(ws, 3)
+
+
 def log_uniform_sizes(n: int, lo: int, hi: int, seed: int) -> np.ndarray:
     rng = np.random.default_rng(seed)
     return np.exp(rng.uniform(np.log(lo), np.log(hi), n)).astype(np.int64)

@@ -10,7 +10,16 @@ import pytest
 import pihm_gpu.watershed as W
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-REF_EXAMPLE = "/root/reference/benchmark/input"
+
+
+def _example_dir():
+    """benchmark/input of the reference checkout ($PIHM_REFERENCE_SRC, or the
+    one the reference harness was built from); skips when there is none."""
+    import oracle
+    src = oracle.reference_src()
+    if src is None or not os.path.isdir(os.path.join(src, "benchmark", "input", "example")):
+        pytest.skip("the reference's example deck is not here")
+    return os.path.join(src, "benchmark", "input")
 
 
 def _deck_mod():
@@ -73,8 +82,7 @@ def test_bundled_example_deck():
     """The reference's bundled 535-element example (benchmark/input/example)
     against the arrays and initial state its own readers produce
     (tests/golden/example_watershed.npz, example_calls.npz)."""
-    if not os.path.isdir(os.path.join(REF_EXAMPLE, "example")):
-        pytest.skip("the reference's example deck is not here")
+    REF_EXAMPLE = _example_dir()
     deck = _deck_mod()
     d = deck.Deck.read(os.path.join(REF_EXAMPLE, "example"), "example",
                        lc_table=os.path.join(REF_EXAMPLE, "vegprmt.tbl"))

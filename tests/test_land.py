@@ -12,7 +12,16 @@ import pihm_gpu.land as L
 from parity import land_deck, land_states
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-REF_EXAMPLE = "/root/reference/benchmark/input"
+
+
+def _example_dir():
+    """benchmark/input of the reference checkout ($PIHM_REFERENCE_SRC, or the
+    one the reference harness was built from); skips when there is none."""
+    import oracle
+    src = oracle.reference_src()
+    if src is None or not os.path.isdir(os.path.join(src, "benchmark", "input", "example")):
+        pytest.skip("the reference's example deck is not here")
+    return os.path.join(src, "benchmark", "input")
 FIELDS = ("prcp", "pcpdrp", "edir", "ett", "ec", "drip", "cmc", "sneqv")
 
 
@@ -111,8 +120,7 @@ def test_deck_land_matches_reference_initialize(tmp_path):
 
 def test_bundled_example_land_matches_reference():
     _have_lib()
-    if not os.path.isdir(os.path.join(REF_EXAMPLE, "example")):
-        pytest.skip("the reference's example deck is not here")
+    REF_EXAMPLE = _example_dir()
     ref = _ref()
     import oracle
     from pihm_gpu import deck as D
