@@ -259,7 +259,8 @@ int pihm_gpu_set_profiling(pihm_gpu_ctx *ctx, int on);
  * 4 finish, 5 edge, 6 permute; n entries are written. */
 int pihm_gpu_kernel_times(pihm_gpu_ctx *ctx, double *ms, int64_t *calls, int n);
 
-/* Diagnostic: the table-driven pow of the right-hand-side kernels,
+/* Diagnostic: the power of the right-hand-side kernels (the integer-pipe
+ * power, the table-driven FP64 pow outside its ranges),
  * fast[i] = pow(x[i], y[i]), and CUDA's pow into cuda_pow[i] when it is not
  * NULL; device arrays of length n, asynchronous on `stream`.  Used by the
  * tests to measure the error of the fast path. */
@@ -271,6 +272,12 @@ int pihm_gpu_selftest_pow(const double *x, const double *y, double *fast,
  * `stream`. */
 int pihm_gpu_selftest_pow_manning(const double *x, int river, double *out, int64_t n,
                                   void *stream);
+/* Diagnostic: the integer-pipe power alone, out[i] = x[i]^y[i] and ok[i] = 1
+ * where x[i] and y[i] are inside its ranges, ok[i] = 0 elsewhere; device
+ * arrays of length n, asynchronous on `stream`.  The tests compare its bits
+ * with the host build of the same integer arithmetic. */
+int pihm_gpu_selftest_pow_int(const double *x, const double *y, double *out, int32_t *ok,
+                              int64_t n, void *stream);
 
 #ifdef __cplusplus
 }

@@ -28,6 +28,7 @@
 
 #include "fp64_cmp.h"
 #include "fp64_tables.h"
+#include "int_math.cuh"
 
 namespace pihm {
 
@@ -149,82 +150,25 @@ __device__ __forceinline__ double pow_fast(double x, double y) {
 }
 
 // Manning exponents: OverlandFlow's 0.6666667 (src/lat_flow.c:279-283) and
-// the river's 2.0 / 3.0 (src/river_flow.c), as offsets from 2/3:
-// fl(0.6666667) - 2/3 and fl(2/3) - 2/3, exact to 2^-100.
+// the river's 2.0 / 3.0 (src/river_flow.c).
 constexpr double kManningSurf = 0.6666667;
-constexpr double kManningSurfDelta = 0x1.1e54c66aaaaabp-25;
 constexpr double kManningRiv = 2.0 / 3.0;
-constexpr double kManningRivDelta = -0x1.5555555555555p-55;
 
-__device__ __forceinline__ float lg2_approx(float x) {
-  float r;
-  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-  return r;
-}
-__device__ __forceinline__ float ex2_approx(float x) {
-  float r;
-  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-  return r;
+// pow_fast as an out-of-line call: the fallback of pow_any, taken by few
+// lanes, so its code and registers stay out of the callers
+static __device__ __noinline__ double pow_slow(double x, double y) { return pow_fast(x, y); }
+
+// x^y: the integer-pipe power (int_math.cuh) where x and y are inside its
+// ranges -- every power of the right-hand side's states -- and pow_fast
+// otherwise (x <= 0, subnormal, huge or tiny x, y zero or extreme, results
+// outside about (1e-29, 8e28)).  Both are within 0.502 ulp of the exact
+// power.
+__device__ __forceinline__ double pow_any(double x, double y) {
+  double r;
+  return im::pow_i(x, y, r) ? r : pow_slow(x, y);
 }
 
-// x^p for p = 2/3 + delta with |delta| <= 2^-24 (the Manning exponents), in
-// about 24 FP64 operations instead of pow_fast's 37:
-//
-//   x^p = x * x^(-1/3) * exp(delta ln x)
-//
-//   x^(-1/3): with x = 2^k m, k = 3q + s (s in {0, 1, 2}), a single-precision
-//     estimate r0 = 2^-q 2^(-(s + lg2 m)/3) from lg2/ex2.approx on [1, 2)
-//     and (-1, 0] (relative error about 2^-22; 2^-q goes into the exponent
-//     field exactly), corrected by the binomial series
-//     (1 - e)^(-1/3) = 1 + e/3 + 2e^2/9 + 14e^3/81 + ... with e = 1 - x r0^3;
-//     r0^2 is exact (r0 has 24 significant bits) and r0^3 is carried as an
-//     exact two-product, so e is exact to 2^-100 and the dropped 14e^3/81 is
-//     below 2^-60;
-//   exp(delta ln x) = 1 + v, v = u + u^2/2 + u^3/6, u = delta ln x,
-//     |u| < 2^-17 over the range below (the next term is below 2^-72); ln x
-//     from the 1024-entry log table (|r| <= 2^-11) and log1p(r) to r^3,
-//     absolute error below 2e-14, which moves u by less than 2^-69;
-//   x r0 = ph + pl exactly, and everything else goes into one correction
-//     term: x^p = ph + (pl + ph w), w = (1 + c)(1 + v) - 1.
-//
-// Error: the final rounding (0.5 ulp) plus about 2^-60 relative
-// (tests/test_fp64_math_gpu.py measures it against 60-digit references).
-// x outside [2^-126, 2^127) (zero, subnormal, huge, negative, inf, NaN)
-// goes to pow_fast(x, p).
-__device__ __forceinline__ double pow_manning(double x, double p, double delta) {
-  const long long xb = __double_as_longlong(x);
-  const unsigned hi = (unsigned)((unsigned long long)xb >> 32);
-  const unsigned lo = (unsigned)xb;
-  const unsigned top = hi >> 20;  // sign and exponent
-  if (top - (1023u - 126u) >= 253u) return pow_fast(x, p);
-  const int k = (int)top - 1023;
-  const int q = (k + 384) / 3 - 128;  // floor(k / 3): k + 384 > 0
-  const int s3 = k - 3 * q;
-  // m in [1, 2) truncated to single precision, and r0 = 2^-q 2^y widened
-  // exactly, y = -(s + lg2 m)/3 in (-1, 0]
-  const float mf = __uint_as_float(0x3F800000u | ((hi & 0xFFFFFu) << 3) | (lo >> 29));
-  const float y = -((float)s3 + lg2_approx(mf)) * (1.0f / 3.0f);
-  const unsigned rb = __float_as_uint(ex2_approx(y));
-  const int rhi = (int)((rb >> 3) + ((1023u - 127u) << 20)) - q * (1 << 20);
-  const double r0 = __hiloint2double(rhi, (int)(rb << 29));
-  // e = 1 - x r0^3, with r0^3 = r3h + r3l
-  const double r2 = r0 * r0;
-  const double r3h = r2 * r0;
-  const double r3l = fma(r2, r0, -r3h);
-  const double e = fma(-x, r3l, fma(-x, r3h, 1.0));
-  const double c = e * fma(e, 2.0 / 9.0, 1.0 / 3.0);
-  // ln x = k ln 2 + G_i + log1p(r), r = m F_i - 1
-  const double m = __longlong_as_double((xb & 0x000FFFFFFFFFFFFFLL) | 0x3FF0000000000000LL);
-  const int i = (int)((xb >> (52 - kTableBits)) & ((1 << kTableBits) - 1));
-  const double r = fma(m, __ldg(&kLogF[i]), -1.0);
-  const double lp = fma(fma(r, 1.0 / 3.0, -0.5), r * r, r);
-  const double lnx = fma((double)k, kLn2Hi, __ldg(&kLogGhi[i])) + lp;
-  const double u = delta * lnx;
-  const double v = fma(u, u * fma(u, 1.0 / 6.0, 0.5), u);
-  const double w = fma(c, v, c + v);
-  const double ph = x * r0;
-  const double pl = fma(x, r0, -ph);
-  return ph + fma(ph, w, pl);
-}
+// the Manning powers h^0.6666667 and h^(2/3)
+__device__ __forceinline__ double pow_manning(double x, double p) { return pow_any(x, p); }
 
 }  // namespace pihm

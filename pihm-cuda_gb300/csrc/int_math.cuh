@@ -1,0 +1,185 @@
+// FP64 logarithm, exponential and power evaluated on the integer pipe.
+//
+// GB300 retires 2 FP64 lanes per clock per SM but 64 integer lanes: a
+// warp-wide FP64 instruction holds the SM's FP64 pipe for 16 cycles, an
+// integer instruction for half a cycle.  The right-hand side's powers
+// (van Genuchten's KrFunc and Psi, Manning's h^0.6666667) therefore run
+// here in 64-bit fixed point with 128-bit products, and only their inputs
+// and outputs are doubles.
+//
+// Representation: a base-2 logarithm is carried in units of 1/1024 ("t
+// units"): x^y = 2^(t/1024) with t = y * 1024 log2 x.
+//
+//   log2k(x):  x = 2^k m, m in [1, 2), M = 2^52 m (the 53-bit mantissa);
+//              i = the top 10 fraction bits of m; F_i = round(4096/c_i)/4096,
+//              c_i = 1 + (i + 1/2)/1024 (kImLogF); r = m F_i - 1 is
+//              M F_i - 2^64 in units of 2^-64, exact in wrapping 64-bit
+//              arithmetic (|r| < 2^-10.4); then
+//                1024 log2 x = 1024 k + H_i + (1024/ln 2) log1p(r),
+//              H_i = -1024 log2 F_i (kImLogH), log1p(r) = r + r^2 T(r),
+//              T = -1/2 + r/3 - r^2/4 + r^3/5 (the next term is below
+//              2^-62).  Returned as k and w = (H_i + (1024/ln 2) log1p r)
+//              in units of 2^-53 (|w| < 2^63).
+//   mul_t:     t = y (1024 k + w 2^-53), the 53 x 64-bit product exact in
+//              128 bits, kept as N = round(t) and f = t - N in units of
+//              2^-64 (|t| < 1.5 * 2^16).
+//   exp2k(t):  j = N mod 1024, q = floor(N / 1024), r = f ln2 / 1024
+//              (|r| <= ln2/2048); 2^(t/1024) = 2^q T_j (1 + expm1 r),
+//              T_j = 2^(j/1024) (kImExpT, units of 2^-63), expm1(r) = r +
+//              r^2 E(r), E = 1/2 + r/6 + r^2/24 + r^3/120 (the next term
+//              is below 2^-78); the 64-bit mantissa is rounded to 53 bits.
+//
+// These are the table-driven reductions of P. T. P. Tang ("Table-driven
+// implementation of the exponential function in IEEE floating-point
+// arithmetic", ACM TOMS 15(2) 1989; "... of the logarithm function ...",
+// ACM TOMS 16(4) 1990) carried out in fixed point.  Error budget, relative
+// to the result of a power: w's roundings times |y| (|y| 2^-63.5), the
+// truncation of t (2^-64 t units, 2^-74.5), the exponential's fixed-point
+// error (about 2^-62), then the final rounding to 53 bits: 0.5 ulp plus a
+// few thousandths of an ulp, so the result is the correctly rounded power
+// except within that distance of a rounding boundary.  tests/test_int_math.py checks the bound against 60-digit
+// references on the CPU build of this file (the arithmetic is integer, so
+// the host and the GPU give the same bits; the GPU test checks that).
+//
+// Ranges: log2k wants x positive and normal with |k| <= 126; mul_t wants y
+// normal with exponent in [-20, 29] and |t| < 1.5 * 2^16 (a power in about
+// (1e-29, 8e28)); each returns false otherwise and the caller takes another
+// path.
+#pragma once
+
+#include <cstdint>
+#include <cstring>
+
+#if defined(__CUDACC__)
+#define PIHM_IM_FN __device__ __forceinline__
+#define PIHM_IM_TABLE static __device__ const
+#define PIHM_IM_LD(v) __ldg(&(v))
+#else
+#define PIHM_IM_FN static inline
+#define PIHM_IM_TABLE static const
+#define PIHM_IM_LD(v) (v)
+#endif
+
+#include "int_tables.h"
+
+namespace pihm {
+namespace im {
+
+typedef __int128 i128;
+
+PIHM_IM_FN int64_t mulhi(int64_t a, int64_t b) {
+#if defined(__CUDA_ARCH__)
+  return __mul64hi(a, b);
+#else
+  return (int64_t)(((i128)a * b) >> 64);
+#endif
+}
+
+PIHM_IM_FN uint64_t dbits(double x) {
+#if defined(__CUDA_ARCH__)
+  return (uint64_t)__double_as_longlong(x);
+#else
+  uint64_t b;
+  std::memcpy(&b, &x, sizeof b);
+  return b;
+#endif
+}
+
+PIHM_IM_FN double bitsd(uint64_t b) {
+#if defined(__CUDA_ARCH__)
+  return __longlong_as_double((long long)b);
+#else
+  double x;
+  std::memcpy(&x, &b, sizeof x);
+  return x;
+#endif
+}
+
+constexpr uint64_t kFrac = 0xFFFFFFFFFFFFFull;
+constexpr int64_t kNMax = 3 * (1ll << 15);  // |t| < 1.5 * 2^16: a normal result
+
+// A value t in t units (1024 log2 of a power) as round(t) and the rest in
+// units of 2^-64: t = n + f 2^-64, f in [-2^63, 2^63).
+struct TVal {
+  int64_t n;
+  int64_t f;
+};
+
+// 1024 log2 x = 1024 k + w 2^-53, for x positive and normal with |k| <= 126.
+PIHM_IM_FN bool log2k(double x, int &k, int64_t &w) {
+  const uint64_t xb = dbits(x);
+  const unsigned top = (unsigned)(xb >> 52);  // sign and biased exponent
+  if (top - 897u >= 253u) return false;       // not positive, or |k| > 126
+  k = (int)top - 1023;
+  const uint64_t M = (xb & kFrac) | (1ull << 52);
+  const unsigned i = (unsigned)(xb >> 42) & 1023u;
+  // r 2^64 = M F_i - 2^64: the low 64 bits of the product, read as signed
+  const int64_t R = (int64_t)(M * (uint64_t)PIHM_IM_LD(kImLogF[i]));
+  const int64_t r = R * 256;  // r 2^72, |r 2^72| < 2^61.6
+  int64_t h = kImL5;          // T(r) 2^62 by Horner's rule
+  h = kImL4 + (mulhi(h, r) >> 8);
+  h = kImL3 + (mulhi(h, r) >> 8);
+  h = kImL2 + (mulhi(h, r) >> 8);
+  const int64_t r2 = mulhi(r, r);               // r^2 2^80
+  const int64_t lp = r + (mulhi(r2, h) >> 6);   // log1p(r) 2^72
+  w = PIHM_IM_LD(kImLogH[i]) + ((mulhi(lp, kImK) + 64) >> 7);
+  return true;
+}
+
+// t = y (1024 k + w 2^-53) for y normal with exponent in [-20, 29] and
+// |t| < 1.5 * 2^16; false otherwise
+PIHM_IM_FN bool mul_t(double y, int k, int64_t w, TVal &t) {
+  const uint64_t yb = dbits(y);
+  const int ey = (int)((yb >> 52) & 2047u) - 1023;
+  if ((unsigned)(ey + 20) >= 50u) return false;
+  const int64_t my = (int64_t)((yb & kFrac) | (1ull << 52));
+  // Q = My (k 2^63 + w) exactly (|My k| < 2^60, |My w| < 2^116); y =
+  // My 2^(ey - 52) and 1024 k + w 2^-53 = (k 2^63 + w) 2^-53, so
+  // t 2^64 = Q 2^(ey - 41), a right shift by 12..61
+  i128 Q = (i128)my * w + ((i128)(my * k) << 63);
+  Q >>= 41 - ey;
+  if (yb >> 63) Q = -Q;
+  const int64_t hi = (int64_t)(Q >> 64);
+  const uint64_t lo = (uint64_t)Q;
+  t.n = hi + (int64_t)(lo >> 63);  // round(t)
+  t.f = (int64_t)lo;               // t - round(t), units of 2^-64
+  return t.n < kNMax && t.n > -kNMax;
+}
+
+// 2^(t/1024) for |t| < 1.5 * 2^16: a normal double
+PIHM_IM_FN double exp2k(TVal t) {
+  const unsigned j = (unsigned)t.n & 1023u;
+  int q = (int)(t.n >> 10);
+  const int64_t r = mulhi(t.f, kImLn2) >> 1;   // f ln2 / 1024 in units of 2^-72
+  int64_t h = kImE120;                         // E(r) 2^62
+  h = kImE24 + (mulhi(h, r) >> 8);
+  h = kImE6 + (mulhi(h, r) >> 8);
+  h = kImE2 + (mulhi(h, r) >> 8);
+  const int64_t r2 = mulhi(r, r);              // r^2 2^80
+  const int64_t e = r + (mulhi(r2, h) >> 6);   // expm1(r) 2^72
+  const uint64_t T = PIHM_IM_LD(kImExpT[j]);   // 2^(j/1024) 2^63
+  uint64_t res = T + (uint64_t)(mulhi((int64_t)(T >> 1), e) >> 7);  // 2^63 T (1 + e)
+  if (!(res >> 63)) {  // below 1 (j = 0, e < 0)
+    res <<= 1;
+    q -= 1;
+  }
+  uint64_t mant = (res >> 11) + ((res >> 10) & 1u);
+  if (mant >> 53) {
+    mant >>= 1;
+    q += 1;
+  }
+  return bitsd(((uint64_t)(q + 1023) << 52) + (mant & kFrac));
+}
+
+// x^y on the integer path; false when x or y is outside its ranges
+PIHM_IM_FN bool pow_i(double x, double y, double &out) {
+  int k;
+  int64_t w;
+  TVal t;
+  if (!log2k(x, k, w) || !mul_t(y, k, w, t)) return false;
+  out = exp2k(t);
+  return true;
+}
+
+}  // namespace im
+}  // namespace pihm

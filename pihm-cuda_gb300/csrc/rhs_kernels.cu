@@ -68,67 +68,28 @@ __device__ __forceinline__ double avg_h_surf(double diff, double hsurf, double h
 // OverLandFlow, src/lat_flow.c:279-283
 __device__ __forceinline__ double overland_flow(double avg_h, double grad_h, double avg_sf,
                                                 double crossa, double avg_rough) {
-  return crossa * pow_manning(avg_h, kManningSurf, kManningSurfDelta) * grad_h /
+  return crossa * pow_manning(avg_h, kManningSurf) * grad_h /
          (sqrt(avg_sf) * avg_rough);
 }
 
-// Below this 1 - satn^m, Psi follows the reference's operations (kr_psi).
-constexpr double kPsiNearSat = 1e-3;
-
 // KrFunc (src/soil.c:8-13) and Psi (src/vert_flow.c:272-278) of one
-// saturation in [SATMIN, 1], sharing one logarithm of satn:
-//   x1 = satn^m = exp(z), z = m ln satn (a double-double), a = 1 - x1,
-//   KrFunc = sqrt(satn) (1 - a^e)^2,
-//   Psi = -((1/satn)^m - 1)^ib / alpha = -(a / x1)^ib / alpha
-//       = -exp(ib (ln a - z)) / alpha.
-// The last form takes ln a, which a^e needs anyway, in place of a division
-// and a third logarithm; the difference ln a - z is carried as a
-// double-double, so Psi stays within an ulp of the reference's form while
-// 1 - satn^m >= kPsiNearSat.  Closer to saturation both forms cancel to a
-// few ulps of 1, each with its own rounding, and Psi takes the reference's
-// form pow(pow(1/satn, m) - 1, ib); exactly 0 at satn = 1.
+// saturation in [SATMIN, 1], in the reference's own operations:
+//   KrFunc = sqrt(satn) (1 - (1 - satn^m)^e) (1 - (1 - satn^m)^e),
+//   Psi    = -((1 / satn)^m - 1)^ib / alpha,
+// m = beta/(beta - 1), e = (beta - 1)/beta, ib = 1/beta formed at load as
+// the reference forms them.  Recharge's head gradient 0.5 deficit + Psi and
+// Infil's surfh + zmax - (Psi + zmax - 0.5 dinf) cancel by up to four
+// orders of magnitude near equilibrium, so Psi has to carry the reference's
+// roundings: each power is correctly rounded but for a rare last bit
+// (pow_any), and 1/satn and the division by alpha are IEEE divisions as in
+// the reference.  The powers run on the integer pipe.
 // sq returns sqrt(satn), which EffKinf's macropore branch needs too.
-__device__ __forceinline__ void kr_psi(double satn, double vm, double vg_e, double vg_ib, double inv_alpha,
+__device__ __forceinline__ void kr_psi(double satn, double vm, double vg_e, double vg_ib, double alpha,
                                        double &satkfunc, double &psi, double &sq) {
   sq = sqrt(satn);
-  double lh, ll;
-  if (!log_dd_fast(satn, lh, ll)) {  // not positive and normal (NaN state)
-    const double t = 1.0 - pow_fast(1.0 - pow_fast(satn, vm), vg_e);
-    satkfunc = sq * t * t;
-    psi = -pow_fast(pow_fast(1.0 / satn, vm) - 1.0, vg_ib) * inv_alpha;
-    return;
-  }
-  const double x1 = pow_from_log(satn, lh, ll, vm);  // satn^m, as pow_fast(satn, m)
-  const double a = 1.0 - x1;
-  // a == 0 (satn^m == 1: a full column, where x1 == 1 and a / x1 == a) runs
-  // the table path on a stand-in argument, and its powers of +0 replace the
-  // results below, so that such lanes do not split the warp
-  const bool a0 = cmp::eq0(a);
-  double zh, zl, ah, al;
-  mul_dd(vm, lh, ll, zh, zl);  // the z pow_from_log formed
-  if (!cmp::abs_lt_c(zh, 700.0) || !log_dd_fast(a0 ? 0.5 : a, ah, al)) {
-    // outside the table path's ranges
-    const double t = 1.0 - pow_fast(a, vg_e);
-    satkfunc = sq * t * t;
-    psi = -pow_fast(a / x1, vg_ib) * inv_alpha;
-    return;
-  }
-  double pe = pow_from_log(a, ah, al, vg_e);  // as pow_fast(a, e)
-  double dh, dl, qh, ql, p;
-  sub_dd(ah, al, zh, zl, dh, dl);  // ln(a / x1)
-  mul_dd(vg_ib, dh, dl, qh, ql);
-  if (!exp_dd_checked(qh, ql, p)) p = pow(a / x1, vg_ib);
-  if (a0) {
-    pe = pow_fast(a, vg_e);
-    p = pow_fast(a, vg_ib);
-  } else if (cmp::lt_c(a, kPsiNearSat)) {
-    // near saturation (1/satn)^m - 1 is a few ulps of 1, so its value is set
-    // by the rounding of the reference's own operations: take them
-    p = pow_fast(pow_fast(1.0 / satn, vm) - 1.0, vg_ib);
-  }
-  const double t = 1.0 - pe;
+  const double t = 1.0 - pow_any(1.0 - pow_any(satn, vm), vg_e);
   satkfunc = sq * t * t;
-  psi = -p * inv_alpha;
+  psi = -pow_any(pow_any(1.0 / satn, vm) - 1.0, vg_ib) / alpha;
 }
 
 // Batch engine: whether the watershed of item idx sits out this evaluation
@@ -366,7 +327,7 @@ __global__ void __launch_bounds__(kEdgeBlock) k_edge(DevMesh m, const double *RE
   if (t < q_n) {
     const int qe = q_e[t];
     const double h = q_h[t];
-    m.eflux_ovl[qe] = h * pow_manning(h, kManningSurf, kManningSurfDelta) * q_d[t] * rsqrt(q_sf[t]) *
+    m.eflux_ovl[qe] = h * pow_manning(h, kManningSurf) * q_d[t] * rsqrt(q_sf[t]) *
                       m.e_ovlk[qe];
   }
 }
@@ -467,7 +428,7 @@ __global__ void __launch_bounds__(256, 3) k_elem_main(DevMesh m, const double *R
     satn = unsat / deficit;
     satn = cmp::gt_c(satn, 1.0) ? 1.0 : satn;
     satn = cmp::lt_c(satn, kSatMin) ? kSatMin : satn;
-    kr_psi(satn, m.vg_m[i], m.vg_e[i], m.vg_ib[i], m.inv_alpha[i], satkfunc, psi_u, sq);
+    kr_psi(satn, m.vg_m[i], m.vg_e[i], m.vg_ib[i], m.alpha[i], satkfunc, psi_u, sq);
   }
   // Infil's saturation: the same one, except in Flux-PIHM, where it is
   // Noah's top-layer moisture (src/vert_flow.c:94-98) and Recharge keeps
@@ -478,7 +439,7 @@ __global__ void __launch_bounds__(256, 3) k_elem_main(DevMesh m, const double *R
     s = cmp::gt_c(s, 1.0) ? 1.0 : s;
     s = cmp::lt_c(s, kSatMin) ? kSatMin : s;
     satn_i = s;
-    kr_psi(s, m.vg_m[i], m.vg_e[i], m.vg_ib[i], m.inv_alpha[i], satkfunc_i, psi_i, sq_i);
+    kr_psi(s, m.vg_m[i], m.vg_e[i], m.vg_ib[i], m.alpha[i], satkfunc_i, psi_i, sq_i);
   }
   // KrFunc(beta, 1) == 1 exactly: pow(1 - pow(1, m), e) == pow(0, e) == 0
   double infil;
@@ -820,7 +781,7 @@ __global__ void __launch_bounds__(128) k_river(DevMesh m, const double *RESTRICT
       const double avg_perim = m.r_perim[s];
       const double crossa = m.r_crossa[s];
       q = sqrt(grad_h) * crossa *
-          (cmp::gt0(avg_perim) ? pow_manning(crossa / avg_perim, kManningRiv, kManningRivDelta) : 0.0) /
+          (cmp::gt0(avg_perim) ? pow_manning(crossa / avg_perim, kManningRiv) : 0.0) /
           r.rough;
     } else {  // kCritDpth (other values are rejected at load)
       const double crossa = m.r_crossa[s];

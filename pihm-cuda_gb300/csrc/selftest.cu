@@ -1,4 +1,4 @@
-// Diagnostic entry points: the table-driven pow of the right-hand-side kernels
+// Diagnostic entry points: the power of the right-hand-side kernels (pow_any)
 // next to CUDA's pow, and the Manning-exponent power, element by element, so
 // tests can measure their error.
 #include <cstdint>
@@ -9,15 +9,14 @@ namespace {
 __global__ void k_pow_pair(const double *x, const double *y, double *fast, double *ref, long long n) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  fast[i] = pihm::pow_fast(x[i], y[i]);
+  fast[i] = pihm::pow_any(x[i], y[i]);
   if (ref) ref[i] = pow(x[i], y[i]);
 }
 
 __global__ void k_pow_manning(const double *x, int river, double *out, long long n) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  out[i] = river ? pihm::pow_manning(x[i], pihm::kManningRiv, pihm::kManningRivDelta)
-                 : pihm::pow_manning(x[i], pihm::kManningSurf, pihm::kManningSurfDelta);
+  out[i] = river ? pihm::pow_manning(x[i], pihm::kManningRiv) : pihm::pow_manning(x[i], pihm::kManningSurf);
 }
 }  // namespace
 
@@ -32,5 +31,24 @@ extern "C" int pihm_gpu_selftest_pow_manning(const double *x, int river, double 
                                              void *stream) {
   if (n <= 0 || !x || !out) return -1;
   k_pow_manning<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(x, river, out, n);
+  return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
+
+namespace {
+__global__ void k_pow_int(const double *x, const double *y, double *out, int32_t *ok, long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double r = 0.0;
+  ok[i] = pihm::im::pow_i(x[i], y[i], r) ? 1 : 0;
+  out[i] = r;
+}
+}  // namespace
+
+// The integer-pipe power (int_math.cuh) alone, element by element: out[i] =
+// x[i]^y[i] where ok[i] = 1, ok[i] = 0 where x or y is outside its ranges.
+extern "C" int pihm_gpu_selftest_pow_int(const double *x, const double *y, double *out, int32_t *ok,
+                                         int64_t n, void *stream) {
+  if (n <= 0 || !x || !y || !out || !ok) return -1;
+  k_pow_int<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(x, y, out, ok, n);
   return cudaGetLastError() == cudaSuccess ? 0 : -2;
 }

@@ -1,0 +1,34 @@
+// Host build of the integer-pipe logarithm / exponential / power
+// (pihm-cuda_gb300/csrc/int_math.cuh) for the CPU tests: the arithmetic is
+// integer, so these functions return the bits the GPU kernels compute.
+#include <cstdint>
+
+#include "int_math.cuh"
+
+extern "C" {
+
+// out[i] = x[i]^y[i] on the integer path; ok[i] = 0 where it declines
+void im_pow(const double *x, const double *y, double *out, int32_t *ok, int64_t n) {
+  for (int64_t i = 0; i < n; i++) {
+    double r = 0.0;
+    ok[i] = pihm::im::pow_i(x[i], y[i], r) ? 1 : 0;
+    out[i] = r;
+  }
+}
+
+// 1024 log2 x as (k, w 2^-53)
+void im_log2k(const double *x, int32_t *k, int64_t *w, int32_t *ok, int64_t n) {
+  for (int64_t i = 0; i < n; i++) {
+    int kk = 0;
+    int64_t ww = 0;
+    ok[i] = pihm::im::log2k(x[i], kk, ww) ? 1 : 0;
+    k[i] = kk;
+    w[i] = ww;
+  }
+}
+
+// 2^(t / 1024) for t = tn + tf 2^-64
+void im_exp2k(const int64_t *tn, const int64_t *tf, double *out, int64_t n) {
+  for (int64_t i = 0; i < n; i++) out[i] = pihm::im::exp2k(pihm::im::TVal{tn[i], tf[i]});
+}
+}

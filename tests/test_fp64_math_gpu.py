@@ -102,9 +102,9 @@ def _manning(x, river):
 @pytest.mark.parametrize("river,p", [(0, 0.6666667), (1, 2.0 / 3.0)])
 def test_pow_manning_error_bound(river, p):
     """x^0.6666667 (overland flow) and x^(2/3) (channel flow) through the
-    cube-root path: within 0.6 ulp of the exact power of the double exponent
-    over ponding depths and hydraulic radii, and over the whole range the
-    path covers, [2^-126, 2^127)."""
+    integer-pipe power: within 0.6 ulp of the exact power of the double
+    exponent over ponding depths and hydraulic radii, and over the whole range
+    the path covers, [2^-126, 2^127)."""
     rng = np.random.default_rng(11 + river)
     typical = np.exp(rng.uniform(np.log(1e-9), np.log(1e3), 6000))
     wide = np.exp2(rng.uniform(-126.0, 126.99, 3000))

@@ -1,0 +1,109 @@
+"""The integer-pipe logarithm, exponential and power of the right-hand-side
+kernels (pihm-cuda_gb300/csrc/int_math.cuh).
+
+The arithmetic is integer, so the header compiled for the host
+(tests/int_math_host.cpp) gives the bits the GPU computes: the CPU test
+measures its error against 200-bit references on the argument ranges the
+model produces (van Genuchten powers of saturation and their complements,
+Manning's h^0.6666667) and on wide ranges, and the GPU test checks that the
+device returns the same bits as the host build."""
+import ctypes
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(os.path.dirname(HERE), "pihm-cuda_gb300", "csrc")
+P = ctypes.c_void_p
+
+
+@pytest.fixture(scope="module")
+def host_lib(tmp_path_factory):
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not found")
+    so = str(tmp_path_factory.mktemp("im") / "libim.so")
+    subprocess.run([gxx, "-std=c++17", "-O2", "-fPIC", "-shared", "-I", CSRC,
+                    os.path.join(HERE, "int_math_host.cpp"), "-o", so], check=True)
+    return ctypes.CDLL(so)
+
+
+def host_pow(lib, x, y):
+    x = np.ascontiguousarray(x, np.float64)
+    y = np.ascontiguousarray(y, np.float64)
+    out = np.empty_like(x)
+    ok = np.empty(x.size, np.int32)
+    lib.im_pow(P(x.ctypes.data), P(y.ctypes.data), P(out.ctypes.data), P(ok.ctypes.data),
+               ctypes.c_int64(x.size))
+    return out, ok.astype(bool)
+
+
+def model_cases(rng, n):
+    beta = rng.uniform(1.2, 2.5, n)
+    m = beta / (beta - 1.0)
+    satn = rng.uniform(0.1, 1.0, n)
+    a = np.exp(rng.uniform(np.log(1e-15), 0.0, n))
+    return {
+        "satn^m": (satn, m),
+        "(1/satn)^m": (1.0 / satn, m),
+        "(1-satn^m)^e": (a, (beta - 1.0) / beta),
+        "v^(1/beta)": (np.exp(rng.uniform(np.log(1e-12), np.log(1e4), n)), 1.0 / beta),
+        "h^0.6666667": (np.exp(rng.uniform(np.log(1e-9), np.log(20.0), n)), np.full(n, 0.6666667)),
+        "h^(2/3)": (np.exp(rng.uniform(np.log(1e-6), np.log(50.0), n)), np.full(n, 2.0 / 3.0)),
+        "wide": (np.exp(rng.uniform(-40.0, 40.0, n)), rng.uniform(-3.0, 3.0, n)),
+    }
+
+
+def test_error_against_high_precision_references(host_lib):
+    mpmath = pytest.importorskip("mpmath")
+    mpmath.mp.prec = 200
+    rng = np.random.default_rng(2024)
+    for name, (x, y) in model_cases(rng, 4000).items():
+        got, ok = host_pow(host_lib, x, y)
+        if name != "wide":
+            assert ok.all(), name  # every power of the model takes the integer path
+        worst, misrounded = 0.0, 0
+        for k in np.nonzero(ok)[0]:
+            exact = mpmath.power(mpmath.mpf(float(x[k])), mpmath.mpf(float(y[k])))
+            ulp = np.spacing(abs(float(exact)))
+            err = float(abs(mpmath.mpf(float(got[k])) - exact) / ulp)
+            worst = max(worst, err)
+            misrounded += err > 0.5
+        print(f"{name}: worst {worst:.4f} ulp, {misrounded} of {int(ok.sum())} not correctly rounded")
+        assert worst < 0.502, (name, worst)
+        assert misrounded <= 0.005 * ok.sum(), (name, misrounded)
+
+
+def test_exact_cases_and_declined_arguments(host_lib):
+    x = np.array([1.0, 0.5, 2.0, 4.0, 0.25, 8.0, 1.0, 0.0, -1.0, np.nan, np.inf, 1e-310, 2.0 ** 130, 2.0, 2.0])
+    y = np.array([3.7, 2.0, 10.0, 0.5, -1.5, 1.0 / 3.0, 0.0, 0.5, 0.5, 0.5, 0.5, 0.5, 0.5, 1e-9, 1e12])
+    got, ok = host_pow(host_lib, x, y)
+    assert ok[:6].all()
+    assert list(got[:6]) == [1.0, 0.25, 1024.0, 2.0, 8.0, 2.0]
+    # y = 0, zero, negative, NaN, infinite, subnormal or huge x, tiny or huge
+    # exponents: declined (the kernels use the FP64 path there)
+    assert not ok[6:].any()
+
+
+@pytest.mark.gpu
+def test_device_bits_equal_host_bits(host_lib):
+    import torch
+    from pihm_gpu import capi
+    lib = capi.load()
+    f = lib.pihm_gpu_selftest_pow_int
+    f.argtypes = [P] * 4 + [ctypes.c_int64, P]
+    f.restype = ctypes.c_int
+    rng = np.random.default_rng(77)
+    for name, (x, y) in model_cases(rng, 200_000).items():
+        want, ok_h = host_pow(host_lib, x, y)
+        tx, ty = torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()
+        out = torch.empty_like(tx)
+        ok = torch.empty(x.size, dtype=torch.int32, device="cuda")
+        assert f(tx.data_ptr(), ty.data_ptr(), out.data_ptr(), ok.data_ptr(), x.size, None) == 0
+        torch.cuda.synchronize()
+        assert np.array_equal(ok.cpu().numpy().astype(bool), ok_h), name
+        got = out.cpu().numpy()
+        assert np.array_equal(got[ok_h].view(np.int64), want[ok_h].view(np.int64)), name
