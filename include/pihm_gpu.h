@@ -278,6 +278,13 @@ int pihm_gpu_selftest_pow_manning(const double *x, int river, double *out, int64
  * with the host build of the same integer arithmetic. */
 int pihm_gpu_selftest_pow_int(const double *x, const double *y, double *out, int32_t *ok,
                               int64_t n, void *stream);
+/* Diagnostic: the integer-pipe division and square root alone,
+ * q[i] = a[i] / b[i] and r[i] = sqrt(a[i]); bit 0 of ok[i] is set where the
+ * division took the integer path, bit 1 where the square root did; device
+ * arrays of length n, asynchronous on `stream`.  Where they are taken, both
+ * are the IEEE results bit for bit. */
+int pihm_gpu_selftest_div_sqrt_int(const double *a, const double *b, double *q, double *r,
+                                   int32_t *ok, int64_t n, void *stream);
 
 #ifdef __cplusplus
 }

@@ -168,6 +168,18 @@ __device__ __forceinline__ double pow_any(double x, double y) {
   return im::pow_i(x, y, r) ? r : pow_slow(x, y);
 }
 
+// a / b and sqrt(x), correctly rounded: the integer-pipe paths where the
+// operands and the result are normal, the FP64 instructions otherwise (the
+// same bits either way)
+__device__ __forceinline__ double div_any(double a, double b) {
+  double q;
+  return im::div_i(a, b, q) ? q : a / b;
+}
+__device__ __forceinline__ double sqrt_any(double x) {
+  double r;
+  return im::sqrt_i(x, r) ? r : sqrt(x);
+}
+
 // the Manning powers h^0.6666667 and h^(2/3)
 __device__ __forceinline__ double pow_manning(double x, double p) { return pow_any(x, p); }
 

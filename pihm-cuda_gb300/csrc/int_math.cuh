@@ -47,6 +47,7 @@
 // path.
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 
@@ -178,6 +179,155 @@ PIHM_IM_FN bool pow_i(double x, double y, double &out) {
   TVal t;
   if (!log2k(x, k, w) || !mul_t(y, k, w, t)) return false;
   out = exp2k(t);
+  return true;
+}
+
+
+// ---------------------------------------------------------------------------
+// Division and square root, correctly rounded (round to nearest even), on
+// the integer pipe.  A single-precision reciprocal (or reciprocal square
+// root) of the leading 24 bits seeds two Newton steps in 64-bit fixed point
+// (relative error about 2^-60), which give the 53-bit result to within a
+// small fraction of a unit; an exact 128-bit comparison against the
+// rounding midpoint then decides the last bit.  The results are therefore
+// the IEEE quotient and root bit for bit, whatever the seed's own rounding
+// (the host build seeds with a correctly rounded float, the GPU with
+// rcp.approx / rsqrt.approx).  Operands or results outside the normal range
+// are declined (false) and the caller uses the FP64 instruction.
+// ---------------------------------------------------------------------------
+
+PIHM_IM_FN float rcp_seed(float x) {
+#if defined(__CUDA_ARCH__)
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+#else
+  return 1.0f / x;
+#endif
+}
+
+PIHM_IM_FN float rsqrt_seed(float x) {
+#if defined(__CUDA_ARCH__)
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+#else
+  return 1.0f / std::sqrt(x);
+#endif
+}
+
+PIHM_IM_FN uint64_t umulhi(uint64_t a, uint64_t b) {
+#if defined(__CUDA_ARCH__)
+  return __umul64hi(a, b);
+#else
+  return (uint64_t)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+PIHM_IM_FN uint32_t fbits(float x) {
+#if defined(__CUDA_ARCH__)
+  return __float_as_uint(x);
+#else
+  uint32_t b;
+  std::memcpy(&b, &x, sizeof b);
+  return b;
+#endif
+}
+
+PIHM_IM_FN float bitsf(uint32_t b) {
+#if defined(__CUDA_ARCH__)
+  return __uint_as_float(b);
+#else
+  float x;
+  std::memcpy(&x, &b, sizeof x);
+  return x;
+#endif
+}
+
+// a seed r (a float in (0.25, 1]) as r 2^63, at most 2^63 - 1
+PIHM_IM_FN uint64_t seed_fixed(float r) {
+  const uint32_t rb = fbits(r);
+  const int ex = (int)(rb >> 23) - 127;  // -2 or -1 ... 0
+  const uint64_t m = (uint64_t)((rb & 0x7FFFFFu) | 0x800000u);  // 2^23 (1 + f)
+  const uint64_t v = m << (40 + ex);
+  return v >> 63 ? 0x7FFFFFFFFFFFFFFFull : v;
+}
+
+// q = a / b for normal a, b with a normal quotient
+PIHM_IM_FN bool div_i(double a, double b, double &q) {
+  const uint64_t ab = dbits(a), bb = dbits(b);
+  const unsigned ea = (unsigned)(ab >> 52) & 2047u, eb = (unsigned)(bb >> 52) & 2047u;
+  if (ea - 1u >= 2046u || eb - 1u >= 2046u) return false;  // zero, subnormal, inf, nan
+  const uint64_t Ma = (ab & kFrac) | (1ull << 52), Mb = (bb & kFrac) | (1ull << 52);
+  // 1/mb, mb = Mb 2^-52 in [1, 2): R = r 2^63
+  uint64_t R = seed_fixed(rcp_seed(bitsf(0x3F800000u | (uint32_t)((Mb & kFrac) >> 29))));
+  const uint64_t B = Mb << 11;  // mb 2^63
+#pragma unroll
+  for (int it = 0; it < 2; it++) {
+    // e = 1 - mb r in units of 2^-62; r <- r (1 + e)
+    const int64_t e = (int64_t)((1ull << 62) - umulhi(B, R));
+    R = (uint64_t)((int64_t)R + mulhi((int64_t)R, e) * 4);
+  }
+  // ma r 2^62 in (2^61, 2^63)
+  const uint64_t Q = umulhi(Ma << 11, R);
+  int ex = (int)ea - (int)eb;
+  uint64_t q0;
+  int s;  // quotient bits: a / b = Ma 2^s / Mb in units of the result's ulp
+  if (Q >> 62) {
+    q0 = Q >> 10;
+    s = 52;
+  } else {
+    q0 = Q >> 9;
+    s = 53;
+    ex -= 1;
+  }
+  // the exact quotient against the midpoint q0 + 1/2:
+  //   2 Ma 2^s  vs  (2 q0 + 1) Mb
+  const i128 lhs = (i128)Ma << (s + 1);
+  const i128 rhs = (i128)(2 * q0 + 1) * (i128)Mb;
+  uint64_t mant = q0 + ((lhs > rhs) || (lhs == rhs && (q0 & 1u)));
+  if (mant >> 53) {
+    mant >>= 1;
+    ex += 1;
+  }
+  const int eq = ex + 1023;
+  if (eq < 1 || eq > 2046) return false;
+  q = bitsd((((ab ^ bb) >> 63) << 63) | ((uint64_t)eq << 52) | (mant & kFrac));
+  return true;
+}
+
+// sqrt(x) for positive normal x
+PIHM_IM_FN bool sqrt_i(double x, double &r) {
+  const uint64_t xb = dbits(x);
+  const unsigned top = (unsigned)(xb >> 52);  // sign and biased exponent
+  if (top - 1u >= 2046u) return false;       // not positive and normal
+  const int ex = (int)top - 1023;
+  const int odd = ex & 1;
+  // x = m 2^(ex - odd), m = M 2^-52 in [1, 4)
+  const uint64_t M = ((xb & kFrac) | (1ull << 52)) << odd;
+  const float mf = bitsf((uint32_t)(0x3F800000u + ((uint32_t)odd << 23)) | (uint32_t)((xb & kFrac) >> 29));
+  uint64_t Y = seed_fixed(rsqrt_seed(mf));  // 1/sqrt(m) 2^63
+  const uint64_t Mm = M << 10;               // m 2^62
+#pragma unroll
+  for (int it = 0; it < 2; it++) {
+    // e = 1 - m y^2 in units of 2^-60; y <- y (1 + e / 2)
+    const uint64_t y2 = umulhi(Y, Y);  // y^2 2^62
+    const int64_t e = (int64_t)((1ull << 60) - umulhi(Mm, y2));
+    Y = (uint64_t)((int64_t)Y + mulhi((int64_t)Y, e) * 8);
+  }
+  // sqrt(m) 2^61 = m y 2^61, then 53 bits
+  const uint64_t S = umulhi(Mm, Y);
+  const uint64_t s0 = S >> 9;
+  // round(sqrt(M 2^52)): (2 s0 + 1)^2 against 4 M 2^52 (never equal)
+  const unsigned __int128 lhs = (unsigned __int128)M << 54;
+  const unsigned __int128 rhs = (unsigned __int128)(2 * s0 + 1) * (2 * s0 + 1);
+  uint64_t mant = s0 + (lhs > rhs);
+  int er = (ex - odd) / 2;
+  if (mant >> 53) {
+    mant >>= 1;
+    er += 1;
+  }
+  r = bitsd(((uint64_t)(er + 1023) << 52) | (mant & kFrac));
   return true;
 }
 

@@ -86,10 +86,10 @@ __device__ __forceinline__ double overland_flow(double avg_h, double grad_h, dou
 // sq returns sqrt(satn), which EffKinf's macropore branch needs too.
 __device__ __forceinline__ void kr_psi(double satn, double vm, double vg_e, double vg_ib, double alpha,
                                        double &satkfunc, double &psi, double &sq) {
-  sq = sqrt(satn);
+  sq = sqrt_any(satn);
   const double t = 1.0 - pow_any(1.0 - pow_any(satn, vm), vg_e);
   satkfunc = sq * t * t;
-  psi = -pow_any(pow_any(1.0 / satn, vm) - 1.0, vg_ib) / alpha;
+  psi = div_any(-pow_any(pow_any(div_any(1.0, satn), vm) - 1.0, vg_ib), alpha);
 }
 
 // Batch engine: whether the watershed of item idx sits out this evaluation
@@ -219,11 +219,11 @@ __global__ void __launch_bounds__(kPrepBlock) k_elem_prep(DevMesh m, const doubl
   const int t = threadIdx.x;
   if (t < qs_n) {
     const int e = qs_i[t];
-    const double sh = sqrt(qs_x[t]);
+    const double sh = sqrt_any(qs_x[t]);
     m.surfh[e] = sh;
     m.head[e] = sh + m.zmax[e];
   }
-  if (t < qd_n) m.effk[qd_i[t]] = qd_num[t] / qd_den[t];
+  if (t < qd_n) m.effk[qd_i[t]] = div_any(qd_num[t], qd_den[t]);
 }
 
 // ---------------------------------------------------------------------------
@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(256) k_elem_grad(DevMesh m, const double *REST
   // DhByDl(nabr_y, nabr_x, h) and DhByDl(nabr_x, nabr_y, h)
   const double dhdx = -1.0 * (y2 * (h[1] - h[0]) + y1 * (h[0] - h[2]) + y0 * (h[2] - h[1])) * m.inv_den_x[i];
   const double dhdy = -1.0 * (x2 * (h[1] - h[0]) + x1 * (h[0] - h[2]) + x0 * (h[2] - h[1])) * m.inv_den_y[i];
-  m.gradmag[i] = sqrt(dhdx * dhdx + dhdy * dhdy);
+  m.gradmag[i] = sqrt_any(dhdx * dhdx + dhdy * dhdy);
 }
 
 // ---------------------------------------------------------------------------
@@ -401,7 +401,7 @@ __global__ void __launch_bounds__(256, 3) k_elem_main(DevMesh m, const double *R
     else edir_unsat = edir;
     double gwet = 0.0;
     if (cmp::gt0(ett) && m.noah_wtin[i]) {
-      gwet = m.noah_etgw[i] / ett;
+      gwet = div_any(m.noah_etgw[i], ett);
       gwet = cmp::gt_c(gwet, 1.0) ? 1.0 : gwet;
       gwet = cmp::lt0(gwet) ? 0.0 : gwet;
     }
@@ -425,7 +425,7 @@ __global__ void __launch_bounds__(256, 3) k_elem_main(DevMesh m, const double *R
   double satn = 1.0, satkfunc = 1.0, psi_u = 0.0, sq = 1.0;
   if (!gw_in_dinf) {
     const double deficit = depth - gw;
-    satn = unsat / deficit;
+    satn = div_any(unsat, deficit);
     satn = cmp::gt_c(satn, 1.0) ? 1.0 : satn;
     satn = cmp::lt_c(satn, kSatMin) ? kSatMin : satn;
     kr_psi(satn, m.vg_m[i], m.vg_e[i], m.vg_ib[i], m.alpha[i], satkfunc, psi_u, sq);
@@ -465,7 +465,7 @@ __global__ void __launch_bounds__(256, 3) k_elem_main(DevMesh m, const double *R
       h_u = psi_c + zmax - 0.5 * dinf;
       esatn = satn_i;
     }
-    double dh_by_dz = (surfh + zmax - h_u) / (0.5 * (surfh + dinf));
+    double dh_by_dz = div_any(surfh + zmax - h_u, 0.5 * (surfh + dinf));
     dh_by_dz = (cmp::le0(surfh) && cmp::gt0(dh_by_dz)) ? 0.0 : dh_by_dz;
     // EffKinf, src/vert_flow.c:211-270
     double kinf;
@@ -478,7 +478,7 @@ __global__ void __launch_bounds__(256, 3) k_elem_main(DevMesh m, const double *R
     } else if (cmp::lt_v(applrate, dh_by_dz * (kmac_a + kinf_mat * satkfunc_i))) {
       // KrFunc(2, satn): pow(satn, 2) and pow(., 0.5) are a product and
       // sqrt; sqrt(esatn) is kr_psi's (1 when esatn is 1)
-      const double t2 = 1.0 - sqrt(1.0 - esatn * esatn);
+      const double t2 = 1.0 - sqrt_any(1.0 - esatn * esatn);
       kinf = kinf_mat * satkfunc_i + kmac_a * (sq_i * t2 * t2);
     } else {
       kinf = kinf_mat * satkfunc_i + kmac_a;

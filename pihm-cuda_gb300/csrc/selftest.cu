@@ -52,3 +52,27 @@ extern "C" int pihm_gpu_selftest_pow_int(const double *x, const double *y, doubl
   k_pow_int<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(x, y, out, ok, n);
   return cudaGetLastError() == cudaSuccess ? 0 : -2;
 }
+
+namespace {
+__global__ void k_div_sqrt_int(const double *a, const double *b, double *q, double *r, int32_t *ok,
+                               long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double qq = 0.0, rr = 0.0;
+  const bool okq = pihm::im::div_i(a[i], b[i], qq);
+  const bool okr = pihm::im::sqrt_i(a[i], rr);
+  q[i] = qq;
+  r[i] = rr;
+  ok[i] = (okq ? 1 : 0) | (okr ? 2 : 0);
+}
+}  // namespace
+
+// The integer-pipe division and square root alone: q[i] = a[i] / b[i] and
+// r[i] = sqrt(a[i]); bit 0 of ok[i] set where the division took the integer
+// path, bit 1 where the square root did.
+extern "C" int pihm_gpu_selftest_div_sqrt_int(const double *a, const double *b, double *q, double *r,
+                                              int32_t *ok, int64_t n, void *stream) {
+  if (n <= 0 || !a || !b || !q || !r || !ok) return -1;
+  k_div_sqrt_int<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(a, b, q, r, ok, n);
+  return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}

@@ -32,3 +32,23 @@ void im_exp2k(const int64_t *tn, const int64_t *tf, double *out, int64_t n) {
   for (int64_t i = 0; i < n; i++) out[i] = pihm::im::exp2k(pihm::im::TVal{tn[i], tf[i]});
 }
 }
+
+extern "C" {
+// q[i] = a[i] / b[i] on the integer path; ok[i] = 0 where it declines
+void im_div(const double *a, const double *b, double *q, int32_t *ok, int64_t n) {
+  for (int64_t i = 0; i < n; i++) {
+    double r = 0.0;
+    ok[i] = pihm::im::div_i(a[i], b[i], r) ? 1 : 0;
+    q[i] = r;
+  }
+}
+
+// r[i] = sqrt(x[i]) on the integer path; ok[i] = 0 where it declines
+void im_sqrt(const double *x, double *r, int32_t *ok, int64_t n) {
+  for (int64_t i = 0; i < n; i++) {
+    double v = 0.0;
+    ok[i] = pihm::im::sqrt_i(x[i], v) ? 1 : 0;
+    r[i] = v;
+  }
+}
+}

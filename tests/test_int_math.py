@@ -2,11 +2,12 @@
 kernels (pihm-cuda_gb300/csrc/int_math.cuh).
 
 The arithmetic is integer, so the header compiled for the host
-(tests/int_math_host.cpp) gives the bits the GPU computes: the CPU test
-measures its error against 200-bit references on the argument ranges the
-model produces (van Genuchten powers of saturation and their complements,
-Manning's h^0.6666667) and on wide ranges, and the GPU test checks that the
-device returns the same bits as the host build."""
+(tests/int_math_host.cpp) gives the bits the GPU computes: the CPU tests
+measure the power's error against 200-bit references on the argument ranges
+the model produces (van Genuchten powers of saturation and their complements,
+Manning's h^0.6666667) and on wide ranges, and hold the division and square
+root to the IEEE results bit for bit; the GPU tests check that the device
+returns the same bits as the host build."""
 import ctypes
 import os
 import shutil
@@ -107,3 +108,67 @@ def test_device_bits_equal_host_bits(host_lib):
         assert np.array_equal(ok.cpu().numpy().astype(bool), ok_h), name
         got = out.cpu().numpy()
         assert np.array_equal(got[ok_h].view(np.int64), want[ok_h].view(np.int64)), name
+
+
+def host_div_sqrt(lib, a, b):
+    a = np.ascontiguousarray(a, np.float64)
+    b = np.ascontiguousarray(b, np.float64)
+    q, r = np.empty_like(a), np.empty_like(a)
+    okq, okr = np.empty(a.size, np.int32), np.empty(a.size, np.int32)
+    lib.im_div(P(a.ctypes.data), P(b.ctypes.data), P(q.ctypes.data), P(okq.ctypes.data), ctypes.c_int64(a.size))
+    lib.im_sqrt(P(a.ctypes.data), P(r.ctypes.data), P(okr.ctypes.data), ctypes.c_int64(a.size))
+    return q, okq.astype(bool), r, okr.astype(bool)
+
+
+def div_sqrt_cases(rng, n):
+    bits = lambda: np.frombuffer(rng.integers(0, 2 ** 63, n, dtype=np.int64).tobytes(), np.float64)  # noqa: E731
+    sign = lambda: rng.choice([-1.0, 1.0], n)  # noqa: E731
+    near1 = lambda: 1.0 + rng.integers(-4000, 4000, n) * 2.0 ** -52  # noqa: E731
+    return {
+        "model": (rng.uniform(0.0, 10.0, n), rng.uniform(0.1, 10.0, n)),
+        "wide": (np.exp(rng.uniform(-340, 340, n)) * sign(), np.exp(rng.uniform(-340, 340, n)) * sign()),
+        "near one": (near1() * rng.choice([1.0, 2.0, 4.0], n), near1()),
+        "integers": (rng.integers(1, 1 << 53, n).astype(np.float64), rng.integers(1, 1 << 26, n).astype(np.float64)),
+        "squares": ((rng.integers(1, 1 << 26, n).astype(np.float64)) ** 2, np.full(n, 3.0)),
+        "bit patterns": (np.abs(bits()), bits()),
+    }
+
+
+def test_division_and_sqrt_are_ieee_bit_for_bit(host_lib):
+    rng = np.random.default_rng(99)
+    for name, (a, b) in div_sqrt_cases(rng, 400_000).items():
+        q, okq, r, okr = host_div_sqrt(host_lib, a, b)
+        with np.errstate(all="ignore"):
+            wq, wr = a / b, np.sqrt(a)
+        assert okq.mean() > 0.7 and okr[a > 0].mean() > 0.99, name
+        assert np.array_equal(q[okq].view(np.int64), wq[okq].view(np.int64)), name
+        assert np.array_equal(r[okr].view(np.int64), wr[okr].view(np.int64)), name
+    # zeros, subnormals, infinities, NaN and out-of-range quotients are
+    # declined; the square root declines negative arguments too
+    a = np.array([0.0, 5e-324, np.inf, np.nan, 1.0, 1e300, 1e-300, -4.0])
+    b = np.array([1.0, 1.0, 1.0, 1.0, 0.0, 1e-300, 1e300, 1.0])
+    q, okq, _, okr = host_div_sqrt(host_lib, a, b)
+    assert list(okq) == [False] * 7 + [True] and q[7] == -4.0
+    assert list(okr) == [False, False, False, False, True, True, True, False]
+
+
+@pytest.mark.gpu
+def test_device_division_and_sqrt_bits_equal_host_bits(host_lib):
+    import torch
+    from pihm_gpu import capi
+    lib = capi.load()
+    f = lib.pihm_gpu_selftest_div_sqrt_int
+    f.argtypes = [P] * 5 + [ctypes.c_int64, P]
+    f.restype = ctypes.c_int
+    rng = np.random.default_rng(5)
+    for name, (a, b) in div_sqrt_cases(rng, 500_000).items():
+        q, okq, r, okr = host_div_sqrt(host_lib, a, b)
+        ta, tb = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+        gq, gr = torch.empty_like(ta), torch.empty_like(ta)
+        ok = torch.empty(a.size, dtype=torch.int32, device="cuda")
+        assert f(ta.data_ptr(), tb.data_ptr(), gq.data_ptr(), gr.data_ptr(), ok.data_ptr(), a.size, None) == 0
+        torch.cuda.synchronize()
+        o = ok.cpu().numpy()
+        assert np.array_equal((o & 1).astype(bool), okq) and np.array_equal((o & 2).astype(bool), okr), name
+        assert np.array_equal(gq.cpu().numpy()[okq].view(np.int64), q[okq].view(np.int64)), name
+        assert np.array_equal(gr.cpu().numpy()[okr].view(np.int64), r[okr].view(np.int64)), name
