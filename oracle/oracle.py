@@ -83,6 +83,7 @@ class Oracle:
         lib.oracle_destroy.argtypes = [ctypes.c_void_p]
         lib.oracle_num_threads.restype = ctypes.c_int
         lib.oracle_set_num_threads.argtypes = [ctypes.c_int]
+        lib.oracle_set_ulp_perturb.argtypes = [ctypes.c_void_p, ctypes.c_int]
         self.lib = lib
         self.ws = ws
         self.desc = MeshDesc.from_arrays(ws.nelem, ws.nriver, ws.arrays)
@@ -101,6 +102,12 @@ class Oracle:
     @property
     def threads(self) -> int:
         return self.lib.oracle_num_threads()
+
+    def set_ulp_perturb(self, s: int):
+        """+1 / -1: every pow() and log() result of this model's evaluations
+        moves by one unit in the last place in that direction; 0: the
+        reference's arithmetic exactly (the default)."""
+        self.lib.oracle_set_ulp_perturb(self.h, int(s))
 
     def set_forcing(self, pcpdrp=None, edir=None, ett=None):
         self.lib.oracle_set_forcing(self.h, f64p(_c(pcpdrp)), f64p(_c(edir)),

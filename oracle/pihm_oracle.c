@@ -92,6 +92,7 @@ typedef struct river_t {
 } river_t;
 
 struct oracle_model {
+    int ulp_perturb; /* see oracle_set_ulp_perturb */
     int nelem, nriver;
     int noah; /* 1: the Flux-PIHM (_NOAH_) variants of EtExtract and Infil */
     int surf_mode, riv_mode;
@@ -100,6 +101,8 @@ struct oracle_model {
     river_t *river;
     double *dhbydx, *dhbydy;
 };
+
+void oracle_set_ulp_perturb(oracle_model *m, int s) { m->ulp_perturb = (s > 0) - (s < 0); }
 
 int oracle_num_threads(void)
 {
@@ -265,19 +268,38 @@ void oracle_set_river_edge_ovlflow(oracle_model *m, const double *ovlflow)
 /* Soil hydraulics                                                    */
 /* ------------------------------------------------------------------ */
 
+/* Last-bit sensitivity of the reference's arithmetic (test infrastructure):
+ * with a model's ulp_perturb set to +1 or -1, every pow() and log() result of
+ * its evaluations moves by one unit in the last place in that direction.  Two
+ * correct libms can differ by that much, and the tests use the rows' movement
+ * to bound how far the reference's own roundings let each row go.  With
+ * ulp_perturb 0 (the default) the arithmetic is exactly the reference's.
+ * Evaluations of different models must not overlap in time (they do not: one
+ * evaluation at a time, each setting this from its model). */
+static int g_ulp_perturb = 0;
+
+static double nudge(double r)
+{
+    if (g_ulp_perturb == 0 || r == 0.0 || !isfinite(r)) return r;
+    return nextafter(r, g_ulp_perturb > 0 ? INFINITY : -INFINITY);
+}
+
+static double ppow(double x, double y) { return nudge(pow(x, y)); }
+static double plog(double x) { return nudge(log(x)); }
+
 /* KrFunc, src/soil.c:8-13 */
 static double KrFunc(double beta, double satn)
 {
     return sqrt(satn) *
-        (1.0 - pow(1.0 - pow(satn, beta / (beta - 1.0)), (beta - 1.0) / beta)) *
-        (1.0 - pow(1.0 - pow(satn, beta / (beta - 1.0)), (beta - 1.0) / beta));
+        (1.0 - ppow(1.0 - ppow(satn, beta / (beta - 1.0)), (beta - 1.0) / beta)) *
+        (1.0 - ppow(1.0 - ppow(satn, beta / (beta - 1.0)), (beta - 1.0) / beta));
 }
 
 /* Psi, src/vert_flow.c:272-278 */
 static double Psi(double satn, double alpha, double beta)
 {
     satn = (satn < SATMIN) ? SATMIN : satn;
-    return -pow(pow(1.0 / satn, beta / (beta - 1.0)) - 1.0, 1.0 / beta) / alpha;
+    return -ppow(ppow(1.0 / satn, beta / (beta - 1.0)) - 1.0, 1.0 / beta) / alpha;
 }
 
 /* SurfH, src/hydrol.c:100-134 (DEPRSTG != 0 branch) */
@@ -350,7 +372,7 @@ static double DhByDl(const double *l1, const double *l2, const double *surfh)
 static double OverLandFlow(double avg_h, double grad_h, double avg_sf,
                            double crossa, double avg_rough)
 {
-    return crossa * pow(avg_h, 0.6666667) * grad_h /
+    return crossa * ppow(avg_h, 0.6666667) * grad_h /
         (sqrt(avg_sf) * avg_rough);
 }
 
@@ -711,7 +733,7 @@ static double RiverCroSectArea(int order, double depth, double coeff)
         cs_area = 4.0 * depth * sqrt(depth) / (3.0 * sqrt(coeff));
         break;
     case CUBIC:
-        cs_area = 3.0 * pow(depth, 4.0 / 3.0) / (2.0 * pow(coeff, 1.0 / 3.0));
+        cs_area = 3.0 * ppow(depth, 4.0 / 3.0) / (2.0 * ppow(coeff, 1.0 / 3.0));
         break;
     default: break;
     }
@@ -730,16 +752,16 @@ static double RiverPerim(int order, double depth, double coeff)
         break;
     case QUADRATIC:
         perim = sqrt(depth * (1.0 + 4.0 * coeff * depth) / coeff) +
-            log(2.0 * sqrt(coeff * depth) + sqrt(1.0 + 4.0 * coeff * depth)) /
+            plog(2.0 * sqrt(coeff * depth) + sqrt(1.0 + 4.0 * coeff * depth)) /
             (2.0 * coeff);
         break;
     case CUBIC:
-        perim = 2.0 * ((pow(depth * (1.0 + 9.0 * pow(coeff, 2.0 / 3.0) *
+        perim = 2.0 * ((ppow(depth * (1.0 + 9.0 * ppow(coeff, 2.0 / 3.0) *
                                       depth), 0.5) / 3.0) +
-                       (log(3.0 * pow(coeff, 1.0 / 3.0) * sqrt(depth) +
-                            pow(1.0 + 9.0 * pow(coeff, 2.0 / 3.0) * depth,
+                       (plog(3.0 * ppow(coeff, 1.0 / 3.0) * sqrt(depth) +
+                            ppow(1.0 + 9.0 * ppow(coeff, 2.0 / 3.0) * depth,
                                 0.5)) /
-                        (9.0 * pow(coeff, 1.0 / 3.0))));
+                        (9.0 * ppow(coeff, 1.0 / 3.0))));
         break;
     default: break;
     }
@@ -817,7 +839,7 @@ static double OutletFlux(const river_t *r)
         avg_perim = RiverPerim(r->intrpl_ord, r->stage, r->coeff);
         crossa = RiverCroSectArea(r->intrpl_ord, r->stage, r->coeff);
         discharge = sqrt(grad_h) * crossa *
-            ((avg_perim > 0.0) ? pow(crossa / avg_perim, 2.0 / 3.0) : 0.0) /
+            ((avg_perim > 0.0) ? ppow(crossa / avg_perim, 2.0 / 3.0) : 0.0) /
             r->rough;
         (void)avg_h;
         break;
@@ -1036,6 +1058,7 @@ int oracle_rhs(oracle_model *m, double t, const double *y, double *dy)
     int nan_found = 0;
     (void)t;
 
+    g_ulp_perturb = m->ulp_perturb;
     for (i = 0; i < size; i++) dy[i] = 0.0;
 
 #if defined(_OPENMP)

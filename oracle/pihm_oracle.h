@@ -65,6 +65,10 @@ void oracle_land_monthly(long long t, int lc, double *out3);
 /* Number of OpenMP threads the oracle runs with (1 without OpenMP). */
 int oracle_num_threads(void);
 void oracle_set_num_threads(int n);
+/* s = +1 / -1: every pow() and log() result of this model's evaluations moves
+ * by one unit in the last place in that direction (the last-bit sensitivity
+ * the tests measure); 0, the default: the reference's arithmetic exactly. */
+void oracle_set_ulp_perturb(oracle_model *m, int s);
 
 #ifdef __cplusplus
 }

@@ -11,15 +11,21 @@ with scale = sum of |terms| of that row, e.g. for the surface row
 |pcpdrp| + |infil| + |edir_surf| + sum_j |ovlflow_j| / area
 (src/ode.c:111-209 and :228-300 for the row definitions).
 
-Recharge is itself a difference: kavg (0.5 deficit + Psi) / (0.5 depth)
-(src/vert_flow.c:132-170), and near equilibrium 0.5 deficit + Psi cancels by
-up to four orders of magnitude.  A Psi one ulp away from the reference's --
-what two correct libms' pow can give -- then moves the unsaturated and
-groundwater rows by up to 3.4e-12 of their terms on the 1M-element benchmark
-mesh (measured by perturbing the restatement's Psi by one ulp).  When the
-state is passed, Recharge's term therefore counts with the magnitude of its
-two addends, kavg (0.5 deficit + |Psi|) / (0.5 depth) (recharge_magnitude);
-everywhere else the scale is unchanged.
+Some terms are themselves computed as differences that cancel: Recharge's
+head gradient 0.5 deficit + Psi near equilibrium (src/vert_flow.c:132-170),
+KrFunc's 1 - (1 - satn^m)^e at low saturation (src/soil.c:8-13), Infil's
+surfh + zmax - (Psi + zmax - 0.5 dinf).  There the reference's own roundings
+fix the result only to a few parts in 1e12: a power one ulp away from
+glibc's -- what any other correct libm may return -- moves such a row by up to
+a few times 1e-12 of its terms on the 1M-element benchmark mesh.  Where a test
+passes an envelope, the bar of each row is widened by it:
+
+    |gpu - ref| <= RTOL * max(|ref|, scale) + envelope,
+
+envelope = |ref(+1 ulp) - ref| + |ref(-1 ulp) - ref|, the movement of the
+reference's result when every pow() and log() it evaluates is moved by one
+unit in the last place up, then down (Oracle.set_ulp_perturb, the same
+calls, the same state).  Rows that are not sensitive keep the 1e-12 bar.
 """
 from __future__ import annotations
 
@@ -28,45 +34,8 @@ import numpy as np
 RTOL = 1e-12
 
 
-SATMIN = 0.1  # src/include/pihm_const.h
-
-
-def recharge_magnitude(ws, y, rechg):
-    """|Recharge| counted by its two addends where Recharge evaluates its
-    own gradient: kavg (0.5 deficit + |Psi|) / (0.5 depth), with Psi,
-    KrFunc and AvgKv (arithmetic mean) as src/vert_flow.c:132-209 and
-    src/soil.c:8-13 form them (numpy's pow: this is a tolerance scale, not
-    a result); |rechg| elsewhere (water table within the infiltration
-    depth, where Recharge equals Infil)."""
-    a = ws.arrays
-    ne = ws.nelem
-    y = np.asarray(y, np.float64)
-    unsat = np.maximum(y[ne:2 * ne], 0.0)
-    gw = np.maximum(y[2 * ne:3 * ne], 0.0)
-    depth, dinf, beta, alpha = a["depth"], a["dinf"], a["beta"], a["alpha"]
-    ksatv, dmac, kmacv, areafh = a["ksatv"], a["dmac"], a["kmacv"], a["areafh"]
-    own = ~(gw > depth - dinf)
-    deficit = depth - gw
-    with np.errstate(all="ignore"):
-        satn = np.clip(unsat / deficit, SATMIN, 1.0)
-        m = beta / (beta - 1.0)
-        psi = -np.power(np.power(1.0 / satn, m) - 1.0, 1.0 / beta) / alpha
-        kr = np.sqrt(satn) * (1.0 - np.power(1.0 - np.power(satn, m), (beta - 1.0) / beta)) ** 2
-        deep = deficit > dmac
-        k2 = np.where(deep, kr * ksatv, np.where(areafh > 0.0, kmacv * areafh + ksatv * (1.0 - areafh), ksatv))
-        d1 = np.where(deep, dmac, deficit)
-        d2 = np.where(deep, deficit - dmac, dmac - deficit)
-        d3 = np.where(deep, gw, gw - (dmac - deficit))
-        kavg = (kr * ksatv * d1 + k2 * d2 + ksatv * d3) / (d1 + d2 + d3)
-        mag = np.abs(kavg) * (0.5 * deficit + np.abs(psi)) / (0.5 * depth)
-    mag = np.where(np.isfinite(mag), mag, 0.0)
-    r = np.abs(np.asarray(rechg, np.float64))
-    return np.where(own, np.maximum(r, mag), r)
-
-
-def row_scales(ws, fx, pcpdrp, edir, ett, y=None):
-    """Sum of |terms| of every ydot row, from a flux set (oracle diagnostics);
-    with the state y, Recharge counts by its addends (recharge_magnitude)."""
+def row_scales(ws, fx, pcpdrp, edir, ett):
+    """Sum of |terms| of every ydot row, from a flux set (oracle diagnostics)."""
     a = ws.arrays
     ne, nr = ws.nelem, ws.nriver
     area = a["area"]
@@ -75,7 +44,7 @@ def row_scales(ws, fx, pcpdrp, edir, ett, y=None):
     sub = np.abs(fx["subsurf"].reshape(ne, 3)).sum(1)
     et = np.abs(fx["et_split"].reshape(ne, 5))
     infil = np.abs(fx["infil"])
-    rechg = np.abs(fx["rechg"]) if y is None else recharge_magnitude(ws, y, fx["rechg"])
+    rechg = np.abs(fx["rechg"])
     s_surf = np.abs(pcpdrp) + infil + et[:, 0] + ovl / area
     s_unsat = (infil + rechg + et[:, 1] + et[:, 3]) / por
     s_gw = (rechg + et[:, 2] + et[:, 4] + sub / area) / por
@@ -86,11 +55,16 @@ def row_scales(ws, fx, pcpdrp, edir, ett, y=None):
     return np.concatenate([s_surf, s_unsat, s_gw, s_stage, s_rgw])
 
 
-def compare(got, want, scale, rtol=RTOL):
-    """Returns (ok, worst normalised error, index)."""
+def compare(got, want, scale, rtol=RTOL, envelope=None):
+    """Returns (ok, worst normalised error, index).  With an envelope (the
+    reference's last-bit movement, see above) a row's error is counted net
+    of it."""
     den = np.maximum(np.abs(want), scale)
     den = np.where(den > 0, den, 1.0)
-    err = np.abs(got - want) / den
+    diff = np.abs(got - want)
+    if envelope is not None:
+        diff = np.maximum(diff - envelope, 0.0)
+    err = diff / den
     err = np.where(got == want, 0.0, err)
     k = int(np.argmax(err)) if err.size else 0
     worst = float(err[k]) if err.size else 0.0

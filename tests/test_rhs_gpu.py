@@ -22,7 +22,7 @@ def _check_call(o, g, ws, sc, calls=3, label=""):
         got, rc_g = g.rhs_host(yk)
         assert rc_o == 0 and rc_g == 0
         fx = o.fluxes()
-        scale = row_scales(ws, fx, sc["pcpdrp"], sc["edir"], sc["ett"], y=yk)
+        scale = row_scales(ws, fx, sc["pcpdrp"], sc["edir"], sc["ett"])
         ok, worst, idx = compare(got, want, scale)
         assert ok, f"{label} call {k}: worst {worst:.3e} at {idx} got {got[idx]!r} want {want[idx]!r}"
 

@@ -16,11 +16,13 @@ compared here on:
   * a batch holding a 100,000-element watershed beside small ones, bit for
     bit with its run alone.
 
-Each row is held to the 1e-12 row-scale bar of tests/parity.py (with
-Recharge counted by its two addends, which the one-ulp sensitivity of Psi at
-this size requires), against the OpenMP restatement of the reference ODE()
-(src/ode.c:4-399) making the same call sequence.  The worst normalised error of each configuration is printed
-(pytest -s shows it)."""
+Each row is held to the 1e-12 row-scale bar of tests/parity.py, widened only
+by the reference's own last-bit envelope (rows that are differences of
+nearly equal quantities, where a power one ulp away moves the result by more
+than 1e-12), against the OpenMP restatement of the reference ODE()
+(src/ode.c:4-399) making the same call sequence.  The worst normalised error
+of each configuration, and how many rows needed the envelope, are printed
+(pytest -s shows them)."""
 import numpy as np
 import pytest
 
@@ -32,19 +34,24 @@ pytestmark = pytest.mark.gpu
 
 
 def _models(ws, forcing, ws0, ovl, noah=None):
+    """The GPU model and three oracles: the reference's arithmetic, and the
+    same with every pow()/log() result one ulp up, one ulp down (the
+    envelope of tests/parity.py)."""
     import torch
     from oracle import Oracle
     from pihm_gpu.capi import GpuRhs
     g = GpuRhs(ws)
     g.set_stream(torch.cuda.current_stream().cuda_stream)
-    o = Oracle(ws, omp=True)
-    for m in (g, o):
+    oracles = [Oracle(ws, omp=True) for _ in range(3)]
+    oracles[1].set_ulp_perturb(+1)
+    oracles[2].set_ulp_perturb(-1)
+    for m in [g] + oracles:
         if noah is not None:
             m.set_noah(noah)
         m.set_forcing(*forcing)
         m.set_ws0_surf(ws0)
         m.set_river_edge_ovlflow(ovl)
-    return g, o
+    return g, oracles
 
 
 def _device_call(g, y):
@@ -62,27 +69,37 @@ def _device_call(g, y):
 
 def _run_sequence(ws, states, forcing, ws0, ovl, noah, via):
     """Consecutive calls (the carried river-edge flux of one call feeds the
-    next) on the GPU and in the oracle; returns the worst normalised error."""
-    g, o = _models(ws, forcing, ws0, ovl, noah)
-    worst_all = strict_all = 0.0
+    next) on the GPU and in the oracles; returns the worst normalised error
+    net of the last-bit envelope, the worst without it, and the number of
+    rows whose error exceeds the plain 1e-12 bar."""
+    g, (o, op, om) = _models(ws, forcing, ws0, ovl, noah)
+    worst_all = plain_all = 0.0
+    over = 0
     try:
         for k, y in enumerate(states):
             want, rc_o = o.rhs(y)
+            up, rc_p = op.rhs(y)
+            dn, rc_m = om.rhs(y)
             if via == "device":
                 got, rc_g = _device_call(g, y)
             else:
                 got, rc_g = g.rhs_host(y)
-            assert rc_o == 0 and rc_g == 0, (via, k, rc_o, rc_g)
-            fx = o.fluxes()
-            ok, worst, idx = compare(got, want, row_scales(ws, fx, *forcing, y=y))
-            assert ok, f"{via} call {k}: worst {worst:.3e} at row {idx}: got {got[idx]!r} want {want[idx]!r}"
+            assert rc_o == 0 and rc_p == 0 and rc_m == 0 and rc_g == 0, (via, k, rc_o, rc_g)
+            scale = row_scales(ws, o.fluxes(), *forcing)
+            env = np.abs(up - want) + np.abs(dn - want)
+            ok, worst, idx = compare(got, want, scale, envelope=env)
+            assert ok, (f"{via} call {k}: worst {worst:.3e} at row {idx}: got {got[idx]!r} want {want[idx]!r} "
+                        f"envelope {env[idx]!r}")
             worst_all = max(worst_all, worst)
-            # the same comparison with Recharge counted as one term
-            strict_all = max(strict_all, compare(got, want, row_scales(ws, fx, *forcing))[1])
+            _, plain, _ = compare(got, want, scale)
+            plain_all = max(plain_all, plain)
+            den = np.maximum(np.maximum(np.abs(want), scale), 1e-300)
+            over += int(np.sum(np.abs(got - want) > RTOL * den))
     finally:
         g.close()
-        o.close()
-    return worst_all, strict_all
+        for m in (o, op, om):
+            m.close()
+    return worst_all, plain_all, over
 
 
 @pytest.fixture(scope="module")
@@ -97,9 +114,9 @@ def test_headline_mesh_against_oracle(headline, via, first):
     states = [WL.rhs_state(base, k) for k in range(first, first + 3)]
     rng = np.random.default_rng(31 + first)
     ovl = rng.normal(0.0, 1e-3, 3 * ws.nelem)
-    worst, strict = _run_sequence(ws, states, WL.rhs_forcing(ws), base[:ws.nelem], ovl, None, via)
-    print(f"\n1M-element mesh via {via}: worst normalised error {worst:.3e} (bar {RTOL:.0e}; "
-          f"{strict:.3e} with Recharge as one term)")
+    worst, plain, over = _run_sequence(ws, states, WL.rhs_forcing(ws), base[:ws.nelem], ovl, None, via)
+    print(f"\n1M-element mesh via {via}: worst normalised error {worst:.3e} net of the last-bit envelope "
+          f"(bar {RTOL:.0e}); without it {plain:.3e}, {over} of {3 * ws.neq} rows above 1e-12")
 
 
 @pytest.mark.parametrize("via", ["device", "host"])
@@ -113,9 +130,9 @@ def test_flux_pihm_200k_against_oracle(via):
     ett = np.where(rng.random(ne) < 0.15, 0.0, ett)  # some elements without transpiration
     noah = W.noah_inputs(ws, 2, nlayers=4)
     ovl = rng.normal(0.0, 1e-3, 3 * ne)
-    worst, strict = _run_sequence(ws, states, (pcpdrp, edir, ett), base[:ne], ovl, noah, via)
-    print(f"\n200k-element Flux-PIHM mesh via {via}: worst normalised error {worst:.3e} (bar {RTOL:.0e}; "
-          f"{strict:.3e} with Recharge as one term)")
+    worst, plain, over = _run_sequence(ws, states, (pcpdrp, edir, ett), base[:ne], ovl, noah, via)
+    print(f"\n200k-element Flux-PIHM mesh via {via}: worst normalised error {worst:.3e} net of the last-bit "
+          f"envelope (bar {RTOL:.0e}); without it {plain:.3e}, {over} of {3 * ws.neq} rows above 1e-12")
 
 
 def test_batch_with_a_large_watershed_matches_its_solo_runs():
