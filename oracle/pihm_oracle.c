@@ -284,7 +284,13 @@ static double nudge(double r)
     return nextafter(r, g_ulp_perturb > 0 ? INFINITY : -INFINITY);
 }
 
-static double ppow(double x, double y) { return nudge(pow(x, y)); }
+/* exact results (pow(1, y) = 1, pow(x, 1) = x, log(1) = 0) are exact in
+ * every libm and stay as they are */
+static double ppow(double x, double y)
+{
+    const double r = pow(x, y);
+    return (x == 1.0 || y == 1.0 || y == 0.0) ? r : nudge(r);
+}
 static double plog(double x) { return nudge(log(x)); }
 
 /* KrFunc, src/soil.c:8-13 */

@@ -335,7 +335,10 @@ __global__ void __launch_bounds__(kEdgeBlock) k_edge(DevMesh m, const double *RE
 // ---------------------------------------------------------------------------
 // k_elem_main
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256, 3) k_elem_main(DevMesh m, const double *RESTRICT y,
+#ifndef PIHM_ELEM_MAIN_MINB
+#define PIHM_ELEM_MAIN_MINB 3
+#endif
+__global__ void __launch_bounds__(256, PIHM_ELEM_MAIN_MINB) k_elem_main(DevMesh m, const double *RESTRICT y,
                                                     double *RESTRICT ydot) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   int sy;
