@@ -336,9 +336,13 @@ __global__ void __launch_bounds__(kEdgeBlock) k_edge(DevMesh m, const double *RE
 // k_elem_main
 // ---------------------------------------------------------------------------
 #ifndef PIHM_ELEM_MAIN_MINB
-#define PIHM_ELEM_MAIN_MINB 3
+#define PIHM_ELEM_MAIN_MINB 2
 #endif
-__global__ void __launch_bounds__(256, PIHM_ELEM_MAIN_MINB) k_elem_main(DevMesh m, const double *RESTRICT y,
+#ifndef PIHM_ELEM_MAIN_BLOCK
+#define PIHM_ELEM_MAIN_BLOCK 512
+#endif
+constexpr int kMainBlock = PIHM_ELEM_MAIN_BLOCK;
+__global__ void __launch_bounds__(kMainBlock, PIHM_ELEM_MAIN_MINB) k_elem_main(DevMesh m, const double *RESTRICT y,
                                                     double *RESTRICT ydot) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   int sy;
@@ -1009,7 +1013,7 @@ cudaError_t launch_rhs(const DevMesh &m, const double *y, double *ydot, cudaStre
       ++*launches;
     }
     on = prof_begin(prof, K_MAIN, st);
-    k_elem_main<<<blocks_for(m.ne_run, 256), 256, 0, st>>>(m, y, ydot);
+    k_elem_main<<<blocks_for(m.ne_run, kMainBlock), kMainBlock, 0, st>>>(m, y, ydot);
     prof_end(prof, on, st);
     ++*launches;
   }
