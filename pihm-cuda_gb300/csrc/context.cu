@@ -232,6 +232,7 @@ void pihm_gpu_destroy(pihm_gpu_ctx *c) {
   if (c->d_dyn) cudaFree(c->d_dyn);
   if (c->d_noah) cudaFree(c->d_noah);
   if (c->d_land) cudaFree(c->d_land);
+  noah_free(c);
   if (c->side.fork) cudaEventDestroy(c->side.fork);
   if (c->side.join) cudaEventDestroy(c->side.join);
   if (c->side.side) cudaStreamDestroy(c->side.side);

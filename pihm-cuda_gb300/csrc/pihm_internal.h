@@ -201,6 +201,10 @@ cudaError_t launch_rhs(const DevMesh &m, const double *y, double *ydot, cudaStre
                        long long *launches, Profiler *prof, const RhsStreams *side = nullptr,
                        const double *y_ref = nullptr, const int32_t *iperm = nullptr);
 
+// Noah land-surface model planes (noah.cu, include/pihm_noah.h)
+struct NoahPlanes;
+void noah_free(pihm_gpu_ctx *c);
+
 }  // namespace pihm
 
 struct pihm_gpu_ctx {
@@ -230,4 +234,7 @@ struct pihm_gpu_ctx {
   int64_t land_t_lo, land_t_hi;  // model times every forcing series covers
   int land_month;                // month ra_num holds (-1: none yet)
   pihm::RhsStreams side;   // river kernel beside the element kernels
+  void *d_noahlsm;              // Noah land-surface model (pihm_gpu_noah_init), or null
+  pihm::NoahPlanes *noahlsm;    // its planes
+  int noah_first;               // no model step has ended since pihm_gpu_noah_init
 };
