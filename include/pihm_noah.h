@@ -81,11 +81,15 @@ int pihm_gpu_noah_set_forcing(pihm_gpu_ctx *ctx, const pihm_noah_forcing *f);
 /* Noah() over dt seconds (the land-surface step), then the right-hand side's
  * Flux-PIHM inputs from its results; asynchronous on the context's stream. */
 int pihm_gpu_noah_step(pihm_gpu_ctx *ctx, double dt);
+/* The state a run starts from (device, internal order): the previous state
+ * MassBalance compares the first model step's end with, as the reference's
+ * Initialize sets ws0 (src/initialize.c:700).  Without it the first
+ * pihm_gpu_noah_post_step takes its own y as the previous state. */
+int pihm_gpu_noah_begin(pihm_gpu_ctx *ctx, const double *y0_dev);
 /* After a model step of `stepsize` seconds that ended at the device state
  * y (internal order): Summary's _NOAH_ part and NoahHydrol, then the
  * right-hand side's inputs.  Needs the last evaluation's fluxes, which the
- * context keeps while Noah is attached.  The first call after
- * pihm_gpu_noah_init takes y as the previous state too. */
+ * context keeps while Noah is attached. */
 int pihm_gpu_noah_post_step(pihm_gpu_ctx *ctx, const double *y_dev, double stepsize);
 
 /* Fields that can be read back (reference order). */

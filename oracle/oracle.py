@@ -234,6 +234,37 @@ class Reference:
     def set_noah(self, noah: dict):
         _set_noah(self.lib.ref_set_noah, noah)
 
+    # the Noah land-surface model (Flux-PIHM build): Noah(), Summary(),
+    # NoahHydrol() of the reference on the model built by build()
+    def noah_load(self, params: dict, state: dict, y0):
+        from pihm_gpu import noah as N
+        lib = self.lib
+        lib.ref_noah_load.argtypes = [ctypes.POINTER(N.NoahParams), ctypes.POINTER(N.NoahState), _F64P]
+        lib.ref_noah_forcing.argtypes = [ctypes.POINTER(N.NoahForcing)]
+        lib.ref_noah_step.argtypes = [ctypes.c_double]
+        lib.ref_noah_post.argtypes = [_F64P, ctypes.c_double]
+        lib.ref_noah_get.argtypes = [ctypes.c_int, _F64P]
+        ps, kp = N.params_struct(params)
+        ss, ks = N.state_struct(state)
+        assert lib.ref_noah_load(ctypes.byref(ps), ctypes.byref(ss), f64p(_c(y0))) == 0
+
+    def noah_forcing(self, forcing: dict):
+        from pihm_gpu import noah as N
+        fs, kf = N.forcing_struct(forcing)
+        assert self.lib.ref_noah_forcing(ctypes.byref(fs)) == 0
+
+    def noah_step(self, dt: float):
+        assert self.lib.ref_noah_step(float(dt)) == 0
+
+    def noah_post(self, y, dt: float):
+        assert self.lib.ref_noah_post(f64p(_c(y)), float(dt)) == 0
+
+    def noah_get(self, name: str) -> np.ndarray:
+        from pihm_gpu import noah as N
+        out = np.zeros(N.field_shape(name, self.ne))
+        assert self.lib.ref_noah_get(N.field_id(name), f64p(out.reshape(-1))) == 0
+        return out
+
     # land-surface step of a loaded deck (ApplyForc + IntcpSnowEt)
     def land_set_state(self, unsat=None, gw=None, cmc=None, sneqv=None):
         keep = [_c(a) for a in (unsat, gw, cmc, sneqv)]

@@ -18,6 +18,9 @@
  */
 #include "pihm.h"
 #include "pihm_gpu.h"
+#if defined(_NOAH_)
+#include "pihm_noah.h"
+#endif
 
 #include <unistd.h>
 
@@ -408,6 +411,169 @@ void ref_get_gwet(double *gwet)
 {
     int i;
     for (i = 0; i < nelem; i++) gwet[i] = g_pihm->elem[i].ps.gwet;
+}
+
+/* ---- The Noah land-surface model (src/noah/noah.c, lsm_func.c) ---------
+ * The same parameter, state and forcing structs the GPU library takes
+ * (include/pihm_noah.h) fill the element records of the model built by
+ * ref_build; Noah(), Summary() and NoahHydrol() are the reference's own. */
+#define FILL_LAYERS(dst, src, i, n)                                          \
+    do {                                                                      \
+        int k_;                                                               \
+        for (k_ = 0; k_ < MAXLYR; k_++)                                       \
+            (dst)[k_] = (k_ < (n)) ? (src)[(size_t)MAXLYR * (i) + k_] : BADVAL; \
+    } while (0)
+
+int ref_noah_load(const pihm_noah_params *p, const pihm_noah_state *s, const double *y0)
+{
+    int i, k;
+    if (!g_pihm || p->nelem != nelem) return -1;
+    for (i = 0; i < nelem; i++) {
+        elem_struct *e = &g_pihm->elem[i];
+        const int ns = p->nsoil[i];
+        e->ps.nsoil = ns;
+        e->ps.nroot = p->nroot[i];
+        FILL_LAYERS(e->ps.sldpth, p->sldpth, i, ns);
+        FILL_LAYERS(e->ps.rtdis, p->rtdis, i, p->nroot[i]);
+        /* DefSldpth's depths below the surface, noah/lsm_func.c:152-156 */
+        e->ps.zsoil[0] = -e->ps.sldpth[0];
+        for (k = 1; k < ns; k++) e->ps.zsoil[k] = -e->ps.sldpth[k] + e->ps.zsoil[k - 1];
+        e->lc.isurban = p->isurban ? p->isurban[i] : 0;
+        e->soil.smcmax = p->smcmax[i]; e->soil.smcmin = p->smcmin[i];
+        e->soil.smcref = p->smcref[i]; e->soil.smcwlt = p->smcwlt[i];
+        e->soil.smcdry = p->smcdry[i]; e->soil.quartz = p->quartz[i];
+        e->soil.csoil = p->csoil[i]; e->soil.alpha = p->alpha[i];
+        e->soil.beta = p->beta[i]; e->soil.ksatv = p->ksatv[i];
+        e->soil.porosity = p->porosity[i]; e->soil.depth = p->depth[i];
+        e->topo.area = p->area[i];
+        e->lc.shdfac = p->shdfac[i]; e->lc.cmcfactr = p->cmcfactr[i];
+        e->lc.laimax = p->laimax[i]; e->lc.laimin = p->laimin[i];
+        e->lc.emissmax = p->emissmax[i]; e->lc.emissmin = p->emissmin[i];
+        e->lc.albedomax = p->albedomax[i]; e->lc.albedomin = p->albedomin[i];
+        e->lc.z0max = p->z0max[i]; e->lc.z0min = p->z0min[i];
+        e->lc.snup = p->snup[i]; e->lc.cfactr = p->cfactr[i];
+        e->epc.rgl = p->rgl[i]; e->epc.rsmin = p->rsmin[i];
+        e->epc.rsmax = p->rsmax[i]; e->epc.topt = p->topt[i]; e->epc.hs = p->hs[i];
+        e->ps.sbeta = p->sbeta[i]; e->ps.salp = p->salp[i]; e->ps.frzx = p->frzx[i];
+        e->ps.fxexp = p->fxexp[i]; e->ps.czil = p->czil[i]; e->ps.lvcoef = p->lvcoef[i];
+        e->ps.zbot = p->zbot[i]; e->ps.tbot = p->tbot[i]; e->ps.zlvl = p->zlvl[i];
+        e->ps.zlvl_wind = p->zlvl_wind[i]; e->ps.snoalb = p->snoalb[i];
+        FILL_LAYERS(e->ws.smc, s->smc, i, ns);
+        FILL_LAYERS(e->ws.sh2o, s->sh2o, i, ns);
+        FILL_LAYERS(e->es.stc, s->stc, i, ns);
+        e->es.t1 = s->t1[i]; e->ws.cmc = s->cmc[i]; e->ws.sneqv = s->sneqv[i];
+        e->ps.snowh = s->snowh[i]; e->ps.sndens = s->sndens[i]; e->ps.ch = s->ch[i];
+        e->ps.cm = s->cm[i]; e->ps.snotime1 = s->snotime1[i]; e->ps.albedo = s->albedo[i];
+        e->ps.emissi = s->emissi[i]; e->ps.q1 = s->q1[i]; e->ps.ribb = s->ribb[i];
+        e->ps.fcr = s->fcr[i];
+        e->ps.nwtbl = ns;
+        for (k = 0; k < MAXLYR; k++) {
+            e->wf.et[k] = 0.0;
+            e->wf.runoff2_lyr[k] = 0.0;
+            e->wf.smflxv[k] = 0.0;
+            e->ps.satdpth[k] = 0.0;
+        }
+        e->wf.edir = 0.0; e->wf.ett = 0.0; e->wf.ec = 0.0; e->wf.pcpdrp = 0.0;
+        e->wf.runoff2 = 0.0; e->wf.runoff3 = 0.0; e->wf.infil = 0.0;
+        /* the previous model step's state, for MassBalance */
+        e->ws.surf = y0[i]; e->ws.unsat = y0[nelem + i]; e->ws.gw = y0[2 * nelem + i];
+        e->ws0 = e->ws;
+    }
+    return 0;
+}
+
+int ref_noah_forcing(const pihm_noah_forcing *f)
+{
+    int i;
+    if (!g_pihm) return -1;
+    for (i = 0; i < nelem; i++) {
+        elem_struct *e = &g_pihm->elem[i];
+        e->wf.prcp = f->prcp[i]; e->es.sfctmp = f->sfctmp[i]; e->ps.rh = f->rh[i];
+        e->ps.sfcspd = f->sfcspd[i]; e->ef.soldn = f->soldn[i];
+        e->ef.longwave = f->longwave[i]; e->ps.sfcprs = f->sfcprs[i];
+        e->ps.proj_lai = f->lai[i];
+    }
+    return 0;
+}
+
+/* Noah() over dt (src/noah/noah.c:3-55) */
+int ref_noah_step(double dt)
+{
+    if (!g_pihm) return -1;
+    Noah(g_pihm->elem, dt);
+    return 0;
+}
+
+/* After a model step ending at y: Summary() (src/update.c:3-99, with its
+ * _NOAH_ part) and NoahHydrol() (src/noah/noah.c:57-160).  The fluxes
+ * MassBalance reads are the last ref_ode() evaluation's. */
+int ref_noah_post(const double *y, double dt)
+{
+    N_Vector v;
+    if (!g_pihm) return -1;
+    v = N_VMake_Serial(NumStateVar(), (realtype *)y);
+    Summary(g_pihm->elem, g_pihm->river, v, dt);
+    N_VDestroy(v);
+    NoahHydrol(g_pihm->elem, dt);
+    return 0;
+}
+
+/* A field of pihm_gpu_noah_get's list (include/pihm_noah.h), reference
+ * order; per-layer fields [nelem][MAXLYR] */
+int ref_noah_get(int field, double *out)
+{
+    int i, k;
+    if (!g_pihm) return -1;
+    for (i = 0; i < nelem; i++) {
+        const elem_struct *e = &g_pihm->elem[i];
+        const double *lay = NULL;
+        double v = 0.0;
+        switch (field) {
+        case PIHM_NOAH_SMC: lay = e->ws.smc; break;
+        case PIHM_NOAH_SH2O: lay = e->ws.sh2o; break;
+        case PIHM_NOAH_STC: lay = e->es.stc; break;
+        case PIHM_NOAH_ET: lay = e->wf.et; break;
+        case PIHM_NOAH_RUNOFF2_LYR: lay = e->wf.runoff2_lyr; break;
+        case PIHM_NOAH_SMFLXV: lay = e->wf.smflxv; break;
+        case PIHM_NOAH_T1: v = e->es.t1; break;
+        case PIHM_NOAH_CMC: v = e->ws.cmc; break;
+        case PIHM_NOAH_SNEQV: v = e->ws.sneqv; break;
+        case PIHM_NOAH_SNOWH: v = e->ps.snowh; break;
+        case PIHM_NOAH_SNDENS: v = e->ps.sndens; break;
+        case PIHM_NOAH_CH: v = e->ps.ch; break;
+        case PIHM_NOAH_CM: v = e->ps.cm; break;
+        case PIHM_NOAH_ALBEDO: v = e->ps.albedo; break;
+        case PIHM_NOAH_EMISSI: v = e->ps.emissi; break;
+        case PIHM_NOAH_Q1: v = e->ps.q1; break;
+        case PIHM_NOAH_FCR: v = e->ps.fcr; break;
+        case PIHM_NOAH_EDIR: v = e->wf.edir; break;
+        case PIHM_NOAH_EC: v = e->wf.ec; break;
+        case PIHM_NOAH_ETT: v = e->wf.ett; break;
+        case PIHM_NOAH_ESNOW: v = e->wf.esnow; break;
+        case PIHM_NOAH_ETP: v = e->wf.etp; break;
+        case PIHM_NOAH_DRIP: v = e->wf.drip; break;
+        case PIHM_NOAH_PCPDRP: v = e->wf.pcpdrp; break;
+        case PIHM_NOAH_SNOMLT: v = e->wf.snomlt; break;
+        case PIHM_NOAH_SSOIL: v = e->ef.ssoil; break;
+        case PIHM_NOAH_SHEAT: v = e->ef.sheat; break;
+        case PIHM_NOAH_RUNOFF2: v = e->wf.runoff2; break;
+        case PIHM_NOAH_RUNOFF3: v = e->wf.runoff3; break;
+        case PIHM_NOAH_INFIL: v = e->wf.infil; break;
+        case PIHM_NOAH_NWTBL: v = e->ps.nwtbl; break;
+        case PIHM_NOAH_SNOTIME1: v = e->ps.snotime1; break;
+        case PIHM_NOAH_SNCOVR: v = e->ps.sncovr; break;
+        case PIHM_NOAH_BETA: v = e->ps.beta; break;
+        case PIHM_NOAH_ETA: v = e->wf.eta; break;
+        case PIHM_NOAH_SOILM: v = e->ws.soilm; break;
+        default: return -1;
+        }
+        if (lay) {
+            for (k = 0; k < MAXLYR; k++) out[(size_t)MAXLYR * i + k] = (k < e->ps.nsoil) ? lay[k] : 0.0;
+        } else {
+            out[i] = v;
+        }
+    }
+    return 0;
 }
 #else
 /* Forcing step of src/pihm.c:21-66 for a model loaded by ref_load_example:

@@ -189,6 +189,14 @@ __global__ void __launch_bounds__(kNoahBlock) k_noah_post(NoahPlanes P, DevMesh 
   store_col(P, i, c);
 }
 
+// ws0 from the state a run starts from
+__global__ void __launch_bounds__(256) k_noah_begin(NoahPlanes P, const double *y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.ne) return;
+  P.s[NS_UNSAT0][i] = y[P.ne + i];
+  P.s[NS_GW0][i] = y[2 * P.ne + i];
+}
+
 // The Flux-PIHM right-hand side's inputs from Noah's state and outputs.
 __global__ void __launch_bounds__(256) k_noah_inputs(NoahPlanes P, DevMesh m) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -381,6 +389,15 @@ extern "C" int pihm_gpu_noah_step(pihm_gpu_ctx *c, double dt) {
   k_noah_step<<<(P.ne + kNoahBlock - 1) / kNoahBlock, kNoahBlock, 0, c->stream>>>(P, dt, c->m.err);
   c->launches++;
   return cuda_rc(cudaGetLastError()) ?: launch_inputs(c);
+}
+
+extern "C" int pihm_gpu_noah_begin(pihm_gpu_ctx *c, const double *y0_dev) {
+  if (!c || !c->noahlsm || !y0_dev) return PIHM_GPU_ERR_ARG;
+  const NoahPlanes &P = *c->noahlsm;
+  k_noah_begin<<<(P.ne + 255) / 256, 256, 0, c->stream>>>(P, y0_dev);
+  c->noah_first = 0;
+  c->launches++;
+  return cuda_rc(cudaGetLastError());
 }
 
 extern "C" int pihm_gpu_noah_post_step(pihm_gpu_ctx *c, const double *y_dev, double stepsize) {

@@ -182,6 +182,50 @@ class GpuRhs:
         _check("pihm_gpu_set_noah", f(self.h, f64p(et), nl, i32p(nw), i32p(nr),
                                       *(f64p(_c(noah[k])) for k in ("sh2o0", "smcmin", "smcmax", "fcr"))))
 
+    def post_step(self, y_ptr: int):
+        """pihm_gpu_post_step: ws0 <- the device state y_ptr (internal order)
+        after a model step, as Summary sets it."""
+        f = self.lib.pihm_gpu_post_step
+        f.argtypes = [_VP, _VP]
+        f.restype = ctypes.c_int
+        _check("pihm_gpu_post_step", f(self.h, _VP(y_ptr)))
+
+    # ---- the Noah land-surface model (include/pihm_noah.h) ----
+    def noah_init(self, params: dict, state: dict):
+        """Attach Noah (pihm_gpu.noah.synthetic_noah's dicts, reference order)."""
+        from . import noah as N
+        N.bind(self.lib)
+        ps, kp = N.params_struct(params)
+        ss, ks = N.state_struct(state)
+        _check("pihm_gpu_noah_init", self.lib.pihm_gpu_noah_init(self.h, ctypes.byref(ps), ctypes.byref(ss)))
+
+    def noah_set_state(self, state: dict):
+        from . import noah as N
+        ss, ks = N.state_struct(state)
+        _check("pihm_gpu_noah_set_state", self.lib.pihm_gpu_noah_set_state(self.h, ctypes.byref(ss)))
+
+    def noah_set_forcing(self, forcing: dict):
+        from . import noah as N
+        fs, kf = N.forcing_struct(forcing)
+        _check("pihm_gpu_noah_set_forcing", self.lib.pihm_gpu_noah_set_forcing(self.h, ctypes.byref(fs)))
+
+    def noah_step(self, dt: float):
+        _check("pihm_gpu_noah_step", self.lib.pihm_gpu_noah_step(self.h, float(dt)))
+
+    def noah_begin(self, y0_ptr: int):
+        """The state the run starts from (device, internal order)."""
+        _check("pihm_gpu_noah_begin", self.lib.pihm_gpu_noah_begin(self.h, _VP(y0_ptr)))
+
+    def noah_post_step(self, y_ptr: int, stepsize: float):
+        """After a model step ending at the device state y_ptr (internal order)."""
+        _check("pihm_gpu_noah_post_step", self.lib.pihm_gpu_noah_post_step(self.h, _VP(y_ptr), float(stepsize)))
+
+    def noah_get(self, name: str) -> np.ndarray:
+        from . import noah as N
+        out = np.zeros(N.field_shape(name, self.ws.nelem))
+        _check("pihm_gpu_noah_get", self.lib.pihm_gpu_noah_get(self.h, N.field_id(name), f64p(out.reshape(-1))))
+        return out
+
     def set_diagnostics(self, on: bool):
         _check("pihm_gpu_set_diagnostics", self.lib.pihm_gpu_set_diagnostics(self.h, int(on)))
 
