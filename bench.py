@@ -312,34 +312,39 @@ def bench_batched():
     }
 
 
-FLUX_NELEM, FLUX_LAYERS, FLUX_STATES, FLUX_STEPS = 200_000, 4, 40, 10
+FLUX_NELEM, FLUX_LAYERS, FLUX_STATES, FLUX_STEPS, FLUX_LSM = 200_000, 4, 40, 60, 3600.0
 
 
 def bench_flux_pihm():
-    """Flux-PIHM right-hand side (Noah's per-step inputs fused into the
-    element kernel) on a 200,000-element mesh with 4 soil layers, beside the
-    plain right-hand side on the same states, and a short solve with the Noah
-    inputs renewed every model hour."""
+    """Flux-PIHM (the c2 configuration, 200,000 elements, 4 Noah soil
+    layers): the right-hand side with Noah's outputs fused into the element
+    kernel beside the plain right-hand side on the same states; the Noah
+    land-surface step and its post-model-step update (include/pihm_noah.h)
+    timed alone; and a coupled run of the reference's Flux-PIHM model-step
+    loop on the device (pihm_gpu.single.NoahWatershed: hourly forcing, Noah
+    every land-surface step of an hour, the integration of each 60 s model
+    step, Summary and NoahHydrol) for FLUX_STEPS model steps of the
+    configuration's 3 days."""
     import numpy as np
     import torch
     import pihm_gpu.watershed as W
+    from pihm_gpu import noah as N
     from pihm_gpu import workloads as WL
     from pihm_gpu.capi import GpuRhs
-    from pihm_gpu.single import GpuWatershed
+    from pihm_gpu.single import NoahWatershed
     from pihm_gpu.solver import StepControl, run_steps
     ws = W.generate(FLUX_NELEM, WL.river_count(FLUX_NELEM), seed=2)
     dev = torch.device("cuda", torch.cuda.current_device())
     stream = torch.cuda.Stream(device=dev)
     base = W.reference_state(ws, 3)
+    params, state = N.synthetic_noah(ws, seed=2, nlayers=FLUX_LAYERS)
     gen = torch.Generator(device=dev)
     gen.manual_seed(99)
-    res = {}
+    res, noah_ms = {}, {}
     for mode in ("plain", "noah"):
         g = GpuRhs(ws, stream=stream.cuda_stream)
         g.set_forcing(*W.random_forcing(ws, 5))
         g.set_ws0_surf(base[:ws.nelem])
-        if mode == "noah":
-            g.set_noah(W.noah_inputs(ws, 2, nlayers=FLUX_LAYERS))
         with torch.cuda.stream(stream):
             b = torch.from_numpy(base).to(dev)
             ref = torch.stack([b * (0.9 + 0.2 * torch.rand(ws.neq, generator=gen, device=dev, dtype=torch.float64))
@@ -348,6 +353,12 @@ def bench_flux_pihm():
             for k in range(FLUX_STATES):
                 g.to_internal(ref[k].data_ptr(), st[k].data_ptr())
             yd = torch.empty((1, ws.neq), dtype=torch.float64, device=dev)
+        if mode == "noah":
+            # the right-hand side's Noah inputs from the device Noah itself
+            g.noah_init(params, state)
+            g.noah_begin(st[0].data_ptr())
+            g.noah_set_forcing(N.forcing(ws, 12, seed=2))
+            g.noah_step(FLUX_LSM)
         for k in range(3):
             g.rhs_device(st[k].data_ptr(), yd[0].data_ptr())
         stream.synchronize()
@@ -359,27 +370,47 @@ def bench_flux_pihm():
         e1.synchronize()
         assert g.status() == 0
         res[mode] = FLUX_NELEM * FLUX_STATES / (e0.elapsed_time(e1) * 1e-3)
+        if mode == "noah":
+            # Noah's land-surface step and its post-step alone, CUDA events
+            for name, fn in (("noah_step", lambda k: g.noah_step(FLUX_LSM)),
+                             ("noah_post_step", lambda k: g.noah_post_step(st[k].data_ptr(), 60.0))):
+                fn(0)
+                stream.synchronize()
+                e0.record(stream)
+                for k in range(5):
+                    fn(k)
+                e1.record(stream)
+                e1.synchronize()
+                noah_ms[name] = e0.elapsed_time(e1) / 5
+            assert g.status() == 0
         g.close()
-    # a short solve: Noah's inputs renewed every model hour
-    pcp, edir, ett = WL.step_forcing(ws, FLUX_STEPS, 60.0, seed=8)
-    m = GpuWatershed(ws, W.relax_state(ws), pcp, edir, ett)
-    base_forcing = m.set_forcing
-
-    def forcing(k):
-        if k % 60 == 0:
-            m.g.set_noah(W.noah_inputs(ws, 100 + k // 60, nlayers=FLUX_LAYERS))
-        base_forcing(k)
+    # the coupled run
+    m = NoahWatershed(ws, W.relax_state(ws), params, state, lambda h: N.forcing(ws, h, seed=2),
+                      lsm_step=FLUX_LSM)
+    torch.cuda.synchronize()
     t = time.perf_counter()
-    r = run_steps(m, StepControl(), FLUX_STEPS, forcing, outlet=int(np.where(ws.arrays["down"] < 0)[0][0]))
+    r = run_steps(m, StepControl(), FLUX_STEPS, m.set_forcing, outlet=int(np.where(ws.arrays["down"] < 0)[0][0]))
+    torch.cuda.synchronize()
     solve_s = time.perf_counter() - t
+    noah_steps = m.noah_steps
+    sneqv = m.g.noah_get("sneqv")
     m.close()
+    evals = int(r["stats"].nfe + r["stats"].nfes)
+    hours = FLUX_STEPS * 60.0 / 3600.0
     return {"metric": "Flux-PIHM RHS element-evals/s", "unit": "elem-evals/s", "value": res["noah"],
             "plain_rhs_value": res["plain"],
-            "workload": f"{FLUX_NELEM} elements, {ws.nriver} segments, {FLUX_LAYERS} Noah soil layers "
-                        f"(synthetic per-step Noah outputs), {FLUX_STATES} jittered states; solve: "
-                        f"{FLUX_STEPS} model steps of 60 s from RelaxIc",
-            "solve_s": solve_s, "solve_steps": int(r["stats"].nst),
-            "note": "Noah (SFLX) itself is not on this path: its per-step outputs are generated"}
+            "workload": f"{FLUX_NELEM} elements, {ws.nriver} segments, {FLUX_LAYERS} Noah soil layers, Noah on the "
+                        f"device (pihm_gpu_noah_*), {FLUX_STATES} jittered states",
+            "noah_ms": noah_ms,
+            "noah_element_steps_per_s": FLUX_NELEM / (noah_ms["noah_step"] * 1e-3),
+            "coupled_run": {"model_steps": FLUX_STEPS, "simulated_hours": hours, "wall_s": solve_s,
+                            "noah_steps": noah_steps, "integrator_steps": int(r["stats"].nst), "rhs_evals": evals,
+                            "elem_evals_per_s": FLUX_NELEM * evals / solve_s,
+                            "simulated_hours_per_wall_hour": hours * 3600.0 / solve_s,
+                            "fraction_of_the_3_day_run": hours / 72.0,
+                            "snow_covered_elements": int((sneqv > 0).sum()),
+                            "workload": "RelaxIc, hourly synthetic Noah forcing (pihm_gpu.noah.forcing), land-surface "
+                                        f"step {int(FLUX_LSM)} s, model step 60 s, reltol 1e-4"}}
 
 
 LAND_STEPS = 96            # one day of 900 s land-surface steps

@@ -41,6 +41,9 @@ enum NoahScalar {
   // outputs
   NS_EDIR, NS_EC, NS_ETT, NS_ESNOW, NS_ETP, NS_DRIP, NS_PCPDRP, NS_SNOMLT, NS_SSOIL, NS_SHEAT, NS_RUNOFF2,
   NS_RUNOFF3, NS_INFIL, NS_SNCOVR, NS_BETA_S, NS_ETA, NS_SOILM,
+  // kept from step to step like the reference's wf.etns, which SnoPac's dew
+  // branch leaves unchanged and SFlx then reads
+  NS_ETNS,
   // the previous model step's groundwater and unsaturated storage (ws0)
   NS_GW0, NS_UNSAT0,
   NS_COUNT
@@ -104,6 +107,7 @@ __device__ void load_col(const NoahPlanes &P, int i, Col &c) {
   c.ssoil = s[NS_SSOIL][i]; c.sheat = s[NS_SHEAT][i]; c.runoff2 = s[NS_RUNOFF2][i];
   c.runoff3 = s[NS_RUNOFF3][i]; c.infil = s[NS_INFIL][i]; c.sncovr = s[NS_SNCOVR][i];
   c.beta_s = s[NS_BETA_S][i]; c.eta = s[NS_ETA][i]; c.soilm = s[NS_SOILM][i];
+  c.etns = s[NS_ETNS][i];
 }
 
 // What a step changes: the state, the outputs and -- for urban land, where
@@ -134,6 +138,7 @@ __device__ void store_col(const NoahPlanes &P, int i, const Col &c) {
   s[NS_SSOIL][i] = c.ssoil; s[NS_SHEAT][i] = c.sheat; s[NS_RUNOFF2][i] = c.runoff2;
   s[NS_RUNOFF3][i] = c.runoff3; s[NS_INFIL][i] = c.infil; s[NS_SNCOVR][i] = c.sncovr;
   s[NS_BETA_S][i] = c.beta_s; s[NS_ETA][i] = c.eta; s[NS_SOILM][i] = c.soilm;
+  s[NS_ETNS][i] = c.etns;
 }
 
 constexpr int kNoahBlock = 128;

@@ -75,6 +75,36 @@ class GpuWatershed:
         self.g.close()
 
 
+class NoahWatershed(GpuWatershed):
+    """Flux-PIHM on the device: the model-step loop of the reference built
+    with _NOAH_ (src/pihm.c:21-123) -- every land-surface step the step's
+    forcing and Noah() (include/pihm_noah.h), then the integration to the end
+    of each model step, Summary and NoahHydrol -- with Noah's state and the
+    right-hand side's Noah inputs kept on the device.  forcing(hour) returns
+    the per-element forcing dict of pihm_gpu.noah.forcing for the land-surface
+    step that starts at that hour; lsm_step is the land-surface step (s)."""
+
+    def __init__(self, ws, y0, params: dict, state: dict, forcing, lsm_step: float = 3600.0, order=1):
+        zero = np.zeros(1)
+        super().__init__(ws, y0, zero, zero, zero, order=order)
+        self.g.noah_init(params, state)
+        self.g.noah_begin(self.device_state())
+        self.forcing = forcing
+        self.lsm_step = float(lsm_step)
+        self.noah_steps = 0
+
+    def set_forcing(self, k):
+        t = k * self.ws.stepsize
+        if t % self.lsm_step == 0:
+            self.g.noah_set_forcing(self.forcing(int(t // 3600)))
+            self.g.noah_step(self.lsm_step)
+            self.noah_steps += 1
+
+    def post_step(self):
+        assert self.lib.pihm_gpu_summary(self.g.h, self.y) == 0
+        self.g.noah_post_step(self.device_state(), float(self.ws.stepsize))
+
+
 def solve_alone(case: dict):
     """One watershed through the plain path: final state, outlet series, counters."""
     from .solver import run_steps

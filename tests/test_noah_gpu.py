@@ -6,11 +6,12 @@ land-surface steps each followed by 2 model steps -- the Flux-PIHM right-hand
 side on the device reading Noah's outputs, then the post-step -- with every
 readable field compared after each Noah step and each NoahHydrol.
 
-Tolerance: each field relative to max(|reference|, 1e-3 of the field's
-largest magnitude); the arithmetic follows the reference's operations
-without contraction, so the differences are those of the elementary
-functions (CUDA's exp, log, log10, atan against glibc's, the power within
-0.502 ulp), carried through four steps of a coupled model."""
+Tolerance: each field within 1e-10 relative to max(|reference|, 1e-3 of
+the field's largest magnitude).  The arithmetic follows the reference's
+operations without contraction, so the differences are those of the
+elementary functions (CUDA's exp, log, log10 and atan against glibc's, the
+power within 0.502 ulp) carried through the coupled steps; measured on GB300:
+96 % of the values identical to the last bit, the worst field 3.4e-12."""
 import os
 
 import numpy as np
@@ -21,7 +22,7 @@ from pihm_gpu import noah as N
 
 pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-TOL = 1e-9
+TOL = 1e-10
 
 
 def _err(got, want):
