@@ -524,6 +524,29 @@ def bench_solve(ws, hours):
     m.close()
     st = r["stats"]
     evals = int(st.nfe + st.nfes)
+    # GMRES scalars on the device (the default) against the plain iteration
+    # that reads every norm, dot product and status back: the first model
+    # steps of the same solve both ways, host clock
+    gmres = None
+    try:
+        k3 = min(nsteps, 10)
+        runs = {}
+        for mode in (-1, 0):
+            m3 = GpuWatershed(ws, W.relax_state(ws), pcp, edir, ett)
+            m3.g.set_diagnostics(False)
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            r3 = run_steps(m3, StepControl(), k3, m3.set_forcing, record_every=k3, deferred_scalars=mode)
+            torch.cuda.synchronize()
+            runs[mode] = (time.perf_counter() - t, r3)
+            m3.close()
+        (td, rd), (tp, rp) = runs[-1], runs[0]
+        gmres = {"model_steps": k3, "integrator_steps": int(rd["stats"].nst), "gmres_iters": int(rd["stats"].nli),
+                 "device_scalars_s": td, "plain_s": tp, "speedup": tp / td,
+                 "bit_identical": bool(np.array_equal(rd["states"], rp["states"])),
+                 "mode": int(rd["deferred_scalars"])}
+    except Exception as exc:
+        gmres = {"error": repr(exc)}
     # the same solve as a batch of one in the batch engine (each round's
     # vector operations fused per watershed, bit-identical to the plain path)
     engine = None
@@ -573,6 +596,7 @@ def bench_solve(ws, hours):
         cpu = {"error": repr(exc)}
     return {"metric": "solve: RHS element-evals/s inside the solve", "unit": "elem-evals/s",
             "value": ws.nelem * evals / wall, "batch_engine": engine, "rhs_device_time": rhs_ms,
+            "gmres_scalars": gmres,
             "cpu_baseline": cpu,
             "workload": f"{ws.nelem} elements, {ws.nriver} segments, {nsteps} model steps of 60 s "
                         f"({hours} simulated hours) from RelaxIc, hourly synthetic forcing, reltol 1e-4",

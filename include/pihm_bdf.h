@@ -67,6 +67,24 @@ int pihm_bdf_set_max_step(pihm_bdf *mem, double hmax);
 int pihm_bdf_set_max_num_steps(pihm_bdf *mem, long mxsteps);
 int pihm_bdf_set_stab_lim_det(pihm_bdf *mem, int on);
 int pihm_bdf_set_stop_time(pihm_bdf *mem, double tstop);
+/* GMRES scalars kept with the vectors (no CVODE counterpart; the solution is
+ * the same to the last bit).  Within each GMRES iteration the norm that sets
+ * the difference-quotient increment and the modified Gram-Schmidt dot
+ * products feed the linear sums that use them where the vectors live
+ * (N_VDotProdSlot_PihmGpu, N_VLinearSumCoef_PihmGpu, ...) and are read back
+ * once, together with the right-hand side's status when that is this
+ * library's pihm_gpu_ode on the vectors' stream (pihm_gpu_ode_launch): one
+ * host round trip per iteration instead of one per reduction and per
+ * evaluation.  setting -1 (default): on for device vectors of this library
+ * integrated with pihm_gpu_ode; 1: on for any vectors (host vectors keep
+ * the values on the host; a right-hand side other than pihm_gpu_ode reports
+ * at once, and recoverable failures are retried as CVODE retries them);
+ * 0: off. */
+int pihm_bdf_set_deferred_scalars(pihm_bdf *mem, int setting);
+/* How the last solve ran its GMRES iterations: 0 plain, 1 scalars kept on
+ * the host side of the operations table, 2 kept on the device (3: and the
+ * right-hand side's status read back with them); -1 before the first. */
+int pihm_bdf_get_deferred_scalars(const pihm_bdf *mem);
 /* Advance to tout (CV_NORMAL): yout receives y(tout) (or y(tstop)). */
 int pihm_bdf_solve(pihm_bdf *mem, double tout, N_Vector yout, double *tret);
 int pihm_bdf_get_stats(const pihm_bdf *mem, pihm_bdf_stats *stats);

@@ -127,6 +127,8 @@ void pihm_gpu_destroy(pihm_gpu_ctx *ctx);
 
 /* Stream all later work of this context is issued on (cudaStream_t). */
 int pihm_gpu_set_stream(pihm_gpu_ctx *ctx, void *stream);
+/* The stream the context issues its work on (NULL = legacy default). */
+void *pihm_gpu_get_stream(const pihm_gpu_ctx *ctx);
 int pihm_gpu_sizes(const pihm_gpu_ctx *ctx, int32_t *nelem, int32_t *nriver,
                    int64_t *neq);
 /* Internal position of every element and segment: perm[internal] = reference

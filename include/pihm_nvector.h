@@ -139,6 +139,57 @@ int pihm_gpu_nv_wrms_norm(const double *x, const double *w, int64_t n, void *str
 int pihm_gpu_nv_dot_prod(const double *x, const double *y, int64_t n, void *stream,
                          double *result);
 
+/* ---------------------------------------------------------------------
+ * Device-resident scalars (no counterpart in SUNDIALS 2.7, whose reductions
+ * all return to the host).  Inside one GMRES iteration (SpgmrSolve,
+ * cvode/src/sundials/sundials_spgmr.c:165-405) the norm that sets the
+ * difference-quotient increment (CVSpilsDQJtimes, cvode_spils.c:665-705)
+ * and the Gram-Schmidt dot products (ModifiedGS, sundials_iterative.c) are
+ * only coefficients of the next linear sums until the Hessenberg column is
+ * complete.  These entry points keep such values in the vector family's
+ * slot array on the device, use them there, and read them back in one copy.
+ * --------------------------------------------------------------------- */
+#define PIHM_NV_SLOTS 16
+/* A linear-sum coefficient: a host constant, or derived from slot s. */
+typedef struct pihm_nv_coef {
+  int32_t kind; /* PIHM_NV_COEF_* */
+  int32_t slot;
+  double value; /* for PIHM_NV_COEF_HOST */
+} pihm_nv_coef;
+enum {
+  PIHM_NV_COEF_HOST = 0,   /* value */
+  PIHM_NV_COEF_NEG,        /* -s */
+  PIHM_NV_COEF_INV,        /* 1/s */
+  PIHM_NV_COEF_INV_INV,    /* 1/(1/s), rounded twice */
+  PIHM_NV_COEF_NEG_INV_INV /* -(1/(1/s)) */
+};
+/* slot <- N_VDotProd(x, y), left on the device; asynchronous. */
+int N_VDotProdSlot_PihmGpu(N_Vector x, N_Vector y, int slot);
+/* slot <- N_VWrmsNorm(x, w), left on the device; asynchronous. */
+int N_VWrmsNormSlot_PihmGpu(N_Vector x, N_Vector w, int slot);
+/* N_VLinearSum(a, x, b, y, z) with a and b formed on the device from the
+ * slots; the serial N_Vector's case analysis (a == 1, b == -1, a == b, ...)
+ * is made there from the values, so every element equals N_VLinearSum's
+ * with the same coefficients.  Asynchronous. */
+int N_VLinearSumCoef_PihmGpu(const pihm_nv_coef *a, N_Vector x, const pihm_nv_coef *b, N_Vector y,
+                             N_Vector z);
+/* Copy slots 0..count-1 of v's family to out[] -- and, when dev_word is not
+ * null, one 32-bit device word to *word_out -- with one synchronisation of
+ * v's stream.  Returns 0, -1 (bad argument) or -2 (CUDA error). */
+int N_VFetchSlots_PihmGpu(N_Vector v, int count, double *out, const unsigned int *dev_word,
+                          unsigned int *word_out);
+/* The stream a device vector's operations run on. */
+void *N_VGetStream_PihmGpu(N_Vector v);
+
+/* pihm_gpu_ode for device vectors without reading back the status: the
+ * evaluation is queued on the context's stream and a NaN derivative shows
+ * in the context's error word (pihm_gpu_error_word), which pihm_gpu_status
+ * reads and clears.  Returns 0, or -1 if the evaluation could not be
+ * queued. */
+int pihm_gpu_ode_launch(double t, N_Vector y, N_Vector ydot, void *user_data);
+/* Device address of the context's error word (nonzero after a NaN). */
+const unsigned int *pihm_gpu_error_word(struct pihm_gpu_ctx *ctx);
+
 /* WRMS norm, sqrt(sum_i (x_i w_i)^2 / n), for callers that cannot allocate
  * device memory (no counterpart in the reference).  pihm_gpu_nv_wrms_norm
  * creates a workspace with cudaMalloc the first time a stream uses it; code

@@ -9,13 +9,32 @@
 // from one evaluation to the next).
 #include "bdf_core.h"
 #include "pihm_bdf.h"
+#include "pihm_gpu.h"
+#include "pihm_nvector.h"
 
 namespace {
+
+static_assert((int)pihm::bdf::COEF_HOST == PIHM_NV_COEF_HOST && (int)pihm::bdf::COEF_NEG == PIHM_NV_COEF_NEG &&
+                  (int)pihm::bdf::COEF_INV == PIHM_NV_COEF_INV &&
+                  (int)pihm::bdf::COEF_INV_INV == PIHM_NV_COEF_INV_INV &&
+                  (int)pihm::bdf::COEF_NEG_INV_INV == PIHM_NV_COEF_NEG_INV_INV,
+              "coefficient kinds");
 
 struct NVectorOps {
   using Vec = N_Vector;
   pihm_bdf_rhs_fn f = nullptr;
   void *user_data = nullptr;
+  // GMRES scalars kept with the vectors (pihm_bdf_set_deferred_scalars):
+  // -1 automatic (device vectors of this library with its own right-hand
+  // side), 0 off, 1 on for any vectors
+  int deferred_setting = -1;
+  // decided at the first GMRES iteration of a solve: 0 off, 1 host slots
+  // (operations through the table, values kept here), 2 device slots
+  int mode = -1;
+  bool rhs_deferrable = false;  // the right-hand side's status joins the slot read-back
+  bool rhs_pending = false;
+  Vec slot_vec = nullptr;
+  double host_slots[PIHM_NV_SLOTS] = {0};
 
   Vec clone(Vec w) { return w->ops->nvclone(w); }
   void destroy(Vec v) {
@@ -60,6 +79,72 @@ struct NVectorOps {
   pihm::Ready<double> wrms(Vec x, Vec w) { return {x->ops->nvwrmsnorm(x, w)}; }
   pihm::Ready<double> vmin(Vec x) { return {x->ops->nvmin(x)}; }
   pihm::Ready<int> rhs(double t, Vec y, Vec ydot) { return {f(t, y, ydot, user_data)}; }
+
+  // ---- device-resident GMRES scalars (bdf_core.h atimes_gs_deferred) ----
+  static bool is_device(Vec v) { return v && v->ops && v->ops->nvgetvectorid == N_VGetVectorID_PihmGpu; }
+
+  bool deferred_scalars(Vec v) {
+    if (mode < 0) {
+      const bool own_rhs = f == pihm_gpu_ode && user_data &&
+                           N_VGetStream_PihmGpu(v) == pihm_gpu_get_stream((const pihm_gpu_ctx *)user_data);
+      if (deferred_setting == 0 || (deferred_setting < 0 && !(is_device(v) && own_rhs))) mode = 0;
+      else mode = is_device(v) ? 2 : 1;
+      rhs_deferrable = mode == 2 && own_rhs;
+      slot_vec = v;
+    }
+    return mode > 0;
+  }
+  double host_coef_value(const pihm::bdf::Coef &c) const {
+    switch (c.kind) {
+      case pihm::bdf::COEF_NEG: return -host_slots[c.slot];
+      case pihm::bdf::COEF_INV: return 1.0 / host_slots[c.slot];
+      case pihm::bdf::COEF_INV_INV: return 1.0 / (1.0 / host_slots[c.slot]);
+      case pihm::bdf::COEF_NEG_INV_INV: return -(1.0 / (1.0 / host_slots[c.slot]));
+      default: return c.value;
+    }
+  }
+  pihm::ReadyVoid dot_slot(Vec x, Vec y, int slot) {
+    if (mode == 2) N_VDotProdSlot_PihmGpu(x, y, slot);
+    else host_slots[slot] = x->ops->nvdotprod(x, y);
+    return {};
+  }
+  pihm::ReadyVoid wrms_slot(Vec x, Vec w, int slot) {
+    if (mode == 2) N_VWrmsNormSlot_PihmGpu(x, w, slot);
+    else host_slots[slot] = x->ops->nvwrmsnorm(x, w);
+    return {};
+  }
+  pihm::ReadyVoid linear_sum_coef(pihm::bdf::Coef a, Vec x, pihm::bdf::Coef b, Vec y, Vec z) {
+    if (mode == 2) {
+      const pihm_nv_coef ca = {a.kind, a.slot, a.value}, cb = {b.kind, b.slot, b.value};
+      N_VLinearSumCoef_PihmGpu(&ca, x, &cb, y, z);
+    } else {
+      z->ops->nvlinearsum(host_coef_value(a), x, host_coef_value(b), y, z);
+    }
+    return {};
+  }
+  pihm::Ready<int> rhs_deferred(double t, Vec y, Vec ydot) {
+    if (!rhs_deferrable) return {f(t, y, ydot, user_data)};
+    const int rc = pihm_gpu_ode_launch(t, y, ydot, user_data);
+    rhs_pending = rc == 0;
+    return {rc};
+  }
+  // slots 0..count-1 to out; -1 when a deferred right-hand side produced a NaN
+  pihm::Ready<int> fetch_slots(int count, double *out) {
+    if (mode != 2) {
+      for (int i = 0; i < count; i++) out[i] = host_slots[i];
+      return {0};
+    }
+    unsigned int word = 0;
+    const bool pending = rhs_pending;
+    rhs_pending = false;
+    const unsigned int *dev_word = pending ? pihm_gpu_error_word((pihm_gpu_ctx *)user_data) : nullptr;
+    if (N_VFetchSlots_PihmGpu(slot_vec, count, out, dev_word, &word) != 0) return {-1};
+    if (word != 0) {
+      (void)pihm_gpu_status((pihm_gpu_ctx *)user_data);  // reads and clears the word
+      return {-1};
+    }
+    return {0};
+  }
 };
 
 }  // namespace
@@ -73,6 +158,7 @@ pihm_bdf *pihm_bdf_create(void) { return new pihm_bdf(); }
 int pihm_bdf_init(pihm_bdf *m, pihm_bdf_rhs_fn f, double t0, N_Vector y0) {
   if (!m || !f || !y0) return PIHM_BDF_ILL_INPUT;
   m->ops.f = f;
+  m->ops.mode = -1;
   return pihm::run_sync(m->init(t0, y0));
 }
 
@@ -92,6 +178,19 @@ int pihm_bdf_ss_tolerances(pihm_bdf *m, double reltol, double abstol) {
 int pihm_bdf_set_user_data(pihm_bdf *m, void *user_data) {
   if (!m) return PIHM_BDF_ILL_INPUT;
   m->ops.user_data = user_data;
+  m->ops.mode = -1;
+  return PIHM_BDF_SUCCESS;
+}
+
+int pihm_bdf_get_deferred_scalars(const pihm_bdf *m) {
+  if (!m) return PIHM_BDF_ILL_INPUT;
+  return m->ops.mode == 2 && m->ops.rhs_deferrable ? 3 : m->ops.mode;
+}
+
+int pihm_bdf_set_deferred_scalars(pihm_bdf *m, int setting) {
+  if (!m || setting < -1 || setting > 1) return PIHM_BDF_ILL_INPUT;
+  m->ops.deferred_setting = setting;
+  m->ops.mode = -1;
   return PIHM_BDF_SUCCESS;
 }
 

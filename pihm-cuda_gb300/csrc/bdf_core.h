@@ -88,6 +88,16 @@ inline double sun_powi(double b, int e) {
 inline double sun_max(double a, double b) { return (a > b) ? a : b; }
 inline double sun_min(double a, double b) { return (a < b) ? a : b; }
 
+// A linear-sum coefficient held as a reduction result on the vectors' side
+// (policies with device-resident scalars): a constant, or -s, 1/s, 1/(1/s),
+// -(1/(1/s)) of slot s.
+enum CoefKind { COEF_HOST = 0, COEF_NEG, COEF_INV, COEF_INV_INV, COEF_NEG_INV_INV };
+struct Coef {
+  int kind, slot;
+  double value;
+};
+constexpr Coef host_coef(double v) { return {COEF_HOST, 0, v}; }
+
 struct Stats {
   long nst, nfe, nni, ncfn, netf, nli, nfes, njtimes, ncfl, nor;
   int qlast, qcur;
@@ -450,6 +460,13 @@ struct BdfCore {
       co_await ops.linear_sum(ONE, V[k], -Hes[i][k_minus_1], V[i], V[k]);
     }
     *new_vk_norm = sun_sqrt(co_await ops.dot(V[k], V[k]));
+    co_return co_await gs_reorthogonalize(k, i0, vk_norm, new_vk_norm);
+  }
+
+  // ModifiedGS after the first pass: reorthogonalise V[k] against V[i0..k-1]
+  // when its norm dropped by more than GS_FACTOR
+  Task<int> gs_reorthogonalize(int k, int i0, double vk_norm, double *new_vk_norm) {
+    const int k_minus_1 = k - 1;
     double temp = GS_FACTOR * vk_norm;
     if ((temp + (*new_vk_norm)) != temp) co_return 0;
     double new_norm_2 = ZERO;
@@ -465,6 +482,75 @@ struct BdfCore {
       const double new_product = (*new_vk_norm) * (*new_vk_norm) - new_norm_2;
       *new_vk_norm = (new_product > ZERO) ? sun_sqrt(new_product) : ZERO;
     }
+    co_return 0;
+  }
+
+  // ---- GMRES with device-resident scalars (policies that provide them) ----
+  // Slots: the norm that sets the difference-quotient increment, ||V[k]||^2
+  // before and after Gram-Schmidt, and the Hessenberg column.
+  enum { SLOT_VNORM = 0, SLOT_VK = 1, SLOT_NEW = 2, SLOT_H = 3 };
+  static constexpr bool kDeferredOps = requires(Ops &o, Vec v) { o.deferred_scalars(v); };
+
+  bool deferred_scalars() {
+    if constexpr (kDeferredOps) return ops.deferred_scalars(V[0]);
+    else return false;
+  }
+
+  // One GMRES iteration: V[li] unscaled, the difference-quotient product
+  // (dq_atimes), rescaled, and modified_gs's first pass, with the norm that
+  // sets sig and the Gram-Schmidt dot products used where the vectors are
+  // and read back together (with a deferred right-hand side's status) once.
+  // The operations, their order and every value are those of the plain
+  // iteration; only the round trips are fewer.
+  Task<int> atimes_gs_deferred(int li, Vec weight, double *new_vk_norm) {
+    const int k = li + 1;
+    co_await ops.div(V[li], weight, vtemp);
+    // dq_atimes(vtemp, V[k]): sig = 1/||vtemp||_wrms
+    co_await ops.wrms_slot(vtemp, ewt, SLOT_VNORM);
+    co_await ops.linear_sum_coef({COEF_INV, SLOT_VNORM, 0}, vtemp, host_coef(ONE), ycur, ytemp);
+    int retval = co_await ops.rhs_deferred(tn, ytemp, V[k]);
+    nfes++;
+    if (retval == 0) {
+      co_await ops.linear_sum_coef({COEF_INV_INV, SLOT_VNORM, 0}, V[k], {COEF_NEG_INV_INV, SLOT_VNORM, 0}, fcur,
+                                   V[k]);
+    } else {
+      // a right-hand side that reports at once and failed: dq_atimes's
+      // retries with sig read back
+      if (retval < 0) co_return -1;
+      double s0[1];
+      (void)co_await ops.fetch_slots(1, s0);
+      double sig = ONE / s0[0];
+      for (int iter = 1; iter < MAX_ITERS && retval > 0; iter++) {
+        sig *= PT25;
+        co_await ops.linear_sum(sig, vtemp, ONE, ycur, ytemp);
+        retval = co_await ops.rhs(tn, ytemp, V[k]);
+        nfes++;
+        if (retval < 0) co_return -1;
+      }
+      if (retval > 0) co_return +1;
+      const double siginv = ONE / sig;
+      co_await ops.linear_sum(siginv, V[k], -siginv, fcur, V[k]);
+    }
+    njtimes++;
+    co_await ops.linear_sum(ONE, vtemp, -gamma, V[k], V[k]);
+    co_await ops.scale(ONE, V[k], vtemp);
+    co_await ops.prod(weight, vtemp, V[k]);
+    // modified_gs(k, maxl): the first pass
+    const int i0 = (k - maxl > 0) ? k - maxl : 0;
+    co_await ops.dot_slot(V[k], V[k], SLOT_VK);
+    for (int i = i0; i < k; i++) {
+      co_await ops.dot_slot(V[i], V[k], SLOT_H + i);
+      co_await ops.linear_sum_coef(host_coef(ONE), V[k], {COEF_NEG, SLOT_H + i, 0}, V[i], V[k]);
+    }
+    co_await ops.dot_slot(V[k], V[k], SLOT_NEW);
+    double s[SLOT_H + MAXL];
+    if ((co_await ops.fetch_slots(SLOT_H + k, s)) < 0) {
+      njtimes--;  // the deferred evaluation failed: dq_atimes returns before counting it
+      co_return -1;
+    }
+    for (int i = i0; i < k; i++) Hes[i][k - 1] = s[SLOT_H + i];
+    *new_vk_norm = sun_sqrt(s[SLOT_NEW]);
+    (void)co_await gs_reorthogonalize(k, i0, sun_sqrt(s[SLOT_VK]), new_vk_norm);
     co_return 0;
   }
 
@@ -529,6 +615,7 @@ struct BdfCore {
   // no restarts.  The solution is left in xsol.
   Task<int> spgmr(Vec b, Vec weight, double delta, int *nli_inc) {
     const int l_max = maxl;
+    const bool deferred = deferred_scalars();
     int l_plus_1 = 0, krydim = 0;
     bool converged = false;
     *nli_inc = 0;
@@ -550,13 +637,23 @@ struct BdfCore {
     for (int li = 0; li < l_max; li++) {
       (*nli_inc)++;
       krydim = l_plus_1 = li + 1;
-      co_await ops.div(V[li], weight, vtemp);
-      const int ier = co_await dq_atimes(vtemp, V[l_plus_1]);
-      if (ier != 0) co_return (ier < 0) ? SPGMR_ATIMES_FAIL_UNREC : SPGMR_ATIMES_FAIL_REC;
-      co_await ops.scale(ONE, V[l_plus_1], vtemp);
-      co_await ops.prod(weight, vtemp, V[l_plus_1]);
       double hnorm = 0;
-      (void)co_await modified_gs(l_plus_1, l_max, &hnorm);
+      bool iterated = false;
+      if constexpr (kDeferredOps) {
+        if (deferred) {
+          const int ier = co_await atimes_gs_deferred(li, weight, &hnorm);
+          if (ier != 0) co_return (ier < 0) ? SPGMR_ATIMES_FAIL_UNREC : SPGMR_ATIMES_FAIL_REC;
+          iterated = true;
+        }
+      }
+      if (!iterated) {
+        co_await ops.div(V[li], weight, vtemp);
+        const int ier = co_await dq_atimes(vtemp, V[l_plus_1]);
+        if (ier != 0) co_return (ier < 0) ? SPGMR_ATIMES_FAIL_UNREC : SPGMR_ATIMES_FAIL_REC;
+        co_await ops.scale(ONE, V[l_plus_1], vtemp);
+        co_await ops.prod(weight, vtemp, V[l_plus_1]);
+        (void)co_await modified_gs(l_plus_1, l_max, &hnorm);
+      }
       Hes[l_plus_1][li] = hnorm;
       if (qr_fact(krydim, li) != 0) co_return SPGMR_QRFACT_FAIL;
       rotation_product *= givens[2 * li + 1];

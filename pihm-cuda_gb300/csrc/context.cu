@@ -247,6 +247,8 @@ int pihm_gpu_set_stream(pihm_gpu_ctx *c, void *stream) {
   return PIHM_GPU_OK;
 }
 
+void *pihm_gpu_get_stream(const pihm_gpu_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
 int pihm_gpu_sizes(const pihm_gpu_ctx *c, int32_t *ne, int32_t *nr, int64_t *neq) {
   if (!c) return PIHM_GPU_ERR_ARG;
   if (ne) *ne = c->ne;

@@ -35,15 +35,20 @@ extern "C" {
 // vectors' stream; host N_Vectors go through the host-buffer path.  A NaN
 // derivative returns -1 (CV_RHSFUNC_FAIL path) where the reference exits
 // (src/ode.c:401-410).
+static int ode_launch_device(pihm_gpu_ctx *c, N_Vector y, N_Vector ydot) {
+  if (N_VGetLength_PihmGpu(y) != c->neq || N_VGetLength_PihmGpu(ydot) != c->neq) return -1;
+  c->m.diag = c->diag;
+  return pihm::launch_rhs(c->m, N_VGetDeviceArrayPointer_PihmGpu(y), N_VGetDeviceArrayPointer_PihmGpu(ydot),
+                          c->stream, &c->launches, c->prof, &c->side) == cudaSuccess
+             ? 0
+             : -1;
+}
+
 int pihm_gpu_ode(double t, N_Vector y, N_Vector ydot, void *user_data) {
   pihm_gpu_ctx *c = (pihm_gpu_ctx *)user_data;
   if (!c || !y || !ydot) return -1;
   if (is_device_vector(y) && is_device_vector(ydot)) {
-    if (N_VGetLength_PihmGpu(y) != c->neq || N_VGetLength_PihmGpu(ydot) != c->neq) return -1;
-    c->m.diag = c->diag;
-    if (pihm::launch_rhs(c->m, N_VGetDeviceArrayPointer_PihmGpu(y), N_VGetDeviceArrayPointer_PihmGpu(ydot),
-                         c->stream, &c->launches, c->prof, &c->side) != cudaSuccess)
-      return -1;
+    if (ode_launch_device(c, y, ydot)) return -1;
     if (c->nan_check_deferred) return 0;
     return pihm_gpu_status(c) == PIHM_GPU_OK ? 0 : -1;
   }
@@ -53,6 +58,15 @@ int pihm_gpu_ode(double t, N_Vector y, N_Vector ydot, void *user_data) {
   }
   return -1;
 }
+
+int pihm_gpu_ode_launch(double t, N_Vector y, N_Vector ydot, void *user_data) {
+  (void)t;
+  pihm_gpu_ctx *c = (pihm_gpu_ctx *)user_data;
+  if (!c || !is_device_vector(y) || !is_device_vector(ydot)) return -1;
+  return ode_launch_device(c, y, ydot);
+}
+
+const unsigned int *pihm_gpu_error_word(pihm_gpu_ctx *c) { return c ? c->m.err : nullptr; }
 
 int pihm_gpu_set_nan_check(pihm_gpu_ctx *c, int deferred) {
   if (!c) return PIHM_GPU_ERR_ARG;

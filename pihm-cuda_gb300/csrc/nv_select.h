@@ -79,7 +79,7 @@ struct EwCall {
 
 // N_VLinearSum: z = a*x + b*y, nvector_serial.c:421-506
 template <class H>
-EwCall<H> select_linear_sum(double a, H x, double b, H y, H z) {
+PIHM_HD EwCall<H> select_linear_sum(double a, H x, double b, H y, H z) {
   if (b == 1.0 && z == y) {
     if (a == 1.0) return {EW_AXPY1, a, b, x, y, z};
     if (a == -1.0) return {EW_AXPYM1, a, b, x, y, z};
@@ -118,6 +118,30 @@ EwCall<H> select_scale(double c, H x, H z) {
   if (c == 1.0) return {EW_COPY, 0, 0, x, x, z};
   if (c == -1.0) return {EW_NEG, 0, 0, x, x, z};
   return {EW_SCALE, c, 0, x, x, z};
+}
+
+// Coefficients of a linear sum taken from device-resident reduction results
+// (slots): the values a GMRES iteration forms on the host from a norm or a
+// dot product -- sig = 1/||v|| and 1/sig in the difference-quotient product,
+// -h in Gram-Schmidt -- formed here with the same IEEE operations.
+enum CoefKind { COEF_HOST = 0, COEF_NEG, COEF_INV, COEF_INV_INV, COEF_NEG_INV_INV };
+
+PIHM_HD inline double coef_div(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __ddiv_rn(a, b);
+#else
+  return a / b;
+#endif
+}
+
+PIHM_HD inline double coef_value(int kind, double value, double s) {
+  switch (kind) {
+    case COEF_NEG: return -s;
+    case COEF_INV: return coef_div(1.0, s);
+    case COEF_INV_INV: return coef_div(1.0, coef_div(1.0, s));
+    case COEF_NEG_INV_INV: return -coef_div(1.0, coef_div(1.0, s));
+    default: return value;
+  }
 }
 
 }  // namespace pihm_nv

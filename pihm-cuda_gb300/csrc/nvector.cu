@@ -34,12 +34,14 @@ struct Scratch {
   double *partials = nullptr;   // [kMaxBlocks]
   unsigned int *ticket = nullptr;
   double *result = nullptr;     // [2] value, flag
-  double *host = nullptr;       // pinned [2]
+  double *slots = nullptr;      // [2 * PIHM_NV_SLOTS] value, flag per slot
+  double *host = nullptr;       // pinned [2 + 2 * PIHM_NV_SLOTS + 1]
 };
 
 // Scratch layout: partial values [kMaxBlocks], partial flags [kMaxBlocks],
-// result [2], ticket.
-constexpr size_t kScratchDoubles = 2 * kMaxBlocks + 4;
+// result [2], ticket, one spare, slots [2 * PIHM_NV_SLOTS].
+constexpr size_t kScratchDoubles = 2 * kMaxBlocks + 4 + 2 * PIHM_NV_SLOTS;
+constexpr size_t kHostDoubles = 2 + 2 * PIHM_NV_SLOTS + 1;
 
 static int scratch_alloc(Scratch &s) {
   void *p = nullptr;
@@ -48,8 +50,9 @@ static int scratch_alloc(Scratch &s) {
   s.partials = (double *)c;
   s.result = (double *)(c + sizeof(double) * 2 * kMaxBlocks);
   s.ticket = (unsigned int *)(c + sizeof(double) * (2 * kMaxBlocks + 2));
+  s.slots = (double *)(c + sizeof(double) * (2 * kMaxBlocks + 4));
   if (cudaMemset(p, 0, sizeof(double) * kScratchDoubles) != cudaSuccess) return -1;
-  if (cudaMallocHost(&s.host, sizeof(double) * 2) != cudaSuccess) return -1;
+  if (cudaMallocHost(&s.host, sizeof(double) * kHostDoubles) != cudaSuccess) return -1;
   return 0;
 }
 
@@ -143,7 +146,8 @@ template <int OP>
 __global__ void __launch_bounds__(kThreads) k_red(long long n, const double *__restrict__ x,
                                                   const double *__restrict__ y, double *__restrict__ z,
                                                   double *partials, double *partials_f,
-                                                  unsigned int *ticket, double *result) {
+                                                  unsigned int *ticket, double *result,
+                                                  long long wrms_n) {
   __shared__ Pair sh[kThreads / 32];
   __shared__ bool last;
   Pair acc = red_identity<OP>();
@@ -211,9 +215,57 @@ __global__ void __launch_bounds__(kThreads) k_red(long long n, const double *__r
   }
   v = red_block<OP>(v, sh);
   if (threadIdx.x == 0) {
-    result[0] = v.v;
+    // wrms_n > 0: the WRMS norm sqrt(sum / n) itself, as N_VWrmsNorm forms it
+    result[0] = wrms_n > 0 ? __dsqrt_rn(__ddiv_rn(v.v, (double)wrms_n)) : v.v;
     result[1] = v.f;
     *ticket = 0u;
+  }
+}
+
+// z = a*x + b*y with a and b formed from device-resident slots: one thread
+// of each block forms the coefficients and makes the serial N_Vector's case
+// analysis from their values (operand tags 0 = x, 1 = y; ztag 0 when z is x,
+// 1 when z is y, 2 otherwise), then the block runs the chosen variant.
+template <int OP>
+__device__ __forceinline__ void ew_loop(long long n, double a, double b, const double *x, const double *y,
+                                        double *z) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double xv = ew_reads_x(OP) ? x[i] : 0.0;
+    const double yv = ew_reads_y(OP) ? y[i] : 0.0;
+    const double zv = ew_reads_z(OP) ? z[i] : 0.0;
+    z[i] = ew_eval<OP>(a, b, xv, yv, zv);
+  }
+}
+
+__global__ void k_lin_coef(long long n, int ka, int sa, double va, int kb, int sb, double vb, int ztag,
+                           const double *x, const double *y, double *z, const double *slots) {
+  __shared__ int s_op, s_xt, s_yt;
+  __shared__ double s_a, s_b;
+  if (threadIdx.x == 0) {
+    const double a = coef_value(ka, va, ka == COEF_HOST ? 0.0 : slots[2 * sa]);
+    const double b = coef_value(kb, vb, kb == COEF_HOST ? 0.0 : slots[2 * sb]);
+    const EwCall<int> c = select_linear_sum<int>(a, 0, b, 1, ztag);
+    s_op = c.op;
+    s_a = c.a;
+    s_b = c.b;
+    s_xt = c.x;
+    s_yt = c.y;
+  }
+  __syncthreads();
+  const double *px = s_xt == 0 ? x : y, *py = s_yt == 0 ? x : y;
+  const double a = s_a, b = s_b;
+  switch (s_op) {
+    case EW_LIN: ew_loop<EW_LIN>(n, a, b, px, py, z); break;
+    case EW_LIN1: ew_loop<EW_LIN1>(n, a, b, px, py, z); break;
+    case EW_LIN2: ew_loop<EW_LIN2>(n, a, b, px, py, z); break;
+    case EW_SUM: ew_loop<EW_SUM>(n, a, b, px, py, z); break;
+    case EW_DIFF: ew_loop<EW_DIFF>(n, a, b, px, py, z); break;
+    case EW_SCALESUM: ew_loop<EW_SCALESUM>(n, a, b, px, py, z); break;
+    case EW_SCALEDIFF: ew_loop<EW_SCALEDIFF>(n, a, b, px, py, z); break;
+    case EW_AXPY: ew_loop<EW_AXPY>(n, a, b, px, py, z); break;
+    case EW_AXPY1: ew_loop<EW_AXPY1>(n, a, b, px, py, z); break;
+    default: ew_loop<EW_AXPYM1>(n, a, b, px, py, z); break;
   }
 }
 
@@ -225,9 +277,9 @@ namespace pihm_nv {
 // carved from the caller's buffer), leave the result in result_dev[0..1].
 template <int OP>
 static int red_launch(long long n, const double *x, const double *y, double *z, double *partials,
-                      unsigned int *ticket, double *result_dev, cudaStream_t st) {
+                      unsigned int *ticket, double *result_dev, cudaStream_t st, long long wrms_n = 0) {
   const unsigned g = red_grid_for(n);
-  k_red<OP><<<g, kThreads, 0, st>>>(n, x, y, z, partials, partials + kMaxBlocks, ticket, result_dev);
+  k_red<OP><<<g, kThreads, 0, st>>>(n, x, y, z, partials, partials + kMaxBlocks, ticket, result_dev, wrms_n);
   return cudaGetLastError() == cudaSuccess ? 0 : -2;
 }
 
@@ -472,6 +524,57 @@ double N_VMinQuotient_PihmGpu(N_Vector num, N_Vector denom) {
   red_family<R_MINQ>(C(num)->fam, L(num), D(num), D(denom), nullptr, r);
   return (r[1] != 0.0) ? r[0] : kBigReal;
 }
+
+// ---------------------------------------------------------------------------
+// device-resident scalars
+// ---------------------------------------------------------------------------
+int N_VDotProdSlot_PihmGpu(N_Vector x, N_Vector y, int slot) {
+  if (!x || !y || slot < 0 || slot >= PIHM_NV_SLOTS) return -1;
+  Scratch &s = C(x)->fam->scratch;
+  return red_launch<R_DOT>(L(x), D(x), D(y), nullptr, s.partials, s.ticket, s.slots + 2 * slot, S(x));
+}
+
+int N_VWrmsNormSlot_PihmGpu(N_Vector x, N_Vector w, int slot) {
+  if (!x || !w || slot < 0 || slot >= PIHM_NV_SLOTS || L(x) <= 0) return -1;
+  Scratch &s = C(x)->fam->scratch;
+  return red_launch<R_WSQ>(L(x), D(x), D(w), nullptr, s.partials, s.ticket, s.slots + 2 * slot, S(x), L(x));
+}
+
+int N_VLinearSumCoef_PihmGpu(const pihm_nv_coef *a, N_Vector x, const pihm_nv_coef *b, N_Vector y,
+                             N_Vector z) {
+  if (!a || !b || !x || !y || !z) return -1;
+  for (const pihm_nv_coef *c : {a, b})
+    if (c->kind < PIHM_NV_COEF_HOST || c->kind > PIHM_NV_COEF_NEG_INV_INV ||
+        (c->kind != PIHM_NV_COEF_HOST && (c->slot < 0 || c->slot >= PIHM_NV_SLOTS)))
+      return -1;
+  const long long n = L(x);
+  if (a->kind == PIHM_NV_COEF_HOST && b->kind == PIHM_NV_COEF_HOST)
+    return linear_sum(a->value, D(x), b->value, D(y), D(z), n, S(z));
+  if (n <= 0) return 0;
+  const int ztag = D(z) == D(x) ? 0 : (D(z) == D(y) ? 1 : 2);
+  k_lin_coef<<<grid_for(n), kThreads, 0, S(z)>>>(n, a->kind, a->slot, a->value, b->kind, b->slot, b->value, ztag,
+                                                  D(x), D(y), D(z), C(z)->fam->scratch.slots);
+  return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
+
+int N_VFetchSlots_PihmGpu(N_Vector v, int count, double *out, const unsigned int *dev_word,
+                          unsigned int *word_out) {
+  if (!v || count < 0 || count > PIHM_NV_SLOTS || (count > 0 && !out) || (dev_word && !word_out)) return -1;
+  Scratch &s = C(v)->fam->scratch;
+  double *h = s.host + 2;  // after the reductions' own result pair
+  if (count > 0 &&
+      cudaMemcpyAsync(h, s.slots, sizeof(double) * 2 * count, cudaMemcpyDeviceToHost, S(v)) != cudaSuccess)
+    return -2;
+  unsigned int *hw = (unsigned int *)(h + 2 * PIHM_NV_SLOTS);
+  if (dev_word && cudaMemcpyAsync(hw, dev_word, sizeof(unsigned int), cudaMemcpyDeviceToHost, S(v)) != cudaSuccess)
+    return -2;
+  if (cudaStreamSynchronize(S(v)) != cudaSuccess) return -2;
+  for (int i = 0; i < count; i++) out[i] = h[2 * i];
+  if (dev_word) *word_out = *hw;
+  return 0;
+}
+
+void *N_VGetStream_PihmGpu(N_Vector v) { return v ? (void *)S(v) : nullptr; }
 
 // ---------------------------------------------------------------------------
 // raw-pointer entry points: a library workspace per stream, created on first

@@ -10,6 +10,13 @@ _D = ctypes.c_double
 _NV = ctypes.c_void_p
 _lib = None
 
+COEF_HOST, COEF_NEG, COEF_INV, COEF_INV_INV, COEF_NEG_INV_INV = range(5)
+
+
+class Coef(ctypes.Structure):
+    """pihm_nv_coef: a linear-sum coefficient, a constant or formed from a slot."""
+    _fields_ = [("kind", ctypes.c_int32), ("slot", ctypes.c_int32), ("value", ctypes.c_double)]
+
 
 def load() -> ctypes.CDLL:
     global _lib
@@ -46,6 +53,12 @@ def load() -> ctypes.CDLL:
         "N_VInvTest_PihmGpu": ([_NV, _NV], ctypes.c_int),
         "N_VConstrMask_PihmGpu": ([_NV, _NV, _NV], ctypes.c_int),
         "N_VMinQuotient_PihmGpu": ([_NV, _NV], _D),
+        "N_VDotProdSlot_PihmGpu": ([_NV, _NV, ctypes.c_int], ctypes.c_int),
+        "N_VWrmsNormSlot_PihmGpu": ([_NV, _NV, ctypes.c_int], ctypes.c_int),
+        "N_VLinearSumCoef_PihmGpu": ([ctypes.POINTER(Coef), _NV, ctypes.POINTER(Coef), _NV, _NV], ctypes.c_int),
+        "N_VFetchSlots_PihmGpu": ([_NV, ctypes.c_int, ctypes.POINTER(_D), _VP, ctypes.POINTER(ctypes.c_uint)],
+                                  ctypes.c_int),
+        "N_VGetStream_PihmGpu": ([_NV], _VP),
         "pihm_gpu_nv_linear_sum": ([_D, _VP, _D, _VP, _VP, ctypes.c_int64, _VP], ctypes.c_int),
         "pihm_gpu_nv_wrms_norm": ([_VP, _VP, ctypes.c_int64, _VP, ctypes.POINTER(_D)], ctypes.c_int),
         "pihm_gpu_nv_dot_prod": ([_VP, _VP, ctypes.c_int64, _VP, ctypes.POINTER(_D)], ctypes.c_int),

@@ -43,6 +43,8 @@ def _bind(lib):
         "pihm_bdf_set_max_num_steps": ([_VP, ctypes.c_long], ctypes.c_int),
         "pihm_bdf_set_stab_lim_det": ([_VP, ctypes.c_int], ctypes.c_int),
         "pihm_bdf_set_stop_time": ([_VP, _D], ctypes.c_int),
+        "pihm_bdf_set_deferred_scalars": ([_VP, ctypes.c_int], ctypes.c_int),
+        "pihm_bdf_get_deferred_scalars": ([_VP], ctypes.c_int),
         "pihm_bdf_solve": ([_VP, _D, _VP, ctypes.POINTER(_D)], ctypes.c_int),
         "pihm_bdf_get_stats": ([_VP, ctypes.POINTER(BdfStats)], ctypes.c_int),
         "pihm_bdf_free": ([_VP], None),
@@ -96,7 +98,7 @@ class Bdf:
 
 
 def run_steps(backend, ctrl: StepControl, nsteps: int, forcing, record_every: int = 0,
-              outlet: int | None = None, water_balance: bool = False):
+              outlet: int | None = None, water_balance: bool = False, deferred_scalars: int | None = None):
     """The reference's model-step loop over `backend`, from t = 0.
 
     backend provides: y (N_Vector handle of the state), rhs (C function
@@ -105,6 +107,9 @@ def run_steps(backend, ctrl: StepControl, nsteps: int, forcing, record_every: in
     forcing(k) is called as backend.set_forcing(k) before step k.
     water_balance: record backend.water_balance(dt) -> (sources, sinks,
     storage) after every step (PrintWaterBal, src/print.c:337-542).
+    deferred_scalars: pihm_bdf_set_deferred_scalars (None keeps the
+    library's default: GMRES scalars kept on the device for device vectors
+    with pihm_gpu_ode; the same solution either way).
     Returns dict(states=[...], outlet=[...], stats=BdfStats, wb=[nsteps][3]).
     """
     bdf = Bdf()
@@ -114,6 +119,8 @@ def run_steps(backend, ctrl: StepControl, nsteps: int, forcing, record_every: in
     bdf.check("ud", lib.pihm_bdf_set_user_data(bdf.h, backend.user_data))
     bdf.check("h0", lib.pihm_bdf_set_init_step(bdf.h, ctrl.initstep))
     bdf.check("stald", lib.pihm_bdf_set_stab_lim_det(bdf.h, 1))
+    if deferred_scalars is not None:
+        bdf.check("deferred", lib.pihm_bdf_set_deferred_scalars(bdf.h, int(deferred_scalars)))
     maxstep = float(ctrl.stepsize)
     bdf.check("hmax", lib.pihm_bdf_set_max_step(bdf.h, maxstep))
     bdf.check("mxstep", lib.pihm_bdf_set_max_num_steps(bdf.h, ctrl.mxstep or ctrl.stepsize * 10))
@@ -145,6 +152,7 @@ def run_steps(backend, ctrl: StepControl, nsteps: int, forcing, record_every: in
             wb.append(backend.water_balance(ctrl.stepsize))
         if record_every and (k + 1) % record_every == 0:
             states.append(backend.read_state())
-    out = dict(states=np.array(states), outlet=np.array(qout), stats=bdf.stats(), wb=np.array(wb))
+    out = dict(states=np.array(states), outlet=np.array(qout), stats=bdf.stats(), wb=np.array(wb),
+               deferred_scalars=lib.pihm_bdf_get_deferred_scalars(bdf.h))
     bdf.close()
     return out

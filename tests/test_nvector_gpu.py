@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 
 import nvector_oracle as NO
+import pihm_gpu.nvector as NV
 
 pytestmark = pytest.mark.gpu
 
@@ -152,3 +153,95 @@ def test_raw_entry_points(nv):
     assert abs(r - NO.wrms(x, w)) <= 1e-13 * NO.wrms(x, w)
     d = nvector.dot_prod(tx.data_ptr(), tw.data_ptr(), n)
     assert abs(d - NO.dot(x, w)) <= 1e-13 * float(np.abs(x * w).sum())
+
+
+def _coef_value(kind, s, value=0.0):
+    # the host forms of pihm_nv_coef (IEEE double, as the integrator forms them)
+    if kind == NV.COEF_NEG:
+        return -s
+    if kind == NV.COEF_INV:
+        return 1.0 / s
+    if kind == NV.COEF_INV_INV:
+        return 1.0 / (1.0 / s)
+    if kind == NV.COEF_NEG_INV_INV:
+        return -(1.0 / (1.0 / s))
+    return value
+
+
+SLOT_VALUES = [1.0, -1.0, 0.37, 2.5, -0.7, 0.7, 3.0, 1e-300]
+
+
+@pytest.mark.parametrize("n", [7, 65_537, 3_060_000])
+def test_device_scalars(nv, n):
+    """Slot reductions equal the reductions that return to the host, bit for
+    bit; linear sums with slot-derived coefficients equal N_VLinearSum with
+    the host-formed coefficients (the case analysis made from the values on
+    the device), for every coefficient kind and z aliasing."""
+    lib, torch = nv
+    rng = np.random.default_rng(300 + n)
+    base = lib.N_VNew_PihmGpu(n, None)
+    vecs = [lib.N_VClone_PihmGpu(base) for _ in range(5)]
+    vx, vy, vz, ve, vo = vecs
+
+    def put(v, a):
+        a = np.ascontiguousarray(a, np.float64)
+        assert lib.N_VCopyFromHost_PihmGpu(v, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))) == 0
+
+    def get(v):
+        out = np.empty(n)
+        assert lib.N_VCopyToHost_PihmGpu(v, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))) == 0
+        return out
+
+    def set_slot(slot, value):
+        e = np.zeros(n)
+        e[0] = value
+        put(ve, e)
+        put(vo, np.ones(n))
+        assert lib.N_VDotProdSlot_PihmGpu(ve, vo, slot) == 0
+
+    def fetch(count, word=None):
+        out = (ctypes.c_double * count)()
+        w = ctypes.c_uint(0)
+        assert lib.N_VFetchSlots_PihmGpu(base, count, out, ctypes.c_void_p(word) if word else None,
+                                         ctypes.byref(w)) == 0
+        return list(out), w.value
+
+    x = rng.normal(size=n)
+    w = rng.uniform(1e3, 1e5, n)
+    put(vx, x)
+    put(vy, w)
+    assert lib.N_VDotProdSlot_PihmGpu(vx, vy, 2) == 0
+    assert lib.N_VWrmsNormSlot_PihmGpu(vx, vy, 3) == 0
+    s2, s3 = fetch(4)[0][2:]
+    assert s2 == lib.N_VDotProd_PihmGpu(vx, vy)
+    assert s3 == lib.N_VWrmsNorm_PihmGpu(vx, vy)
+    # the error word travels with the slots
+    word = torch.tensor([7], dtype=torch.int32, device="cuda")
+    vals, wv = fetch(4, word.data_ptr())
+    assert wv == 7 and vals[2] == s2
+
+    y = rng.normal(size=n)
+    kinds = [NV.COEF_HOST, NV.COEF_NEG, NV.COEF_INV, NV.COEF_INV_INV, NV.COEF_NEG_INV_INV]
+    large = n > 100_000
+    checked = 0
+    for sa in (SLOT_VALUES[:3] if large else SLOT_VALUES):
+        for sb in ((-1.0,) if large else (1.0, -1.0, 0.37, -0.37)):
+            set_slot(0, sa)
+            set_slot(1, sb)
+            for ka in kinds:
+                for kb in ((NV.COEF_NEG, NV.COEF_NEG_INV_INV) if large else kinds):
+                    a = _coef_value(ka, sa, sa)
+                    b = _coef_value(kb, sb, sb)
+                    for alias in (None, "x", "y"):
+                        put(vx, x)
+                        put(vy, y)
+                        vzz = vx if alias == "x" else (vy if alias == "y" else vz)
+                        ca = NV.Coef(ka, 0, sa if ka == NV.COEF_HOST else 0.0)
+                        cb = NV.Coef(kb, 1, sb if kb == NV.COEF_HOST else 0.0)
+                        assert lib.N_VLinearSumCoef_PihmGpu(ctypes.byref(ca), vx, ctypes.byref(cb), vy, vzz) == 0
+                        want = NO.linear_sum(a, x, b, y, alias)
+                        assert np.array_equal(get(vzz), want), (sa, sb, ka, kb, alias)
+                        checked += 1
+    assert checked > 0
+    for v in vecs + [base]:
+        lib.N_VDestroy_PihmGpu(v)

@@ -36,19 +36,25 @@ def _golden():
     return ws, z, ctrl
 
 
-def _run(backend_cls, ws, z, ctrl, **kw):
+def _run(backend_cls, ws, z, ctrl, deferred_scalars=None, **kw):
     nsteps = z["outlet_q"].shape[0]
     b = backend_cls(ws, z["y0"], z["pcp"], z["edir"], z["ett"], **kw)
     try:
         return run_steps(b, ctrl, nsteps, b.set_forcing, record_every=int(z["every"]),
-                         outlet=int(z["outlet"]), water_balance=True)
+                         outlet=int(z["outlet"]), water_balance=True, deferred_scalars=deferred_scalars)
     finally:
         b.close()
 
 
-def test_integrator_reproduces_reference_cvode_on_cpu():
+@pytest.mark.parametrize("deferred", [0, 1], ids=["plain", "deferred_scalars"])
+def test_integrator_reproduces_reference_cvode_on_cpu(deferred):
+    """deferred_scalars runs the GMRES iteration that keeps its norm and
+    Gram-Schmidt dot products with the vectors (bdf_core.h
+    atimes_gs_deferred) with the values held on the host: same operations in
+    the same order, so CVODE's run is reproduced bit for bit either way."""
     ws, z, ctrl = _golden()
-    res = _run(OracleBackend, ws, z, ctrl)
+    res = _run(OracleBackend, ws, z, ctrl, deferred_scalars=deferred)
+    assert res["deferred_scalars"] == deferred
     s = res["stats"]
     got = [s.nst, s.nfe, s.nni, s.ncfn, s.netf, s.nli, s.nfes]
     assert got == list(z["stats"]), (got, list(z["stats"]))
@@ -135,3 +141,38 @@ def test_gpu_solve_hydrograph_and_storages():
     print(f"water-balance residual: GPU {e_gpu:.4g} m3, reference {e_ref:.4g} m3, "
           f"perturbed reference {min(runs):.4g} .. {max(runs):.4g} m3 (storage {z['wb'][-1, 2]:.4g} m3)")
     assert e_gpu <= wenv
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["c0_golden", "generated_60k"])
+def test_gpu_deferred_scalars_same_solve(case):
+    """GMRES with its norm and Gram-Schmidt dot products kept on the device
+    and the right-hand side's status read back with them (the default for
+    pihm_gpu_ode on device vectors) makes the solve of the plain iteration
+    bit for bit: every state, outlet value and counter."""
+    from pihm_gpu import workloads as WL
+    if case == "c0_golden":
+        ws, z, ctrl = _golden()
+        y0, pcp, edir, ett, nsteps = z["y0"], z["pcp"], z["edir"], z["ett"], 240
+        outlet = int(z["outlet"])
+    else:
+        ws = W.generate(60_000, WL.river_count(60_000), seed=4)
+        ctrl, nsteps = StepControl(), 6
+        pcp, edir, ett = WL.step_forcing(ws, nsteps, 60.0, seed=3)
+        y0 = W.relax_state(ws)
+        outlet = int(np.where(np.asarray(ws.arrays["down"]) < 0)[0][0])
+    res = {}
+    for mode in (0, -1):
+        b = GpuBackend(ws, y0, pcp, edir, ett)
+        try:
+            res[mode] = run_steps(b, ctrl, nsteps, b.set_forcing, record_every=nsteps // 2, outlet=outlet,
+                                  deferred_scalars=mode)
+        finally:
+            b.close()
+    assert res[0]["deferred_scalars"] == 0 and res[-1]["deferred_scalars"] == 3
+    s0, s1 = res[0]["stats"], res[-1]["stats"]
+    print(f"{case}: {s1.nst} steps, {s1.nli} GMRES iterations, {s1.nfe + s1.nfes} evaluations")
+    assert [s0.nst, s0.nfe, s0.nni, s0.ncfn, s0.netf, s0.nli, s0.nfes] == \
+        [s1.nst, s1.nfe, s1.nni, s1.ncfn, s1.netf, s1.nli, s1.nfes]
+    assert np.array_equal(res[0]["states"], res[-1]["states"])
+    assert np.array_equal(res[0]["outlet"], res[-1]["outlet"])
