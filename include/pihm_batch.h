@@ -29,6 +29,7 @@
 
 #include "pihm_bdf.h"
 #include "pihm_gpu.h"
+#include "pihm_land.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -64,6 +65,23 @@ typedef struct pihm_batch_job {
     /* spatially uniform forcing per model step [nsteps]: pcpdrp, edir, ett (m/s) */
     const double *pcpdrp, *edir, *ett;
     int32_t outlet;           /* segment whose DOWN_CHANL2CHANL flux is recorded per step, -1: none */
+    /* An input deck's own forcing, as the reference's main loop applies it
+     * (src/pihm.c:15-66); all optional, zero/NULL for the uniform series
+     * above.  The pointers must stay valid until the watershed is released.
+     *   deck      ApplyBc every model step from the deck's .bc series
+     *             (pihm_deck_bc at start + k stepsize); elem_bc/river_bc
+     *             are then unused
+     *   land, forcing   the land-surface step (include/pihm_land.h) every
+     *             lsm_step seconds, ApplyForc + IntcpSnowEt writing this
+     *             watershed's pcpdrp, edir and ett; the uniform series are
+     *             then unused (may be NULL).  The series must cover the run
+     *   cmc0, sneqv0    initial canopy storage and snow (NULL: zeros)
+     *   start     model time of step 0 (s since 1970 UTC) */
+    const struct pihm_deck *deck;
+    const pihm_land_params *land;
+    const pihm_forcing_series *forcing;
+    const double *cmc0, *sneqv0;
+    int64_t start, lsm_step;
 } pihm_batch_job;
 
 enum { PIHM_BATCH_RUNNING = 0, PIHM_BATCH_DONE = 1, PIHM_BATCH_FAILED = 2 };
@@ -115,6 +133,8 @@ typedef struct pihm_batch_info {
     double host_ms, wait_ms, program_ms, rhs_ms;
     int32_t program_variant;  /* variant of the program kernel in use */
     int32_t tuning;           /* 1 while the tuner is still timing variants */
+    int32_t rhs_shape;        /* block shape of the element kernel in use (pihm_batch_set_rhs_shape) */
+    int32_t rhs_tuning;       /* 1 while the tuner is still timing shapes */
 } pihm_batch_info;
 int pihm_batch_get_info(const pihm_batch *b, pihm_batch_info *info);
 int pihm_batch_set_profiling(pihm_batch *b, int on);
@@ -125,6 +145,15 @@ int pihm_batch_set_profiling(pihm_batch *b, int on);
  * 0..2 forces one. */
 int pihm_batch_set_program_variant(pihm_batch *b, int32_t variant);
 
+/* The right-hand side's element kernel (k_elem_main) comes in three block
+ * shapes with the same register budget -- 0: 512 threads x 2 blocks per SM,
+ * 1: 256 x 4, 2: 128 x 8 -- that give identical results: large blocks are
+ * fastest over large arenas, small ones spread a small or sparsely occupied
+ * arena over more SMs.  By default (-1) the engine times them on its first
+ * evaluations over at least 20,000 elements and keeps the fastest per
+ * element; 0..2 forces one. */
+int pihm_batch_set_rhs_shape(pihm_batch *b, int32_t shape);
+
 /* ---- serving --------------------------------------------------------------
  * Requests are submitted with an arrival time (seconds after the start of
  * pihm_serve_run).  From its arrival on, a request is prepared on one of
@@ -133,7 +162,9 @@ int pihm_batch_set_program_variant(pihm_batch *b, int32_t variant);
  * arena has room, join the rounds in flight, and are retired (results copied
  * to the host, arena ranges freed) the moment they finish.  A request larger
  * than the whole arena fails with PIHM_GPU_ERR_NOMEM.  Submit every request
- * before pihm_serve_run; it returns when all have been served. */
+ * before pihm_serve_run; it returns when all have been served.  The job's
+ * arrays are copied at submission; a deck job's deck, land parameters and
+ * forcing series are not and must stay valid until pihm_serve_run returns. */
 typedef struct pihm_serve_record {
     int32_t status;      /* PIHM_BATCH_RUNNING (queued or resident), _DONE, _FAILED */
     int32_t solver_rc;   /* integrator return code, or the admission error */

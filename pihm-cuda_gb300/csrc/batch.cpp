@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "batch_engine.h"
+#include "pihm_deck.h"
 
 using namespace pihm;
 using namespace pihm::batch;
@@ -92,7 +93,10 @@ Task<int> model_run(Sys *s) {
   long nst0 = 0, ncfn0 = 0, nni0 = 0;
   double tret = 0.0;
   for (int k = 0; k < s->nsteps; k++) {
-    co_await o.forcing(s->pcp[k], s->edir[k], s->ett[k]);
+    // the step's forcing: the uniform series, or the deck's boundary values
+    // and land-surface step, which the round that runs this program applies
+    if (!s->land.alloc) co_await o.forcing(s->pcp[k], s->edir[k], s->ett[k]);
+    if (s->has_bc || s->land.alloc) s->pending_k = k;
     const double tout = (double)(k + 1) * ct.stepsize;
     if ((rc = c.set_stop_time(tout)) != bdf::SUCCESS) co_return rc;
     rc = co_await c.solve(tout, Y, &tret);
@@ -310,7 +314,9 @@ void resume(Sys *s) {
 // Validate a job and build everything the arena needs from it on the host.
 int prepare(const pihm_batch_job *job, int surf_mode, int riv_mode, int order, Prepared *p) {
   if (!job || !job->mesh || !job->y0 || !p || job->nsteps < 0 ||
-      (job->nsteps > 0 && (!job->pcpdrp || !job->edir || !job->ett)))
+      (job->nsteps > 0 && !job->land && (!job->pcpdrp || !job->edir || !job->ett)))
+    return PIHM_GPU_ERR_ARG;
+  if (job->land && (!job->forcing || job->lsm_step <= 0 || job->land->nelem != job->mesh->nelem))
     return PIHM_GPU_ERR_ARG;
   const pihm_step_control &c = job->ctrl;
   if (!(c.stepsize > 0.0) || c.reltol < 0 || c.abstol < 0 || !(c.decr > 0.0)) return PIHM_GPU_ERR_ARG;
@@ -322,12 +328,79 @@ int prepare(const pihm_batch_job *job, int surf_mode, int riv_mode, int order, P
   p->y0.assign(job->y0, job->y0 + neq);
   if (job->elem_bc) p->elem_bc.assign(job->elem_bc, job->elem_bc + 3 * (size_t)ne);
   if (job->river_bc) p->river_bc.assign(job->river_bc, job->river_bc + nr);
-  p->pcp.assign(job->pcpdrp, job->pcpdrp + job->nsteps);
-  p->edir.assign(job->edir, job->edir + job->nsteps);
-  p->ett.assign(job->ett, job->ett + job->nsteps);
+  if (!job->land) {
+    p->pcp.assign(job->pcpdrp, job->pcpdrp + job->nsteps);
+    p->edir.assign(job->edir, job->edir + job->nsteps);
+    p->ett.assign(job->ett, job->ett + job->nsteps);
+  }
   p->ctrl = c;
   p->nsteps = job->nsteps;
   p->outlet = job->outlet;
+  // a deck's forcing
+  p->deck = job->deck;
+  if (job->deck) {
+    for (int q = 0; q < 3 * ne && !p->has_bc; q++) p->has_bc = job->mesh->bc_type[q] != 0;
+    for (int r = 0; r < nr && !p->has_bc; r++) p->has_bc = job->mesh->riverbc_type[r] != 0;
+  }
+  p->land = job->land;
+  p->forcing = job->forcing;
+  p->start = job->start;
+  p->lsm_step = job->lsm_step;
+  if (job->land) {
+    p->cmc0.assign(ne, 0.0);
+    p->sneqv0.assign(ne, 0.0);
+    if (job->cmc0) p->cmc0.assign(job->cmc0, job->cmc0 + ne);
+    if (job->sneqv0) p->sneqv0.assign(job->sneqv0, job->sneqv0 + ne);
+  }
+  return PIHM_GPU_OK;
+}
+
+// The deck's forcing of a watershed in the arena: the land-surface instance
+// reading this watershed's mesh planes and writing its forcing planes, its
+// initial storage, and the pinned staging of the boundary values.
+int attach_deck(pihm_batch *B, Sys *s, const Prepared &p) {
+  s->deck = p.deck;
+  s->has_bc = p.has_bc;
+  s->start = p.start;
+  s->lsm_step = p.lsm_step;
+  if (s->has_bc && cudaMallocHost(&s->bc_stage, sizeof(double) * (3 * (size_t)s->ne + s->nr)) != cudaSuccess) {
+    s->bc_stage = nullptr;
+    return PIHM_GPU_ERR_NOMEM;
+  }
+  if (!p.land) return PIHM_GPU_OK;
+  DevMesh &m = B->A.m;
+  const int64_t eo = s->eoff;
+  LandTargets tg{m.depth + eo, m.porosity + eo, m.rzd + eo, m.d_rzd + eo, const_cast<double *>(m.pcpdrp) + eo,
+                 const_cast<double *>(m.edir) + eo, const_cast<double *>(m.ett) + eo};
+  int rc = land_build(p.land, p.forcing, p.im.perm.data(), s->ne, p.im.el[EP_ZMAX].data(), tg, &s->land);
+  if (rc != PIHM_GPU_OK) return rc;
+  // every land-surface step of the run must lie inside the series
+  const int64_t step = (int64_t)p.ctrl.stepsize;
+  const int64_t last = (int64_t)(p.nsteps > 0 ? p.nsteps - 1 : 0) * step;
+  const int64_t t_end = p.start + last - last % p.lsm_step;
+  if (p.start < s->land.t_lo || t_end > s->land.t_hi) return PIHM_GPU_ERR_ARG;
+  return land_set_state(s->land, p.im.perm.data(), p.cmc0.data(), p.sneqv0.data(), B->st);
+}
+
+// ApplyBc at model time t into the arena (pinned staging, asynchronous; the
+// round that applies it synchronises before the staging is reused).
+int stage_bc(pihm_batch *B, Sys *s, int64_t t) {
+  const int ne = s->ne, nr = s->nr;
+  std::vector<double> e(3 * (size_t)ne), r((size_t)nr);
+  if (pihm_deck_bc(s->deck, t, e.data(), r.data()) != PIHM_GPU_OK) return PIHM_GPU_ERR_ARG;
+  double *h = s->bc_stage;
+  for (int j = 0; j < 3; j++)
+    for (int i = 0; i < ne; i++) h[(size_t)j * ne + i] = e[3 * (size_t)s->perm[i] + j];
+  std::copy(r.begin(), r.end(), h + 3 * (size_t)ne);
+  DevMesh &m = B->A.m;
+  const int64_t NE = B->ne_cap;
+  for (int j = 0; j < 3; j++)
+    if (ne && cudaMemcpyAsync((double *)m.elem_bc + j * NE + s->eoff, h + (size_t)j * ne, sizeof(double) * ne,
+                              cudaMemcpyHostToDevice, B->st) != cudaSuccess)
+      return PIHM_GPU_ERR_CUDA;
+  if (nr && cudaMemcpyAsync((double *)m.river_bc + s->roff, h + 3 * (size_t)ne, sizeof(double) * nr,
+                            cudaMemcpyHostToDevice, B->st) != cudaSuccess)
+    return PIHM_GPU_ERR_CUDA;
   return PIHM_GPU_OK;
 }
 
@@ -379,7 +452,8 @@ int admit(pihm_batch *B, const Prepared &p, int32_t *id) {
   s->core.ops.s = s.get();
   Sys *sp = s.get();
   B->slots[slot] = std::move(s);
-  const int prc = place(B, sp, p);
+  int prc = place(B, sp, p);
+  if (prc == PIHM_GPU_OK) prc = attach_deck(B, sp, p);
   if (prc != PIHM_GPU_OK) {
     free_ranges(B, sp);
     B->slots[slot].reset();
@@ -410,6 +484,8 @@ int run_round(pihm_batch *B, bool *any) {
   std::memset(active, 0, B->max_sys);
   int nops = 0, nblocks = 0;
   bool rhs = false;
+  std::vector<Sys *> forcing;  // watersheds whose programs start a model step with a deck's forcing
+  int64_t el_req = 0;          // elements of the watersheds evaluated this round
   // Right-hand-side gating: a watershed that waits for an evaluation is held
   // back while others still have reductions to run, until the waiting ones
   // hold at least rhs_gate of the waiting elements, so that evaluations are
@@ -436,12 +512,14 @@ int run_round(pihm_batch *B, bool *any) {
     r.ry = s->ry;
     r.pad0 = r.pad1 = 0;
     r.bstart = nblocks;
+    if (s->pending_k >= 0) forcing.push_back(s);
     std::memcpy(ops + nops, s->prog.data(), sizeof(Op) * s->prog.size());
     nops += (int)s->prog.size();
     nblocks += (int)pihm_nv::red_grid_for(s->neq);
     if (waiting && s->rhs_req) {
       active[s->slot] = 1;
       rhs = true;
+      el_req += s->ne;
     }
     part.push_back(s);
   }
@@ -460,15 +538,37 @@ int run_round(pihm_batch *B, bool *any) {
     B->tune_next = (B->tune_next + 1) % kProgramVariants;
     cudaEventRecord(B->tev[0], st);
   }
+  // a deck's boundary values for the model step (src/pihm.c:15-28), in
+  // place before any evaluation of the step
+  for (Sys *s : forcing)
+    if (s->has_bc && stage_bc(B, s, s->start + (int64_t)s->pending_k * (int64_t)s->ctrl.stepsize) != PIHM_GPU_OK)
+      return -1;
   if (B->profiling) cudaEventRecord(B->ev[0], st);
   if (launch_program(B->A, (int)part.size(), nblocks, variant, st) != cudaSuccess) return -1;
   B->launches++;
   if (B->profiling) cudaEventRecord(B->ev[1], st);
   if (tune) cudaEventRecord(B->tev[1], st);
+  // the land-surface step (src/pihm.c:30-66) after the program, which ends
+  // the previous model step's state in vector slot 0, and before the
+  // evaluation that starts the step
+  for (Sys *s : forcing) {
+    const int64_t t = s->start + (int64_t)s->pending_k * (int64_t)s->ctrl.stepsize;
+    if (s->land.alloc && (t - s->start) % s->lsm_step == 0) {
+      int64_t n = 0;
+      if (land_launch(s->land, t, (double)s->lsm_step, B->A.vec + s->soff, st, &n) != PIHM_GPU_OK) return -1;
+      B->launches += n;
+    }
+    s->pending_k = -1;
+  }
+  const bool stune = rhs && B->shape_forced < 0 && B->shape_tuning && el_req >= pihm_batch::kShapeMinElems;
+  const int shape = B->shape_forced >= 0 ? B->shape_forced : (stune ? B->shape_next : B->shape_best);
   if (rhs) {
     if (cudaMemsetAsync(B->err_sys, 0, sizeof(unsigned int) * B->max_sys, st) != cudaSuccess) return -1;
+    B->A.m.main_shape = shape;
+    if (stune) cudaEventRecord(B->sev[0], st);
     if (launch_rhs(B->A.m, B->A.rhs_in, B->A.rhs_out, st, &B->launches, nullptr, &B->side) != cudaSuccess)
       return -1;
+    if (stune) cudaEventRecord(B->sev[1], st);
     B->rhs_rounds++;
   }
   if (B->profiling) cudaEventRecord(B->ev[2], st);
@@ -491,6 +591,23 @@ int run_round(pihm_batch *B, bool *any) {
           if (B->tune_ms_per_block[v] / B->tune_n[v] < B->tune_ms_per_block[best] / B->tune_n[best]) best = v;
         B->prog_variant = best;
         B->tuning = false;
+      }
+    }
+  }
+  if (stune) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, B->sev[0], B->sev[1]);
+    B->shape_ms_per_elem[shape] += ms / (double)el_req;
+    B->shape_next = (B->shape_next + 1) % pihm_batch::kShapes;
+    if (++B->shape_n[shape] >= pihm_batch::kTuneSamples) {
+      bool all = true;
+      for (int v = 0; v < pihm_batch::kShapes; v++) all = all && B->shape_n[v] >= pihm_batch::kTuneSamples;
+      if (all) {
+        int best = 0;
+        for (int v = 1; v < pihm_batch::kShapes; v++)
+          if (B->shape_ms_per_elem[v] / B->shape_n[v] < B->shape_ms_per_elem[best] / B->shape_n[best]) best = v;
+        B->shape_best = best;
+        B->shape_tuning = false;
       }
     }
   }
@@ -711,6 +828,8 @@ int pihm_batch_create(const pihm_batch_limits *lim, int surf_mode, int riv_mode,
   }
   for (cudaEvent_t &e : B->tev)
     if (cudaEventCreate(&e) != cudaSuccess) return PIHM_GPU_ERR_CUDA;
+  for (cudaEvent_t &e : B->sev)
+    if (cudaEventCreate(&e) != cudaSuccess) return PIHM_GPU_ERR_CUDA;
   B->update_extents();
   *out = B.release();
   return PIHM_GPU_OK;
@@ -843,6 +962,14 @@ int pihm_batch_get_info(const pihm_batch *B, pihm_batch_info *info) {
   info->rhs_ms = B->rhs_ms;
   info->program_variant = B->prog_forced >= 0 ? B->prog_forced : B->prog_variant;
   info->tuning = B->prog_forced < 0 && B->tuning;
+  info->rhs_shape = B->shape_forced >= 0 ? B->shape_forced : B->shape_best;
+  info->rhs_tuning = B->shape_forced < 0 && B->shape_tuning;
+  return PIHM_GPU_OK;
+}
+
+int pihm_batch_set_rhs_shape(pihm_batch *B, int32_t shape) {
+  if (!B || shape < -1 || shape >= pihm_batch::kShapes) return PIHM_GPU_ERR_ARG;
+  B->shape_forced = shape;
   return PIHM_GPU_OK;
 }
 

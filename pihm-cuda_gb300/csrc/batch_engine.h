@@ -152,6 +152,20 @@ struct Sys {
   uint8_t rhs_out = 0;
   double red_value = 0.0;
   int rhs_rc = 0;
+  // an input deck's forcing (pihm_batch_job.deck / .land)
+  const pihm_deck *deck = nullptr;  // ApplyBc every model step when has_bc
+  bool has_bc = false;
+  LandInstance land;                // the land-surface step; alloc null when absent
+  int64_t start = 0, lsm_step = 0;
+  int32_t pending_k = -1;           // model step whose forcing the next round applies
+  double *bc_stage = nullptr;       // pinned [3 ne + nr], internal order
+
+  Sys() = default;
+  Sys(const Sys &) = delete;
+  ~Sys() {
+    land_release(land);
+    if (bc_stage) cudaFreeHost(bc_stage);
+  }
 };
 
 
@@ -161,6 +175,12 @@ struct Prepared {
   std::vector<double> y0, elem_bc, river_bc, pcp, edir, ett;
   pihm_step_control ctrl{};
   int32_t nsteps = 0, outlet = -1;
+  const pihm_deck *deck = nullptr;
+  bool has_bc = false;
+  const pihm_land_params *land = nullptr;
+  const pihm_forcing_series *forcing = nullptr;
+  std::vector<double> cmc0, sneqv0;
+  int64_t start = 0, lsm_step = 0;
 };
 
 }  // namespace batch
@@ -201,6 +221,18 @@ struct pihm_batch {
   double tune_ms_per_block[pihm::batch::kProgramVariants] = {0};
   int tune_n[pihm::batch::kProgramVariants] = {0};
   cudaEvent_t tev[2] = {nullptr, nullptr};
+  // Tuner of k_elem_main's block shape (DevMesh::main_shape: 512 x 2,
+  // 256 x 4, 128 x 8 per SM): evaluation rounds over at least
+  // kShapeMinElems requesting elements rotate through the shapes and are
+  // timed with events; after kTuneSamples rounds each, the fastest per
+  // requesting element is kept.  Every shape gives the same bits.
+  static constexpr int kShapes = 3;
+  static constexpr int64_t kShapeMinElems = 20000;
+  int shape_best = 0, shape_forced = -1, shape_next = 0;
+  bool shape_tuning = true;
+  double shape_ms_per_elem[kShapes] = {0};
+  int shape_n[kShapes] = {0};
+  cudaEvent_t sev[2] = {nullptr, nullptr};
   pihm::RhsStreams side;  // river kernel beside the element kernels
   int host_pageable = 0;  // the device can access pageable host memory (uploads by one gather kernel)
   // counters and timing (host: building rounds and running the coroutines;
@@ -217,6 +249,8 @@ struct pihm_batch {
     for (cudaEvent_t e : ev)
       if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : tev)
+      if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : sev)
       if (e) cudaEventDestroy(e);
     if (side.fork) cudaEventDestroy(side.fork);
     if (side.join) cudaEventDestroy(side.join);

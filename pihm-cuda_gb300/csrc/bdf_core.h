@@ -533,8 +533,7 @@ struct BdfCore {
     }
     njtimes++;
     co_await ops.linear_sum(ONE, vtemp, -gamma, V[k], V[k]);
-    co_await ops.scale(ONE, V[k], vtemp);
-    co_await ops.prod(weight, vtemp, V[k]);
+    co_await ops.prod(weight, V[k], V[k]);
     // modified_gs(k, maxl): the first pass
     const int i0 = (k - maxl > 0) ? k - maxl : 0;
     co_await ops.dot_slot(V[k], V[k], SLOT_VK);
@@ -620,11 +619,11 @@ struct BdfCore {
     bool converged = false;
     *nli_inc = 0;
     // the initial guess is x = 0 (lsolve zeroes it), so r0 = b; SpgmrSolve
-    // tests N_VDotProd(x, x) == 0 to find that out, a reduction skipped here
-    co_await ops.scale(ONE, b, vtemp);
-    co_await ops.scale(ONE, vtemp, V[0]);
-    co_await ops.scale(ONE, V[0], vtemp);
-    co_await ops.prod(weight, vtemp, V[0]);
+    // tests N_VDotProd(x, x) == 0 to find that out, a reduction skipped here.
+    // SpgmrSolve then copies r0 through vtemp and V[0] (its preconditioning
+    // stubs) before scaling, V[0] = s2 r0; the copies change no value and
+    // vtemp is written before it is next read, so only the product is made.
+    co_await ops.prod(weight, b, V[0]);
     double r_norm, beta, rho;
     r_norm = beta = sun_sqrt(co_await ops.dot(V[0], V[0]));
     if (r_norm <= delta) co_return SPGMR_SUCCESS;
@@ -650,8 +649,8 @@ struct BdfCore {
         co_await ops.div(V[li], weight, vtemp);
         const int ier = co_await dq_atimes(vtemp, V[l_plus_1]);
         if (ier != 0) co_return (ier < 0) ? SPGMR_ATIMES_FAIL_UNREC : SPGMR_ATIMES_FAIL_REC;
-        co_await ops.scale(ONE, V[l_plus_1], vtemp);
-        co_await ops.prod(weight, vtemp, V[l_plus_1]);
+        // SpgmrSolve's copy through vtemp before the scaling changes no value
+        co_await ops.prod(weight, V[l_plus_1], V[l_plus_1]);
         (void)co_await modified_gs(l_plus_1, l_max, &hnorm);
       }
       Hes[l_plus_1][li] = hnorm;
@@ -670,8 +669,8 @@ struct BdfCore {
     for (int k = 0; k < krydim; k++) co_await ops.linear_sum(yg[k], V[k], ONE, xcor, xcor);
     if (converged || rho < beta) {
       co_await ops.div(xcor, weight, xcor);
-      co_await ops.scale(ONE, xcor, vtemp);
-      co_await ops.linear_sum(ONE, xsol, ONE, vtemp, xsol);
+      // SpgmrSolve's copy of xcor through vtemp changes no value
+      co_await ops.linear_sum(ONE, xsol, ONE, xcor, xsol);
       co_return converged ? SPGMR_SUCCESS : SPGMR_RES_REDUCED;
     }
     co_return SPGMR_CONV_FAIL;

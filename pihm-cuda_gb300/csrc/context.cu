@@ -83,7 +83,6 @@ int pihm_gpu_create(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double 
   c->nan_check_deferred = 0;
   c->prof = nullptr;
   c->d_noah = nullptr;
-  c->d_land = nullptr;
   c->host_path = 0;
   c->last_direct = 0;
   {
@@ -231,7 +230,7 @@ void pihm_gpu_destroy(pihm_gpu_ctx *c) {
   if (c->d_static) cudaFree(c->d_static);
   if (c->d_dyn) cudaFree(c->d_dyn);
   if (c->d_noah) cudaFree(c->d_noah);
-  if (c->d_land) cudaFree(c->d_land);
+  pihm::land_release(c->land);
   noah_free(c);
   if (c->side.fork) cudaEventDestroy(c->side.fork);
   if (c->side.join) cudaEventDestroy(c->side.join);
@@ -248,6 +247,12 @@ int pihm_gpu_set_stream(pihm_gpu_ctx *c, void *stream) {
 }
 
 void *pihm_gpu_get_stream(const pihm_gpu_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+int pihm_gpu_set_kernel_shape(pihm_gpu_ctx *c, int shape) {
+  if (!c || shape < 0 || shape > 2) return PIHM_GPU_ERR_ARG;
+  c->m.main_shape = shape;
+  return PIHM_GPU_OK;
+}
 
 int pihm_gpu_sizes(const pihm_gpu_ctx *c, int32_t *ne, int32_t *nr, int64_t *neq) {
   if (!c) return PIHM_GPU_ERR_ARG;

@@ -309,10 +309,11 @@ bool series_ok(int32_t n, const int32_t *len, const int64_t *time, int64_t *lo, 
 
 using namespace pihm;
 
-extern "C" {
+namespace pihm {
 
-int pihm_gpu_land_init(pihm_gpu_ctx *c, const pihm_land_params *p, const pihm_forcing_series *s) {
-  if (!c || !p || !s || p->nelem != c->ne || s->nmeteo < 1 || s->nlai < 0) return PIHM_GPU_ERR_ARG;
+int land_build(const pihm_land_params *p, const pihm_forcing_series *s, const int32_t *perm, int ne,
+               const double *zmax, const LandTargets &tg, LandInstance *out) {
+  if (!p || !s || !out || p->nelem != ne || s->nmeteo < 1 || s->nlai < 0) return PIHM_GPU_ERR_ARG;
   const double *planes[] = {p->albedomin, p->albedomax, p->shdfac, p->cmcfactr, p->cfactr, p->rgl,
                             p->rsmin,     p->rsmax,     p->topt,   p->smcmin,   p->smcwlt, p->smcref,
                             p->zlvl_wind};
@@ -321,7 +322,6 @@ int pihm_gpu_land_init(pihm_gpu_ctx *c, const pihm_land_params *p, const pihm_fo
   if (!p->lc_type || !p->meteo_type || !p->lai_type || !s->meteo_len || !s->meteo_time || !s->meteo_data ||
       (s->nlai > 0 && (!s->lai_len || !s->lai_time || !s->lai_data)))
     return PIHM_GPU_ERR_ARG;
-  const int ne = c->ne;
   for (int r = 0; r < ne; r++)
     if (p->lc_type[r] < 1 || p->lc_type[r] > PIHM_LAND_NLC || p->meteo_type[r] < 1 ||
         p->meteo_type[r] > s->nmeteo || p->lai_type[r] < 0 || p->lai_type[r] > s->nlai)
@@ -340,9 +340,8 @@ int pihm_gpu_land_init(pihm_gpu_ctx *c, const pihm_land_params *p, const pihm_fo
   for (auto &v : hd) v.resize(NE);
   std::vector<int32_t> hi32[3];
   for (auto &v : hi32) v.resize(NE);
-  std::vector<double> zmax(NE);  // the surface elevation plane, read back from the device
   for (int i = 0; i < ne; i++) {
-    const int r = c->h_perm[i];
+    const int r = perm[i];
     hd[0][i] = 0.5 * (p->albedomin[r] + p->albedomax[r]);
     hd[1][i] = p->shdfac[r];
     hd[2][i] = p->cmcfactr[r];
@@ -360,8 +359,6 @@ int pihm_gpu_land_init(pihm_gpu_ctx *c, const pihm_land_params *p, const pihm_fo
     hi32[1][i] = p->meteo_type[r];
     hi32[2][i] = p->lai_type[r];
   }
-  if (cudaMemcpy(zmax.data(), c->m.zmax, sizeof(double) * NE, cudaMemcpyDeviceToHost) != cudaSuccess)
-    return PIHM_GPU_ERR_CUDA;
   for (int i = 0; i < ne; i++) hd[13][i] = 101.325 * 1.0e3 * std::pow((293.0 - 0.0065 * zmax[i]) / 293.0, 5.26);
   std::vector<int32_t> moff(s->nmeteo), loff(s->nlai > 0 ? s->nlai : 1);
   {
@@ -377,16 +374,9 @@ int pihm_gpu_land_init(pihm_gpu_ctx *c, const pihm_land_params *p, const pihm_fo
                        align256(nmk * 8) + align256(nmk * 8 * PIHM_METEO_NVAR) + align256((nlk ? nlk : 1) * 8) +
                        align256((nlk ? nlk : 1) * 8) + 5 * align256(NE * 8) + align256(nm * 8 * kStationVals) +
                        align256(nl * 8) + align256(NE * 8);
-  if (c->d_land) {
-    cudaFree(c->d_land);
-    c->d_land = nullptr;
-    c->m.land_prcp = c->m.land_ec = c->m.land_cmc = c->m.land_sneqv = nullptr;
-  }
-  if (cudaMalloc(&c->d_land, bytes) != cudaSuccess) {
-    c->d_land = nullptr;
-    return PIHM_GPU_ERR_NOMEM;
-  }
-  char *cur = (char *)c->d_land;
+  void *alloc = nullptr;
+  if (cudaMalloc(&alloc, bytes) != cudaSuccess) return PIHM_GPU_ERR_NOMEM;
+  char *cur = (char *)alloc;
   auto take = [&](size_t b) {
     char *r = cur;
     cur += align256(b);
@@ -424,8 +414,7 @@ int pihm_gpu_land_init(pihm_gpu_ctx *c, const pihm_land_params *p, const pihm_fo
   }
   for (int k = 0; k < 5 && e == cudaSuccess; k++) e = cudaMemset(state[k], 0, NE * 8);
   if (e != cudaSuccess) {
-    cudaFree(c->d_land);
-    c->d_land = nullptr;
+    cudaFree(alloc);
     return PIHM_GPU_ERR_CUDA;
   }
   L.albedo = dd[0];
@@ -445,10 +434,10 @@ int pihm_gpu_land_init(pihm_gpu_ctx *c, const pihm_land_params *p, const pihm_fo
   L.lc = di[0];
   L.meteo = di[1];
   L.lai_type = di[2];
-  L.depth = c->m.depth;
-  L.porosity = c->m.porosity;
-  L.rzd = c->m.rzd;
-  L.d_rzd = c->m.d_rzd;
+  L.depth = tg.depth;
+  L.porosity = tg.porosity;
+  L.rzd = tg.rzd;
+  L.d_rzd = tg.d_rzd;
   L.cal_edir = p->cal_edir;
   L.cal_ec = p->cal_ec;
   L.cal_ett = p->cal_ett;
@@ -470,60 +459,101 @@ int pihm_gpu_land_init(pihm_gpu_ctx *c, const pihm_land_params *p, const pihm_fo
   L.ra_num = d_ranum;
   L.nmeteo = s->nmeteo;
   L.nlai = s->nlai;
-  L.pcpdrp = const_cast<double *>(c->m.pcpdrp);
-  L.edir = const_cast<double *>(c->m.edir);
-  L.ett = const_cast<double *>(c->m.ett);
-  c->land = L;
-  c->land_t_lo = lo;
-  c->land_t_hi = hi;
-  c->land_month = -1;
-  c->m.land_prcp = L.prcp;
-  c->m.land_ec = L.ec;
-  c->m.land_cmc = L.cmc;
-  c->m.land_sneqv = L.sneqv;
+  L.pcpdrp = tg.pcpdrp;
+  L.edir = tg.edir;
+  L.ett = tg.ett;
+  out->alloc = alloc;
+  out->L = L;
+  out->t_lo = lo;
+  out->t_hi = hi;
+  out->month = -1;
+  out->ne = ne;
   return PIHM_GPU_OK;
 }
 
-int pihm_gpu_land_set_state(pihm_gpu_ctx *c, const double *cmc, const double *sneqv) {
-  if (!c || !c->d_land) return PIHM_GPU_ERR_ARG;
-  const int ne = c->ne;
+int land_set_state(LandInstance &li, const int32_t *perm, const double *cmc, const double *sneqv,
+                   cudaStream_t st) {
+  const int ne = li.ne;
   std::vector<double> a(ne, 0.0), b(ne, 0.0);
   for (int i = 0; i < ne; i++) {
-    const int r = c->h_perm[i];
+    const int r = perm[i];
     if (cmc) a[i] = cmc[r];
     if (sneqv) b[i] = sneqv[r];
   }
-  return cuda_rc(cudaMemcpyAsync(c->land.cmc, a.data(), sizeof(double) * ne, cudaMemcpyHostToDevice, c->stream)) ?:
-         cuda_rc(cudaMemcpyAsync(c->land.sneqv, b.data(), sizeof(double) * ne, cudaMemcpyHostToDevice, c->stream)) ?:
-         cuda_rc(cudaStreamSynchronize(c->stream));
+  return cuda_rc(cudaMemcpyAsync(li.L.cmc, a.data(), sizeof(double) * ne, cudaMemcpyHostToDevice, st)) ?:
+         cuda_rc(cudaMemcpyAsync(li.L.sneqv, b.data(), sizeof(double) * ne, cudaMemcpyHostToDevice, st)) ?:
+         cuda_rc(cudaStreamSynchronize(st));
 }
 
-int pihm_gpu_land_step(pihm_gpu_ctx *c, int64_t t, double stepsize, const double *y_dev) {
-  if (!c || !c->d_land || !y_dev || !(stepsize > 0.0)) return PIHM_GPU_ERR_ARG;
-  if (t < c->land_t_lo || t > c->land_t_hi) return PIHM_GPU_ERR_ARG;
+int land_launch(LandInstance &li, int64_t t, double stepsize, const double *y_dev, cudaStream_t st,
+                int64_t *launches) {
+  if (!li.alloc || !y_dev || !(stepsize > 0.0)) return PIHM_GPU_ERR_ARG;
+  if (t < li.t_lo || t > li.t_hi) return PIHM_GPU_ERR_ARG;
   // the month of PIHMTime (src/time_func.c:3-22), from gmtime like the reference
   const time_t raw = (time_t)t;
   std::tm tm{};
   if (!gmtime_r(&raw, &tm)) return PIHM_GPU_ERR_ARG;
-  const int ne = c->ne;
+  const int ne = li.ne;
   if (ne == 0) return PIHM_GPU_OK;
   const unsigned grid = (unsigned)((ne + kLandBlock - 1) / kLandBlock);
-  if (tm.tm_mon != c->land_month) {
-    k_land_month<<<grid, kLandBlock, 0, c->stream>>>(c->land, ne, tm.tm_mon);
-    c->launches++;
-    c->land_month = tm.tm_mon;
+  if (tm.tm_mon != li.month) {
+    k_land_month<<<grid, kLandBlock, 0, st>>>(li.L, ne, tm.tm_mon);
+    (*launches)++;
+    li.month = tm.tm_mon;
   }
-  const int nser = c->land.nmeteo + c->land.nlai;
-  k_land_station<<<(nser + 127) / 128, 128, 0, c->stream>>>(c->land, t, tm.tm_mon);
-  k_land_step<<<grid, kLandBlock, 0, c->stream>>>(c->land, y_dev, ne, tm.tm_mon, stepsize);
-  c->launches += 2;
+  const int nser = li.L.nmeteo + li.L.nlai;
+  k_land_station<<<(nser + 127) / 128, 128, 0, st>>>(li.L, t, tm.tm_mon);
+  k_land_step<<<grid, kLandBlock, 0, st>>>(li.L, y_dev, ne, tm.tm_mon, stepsize);
+  *launches += 2;
   return cuda_rc(cudaGetLastError());
 }
 
+void land_release(LandInstance &li) {
+  if (li.alloc) cudaFree(li.alloc);
+  li = LandInstance();
+}
+
+}  // namespace pihm
+
+extern "C" {
+
+int pihm_gpu_land_init(pihm_gpu_ctx *c, const pihm_land_params *p, const pihm_forcing_series *s) {
+  if (!c || !p || p->nelem != c->ne) return PIHM_GPU_ERR_ARG;
+  std::vector<double> zmax((size_t)c->ne);  // the surface elevation plane, read back from the device
+  if (c->ne > 0 && cudaMemcpy(zmax.data(), c->m.zmax, sizeof(double) * c->ne, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return PIHM_GPU_ERR_CUDA;
+  LandTargets tg{c->m.depth, c->m.porosity, c->m.rzd, c->m.d_rzd, const_cast<double *>(c->m.pcpdrp),
+                 const_cast<double *>(c->m.edir), const_cast<double *>(c->m.ett)};
+  LandInstance li;
+  const int rc = land_build(p, s, c->h_perm, c->ne, zmax.data(), tg, &li);
+  if (rc != PIHM_GPU_OK) return rc;
+  land_release(c->land);
+  c->land = li;
+  c->m.land_prcp = li.L.prcp;
+  c->m.land_ec = li.L.ec;
+  c->m.land_cmc = li.L.cmc;
+  c->m.land_sneqv = li.L.sneqv;
+  return PIHM_GPU_OK;
+}
+
+int pihm_gpu_land_set_state(pihm_gpu_ctx *c, const double *cmc, const double *sneqv) {
+  if (!c || !c->land.alloc) return PIHM_GPU_ERR_ARG;
+  return land_set_state(c->land, c->h_perm, cmc, sneqv, c->stream);
+}
+
+int pihm_gpu_land_step(pihm_gpu_ctx *c, int64_t t, double stepsize, const double *y_dev) {
+  if (!c || !c->land.alloc) return PIHM_GPU_ERR_ARG;
+  int64_t n = 0;
+  const int rc = land_launch(c->land, t, stepsize, y_dev, c->stream, &n);
+  c->launches += n;
+  return rc;
+}
+
 int pihm_gpu_land_get(pihm_gpu_ctx *c, int field, double *out) {
-  if (!c || !c->d_land || !out || field < 0 || field >= PIHM_LAND_NFIELD) return PIHM_GPU_ERR_ARG;
-  const double *src[PIHM_LAND_NFIELD] = {c->land.prcp, c->land.pcpdrp, c->land.edir, c->land.ett,
-                                         c->land.ec,   c->land.drip,   c->land.cmc,  c->land.sneqv};
+  if (!c || !c->land.alloc || !out || field < 0 || field >= PIHM_LAND_NFIELD) return PIHM_GPU_ERR_ARG;
+  const LandDev &L = c->land.L;
+  const double *src[PIHM_LAND_NFIELD] = {L.prcp, L.pcpdrp, L.edir, L.ett,
+                                         L.ec,   L.drip,   L.cmc,  L.sneqv};
   const int ne = c->ne;
   std::vector<double> tmp(ne);
   const int rc = cuda_rc(cudaMemcpyAsync(tmp.data(), src[field], sizeof(double) * ne, cudaMemcpyDeviceToHost,

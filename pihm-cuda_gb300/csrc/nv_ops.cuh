@@ -12,14 +12,26 @@
 // a multiply and an add: every element equals what the serial N_Vector
 // computes (cvode/src/nvec_ser/nvector_serial.c:421-1060), including its
 // special cases (a == 1, b == -1, a == b, ...) which change the rounding.
+//
+// Divisions and reciprocals run on the integer pipe (int_math.cuh: a float
+// seed, two fixed-point Newton steps and an exact midpoint test, the IEEE
+// quotient bit for bit) with the FP64 instruction for zeros, subnormals,
+// infinities and NaN: GB300 retires 2 FP64 lanes per clock per SM, and an
+// FP64 division costs about as much pipe time as fifteen additions.
 #pragma once
 
 #include <cmath>
 
+#include "int_math.cuh"
 #include "nv_reduce.cuh"
 #include "nv_select.h"
 
 namespace pihm_nv {
+
+__device__ __forceinline__ double div_rn(double a, double b) {
+  double q;
+  return pihm::im::div_i(a, b, q) ? q : __ddiv_rn(a, b);
+}
 
 // z_i = OP(a, b, x_i, y_i, z_i)
 template <int OP>
@@ -36,12 +48,12 @@ __device__ __forceinline__ double ew_eval(double a, double b, double x, double y
   if (OP == EW_AXPYM1) return __dsub_rn(z, x);
   if (OP == EW_CONST) return a;
   if (OP == EW_PROD) return __dmul_rn(x, y);
-  if (OP == EW_DIV) return __ddiv_rn(x, y);
+  if (OP == EW_DIV) return div_rn(x, y);
   if (OP == EW_SCALE) return __dmul_rn(a, x);
   if (OP == EW_COPY) return x;
   if (OP == EW_NEG) return -x;
   if (OP == EW_ABS) return fabs(x);
-  if (OP == EW_INV) return __drcp_rn(x);
+  if (OP == EW_INV) return div_rn(1.0, x);
   if (OP == EW_ADDCONST) return __dadd_rn(x, b);
   return (fabs(x) >= a) ? 1.0 : 0.0;
 }

@@ -178,7 +178,7 @@ __global__ void __launch_bounds__(kThreads) k_red(long long n, const double *__r
       if (z[i] > 0.0) { double p = __dmul_rn(x[i], y[i]); t.v = __dmul_rn(p, p); }
     } else if (OP == R_INVTEST) {
       if (x[i] == 0.0) t.f = 1.0;
-      else z[i] = __drcp_rn(x[i]);
+      else z[i] = div_rn(1.0, x[i]);
     } else if (OP == R_CONSTR) {
       // cvode/src/nvec_ser/nvector_serial.c:813-841: c = x, x = y, m = z
       const double c = x[i], v = y[i];
@@ -192,7 +192,7 @@ __global__ void __launch_bounds__(kThreads) k_red(long long n, const double *__r
       }
       z[i] = mi;
     } else if (OP == R_MINQ) {
-      if (y[i] != 0.0) { t.v = __ddiv_rn(x[i], y[i]); t.f = 1.0; }
+      if (y[i] != 0.0) { t.v = div_rn(x[i], y[i]); t.f = 1.0; }
     }
     acc = red_combine<OP>(acc, t);
   }

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include "pihm_gpu.h"
+#include "pihm_land.h"
 
 namespace pihm {
 
@@ -110,6 +111,9 @@ struct DevMesh {
   // planes sized ne, nr, nedge, nbank (the capacities, which stay the plane
   // strides) and evaluates items below the high-water marks.
   int32_t ne_run, nr_run, nedge_run, nbank_run;
+  // k_elem_main's block shape (kMainShapes in rhs_kernels.cu): 0 = 512
+  // threads x 2 blocks per SM, 1 = 256 x 4, 2 = 128 x 8 (64 registers each)
+  int32_t main_shape;
   // Batch engine only (null otherwise): the watershed of each item (-1 for a
   // free arena slot), the watersheds evaluated by this call, their model steps
   // and their error words.
@@ -159,6 +163,35 @@ struct LandDev {
   double *station, *lai_value, *ra_num;
   int32_t nmeteo, nlai;
 };
+
+// Where a land-surface instance reads the mesh and writes the right-hand
+// side's forcing: the element planes of one watershed (a context's own, or a
+// watershed's range of the batch arena), internal order.
+struct LandTargets {
+  const double *depth, *porosity, *rzd, *d_rzd;
+  double *pcpdrp, *edir, *ett;
+};
+// A land-surface model instance: its own allocation (parameters, series,
+// state, outputs), the device view, the model times every series covers and
+// the month whose aerodynamic term ra_num holds (-1: none yet).
+struct LandInstance {
+  void *alloc = nullptr;
+  LandDev L{};
+  int64_t t_lo = 0, t_hi = 0;
+  int month = -1;
+  int ne = 0;
+};
+// pihm_gpu_land_init's work for any targets: params and series in reference
+// order, perm[internal] = reference element, zmax in internal order (host).
+int land_build(const pihm_land_params *p, const pihm_forcing_series *s, const int32_t *perm, int ne,
+               const double *zmax, const LandTargets &tg, LandInstance *out);
+int land_set_state(LandInstance &li, const int32_t *perm, const double *cmc, const double *sneqv,
+                   cudaStream_t st);
+// The land-surface step at model time t over `stepsize` seconds, reading the
+// state y_dev (the watershed's own layout); adds the kernels it launched.
+int land_launch(LandInstance &li, int64_t t, double stepsize, const double *y_dev, cudaStream_t st,
+                int64_t *launches);
+void land_release(LandInstance &li);
 
 // Optional per-kernel CUDA-event timing of the right-hand-side launches.
 struct Profiler {
@@ -229,10 +262,7 @@ struct pihm_gpu_ctx {
   long long launches;      // kernels launched by this context so far
   pihm::Profiler *prof;    // non-null while profiling is on
   void *d_noah;            // Flux-PIHM input planes, allocated on first use
-  void *d_land;            // land-surface model (pihm_gpu_land_init), or null
-  pihm::LandDev land;
-  int64_t land_t_lo, land_t_hi;  // model times every forcing series covers
-  int land_month;                // month ra_num holds (-1: none yet)
+  pihm::LandInstance land;  // land-surface model (pihm_gpu_land_init); alloc null when absent
   pihm::RhsStreams side;   // river kernel beside the element kernels
   void *d_noahlsm;              // Noah land-surface model (pihm_gpu_noah_init), or null
   pihm::NoahPlanes *noahlsm;    // its planes

@@ -335,14 +335,13 @@ __global__ void __launch_bounds__(kEdgeBlock) k_edge(DevMesh m, const double *RE
 // ---------------------------------------------------------------------------
 // k_elem_main
 // ---------------------------------------------------------------------------
-#ifndef PIHM_ELEM_MAIN_MINB
-#define PIHM_ELEM_MAIN_MINB 2
-#endif
-#ifndef PIHM_ELEM_MAIN_BLOCK
-#define PIHM_ELEM_MAIN_BLOCK 512
-#endif
-constexpr int kMainBlock = PIHM_ELEM_MAIN_BLOCK;
-__global__ void __launch_bounds__(kMainBlock, PIHM_ELEM_MAIN_MINB) k_elem_main(DevMesh m, const double *RESTRICT y,
+// Block shapes: the same 64-register budget (1,024 resident threads per
+// SM) cut into 512 x 2, 256 x 4 or 128 x 8 blocks.  The largest blocks are
+// fastest on large meshes (276 against 298 and 294 us per 1M elements); on a
+// small mesh or a sparsely occupied batch arena the smaller blocks spread the
+// work over more SMs.  The batch engine tunes the shape per arena.
+template <int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) k_elem_main(DevMesh m, const double *RESTRICT y,
                                                     double *RESTRICT ydot) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   int sy;
@@ -1013,7 +1012,11 @@ cudaError_t launch_rhs(const DevMesh &m, const double *y, double *ydot, cudaStre
       ++*launches;
     }
     on = prof_begin(prof, K_MAIN, st);
-    k_elem_main<<<blocks_for(m.ne_run, kMainBlock), kMainBlock, 0, st>>>(m, y, ydot);
+    switch (m.main_shape) {
+      case 1: k_elem_main<256, 4><<<blocks_for(m.ne_run, 256), 256, 0, st>>>(m, y, ydot); break;
+      case 2: k_elem_main<128, 8><<<blocks_for(m.ne_run, 128), 128, 0, st>>>(m, y, ydot); break;
+      default: k_elem_main<512, 2><<<blocks_for(m.ne_run, 512), 512, 0, st>>>(m, y, ydot); break;
+    }
     prof_end(prof, on, st);
     ++*launches;
   }

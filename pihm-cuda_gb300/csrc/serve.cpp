@@ -29,7 +29,7 @@ struct OwnedJob {
   pihm_gpu_mesh mesh{};
   std::vector<std::vector<int32_t>> ints;
   std::vector<std::vector<double>> dbls;
-  std::vector<double> y0, elem_bc, river_bc, pcp, edir, ett;
+  std::vector<double> y0, elem_bc, river_bc, pcp, edir, ett, cmc0, sneqv0;
   pihm_batch_job job{};
 
   explicit OwnedJob(const pihm_batch_job &j) {
@@ -96,17 +96,21 @@ struct OwnedJob {
     y0.assign(j.y0, j.y0 + 3 * ne + 2 * nr);
     if (j.elem_bc) elem_bc.assign(j.elem_bc, j.elem_bc + 3 * ne);
     if (j.river_bc) river_bc.assign(j.river_bc, j.river_bc + nr);
-    pcp.assign(j.pcpdrp, j.pcpdrp + j.nsteps);
-    edir.assign(j.edir, j.edir + j.nsteps);
-    ett.assign(j.ett, j.ett + j.nsteps);
-    job = j;
+    if (j.pcpdrp) pcp.assign(j.pcpdrp, j.pcpdrp + j.nsteps);
+    if (j.edir) edir.assign(j.edir, j.edir + j.nsteps);
+    if (j.ett) ett.assign(j.ett, j.ett + j.nsteps);
+    if (j.cmc0) cmc0.assign(j.cmc0, j.cmc0 + ne);
+    if (j.sneqv0) sneqv0.assign(j.sneqv0, j.sneqv0 + ne);
+    job = j;  // the deck, land parameters and forcing series stay the caller's
     job.mesh = &mesh;
     job.y0 = y0.data();
     job.elem_bc = elem_bc.empty() ? nullptr : elem_bc.data();
     job.river_bc = river_bc.empty() ? nullptr : river_bc.data();
-    job.pcpdrp = pcp.data();
-    job.edir = edir.data();
-    job.ett = ett.data();
+    job.pcpdrp = j.pcpdrp ? pcp.data() : nullptr;
+    job.edir = j.edir ? edir.data() : nullptr;
+    job.ett = j.ett ? ett.data() : nullptr;
+    job.cmc0 = j.cmc0 ? cmc0.data() : nullptr;
+    job.sneqv0 = j.sneqv0 ? sneqv0.data() : nullptr;
   }
 };
 
@@ -183,7 +187,7 @@ extern "C" {
 
 int pihm_serve_submit(pihm_batch *B, const pihm_batch_job *job, double arrival_s, int32_t *ticket) {
   if (!B || !job || !job->mesh || !job->y0 || !ticket || job->nsteps < 0 ||
-      (job->nsteps > 0 && (!job->pcpdrp || !job->edir || !job->ett)) || !(arrival_s >= 0.0))
+      (job->nsteps > 0 && !job->land && (!job->pcpdrp || !job->edir || !job->ett)) || !(arrival_s >= 0.0))
     return PIHM_GPU_ERR_ARG;
   pihm_serve_state *S = serve_state(B);
   auto r = std::make_unique<Request>();

@@ -41,14 +41,16 @@ class StepControlC(ctypes.Structure):
 class BatchJob(ctypes.Structure):
     _fields_ = [("mesh", ctypes.POINTER(MeshDesc)), ("elem_bc", _F64P), ("river_bc", _F64P),
                 ("y0", _F64P), ("ctrl", StepControlC), ("nsteps", _I32), ("pcpdrp", _F64P),
-                ("edir", _F64P), ("ett", _F64P), ("outlet", _I32)]
+                ("edir", _F64P), ("ett", _F64P), ("outlet", _I32),
+                ("deck", _VP), ("land", _VP), ("forcing", _VP), ("cmc0", _F64P), ("sneqv0", _F64P),
+                ("start", _I64), ("lsm_step", _I64)]
 
 
 class BatchInfo(ctypes.Structure):
     _fields_ = [(n, _I64) for n in ("rounds", "rhs_rounds", "launches", "elem_used", "elem_hwm",
                                     "resident")] + [
         (n, _D) for n in ("host_ms", "wait_ms", "program_ms", "rhs_ms")] + [
-        ("program_variant", _I32), ("tuning", _I32)]
+        ("program_variant", _I32), ("tuning", _I32), ("rhs_shape", _I32), ("rhs_tuning", _I32)]
 
 
 class ServeRecord(ctypes.Structure):
@@ -75,6 +77,35 @@ def _job(ws, y0, ctrl, pcp, edir, ett, outlet, elem_bc, river_bc):
     return job, keep
 
 
+def _deck_job(deck, nsteps: int | None, outlet: int):
+    """A BatchJob running an input deck (pihm_gpu.deck.Deck) with its own
+    forcing -- boundary series every model step, the land-surface step every
+    LSM_STEP -- as pihm_gpu.single.run_deck does; and what it points at
+    (keep both alive, and the deck, while the watershed runs)."""
+    from .single import step_control
+    ctrl = deck.control()
+    ws = deck.watershed()
+    sc = step_control(ctrl)
+    start, stepsize = int(ctrl.start), int(ctrl.step["stepsize"])
+    n = nsteps if nsteps is not None else (int(ctrl.end) - start) // stepsize
+    land = deck.land()
+    p, fs = land.structs()
+    cmc, sneqv = deck.initial_storage()
+    zero = np.zeros(0)
+    job, keep = _job(ws, deck.initial_state(), sc, zero, zero, zero, outlet, None, None)
+    keep.update(land=land, p=p, fs=fs, cmc=np.ascontiguousarray(cmc), sneqv=np.ascontiguousarray(sneqv), ws=ws,
+                deck=deck, surf_mode=ctrl.surf_mode, riv_mode=ctrl.riv_mode)
+    job.nsteps = n
+    job.pcpdrp = job.edir = job.ett = None
+    job.deck = deck.h
+    job.land = ctypes.cast(ctypes.pointer(p), _VP)
+    job.forcing = ctypes.cast(ctypes.pointer(fs), _VP)
+    job.cmc0, job.sneqv0 = f64p(keep["cmc"]), f64p(keep["sneqv"])
+    job.start = start
+    job.lsm_step = int(ctrl.lsm_step)
+    return job, keep
+
+
 def _bind(lib):
     sig = {
         "pihm_batch_create": ([ctypes.POINTER(BatchLimits), ctypes.c_int, ctypes.c_int, ctypes.c_int,
@@ -93,6 +124,7 @@ def _bind(lib):
         "pihm_batch_get_info": ([_VP, ctypes.POINTER(BatchInfo)], ctypes.c_int),
         "pihm_batch_set_profiling": ([_VP, ctypes.c_int], ctypes.c_int),
         "pihm_batch_set_program_variant": ([_VP, _I32], ctypes.c_int),
+        "pihm_batch_set_rhs_shape": ([_VP, _I32], ctypes.c_int),
         "pihm_serve_submit": ([_VP, ctypes.POINTER(BatchJob), _D, ctypes.POINTER(_I32)], ctypes.c_int),
         "pihm_serve_run": ([_VP, _I32], ctypes.c_int),
         "pihm_serve_record_get": ([_VP, _I32, ctypes.POINTER(ServeRecord)], ctypes.c_int),
@@ -130,6 +162,7 @@ class Batch:
         self.h = h
         self.jobs = {}
         self.requests = {}
+        self.keep = {}  # what deck jobs point at, while they run
 
     def close(self):
         if getattr(self, "h", None):
@@ -148,6 +181,20 @@ class Batch:
             return None
         capi._check("pihm_batch_add", rc)
         self.jobs[i.value] = (ws, job.nsteps, outlet)
+        return i.value
+
+    def add_deck(self, deck, nsteps: int | None = None, outlet: int = -1) -> int | None:
+        """Admit an input deck with its own forcing (boundary series, land-surface
+        step), nsteps model steps from START (default: to END); None when the
+        arena has no room for it now.  The deck's modes must be the batch's."""
+        job, keep = _deck_job(deck, nsteps, outlet)
+        i = _I32()
+        rc = self.lib.pihm_batch_add(self.h, ctypes.byref(job), ctypes.byref(i))
+        if rc == -5:
+            return None
+        capi._check("pihm_batch_add", rc)
+        self.jobs[i.value] = (keep["ws"], job.nsteps, outlet)
+        self.keep[i.value] = keep
         return i.value
 
     def add_many(self, cases, threads: int = 16):
@@ -181,6 +228,11 @@ class Batch:
 
     def set_program_variant(self, variant: int):
         capi._check("pihm_batch_set_program_variant", self.lib.pihm_batch_set_program_variant(self.h, variant))
+
+    def set_rhs_shape(self, shape: int):
+        """Force the element kernel's block shape (0..2), or -1 to let the
+        engine time them (the default)."""
+        capi._check("pihm_batch_set_rhs_shape", self.lib.pihm_batch_set_rhs_shape(self.h, shape))
 
     def set_rhs_gate(self, gate: float):
         capi._check("pihm_batch_set_rhs_gate", self.lib.pihm_batch_set_rhs_gate(self.h, gate))
@@ -223,6 +275,17 @@ class Batch:
         capi._check("pihm_serve_submit", self.lib.pihm_serve_submit(self.h, ctypes.byref(job), float(arrival),
                                                                      ctypes.byref(t)))
         self.requests[t.value] = (ws, job.nsteps, outlet)
+        return t.value
+
+    def submit_deck(self, deck, arrival: float, nsteps: int | None = None, outlet: int = -1) -> int:
+        """Queue an input deck with its own forcing arriving `arrival` seconds
+        after serve() starts."""
+        job, keep = _deck_job(deck, nsteps, outlet)
+        t = _I32()
+        capi._check("pihm_serve_submit", self.lib.pihm_serve_submit(self.h, ctypes.byref(job), float(arrival),
+                                                                     ctypes.byref(t)))
+        self.requests[t.value] = (keep["ws"], job.nsteps, outlet)
+        self.keep[("serve", t.value)] = keep
         return t.value
 
     def serve(self, workers: int = 4):

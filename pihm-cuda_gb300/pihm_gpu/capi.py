@@ -49,6 +49,7 @@ def load() -> ctypes.CDLL:
                              ctypes.c_double, ctypes.c_int, ctypes.POINTER(_VP)], ctypes.c_int),
         "pihm_gpu_destroy": ([_VP], None),
         "pihm_gpu_set_stream": ([_VP, _VP], ctypes.c_int),
+        "pihm_gpu_set_kernel_shape": ([_VP, ctypes.c_int], ctypes.c_int),
         "pihm_gpu_sizes": ([_VP, _I32P, _I32P, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
         "pihm_gpu_get_permutation": ([_VP, _I32P, _I32P], ctypes.c_int),
         "pihm_gpu_set_forcing": ([_VP, _F64P, _F64P, _F64P], ctypes.c_int),
@@ -113,6 +114,10 @@ class GpuRhs:
     @property
     def neq(self) -> int:
         return self.ws.neq
+
+    def set_kernel_shape(self, shape: int):
+        """Block shape of the element kernel (0: 512 x 2, 1: 256 x 4, 2: 128 x 8 per SM)."""
+        _check("pihm_gpu_set_kernel_shape", self.lib.pihm_gpu_set_kernel_shape(self.h, int(shape)))
 
     def set_stream(self, stream: int):
         _check("pihm_gpu_set_stream", self.lib.pihm_gpu_set_stream(self.h, _VP(stream)))

@@ -170,3 +170,42 @@ def run_deck(deck, nsteps: int | None = None, record_every: int = 0, outlet: int
                          water_balance=water_balance)
     finally:
         b.close()
+
+
+def _main(argv=None):
+    """python -m pihm_gpu.single: a generated watershed solved on the GPU
+    from RelaxIc with hourly synthetic forcing through the plain path; prints
+    the wall time and the integrator's counters as one JSON line."""
+    import argparse
+    import json
+    import time
+
+    from . import watershed as W
+    from . import workloads as WL
+    from .solver import StepControl, run_steps
+    ap = argparse.ArgumentParser(prog="python -m pihm_gpu.single")
+    ap.add_argument("--nelem", type=int, default=WL.RHS_NELEM)
+    ap.add_argument("--nriver", type=int, default=0, help="default: workloads.river_count(nelem)")
+    ap.add_argument("--seed", type=int, default=WL.RHS_SEED)
+    ap.add_argument("--model-steps", type=int, default=2)
+    ap.add_argument("--deferred-scalars", type=int, default=-1, choices=[-1, 0, 1])
+    a = ap.parse_args(argv)
+    ws = W.generate(a.nelem, a.nriver or WL.river_count(a.nelem), seed=a.seed)
+    pcp, edir, ett = WL.step_forcing(ws, a.model_steps, 60.0, seed=8)
+    m = GpuWatershed(ws, W.relax_state(ws), pcp, edir, ett)
+    m.g.set_diagnostics(False)
+    try:
+        t = time.perf_counter()
+        r = run_steps(m, StepControl(), a.model_steps, m.set_forcing, deferred_scalars=a.deferred_scalars)
+        m.read_state()
+        wall = time.perf_counter() - t
+    finally:
+        m.close()
+    s = r["stats"]
+    print(json.dumps({"nelem": ws.nelem, "nriver": ws.nriver, "model_steps": a.model_steps, "wall_s": wall,
+                      "nst": s.nst, "nfe": s.nfe, "nfes": s.nfes, "nni": s.nni, "nli": s.nli,
+                      "deferred_scalars": r["deferred_scalars"]}))
+
+
+if __name__ == "__main__":
+    _main()

@@ -183,3 +183,21 @@ def test_program_kernel_variants_give_the_same_bits(cases, alone, variant):
     for i, c, want in zip(ids, cases, alone):
         _same(b.result(i), want, f"variant {variant}, watershed {c['ws'].nelem}")
     b.close()
+
+
+@pytest.mark.parametrize("shape", [-1, 0, 1, 2])
+def test_element_kernel_shapes_give_the_same_bits(cases, alone, shape):
+    """Each forced block shape of the element kernel, and the tuner (-1),
+    which rotates through them while it times evaluations, give every
+    watershed the bits of its solo run."""
+    b = Batch(limits_for([c["ws"] for c in cases], 90))
+    b.set_rhs_shape(shape)
+    ids = b.add_many(cases)
+    b.step()
+    inf = b.info()
+    if shape >= 0:
+        assert inf.rhs_shape == shape and not inf.rhs_tuning
+    print(f"shape {shape}: in use {inf.rhs_shape}, tuning {inf.rhs_tuning}")
+    for i, c, want in zip(ids, cases, alone):
+        _same(b.result(i), want, f"shape {shape}, watershed {c['ws'].nelem}")
+    b.close()

@@ -111,7 +111,13 @@ def test_land_step_matches_oracle(seed):
 
 def test_land_step_feeds_the_right_hand_side():
     """After a land-surface step the right-hand side reads its pcpdrp, edir and
-    ett: the GPU evaluation equals the restatement given the same forcing."""
+    ett: the GPU evaluation equals the restatement given the same forcing,
+    within the 1e-12 row bar net of the reference's own last-bit envelope
+    (tests/parity.py: the restatement with every pow and log moved one ulp
+    up and down).  The relaxed state puts full soil columns next to a water
+    table at the column's top, where Psi's pow(1/satn, m) - 1 cancels: one
+    ulp of pow moves such a row by up to 5e-8 of its terms in the reference
+    itself."""
     import oracle
     from parity import compare, row_scales
     from pihm_gpu.capi import GpuRhs
@@ -129,14 +135,24 @@ def test_land_step_feeds_the_right_hand_side():
     g.to_internal(yr.data_ptr(), yi.data_ptr())
     g.land_step(t, 900.0, yi.data_ptr())
     forcing = {k: g.land_get(k) for k in ("pcpdrp", "edir", "ett")}
-    o = oracle.Oracle(ws)
-    o.set_forcing(forcing["pcpdrp"], forcing["edir"], forcing["ett"])
-    want, rc = o.rhs(y)
-    assert rc == 0
+    outs = {}
+    for p in (0, 1, -1):
+        o = oracle.Oracle(ws)
+        o.set_ulp_perturb(p)
+        o.set_forcing(forcing["pcpdrp"], forcing["edir"], forcing["ett"])
+        outs[p], rc = o.rhs(y)
+        assert rc == 0
+        if p == 0:
+            scale = row_scales(ws, o.fluxes(), forcing["pcpdrp"], forcing["edir"], forcing["ett"])
+        o.close()
+    want = outs[0]
+    env = np.maximum(np.abs(outs[1] - want), np.abs(outs[-1] - want))
     got, rc = g.rhs_host(y)
     assert rc == 0
-    ok, worst, idx = compare(got, want, row_scales(ws, o.fluxes(), forcing["pcpdrp"], forcing["edir"], forcing["ett"]))
-    assert ok, f"worst {worst:.3e} at {idx}"
+    ok, worst, idx = compare(got, want, scale, envelope=env)
+    plain = compare(got, want, scale)[1]
+    print(f"land-forced right-hand side: worst {worst:.3e} net of the envelope, {plain:.3e} without it")
+    assert ok, f"worst {worst:.3e} at {idx} (envelope {env[idx]:.3e})"
     assert np.count_nonzero(forcing["pcpdrp"]) > 0 and np.count_nonzero(forcing["edir"]) > 0
 
 

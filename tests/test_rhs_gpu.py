@@ -240,3 +240,39 @@ def test_deck_mesh_straight_to_gpu(tmp_path):
     assert rc == 0
     ok, worst, idx = compare(got, want, row_scales(ws, o.fluxes(), pcpdrp, edir, ett))
     assert ok, (worst, idx)
+
+
+def test_element_kernel_shapes_give_the_same_bits():
+    """k_elem_main's three block shapes (512 x 2, 256 x 4, 128 x 8 per SM)
+    evaluate identical derivatives, over three consecutive calls (the carried
+    river-edge flux included), on a 60,000-element mesh."""
+    import torch
+    from pihm_gpu import workloads as WL
+    from pihm_gpu.capi import GpuRhs
+    ws = W.generate(60_000, WL.river_count(60_000), seed=12)
+    y0 = W.reference_state(ws, 12)
+    pcp, edir, ett = W.random_forcing(ws, 12)
+    dev = torch.device("cuda", 0)
+    out = []
+    for shape in (0, 1, 2):
+        g = GpuRhs(ws)
+        g.set_kernel_shape(shape)
+        g.set_forcing(pcp, edir, ett)
+        g.set_ws0_surf(y0[:ws.nelem])
+        y_ref = torch.from_numpy(y0).to(dev)
+        y = torch.empty_like(y_ref)
+        g.to_internal(y_ref.data_ptr(), y.data_ptr())
+        calls = []
+        for k in range(3):
+            yk = y * (1.0 + 0.01 * k)
+            yd = torch.empty_like(y)
+            torch.cuda.synchronize()
+            g.rhs_device(yk.data_ptr(), yd.data_ptr())
+            torch.cuda.synchronize()
+            calls.append(yd.cpu().numpy())
+        assert g.status() == 0
+        g.close()
+        out.append(calls)
+    for shape in (1, 2):
+        for k in range(3):
+            assert np.array_equal(out[shape][k], out[0][k]), (shape, k)
