@@ -304,7 +304,9 @@ def bench_batched():
                     f"{BATCH_STEPS} model steps of 60 s each from RelaxIc",
         "solve_s": t2 - t1, "admit_s": t1 - t0, "readback_s": t3 - t2, "generate_s": gen_s,
         "elem_evals_per_s": evals / (t2 - t1), "rounds": inf.rounds, "rhs_rounds": inf.rhs_rounds,
-        "gpu_launches": inf.launches,
+        "gpu_launches": inf.launches, "launches_per_round": inf.launches / max(inf.rounds, 1),
+        "tuner": {"program_variant": int(inf.program_variant), "program_tuning": bool(inf.tuning),
+                  "rhs_shape": ["512x2", "256x4", "128x8"][int(inf.rhs_shape)], "rhs_tuning": bool(inf.rhs_tuning)},
         "sequential": {"value": BATCH_N / seq_all, "unit": "solves/s",
                        "sample": (f"all {BATCH_N} watersheds one by one through the plain path (create, "
                                   f"solve, read back), {seq_s:.2f} s" if full else
@@ -313,6 +315,56 @@ def bench_batched():
         "speedup_e2e": (BATCH_N / (t3 - t0)) / (BATCH_N / seq_all),
         "bit_identical_to_plain_path": f"{same}/{len(pick)}",
     }
+
+
+SCAT_STATES, SCAT_EVALS = 20, 60
+
+
+def bench_scattered():
+    """The headline right-hand side on an unstructured mesh of the same size:
+    the Delaunay triangulation of 1,000,000 elements' scattered nodes
+    (pihm_gpu.watershed.generate(mesh="scattered"): irregular node degrees
+    and element sizes, as a mesh generator's output), jittered states,
+    device-resident, CUDA events."""
+    import torch
+    import pihm_gpu.watershed as W
+    from pihm_gpu.capi import GpuRhs
+    t = time.perf_counter()
+    ws = W.generate(NELEM, NRIVER, seed=1, mesh="scattered")
+    gen_s = time.perf_counter() - t
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.Stream(device=dev)
+    g = GpuRhs(ws, stream=stream.cuda_stream)
+    g.set_forcing(*W.random_forcing(ws, 3))
+    base = W.reference_state(ws, 2)
+    g.set_ws0_surf(base[:ws.nelem])
+    with torch.cuda.stream(stream):
+        st = torch.empty((SCAT_STATES, ws.neq), dtype=torch.float64, device=dev)
+        stage = torch.empty(ws.neq, dtype=torch.float64, device=dev)
+        for k in range(SCAT_STATES):
+            stage.copy_(torch.from_numpy(W.jitter(base, 300 + k)))
+            g.to_internal(stage.data_ptr(), st[k].data_ptr())
+        yd = torch.empty((2, ws.neq), dtype=torch.float64, device=dev)
+    for k in range(3):
+        g.rhs_device(st[k].data_ptr(), yd[k % 2].data_ptr())
+    stream.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(SCAT_EVALS):
+        g.rhs_device(st[k % SCAT_STATES].data_ptr(), yd[k % 2].data_ptr())
+    e1.record(stream)
+    e1.synchronize()
+    assert g.status() == 0
+    ms = e0.elapsed_time(e1) / SCAT_EVALS
+    g.set_profiling(True)
+    g.rhs_device(st[0].data_ptr(), yd[0].data_ptr())
+    kt = g.kernel_times()
+    g.close()
+    return {"metric": "RHS element-evals/s", "unit": "elem-evals/s", "value": ws.nelem / (ms * 1e-3),
+            "ms_per_eval": ms, "generate_s": gen_s,
+            "workload": f"{ws.nelem} elements, {ws.nriver} segments, Delaunay mesh of scattered nodes, "
+                        f"{SCAT_STATES} jittered states, {SCAT_EVALS} evaluations",
+            "kernel_ms": {k: v[0] / v[1] for k, v in kt.items()}}
 
 
 FLUX_NELEM, FLUX_LAYERS, FLUX_STATES, FLUX_STEPS, FLUX_LSM = 200_000, 4, 40, 60, 3600.0
@@ -685,6 +737,7 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving leg")
     ap.add_argument("--no-flux", action="store_true", help="skip the Flux-PIHM leg")
     ap.add_argument("--no-land", action="store_true", help="skip the land-surface leg")
+    ap.add_argument("--no-scattered", action="store_true", help="skip the scattered-node mesh leg")
     ap.add_argument("--solve-hours", type=float, default=0.5,
                     help="simulated hours of the 1M-element solve leg (0 skips it)")
     args = ap.parse_args()
@@ -858,9 +911,14 @@ def main():
             cpu["serial"] = {"error": repr(exc)}
 
     # ---- batched watersheds and serving (N = 1 only) ----
-    batched = serving = flux = land = solve = None
+    batched = serving = flux = land = solve = scattered = None
     if rank == 0 and world == 1:
         g.close()
+        if not args.no_scattered:
+            try:
+                scattered = bench_scattered()
+            except Exception as exc:
+                scattered = {"error": repr(exc)}
         if args.solve_hours > 0:
             try:
                 solve = bench_solve(ws, args.solve_hours)
@@ -912,6 +970,7 @@ def main():
             "flux_pihm": flux,
             "land_surface": land,
             "solve": solve,
+            "scattered_mesh": scattered,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

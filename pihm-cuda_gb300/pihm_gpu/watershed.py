@@ -167,6 +167,45 @@ def _triangulate(nx, ny, px, py):
     return np.concatenate([t1, t2], 0).astype(np.int64)
 
 
+def _scattered_points(nelem: int, length: float, rng):
+    """Nodes of an unstructured mesh over the square: boundary nodes spaced
+    along the four sides and interior nodes scattered one per stratum (a
+    uniform point in each cell of a k x k stratification, some strata left
+    empty), so that their Delaunay triangulation has about `nelem` triangles
+    with the irregular node degrees and element sizes of a mesh generator's
+    output rather than a grid's.  Returns px, py, interior, corner."""
+    m = max(2, int(round(math.sqrt(nelem / 2.0))))           # boundary segments per side
+    n_int = max(1, (nelem - 4 * m + 2) // 2)                 # triangles = 2 n_int + 4 m - 2
+    k = int(math.ceil(math.sqrt(n_int)))
+    cells = rng.permutation(k * k)[:n_int]
+    ci, cj = cells % k, cells // k
+    h = length / k
+    ix = (ci + rng.uniform(0.05, 0.95, n_int)) * h
+    iy = (cj + rng.uniform(0.05, 0.95, n_int)) * h
+    t = np.arange(m) / m
+    jit = rng.uniform(-0.3, 0.3, (4, m)) / m
+    jit[:, 0] = 0.0                                          # corners stay put
+    u = np.clip(t + jit, 0.0, 1.0)
+    bx = np.concatenate([u[0] * length, np.full(m, length), (1.0 - u[2]) * length, np.zeros(m)])
+    by = np.concatenate([np.zeros(m), u[1] * length, np.full(m, length), (1.0 - u[3]) * length])
+    px = np.concatenate([bx, ix])
+    py = np.concatenate([by, iy])
+    interior = np.concatenate([np.zeros(4 * m, bool), np.ones(n_int, bool)])
+    corner = np.zeros(px.shape[0], bool)
+    corner[[0, m, 2 * m, 3 * m]] = True
+    return px, py, interior, corner
+
+
+def _delaunay(px, py):
+    """Counter-clockwise Delaunay triangles of the nodes."""
+    from scipy.spatial import Delaunay
+    tri = Delaunay(np.stack([px, py], 1)).simplices.astype(np.int64)
+    a = (px[tri[:, 1]] - px[tri[:, 0]]) * (py[tri[:, 2]] - py[tri[:, 0]]) - \
+        (px[tri[:, 2]] - px[tri[:, 0]]) * (py[tri[:, 1]] - py[tri[:, 0]])
+    tri[a < 0] = tri[a < 0][:, [0, 2, 1]]
+    return tri
+
+
 def _neighbours(tri):
     """nb[t, j] = triangle across the edge opposite node j, or -1."""
     nt = tri.shape[0]
@@ -259,24 +298,35 @@ def _river_eq_wid(order, depth, coeff):
 
 def generate(nelem: int = 1000, nriver: int = 100, seed: int = 0,
              length: float = 10000.0, shuffle: bool = True,
-             shapes: str = "mixed") -> Watershed:
-    """Build one synthetic watershed (reference order, 1-based ids)."""
+             shapes: str = "mixed", mesh: str = "grid") -> Watershed:
+    """Build one synthetic watershed (reference order, 1-based ids).
+
+    mesh: "grid" -- a jittered grid, two triangles per cell with the
+    Delaunay diagonal (regular node degrees); "scattered" -- the Delaunay
+    triangulation of scattered nodes (_scattered_points: irregular degrees
+    and element sizes, as a mesh generator's output)."""
     rng = np.random.default_rng(seed)
-    nx, ny = _grid_shape(nelem)
-    dx = length / (nx - 1)
-    dy = length / (ny - 1)
-    gi, gj = np.meshgrid(np.arange(nx), np.arange(ny), indexing="xy")
-    gi = gi.ravel()
-    gj = gj.ravel()
-    px = gi * dx
-    py = gj * dy
-    jx = rng.uniform(-0.3, 0.3, px.shape) * dx
-    jy = rng.uniform(-0.3, 0.3, py.shape) * dy
-    on_x_side = (gi == 0) | (gi == nx - 1)
-    on_y_side = (gj == 0) | (gj == ny - 1)
-    px = px + np.where(on_x_side, 0.0, jx)
-    py = py + np.where(on_y_side, 0.0, jy)
-    interior = ~(on_x_side | on_y_side)
+    if mesh == "grid":
+        nx, ny = _grid_shape(nelem)
+        dx = length / (nx - 1)
+        dy = length / (ny - 1)
+        gi, gj = np.meshgrid(np.arange(nx), np.arange(ny), indexing="xy")
+        gi = gi.ravel()
+        gj = gj.ravel()
+        px = gi * dx
+        py = gj * dy
+        jx = rng.uniform(-0.3, 0.3, px.shape) * dx
+        jy = rng.uniform(-0.3, 0.3, py.shape) * dy
+        on_x_side = (gi == 0) | (gi == nx - 1)
+        on_y_side = (gj == 0) | (gj == ny - 1)
+        px = px + np.where(on_x_side, 0.0, jx)
+        py = py + np.where(on_y_side, 0.0, jy)
+        interior = ~(on_x_side | on_y_side)
+        corner = on_x_side & on_y_side
+    elif mesh == "scattered":
+        px, py, interior, corner = _scattered_points(nelem, length, rng)
+    else:
+        raise ValueError(f"mesh must be 'grid' or 'scattered', not {mesh!r}")
     nnode = px.shape[0]
 
     hills = [(rng.uniform(0, length), rng.uniform(0, length),
@@ -286,7 +336,7 @@ def generate(nelem: int = 1000, nriver: int = 100, seed: int = 0,
     dep_n = rng.uniform(2.0, 10.0, nnode)
     zmin_n = zmax_n - dep_n
 
-    tri = _triangulate(nx, ny, px, py)
+    tri = _triangulate(nx, ny, px, py) if mesh == "grid" else _delaunay(px, py)
     ne = tri.shape[0]
     perm = rng.permutation(ne) if shuffle else np.arange(ne)
     tri = tri[perm]
@@ -296,7 +346,7 @@ def generate(nelem: int = 1000, nriver: int = 100, seed: int = 0,
     u, v, start = _node_adjacency(tri, nnode)
     has_interior_nb = np.zeros(nnode, bool)
     np.logical_or.at(has_interior_nb, u, interior[v])
-    cand = np.where(~interior & has_interior_nb & ~(on_x_side & on_y_side))[0]
+    cand = np.where(~interior & has_interior_nb & ~corner)[0]
     outlet = int(cand[np.argmin(zmax_n[cand])])
     down_n, filled = _drainage(zmax_n, px, py, interior, outlet, u, v, start)
     in_graph = np.isfinite(filled)

@@ -11,6 +11,7 @@ compared here on:
     generator seed 0) on the benchmark's own perturbed states, three
     consecutive calls through the device-pointer entry point (pihm_gpu_rhs)
     and three through the host-buffer entry point (pihm_gpu_rhs_host);
+  * a 300,000-element Delaunay mesh of scattered nodes, the same way;
   * the Flux-PIHM right-hand side on a 200,000-element mesh with 4 Noah soil
     layers, the same way;
   * a batch holding a 100,000-element watershed beside small ones, bit for
@@ -117,6 +118,23 @@ def test_headline_mesh_against_oracle(headline, via, first):
     worst, plain, over = _run_sequence(ws, states, WL.rhs_forcing(ws), base[:ws.nelem], ovl, None, via)
     print(f"\n1M-element mesh via {via}: worst normalised error {worst:.3e} net of the last-bit envelope "
           f"(bar {RTOL:.0e}); without it {plain:.3e}, {over} of {3 * ws.neq} rows above 1e-12")
+
+
+@pytest.mark.parametrize("via", ["device", "host"])
+def test_scattered_point_mesh_against_oracle(via):
+    """A 300,000-element Delaunay mesh of scattered nodes (irregular node
+    degrees and element sizes, as a mesh generator's output), so the
+    renumbering and the per-block queues are exercised on an unstructured
+    adjacency."""
+    ne = 300_000
+    ws = W.generate(ne, WL.river_count(ne), seed=5, mesh="scattered")
+    base = W.reference_state(ws, 6)
+    states = [W.jitter(base, 600 + k) for k in range(3)]
+    forcing = W.random_forcing(ws, 7)
+    ovl = np.random.default_rng(78).normal(0.0, 1e-3, 3 * ne)
+    worst, plain, over = _run_sequence(ws, states, forcing, base[:ne], ovl, None, via)
+    print(f"\n300k-element scattered-node mesh via {via}: worst normalised error {worst:.3e} net of the last-bit "
+          f"envelope (bar {RTOL:.0e}); without it {plain:.3e}, {over} of {3 * ws.neq} rows above 1e-12")
 
 
 @pytest.mark.parametrize("via", ["device", "host"])
