@@ -85,6 +85,15 @@ int pihm_bdf_set_deferred_scalars(pihm_bdf *mem, int setting);
  * the host side of the operations table, 2 kept on the device (3: and the
  * right-hand side's status read back with them); -1 before the first. */
 int pihm_bdf_get_deferred_scalars(const pihm_bdf *mem);
+/* Host time inside the integrator's vector operations (no CVODE
+ * counterpart), accumulated while on (pihm_bdf_set_op_timing resets it):
+ * issuing element-wise operations (and reductions left on the device),
+ * reductions until their value is back on the host (and slot read-backs),
+ * right-hand-side calls until they return.  Wall time outside these is the
+ * integrator's own host work plus the device time the calls waited for. */
+enum { PIHM_BDF_OPT_ELEMENTWISE = 0, PIHM_BDF_OPT_REDUCTION, PIHM_BDF_OPT_RHS, PIHM_BDF_OPT_COUNT };
+int pihm_bdf_set_op_timing(pihm_bdf *mem, int on);
+int pihm_bdf_get_op_times(const pihm_bdf *mem, double *ms, int64_t *calls);
 /* Advance to tout (CV_NORMAL): yout receives y(tout) (or y(tstop)). */
 int pihm_bdf_solve(pihm_bdf *mem, double tout, N_Vector yout, double *tret);
 int pihm_bdf_get_stats(const pihm_bdf *mem, pihm_bdf_stats *stats);

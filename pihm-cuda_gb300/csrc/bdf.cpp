@@ -7,6 +7,8 @@
 // vector operations and right-hand-side evaluations is the one CVODE makes
 // (and therefore so is the river-edge flux the PIHM right-hand side carries
 // from one evaluation to the next).
+#include <chrono>
+
 #include "bdf_core.h"
 #include "pihm_bdf.h"
 #include "pihm_gpu.h"
@@ -20,10 +22,34 @@ static_assert((int)pihm::bdf::COEF_HOST == PIHM_NV_COEF_HOST && (int)pihm::bdf::
                   (int)pihm::bdf::COEF_NEG_INV_INV == PIHM_NV_COEF_NEG_INV_INV,
               "coefficient kinds");
 
+// Host time spent inside the operations (pihm_bdf_set_op_timing): issuing
+// element-wise operations, reductions until their value is back, right-hand
+// side calls until they return, slot read-backs.
+struct OpTimer {
+  bool on = false;
+  double ms[PIHM_BDF_OPT_COUNT] = {0};
+  long long n[PIHM_BDF_OPT_COUNT] = {0};
+};
+
+struct Scope {
+  OpTimer &t;
+  int k;
+  std::chrono::steady_clock::time_point a;
+  Scope(OpTimer &t_, int k_) : t(t_), k(k_) {
+    if (t.on) a = std::chrono::steady_clock::now();
+  }
+  ~Scope() {
+    if (!t.on) return;
+    t.ms[k] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a).count();
+    t.n[k]++;
+  }
+};
+
 struct NVectorOps {
   using Vec = N_Vector;
   pihm_bdf_rhs_fn f = nullptr;
   void *user_data = nullptr;
+  OpTimer timer;
   // GMRES scalars kept with the vectors (pihm_bdf_set_deferred_scalars):
   // -1 automatic (device vectors of this library with its own right-hand
   // side), 0 off, 1 on for any vectors
@@ -43,42 +69,65 @@ struct NVectorOps {
   bool valid(Vec v) const { return v != nullptr; }
 
   pihm::ReadyVoid linear_sum(double a, Vec x, double b, Vec y, Vec z) {
+    Scope sc(timer, PIHM_BDF_OPT_ELEMENTWISE);
     z->ops->nvlinearsum(a, x, b, y, z);
     return {};
   }
   pihm::ReadyVoid const_(double c, Vec z) {
+    Scope sc(timer, PIHM_BDF_OPT_ELEMENTWISE);
     z->ops->nvconst(c, z);
     return {};
   }
   pihm::ReadyVoid scale(double c, Vec x, Vec z) {
+    Scope sc(timer, PIHM_BDF_OPT_ELEMENTWISE);
     z->ops->nvscale(c, x, z);
     return {};
   }
   pihm::ReadyVoid abs_(Vec x, Vec z) {
+    Scope sc(timer, PIHM_BDF_OPT_ELEMENTWISE);
     z->ops->nvabs(x, z);
     return {};
   }
   pihm::ReadyVoid inv(Vec x, Vec z) {
+    Scope sc(timer, PIHM_BDF_OPT_ELEMENTWISE);
     z->ops->nvinv(x, z);
     return {};
   }
   pihm::ReadyVoid div(Vec x, Vec y, Vec z) {
+    Scope sc(timer, PIHM_BDF_OPT_ELEMENTWISE);
     z->ops->nvdiv(x, y, z);
     return {};
   }
   pihm::ReadyVoid prod(Vec x, Vec y, Vec z) {
+    Scope sc(timer, PIHM_BDF_OPT_ELEMENTWISE);
     z->ops->nvprod(x, y, z);
     return {};
   }
   pihm::ReadyVoid addconst(Vec x, double b, Vec z) {
+    Scope sc(timer, PIHM_BDF_OPT_ELEMENTWISE);
     z->ops->nvaddconst(x, b, z);
     return {};
   }
-  pihm::Ready<double> dot(Vec x, Vec y) { return {x->ops->nvdotprod(x, y)}; }
-  pihm::Ready<double> maxnorm(Vec x) { return {x->ops->nvmaxnorm(x)}; }
-  pihm::Ready<double> wrms(Vec x, Vec w) { return {x->ops->nvwrmsnorm(x, w)}; }
-  pihm::Ready<double> vmin(Vec x) { return {x->ops->nvmin(x)}; }
-  pihm::Ready<int> rhs(double t, Vec y, Vec ydot) { return {f(t, y, ydot, user_data)}; }
+  pihm::Ready<double> dot(Vec x, Vec y) {
+    Scope sc(timer, PIHM_BDF_OPT_REDUCTION);
+    return {x->ops->nvdotprod(x, y)};
+  }
+  pihm::Ready<double> maxnorm(Vec x) {
+    Scope sc(timer, PIHM_BDF_OPT_REDUCTION);
+    return {x->ops->nvmaxnorm(x)};
+  }
+  pihm::Ready<double> wrms(Vec x, Vec w) {
+    Scope sc(timer, PIHM_BDF_OPT_REDUCTION);
+    return {x->ops->nvwrmsnorm(x, w)};
+  }
+  pihm::Ready<double> vmin(Vec x) {
+    Scope sc(timer, PIHM_BDF_OPT_REDUCTION);
+    return {x->ops->nvmin(x)};
+  }
+  pihm::Ready<int> rhs(double t, Vec y, Vec ydot) {
+    Scope sc(timer, PIHM_BDF_OPT_RHS);
+    return {f(t, y, ydot, user_data)};
+  }
 
   // ---- device-resident GMRES scalars (bdf_core.h atimes_gs_deferred) ----
   static bool is_device(Vec v) { return v && v->ops && v->ops->nvgetvectorid == N_VGetVectorID_PihmGpu; }
@@ -104,16 +153,19 @@ struct NVectorOps {
     }
   }
   pihm::ReadyVoid dot_slot(Vec x, Vec y, int slot) {
+    Scope sc(timer, PIHM_BDF_OPT_ELEMENTWISE);
     if (mode == 2) N_VDotProdSlot_PihmGpu(x, y, slot);
     else host_slots[slot] = x->ops->nvdotprod(x, y);
     return {};
   }
   pihm::ReadyVoid wrms_slot(Vec x, Vec w, int slot) {
+    Scope sc(timer, PIHM_BDF_OPT_ELEMENTWISE);
     if (mode == 2) N_VWrmsNormSlot_PihmGpu(x, w, slot);
     else host_slots[slot] = x->ops->nvwrmsnorm(x, w);
     return {};
   }
   pihm::ReadyVoid linear_sum_coef(pihm::bdf::Coef a, Vec x, pihm::bdf::Coef b, Vec y, Vec z) {
+    Scope sc(timer, PIHM_BDF_OPT_ELEMENTWISE);
     if (mode == 2) {
       const pihm_nv_coef ca = {a.kind, a.slot, a.value}, cb = {b.kind, b.slot, b.value};
       N_VLinearSumCoef_PihmGpu(&ca, x, &cb, y, z);
@@ -123,6 +175,7 @@ struct NVectorOps {
     return {};
   }
   pihm::Ready<int> rhs_deferred(double t, Vec y, Vec ydot) {
+    Scope sc(timer, PIHM_BDF_OPT_RHS);
     if (!rhs_deferrable) return {f(t, y, ydot, user_data)};
     const int rc = pihm_gpu_ode_launch(t, y, ydot, user_data);
     rhs_pending = rc == 0;
@@ -130,6 +183,7 @@ struct NVectorOps {
   }
   // slots 0..count-1 to out; -1 when a deferred right-hand side produced a NaN
   pihm::Ready<int> fetch_slots(int count, double *out) {
+    Scope sc(timer, PIHM_BDF_OPT_REDUCTION);
     if (mode != 2) {
       for (int i = 0; i < count; i++) out[i] = host_slots[i];
       return {0};
@@ -179,6 +233,22 @@ int pihm_bdf_set_user_data(pihm_bdf *m, void *user_data) {
   if (!m) return PIHM_BDF_ILL_INPUT;
   m->ops.user_data = user_data;
   m->ops.mode = -1;
+  return PIHM_BDF_SUCCESS;
+}
+
+int pihm_bdf_set_op_timing(pihm_bdf *m, int on) {
+  if (!m) return PIHM_BDF_ILL_INPUT;
+  m->ops.timer = OpTimer();
+  m->ops.timer.on = on != 0;
+  return PIHM_BDF_SUCCESS;
+}
+
+int pihm_bdf_get_op_times(const pihm_bdf *m, double *ms, int64_t *calls) {
+  if (!m || !ms) return PIHM_BDF_ILL_INPUT;
+  for (int k = 0; k < PIHM_BDF_OPT_COUNT; k++) {
+    ms[k] = m->ops.timer.ms[k];
+    if (calls) calls[k] = m->ops.timer.n[k];
+  }
   return PIHM_BDF_SUCCESS;
 }
 

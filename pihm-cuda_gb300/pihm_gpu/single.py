@@ -189,6 +189,7 @@ def _main(argv=None):
     ap.add_argument("--seed", type=int, default=WL.RHS_SEED)
     ap.add_argument("--model-steps", type=int, default=2)
     ap.add_argument("--deferred-scalars", type=int, default=-1, choices=[-1, 0, 1])
+    ap.add_argument("--op-timing", action="store_true", help="host time inside the integrator's operations")
     a = ap.parse_args(argv)
     ws = W.generate(a.nelem, a.nriver or WL.river_count(a.nelem), seed=a.seed)
     pcp, edir, ett = WL.step_forcing(ws, a.model_steps, 60.0, seed=8)
@@ -196,7 +197,8 @@ def _main(argv=None):
     m.g.set_diagnostics(False)
     try:
         t = time.perf_counter()
-        r = run_steps(m, StepControl(), a.model_steps, m.set_forcing, deferred_scalars=a.deferred_scalars)
+        r = run_steps(m, StepControl(), a.model_steps, m.set_forcing, deferred_scalars=a.deferred_scalars,
+                      op_timing=a.op_timing)
         m.read_state()
         wall = time.perf_counter() - t
     finally:
@@ -204,7 +206,8 @@ def _main(argv=None):
     s = r["stats"]
     print(json.dumps({"nelem": ws.nelem, "nriver": ws.nriver, "model_steps": a.model_steps, "wall_s": wall,
                       "nst": s.nst, "nfe": s.nfe, "nfes": s.nfes, "nni": s.nni, "nli": s.nli,
-                      "deferred_scalars": r["deferred_scalars"]}))
+                      "deferred_scalars": r["deferred_scalars"],
+                      **({"op_ms": r["op_ms"], "op_calls": r["op_calls"]} if a.op_timing else {})}))
 
 
 if __name__ == "__main__":

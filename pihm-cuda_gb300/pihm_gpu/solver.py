@@ -45,6 +45,9 @@ def _bind(lib):
         "pihm_bdf_set_stop_time": ([_VP, _D], ctypes.c_int),
         "pihm_bdf_set_deferred_scalars": ([_VP, ctypes.c_int], ctypes.c_int),
         "pihm_bdf_get_deferred_scalars": ([_VP], ctypes.c_int),
+        "pihm_bdf_set_op_timing": ([_VP, ctypes.c_int], ctypes.c_int),
+        "pihm_bdf_get_op_times": ([_VP, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)],
+                                  ctypes.c_int),
         "pihm_bdf_solve": ([_VP, _D, _VP, ctypes.POINTER(_D)], ctypes.c_int),
         "pihm_bdf_get_stats": ([_VP, ctypes.POINTER(BdfStats)], ctypes.c_int),
         "pihm_bdf_free": ([_VP], None),
@@ -98,7 +101,8 @@ class Bdf:
 
 
 def run_steps(backend, ctrl: StepControl, nsteps: int, forcing, record_every: int = 0,
-              outlet: int | None = None, water_balance: bool = False, deferred_scalars: int | None = None):
+              outlet: int | None = None, water_balance: bool = False, deferred_scalars: int | None = None,
+              op_timing: bool = False):
     """The reference's model-step loop over `backend`, from t = 0.
 
     backend provides: y (N_Vector handle of the state), rhs (C function
@@ -110,6 +114,8 @@ def run_steps(backend, ctrl: StepControl, nsteps: int, forcing, record_every: in
     deferred_scalars: pihm_bdf_set_deferred_scalars (None keeps the
     library's default: GMRES scalars kept on the device for device vectors
     with pihm_gpu_ode; the same solution either way).
+    op_timing: record the host time inside the integrator's operations
+    (pihm_bdf_set_op_timing), returned as op_ms / op_calls.
     Returns dict(states=[...], outlet=[...], stats=BdfStats, wb=[nsteps][3]).
     """
     bdf = Bdf()
@@ -121,6 +127,8 @@ def run_steps(backend, ctrl: StepControl, nsteps: int, forcing, record_every: in
     bdf.check("stald", lib.pihm_bdf_set_stab_lim_det(bdf.h, 1))
     if deferred_scalars is not None:
         bdf.check("deferred", lib.pihm_bdf_set_deferred_scalars(bdf.h, int(deferred_scalars)))
+    if op_timing:
+        bdf.check("timing", lib.pihm_bdf_set_op_timing(bdf.h, 1))
     maxstep = float(ctrl.stepsize)
     bdf.check("hmax", lib.pihm_bdf_set_max_step(bdf.h, maxstep))
     bdf.check("mxstep", lib.pihm_bdf_set_max_num_steps(bdf.h, ctrl.mxstep or ctrl.stepsize * 10))
@@ -154,5 +162,10 @@ def run_steps(backend, ctrl: StepControl, nsteps: int, forcing, record_every: in
             states.append(backend.read_state())
     out = dict(states=np.array(states), outlet=np.array(qout), stats=bdf.stats(), wb=np.array(wb),
                deferred_scalars=lib.pihm_bdf_get_deferred_scalars(bdf.h))
+    if op_timing:
+        ms, n = (ctypes.c_double * 3)(), (ctypes.c_int64 * 3)()
+        bdf.check("times", lib.pihm_bdf_get_op_times(bdf.h, ms, n))
+        out["op_ms"] = dict(zip(("elementwise", "reduction", "rhs"), list(ms)))
+        out["op_calls"] = dict(zip(("elementwise", "reduction", "rhs"), list(n)))
     bdf.close()
     return out

@@ -114,7 +114,7 @@ def test_land_step_feeds_the_right_hand_side():
     ett: the GPU evaluation equals the restatement given the same forcing,
     within the 1e-12 row bar net of the reference's own last-bit envelope
     (tests/parity.py: the restatement with every pow and log moved one ulp
-    up and down).  The relaxed state puts full soil columns next to a water
+    up plus the same moved down, as the scale tests take it).  The relaxed state puts full soil columns next to a water
     table at the column's top, where Psi's pow(1/satn, m) - 1 cancels: one
     ulp of pow moves such a row by up to 5e-8 of its terms in the reference
     itself."""
@@ -146,7 +146,7 @@ def test_land_step_feeds_the_right_hand_side():
             scale = row_scales(ws, o.fluxes(), forcing["pcpdrp"], forcing["edir"], forcing["ett"])
         o.close()
     want = outs[0]
-    env = np.maximum(np.abs(outs[1] - want), np.abs(outs[-1] - want))
+    env = np.abs(outs[1] - want) + np.abs(outs[-1] - want)
     got, rc = g.rhs_host(y)
     assert rc == 0
     ok, worst, idx = compare(got, want, scale, envelope=env)
