@@ -256,7 +256,7 @@ def run_reference_arm(args):
 
 BATCH_N, BATCH_LO, BATCH_HI, BATCH_STEPS, BATCH_SEQ_SAMPLE = 256, 2000, 200000, 10, 256
 SERVE_N, SERVE_LO, SERVE_HI, SERVE_STEPS, SERVE_LOAD = 48, 1000, 500000, 10, 0.8
-SERVE_ARENA_ELEM, SERVE_MAX_REQ = 3_000_000, 64
+SERVE_ARENA_BYTES, SERVE_MAX_REQ = 4 << 30, 64  # the arena's device-memory budget (about 3M elements)
 
 
 def _pct(a, q):
@@ -665,19 +665,17 @@ def bench_serving():
     import numpy as np
     import torch
     from pihm_gpu import workloads as WL
-    from pihm_gpu.batch import DONE, Batch, BatchLimits
+    from pihm_gpu.batch import DONE, Batch, limits_for_memory
     from pihm_gpu.single import solve_alone
     t = time.perf_counter()
     cases = WL.make_cases(WL.serving_specs(SERVE_N, SERVE_LO, SERVE_HI, SERVE_STEPS))
     gen_s = time.perf_counter() - t
 
     def limits():
-        lim = BatchLimits()
-        lim.max_elem = SERVE_ARENA_ELEM
-        lim.max_river = SERVE_ARENA_ELEM // 10 + 16
-        lim.max_edge = int(1.6 * SERVE_ARENA_ELEM) + 16
+        # the largest arena in the memory budget: admission is gated by it
+        lim = limits_for_memory(SERVE_ARENA_BYTES, rivers_per_elem=0.1, edges_per_elem=1.6,
+                                records_per_elem=0.0, max_systems=SERVE_MAX_REQ)
         lim.max_record = SERVE_N * SERVE_STEPS
-        lim.max_systems = SERVE_MAX_REQ
         return lim
 
     def serve(arrivals):
@@ -714,9 +712,11 @@ def bench_serving():
         "metric": "served solves/s", "unit": "solves/s", "value": SERVE_N / span,
         "p50_s": _pct(lat, 50), "p99_s": _pct(lat, 99), "mean_s": float(lat.mean()),
         "workload": f"{SERVE_N} requests, {SERVE_LO}..{SERVE_HI} elements (log-uniform), Ksat x U(0.3,3), "
-                    f"Manning n x U(0.5,2), model step 60 or 120 s, {SERVE_STEPS} model steps each, "
+                    f"Manning n x U(0.5,2), model step of 30, 60, 90, 120 or 180 s, {SERVE_STEPS} model steps each, "
                     f"Poisson arrivals at {SERVE_LOAD} of the measured capacity {mu:.2f} solves/s",
-        "arena_elements": SERVE_ARENA_ELEM, "rounds": inf.rounds, "generate_s": gen_s,
+        "arena_elements": int(limits().max_elem), "arena_bytes": SERVE_ARENA_BYTES,
+        "admission": "by the arena's device-memory budget (pihm_batch_limits_for_memory)",
+        "rounds": inf.rounds, "generate_s": gen_s,
         "sequential": {"value": SERVE_N / seq_end, "unit": "solves/s", "p50_s": _pct(seq_lat, 50),
                        "p99_s": _pct(seq_lat, 99), "service_s_total": float(sum(service)),
                        "note": "plain path, one request at a time, first come first served, same arrivals"},

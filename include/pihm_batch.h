@@ -88,6 +88,16 @@ enum { PIHM_BATCH_RUNNING = 0, PIHM_BATCH_DONE = 1, PIHM_BATCH_FAILED = 2 };
 
 int pihm_batch_create(const pihm_batch_limits *lim, int surf_mode, int riv_mode, int order,
                       pihm_batch **out);
+/* Device memory an arena with these limits takes (all of pihm_batch_create's
+ * allocations, at the allocator's 512-byte granularity). */
+int pihm_batch_arena_bytes(const pihm_batch_limits *lim, int64_t *bytes);
+/* The largest arena that fits in `bytes` of device memory -- e.g. a share of
+ * cudaMemGetInfo's free memory -- for watersheds with about rivers_per_elem
+ * segments, edges_per_elem interior edges and records_per_elem hydrograph
+ * entries per element: admission (pihm_batch_add, the serving layer) is then
+ * gated by that memory.  PIHM_GPU_ERR_NOMEM if not even one element fits. */
+int pihm_batch_limits_for_memory(int64_t bytes, double rivers_per_elem, double edges_per_elem,
+                                 double records_per_elem, int32_t max_systems, pihm_batch_limits *out);
 void pihm_batch_destroy(pihm_batch *b);
 int pihm_batch_set_stream(pihm_batch *b, void *stream);
 

@@ -120,10 +120,18 @@ Task<int> model_run(Sys *s) {
   co_return bdf::SUCCESS;
 }
 
+// Counting mode of pihm_batch_create (pihm_batch_arena_bytes): allocations
+// add their size here instead of allocating.
+thread_local int64_t *t_count_bytes = nullptr;
+
 template <class T>
 T *dalloc(size_t n, std::vector<void *> &owned) {
   void *p = nullptr;
   if (n == 0) n = 1;
+  if (t_count_bytes) {
+    *t_count_bytes += (int64_t)((sizeof(T) * n + 511) & ~size_t(511));  // the allocator's granularity
+    return (T *)(uintptr_t)4096;
+  }
   if (cudaMalloc(&p, sizeof(T) * n) != cudaSuccess) return nullptr;
   owned.push_back(p);
   return (T *)p;
@@ -797,6 +805,7 @@ int pihm_batch_create(const pihm_batch_limits *lim, int surf_mode, int riv_mode,
   // download block: results | error words
   B->down_bytes = sizeof(double) * 2 * MS + sizeof(unsigned int) * MS;
   B->d_down = (char *)dalloc<char>(B->down_bytes, o);
+  if (t_count_bytes) return PIHM_GPU_OK;  // sizes counted, nothing allocated
   if (!ok || !m.err || !A.sysinfo || !A.tickets || !B->d_up || !B->d_down ||
       cudaMallocHost(&B->h_up, up_bytes) != cudaSuccess ||
       cudaMallocHost(&B->h_down, B->down_bytes) != cudaSuccess)
@@ -836,6 +845,46 @@ int pihm_batch_create(const pihm_batch_limits *lim, int surf_mode, int riv_mode,
 }
 
 void pihm_batch_destroy(pihm_batch *b) { delete b; }
+
+int pihm_batch_arena_bytes(const pihm_batch_limits *lim, int64_t *bytes) {
+  if (!lim || !bytes) return PIHM_GPU_ERR_ARG;
+  int64_t n = 0;
+  t_count_bytes = &n;
+  pihm_batch *b = nullptr;
+  const int rc = pihm_batch_create(lim, 2, 2, PIHM_GPU_ORDER_RCM, &b);
+  t_count_bytes = nullptr;
+  if (rc != PIHM_GPU_OK) return rc;
+  *bytes = n;
+  return PIHM_GPU_OK;
+}
+
+int pihm_batch_limits_for_memory(int64_t bytes, double rivers_per_elem, double edges_per_elem,
+                                 double records_per_elem, int32_t max_systems, pihm_batch_limits *out) {
+  if (!out || bytes <= 0 || !(rivers_per_elem >= 0.0) || !(edges_per_elem >= 0.0) || !(records_per_elem >= 0.0) ||
+      max_systems <= 0)
+    return PIHM_GPU_ERR_ARG;
+  auto limits = [&](int64_t ne) {
+    pihm_batch_limits l{};
+    l.max_elem = ne;
+    l.max_river = (int64_t)(rivers_per_elem * (double)ne) + 1;
+    l.max_edge = (int64_t)(edges_per_elem * (double)ne) + 16;
+    l.max_record = (int64_t)(records_per_elem * (double)ne) + 1;
+    l.max_systems = max_systems;
+    return l;
+  };
+  // the largest element capacity whose arena fits (bytes grow with it)
+  int64_t lo = 0, hi = INT32_MAX / 3;
+  while (lo < hi) {
+    const int64_t mid = lo + (hi - lo + 1) / 2;
+    const pihm_batch_limits l = limits(mid);
+    int64_t need = 0;
+    if (pihm_batch_arena_bytes(&l, &need) == PIHM_GPU_OK && need <= bytes) lo = mid;
+    else hi = mid - 1;
+  }
+  if (lo < 1) return PIHM_GPU_ERR_NOMEM;
+  *out = limits(lo);
+  return PIHM_GPU_OK;
+}
 
 int pihm_batch_set_rhs_gate(pihm_batch *b, double gate) {
   if (!b || !(gate >= 0.0 && gate <= 1.0)) return PIHM_GPU_ERR_ARG;

@@ -125,6 +125,8 @@ def _bind(lib):
         "pihm_batch_set_profiling": ([_VP, ctypes.c_int], ctypes.c_int),
         "pihm_batch_set_program_variant": ([_VP, _I32], ctypes.c_int),
         "pihm_batch_set_rhs_shape": ([_VP, _I32], ctypes.c_int),
+        "pihm_batch_arena_bytes": ([ctypes.POINTER(BatchLimits), ctypes.POINTER(_I64)], ctypes.c_int),
+        "pihm_batch_limits_for_memory": ([_I64, _D, _D, _D, _I32, ctypes.POINTER(BatchLimits)], ctypes.c_int),
         "pihm_serve_submit": ([_VP, ctypes.POINTER(BatchJob), _D, ctypes.POINTER(_I32)], ctypes.c_int),
         "pihm_serve_run": ([_VP, _I32], ctypes.c_int),
         "pihm_serve_record_get": ([_VP, _I32, ctypes.POINTER(ServeRecord)], ctypes.c_int),
@@ -135,6 +137,26 @@ def _bind(lib):
         f.argtypes = args
         f.restype = res
     return lib
+
+
+def arena_bytes(limits: BatchLimits) -> int:
+    """Device memory an arena with these limits takes."""
+    lib = _bind(capi.load())
+    n = _I64()
+    capi._check("pihm_batch_arena_bytes", lib.pihm_batch_arena_bytes(ctypes.byref(limits), ctypes.byref(n)))
+    return n.value
+
+
+def limits_for_memory(nbytes: int, rivers_per_elem: float = 0.03, edges_per_elem: float = 1.6,
+                      records_per_elem: float = 0.01, max_systems: int = 256) -> BatchLimits:
+    """The largest arena that fits in nbytes of device memory (admission is
+    then gated by that memory)."""
+    lib = _bind(capi.load())
+    lim = BatchLimits()
+    capi._check("pihm_batch_limits_for_memory", lib.pihm_batch_limits_for_memory(
+        int(nbytes), float(rivers_per_elem), float(edges_per_elem), float(records_per_elem), int(max_systems),
+        ctypes.byref(lim)))
+    return lim
 
 
 def limits_for(watersheds, nsteps: int, slack: float = 1.0) -> BatchLimits:

@@ -103,7 +103,7 @@ def batched_specs(n: int = 256, lo: int = 2000, hi: int = 200000, nsteps: int = 
 
 
 def serving_specs(n: int, lo: int = 1000, hi: int = 500000, nsteps: int = 10, seed: int = 1,
-                  stepsizes=(60.0, 120.0)):
+                  stepsizes=(30.0, 60.0, 90.0, 120.0, 180.0)):
     rng = np.random.default_rng(seed)
     sizes = log_uniform_sizes(n, lo, hi, seed + 1)
     out = []
