@@ -231,7 +231,7 @@ void pihm_gpu_destroy(pihm_gpu_ctx *c) {
   if (c->d_dyn) cudaFree(c->d_dyn);
   if (c->d_noah) cudaFree(c->d_noah);
   pihm::land_release(c->land);
-  noah_free(c);
+  pihm::noah_release(c->noahlsm);
   if (c->side.fork) cudaEventDestroy(c->side.fork);
   if (c->side.join) cudaEventDestroy(c->side.join);
   if (c->side.side) cudaStreamDestroy(c->side.side);

@@ -158,7 +158,7 @@ __global__ void __launch_bounds__(kNoahBlock) k_noah_step(NoahPlanes P, double d
 
 // y: the model state after the step (internal order); first: no previous
 // state yet, ws0 is taken from y
-__global__ void __launch_bounds__(kNoahBlock) k_noah_post(NoahPlanes P, DevMesh m, const double *y, double dt,
+__global__ void __launch_bounds__(kNoahBlock) k_noah_post(NoahPlanes P, NoahTargets o, const double *y, double dt,
                                                           int first) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.ne) return;
@@ -176,10 +176,11 @@ __global__ void __launch_bounds__(kNoahBlock) k_noah_post(NoahPlanes P, DevMesh 
   soilw1 = (soilw1 > c.depth) ? c.depth : soilw1;
   soilw1 = (soilw1 < 0.0) ? 0.0 : soilw1;
   double subrunoff = 0.0;
-  for (int j = 0; j < 3; j++) subrunoff += m.d_sub[j * ne + i] / c.area;
+  const int64_t ds = o.stride;
+  for (int j = 0; j < 3; j++) subrunoff += o.d_sub[j * ds + i] / c.area;
   // the last evaluation's ET split: edir_unsat, edir_gw, ett_unsat, ett_gw
-  c.infil = (soilw1 - soilw0) * c.porosity / dt + subrunoff + m.d_et[ne + i] + m.d_et[2 * ne + i] +
-            m.d_et[3 * ne + i] + m.d_et[4 * ne + i];
+  c.infil = (soilw1 - soilw0) * c.porosity / dt + subrunoff + o.d_et[ds + i] + o.d_et[2 * ds + i] +
+            o.d_et[3 * ds + i] + o.d_et[4 * ds + i];
   if (c.infil < 0.0) {
     subrunoff -= c.infil;
     c.infil = 0.0;
@@ -203,7 +204,7 @@ __global__ void __launch_bounds__(256) k_noah_begin(NoahPlanes P, const double *
 }
 
 // The Flux-PIHM right-hand side's inputs from Noah's state and outputs.
-__global__ void __launch_bounds__(256) k_noah_inputs(NoahPlanes P, DevMesh m) {
+__global__ void __launch_bounds__(256) k_noah_inputs(NoahPlanes P, NoahTargets o) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.ne) return;
   const int ne = P.ne;
@@ -212,13 +213,13 @@ __global__ void __launch_bounds__(256) k_noah_inputs(NoahPlanes P, DevMesh m) {
   if (top <= nr)
     for (int j = (top <= 0 ? 0 : top - 1); j < nr; j++) g += P.l[NL_ET][j * ne + i];
   const double smcmin = P.s[NS_SMCMIN][i], smcmax = P.s[NS_SMCMAX][i];
-  const_cast<double *>(m.noah_etgw)[i] = g;
-  const_cast<int32_t *>(m.noah_wtin)[i] = top <= nr;
-  const_cast<double *>(m.noah_satn)[i] = (P.l[NL_SH2O][i] - smcmin) / (smcmax - smcmin);
-  const_cast<double *>(m.noah_fcr)[i] = P.s[NS_FCR][i];
-  const_cast<double *>(m.edir)[i] = P.s[NS_EDIR][i];
-  const_cast<double *>(m.ett)[i] = P.s[NS_ETT][i];
-  const_cast<double *>(m.pcpdrp)[i] = P.s[NS_PCPDRP][i];
+  o.etgw[i] = g;
+  o.wtin[i] = top <= nr;
+  o.satn[i] = (P.l[NL_SH2O][i] - smcmin) / (smcmax - smcmin);
+  o.fcr[i] = P.s[NS_FCR][i];
+  o.edir[i] = P.s[NS_EDIR][i];
+  o.ett[i] = P.s[NS_ETT][i];
+  o.pcpdrp[i] = P.s[NS_PCPDRP][i];
 }
 
 template <class T>
@@ -229,71 +230,61 @@ size_t padded(size_t n) {
 int cuda_rc(cudaError_t e) { return e == cudaSuccess ? PIHM_GPU_OK : PIHM_GPU_ERR_CUDA; }
 
 // reference-order [ne][per] host values -> internal-order [per][ne] device planes
-int upload(pihm_gpu_ctx *c, const double *src, int per, double *const *dst) {
-  const int ne = c->ne;
+int upload(const int32_t *perm, int ne, const double *src, int per, double *const *dst, cudaStream_t st) {
   std::vector<double> h((size_t)ne);
   for (int k = 0; k < per; k++) {
-    for (int i = 0; i < ne; i++) h[i] = src[(size_t)per * c->h_perm[i] + k];
-    if (cudaMemcpyAsync(dst[k], h.data(), sizeof(double) * ne, cudaMemcpyHostToDevice, c->stream) != cudaSuccess ||
-        cudaStreamSynchronize(c->stream) != cudaSuccess)
+    for (int i = 0; i < ne; i++) h[i] = src[(size_t)per * perm[i] + k];
+    if (cudaMemcpyAsync(dst[k], h.data(), sizeof(double) * ne, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
       return PIHM_GPU_ERR_CUDA;
   }
   return PIHM_GPU_OK;
 }
 
-int upload_layers(pihm_gpu_ctx *c, const double *src, double *plane) {
+int upload_layers(const int32_t *perm, int ne, const double *src, double *plane, cudaStream_t st) {
   double *dst[noah::L];
-  for (int k = 0; k < noah::L; k++) dst[k] = plane + (size_t)k * c->ne;
-  return upload(c, src, noah::L, dst);
+  for (int k = 0; k < noah::L; k++) dst[k] = plane + (size_t)k * ne;
+  return upload(perm, ne, src, noah::L, dst, st);
 }
 
-int upload_int(pihm_gpu_ctx *c, const int32_t *src, int32_t *dst) {
-  const int ne = c->ne;
+int upload_int(const int32_t *perm, int ne, const int32_t *src, int32_t *dst) {
   std::vector<int32_t> h((size_t)ne);
-  for (int i = 0; i < ne; i++) h[i] = src[c->h_perm[i]];
+  for (int i = 0; i < ne; i++) h[i] = src[perm[i]];
   return cuda_rc(cudaMemcpy(dst, h.data(), sizeof(int32_t) * ne, cudaMemcpyHostToDevice));
 }
 
-int upload_scalar(pihm_gpu_ctx *c, const double *src, double *dst) { return src ? upload(c, src, 1, &dst) : 0; }
+int upload_scalar(const int32_t *perm, int ne, const double *src, double *dst, cudaStream_t st) {
+  return src ? upload(perm, ne, src, 1, &dst, st) : 0;
+}
 
-int launch_inputs(pihm_gpu_ctx *c) {
-  const NoahPlanes &P = *c->noahlsm;
-  k_noah_inputs<<<(P.ne + 255) / 256, 256, 0, c->stream>>>(P, c->m);
-  c->launches++;
+int launch_inputs(NoahInstance &n, cudaStream_t st, int64_t *launches) {
+  k_noah_inputs<<<(n.ne + 255) / 256, 256, 0, st>>>(*n.P, n.tg);
+  ++*launches;
   return cuda_rc(cudaGetLastError());
 }
 
 }  // namespace
 
-void noah_free(pihm_gpu_ctx *c) {
-  if (c->d_noahlsm) cudaFree(c->d_noahlsm);
-  c->d_noahlsm = nullptr;
-  delete c->noahlsm;
-  c->noahlsm = nullptr;
-}
-
-}  // namespace pihm
-
-using namespace pihm;
-
-extern "C" int pihm_gpu_noah_set_state(pihm_gpu_ctx *c, const pihm_noah_state *s) {
-  if (!c || !c->noahlsm || !s) return PIHM_GPU_ERR_ARG;
-  NoahPlanes &P = *c->noahlsm;
+int noah_set_state(NoahInstance &n, const pihm_noah_state *s, const int32_t *perm, cudaStream_t st) {
+  if (!n.alloc || !s) return PIHM_GPU_ERR_ARG;
+  NoahPlanes &P = *n.P;
+  const int ne = n.ne;
   int rc = PIHM_GPU_OK;
-  if (s->smc) rc = rc ?: upload_layers(c, s->smc, P.l[NL_SMC]);
-  if (s->sh2o) rc = rc ?: upload_layers(c, s->sh2o, P.l[NL_SH2O]);
-  if (s->stc) rc = rc ?: upload_layers(c, s->stc, P.l[NL_STC]);
+  if (s->smc) rc = rc ?: upload_layers(perm, ne, s->smc, P.l[NL_SMC], st);
+  if (s->sh2o) rc = rc ?: upload_layers(perm, ne, s->sh2o, P.l[NL_SH2O], st);
+  if (s->stc) rc = rc ?: upload_layers(perm, ne, s->stc, P.l[NL_STC], st);
   const double *src[] = {s->t1, s->cmc, s->sneqv, s->snowh, s->sndens, s->ch, s->cm, s->snotime1,
                          s->albedo, s->emissi, s->q1, s->ribb, s->fcr};
   const int dst[] = {NS_T1, NS_CMC, NS_SNEQV, NS_SNOWH, NS_SNDENS, NS_CH, NS_CM, NS_SNOTIME1,
                      NS_ALBEDO, NS_EMISSI, NS_Q1, NS_RIBB, NS_FCR};
-  for (int k = 0; k < 13; k++) rc = rc ?: upload_scalar(c, src[k], P.s[dst[k]]);
-  return rc ?: launch_inputs(c) ?: cuda_rc(cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < 13; k++) rc = rc ?: upload_scalar(perm, ne, src[k], P.s[dst[k]], st);
+  int64_t launches = 0;
+  return rc ?: launch_inputs(n, st, &launches) ?: cuda_rc(cudaStreamSynchronize(st));
 }
 
-extern "C" int pihm_gpu_noah_init(pihm_gpu_ctx *c, const pihm_noah_params *p, const pihm_noah_state *s) {
-  if (!c || !p || !s || p->nelem != c->ne || !p->nsoil || !p->sldpth || !p->nroot || !p->rtdis) return PIHM_GPU_ERR_ARG;
-  const int ne = c->ne;
+int noah_build(const pihm_noah_params *p, const pihm_noah_state *s, const int32_t *perm, int ne,
+               const NoahTargets &tg, cudaStream_t st, NoahInstance *out) {
+  if (!p || !s || !out || p->nelem != ne || !p->nsoil || !p->sldpth || !p->nroot || !p->rtdis) return PIHM_GPU_ERR_ARG;
   for (int r = 0; r < ne; r++) {
     // HRT and SRT read the second layer: at least two
     if (p->nsoil[r] < 2 || p->nsoil[r] > noah::L || p->nroot[r] < 1 || p->nroot[r] > p->nsoil[r])
@@ -312,19 +303,22 @@ extern "C" int pihm_gpu_noah_init(pihm_gpu_ctx *c, const pihm_noah_params *p, co
   if (!s->smc || !s->sh2o || !s->stc || !s->t1 || !s->cmc || !s->sneqv || !s->snowh || !s->sndens || !s->ch ||
       !s->cm || !s->snotime1 || !s->albedo || !s->emissi || !s->q1 || !s->ribb || !s->fcr)
     return PIHM_GPU_ERR_ARG;
-  noah_free(c);
   const size_t NE = ne;
   const size_t bytes = NS_COUNT * padded<double>(NE) + NL_COUNT * padded<double>(noah::L * NE) +
                        NI_COUNT * padded<int32_t>(NE);
-  if (cudaMalloc(&c->d_noahlsm, bytes) != cudaSuccess) {
-    c->d_noahlsm = nullptr;
-    return PIHM_GPU_ERR_NOMEM;
+  NoahInstance n;
+  if (cudaMalloc(&n.alloc, bytes) != cudaSuccess) return PIHM_GPU_ERR_NOMEM;
+  n.P = new NoahPlanes();
+  n.tg = tg;
+  n.ne = ne;
+  n.first = 1;
+  if (cudaMemset(n.alloc, 0, bytes) != cudaSuccess) {
+    noah_release(n);
+    return PIHM_GPU_ERR_CUDA;
   }
-  if (cudaMemset(c->d_noahlsm, 0, bytes) != cudaSuccess) return PIHM_GPU_ERR_CUDA;
-  c->noahlsm = new NoahPlanes();
-  NoahPlanes &P = *c->noahlsm;
+  NoahPlanes &P = *n.P;
   P.ne = ne;
-  char *cur = (char *)c->d_noahlsm;
+  char *cur = (char *)n.alloc;
   for (int k = 0; k < NS_COUNT; k++) {
     P.s[k] = (double *)cur;
     cur += padded<double>(NE);
@@ -338,7 +332,7 @@ extern "C" int pihm_gpu_noah_init(pihm_gpu_ctx *c, const pihm_noah_params *p, co
     cur += padded<int32_t>(NE);
   }
   int rc = PIHM_GPU_OK;
-  for (int k = 0; k < kParams && !rc; k++) rc = upload_scalar(c, params[k], P.s[k]);
+  for (int k = 0; k < kParams && !rc; k++) rc = upload_scalar(perm, ne, params[k], P.s[k], st);
   // layer depths below the surface (DefSldpth, noah/lsm_func.c:152-156)
   std::vector<double> zsoil((size_t)noah::L * ne, 0.0);
   for (int r = 0; r < ne; r++) {
@@ -347,86 +341,71 @@ extern "C" int pihm_gpu_noah_init(pihm_gpu_ctx *c, const pihm_noah_params *p, co
     z[0] = -sl[0];
     for (int k = 1; k < p->nsoil[r]; k++) z[k] = -sl[k] + z[k - 1];
   }
-  rc = rc ?: upload_layers(c, p->sldpth, P.l[NL_SLDPTH]);
-  rc = rc ?: upload_layers(c, zsoil.data(), P.l[NL_ZSOIL]);
-  rc = rc ?: upload_layers(c, p->rtdis, P.l[NL_RTDIS]);
-  rc = rc ?: upload_int(c, p->nsoil, P.i[NI_NSOIL]);
-  rc = rc ?: upload_int(c, p->nroot, P.i[NI_NROOT]);
-  if (p->isurban) rc = rc ?: upload_int(c, p->isurban, P.i[NI_ISURBAN]);
+  rc = rc ?: upload_layers(perm, ne, p->sldpth, P.l[NL_SLDPTH], st);
+  rc = rc ?: upload_layers(perm, ne, zsoil.data(), P.l[NL_ZSOIL], st);
+  rc = rc ?: upload_layers(perm, ne, p->rtdis, P.l[NL_RTDIS], st);
+  rc = rc ?: upload_int(perm, ne, p->nsoil, P.i[NI_NSOIL]);
+  rc = rc ?: upload_int(perm, ne, p->nroot, P.i[NI_NROOT]);
+  if (p->isurban) rc = rc ?: upload_int(perm, ne, p->isurban, P.i[NI_ISURBAN]);
   // the water-table layer before the first post-step: below the column
   std::vector<int32_t> nw((size_t)ne);
   for (int r = 0; r < ne; r++) nw[r] = p->nsoil[r];
-  rc = rc ?: upload_int(c, nw.data(), P.i[NI_NWTBL]);
-  if (rc) return rc;
-  // the right-hand side's Flux-PIHM input planes
-  if (!c->d_noah) {
-    const size_t nb = 3 * padded<double>(NE) + padded<int32_t>(NE);
-    if (cudaMalloc(&c->d_noah, nb) != cudaSuccess) {
-      c->d_noah = nullptr;
-      return PIHM_GPU_ERR_NOMEM;
-    }
-    char *q = (char *)c->d_noah;
-    c->m.noah_etgw = (double *)q; q += padded<double>(NE);
-    c->m.noah_satn = (double *)q; q += padded<double>(NE);
-    c->m.noah_fcr = (double *)q; q += padded<double>(NE);
-    c->m.noah_wtin = (int32_t *)q;
+  rc = rc ?: upload_int(perm, ne, nw.data(), P.i[NI_NWTBL]);
+  rc = rc ?: noah_set_state(n, s, perm, st);
+  if (rc) {
+    noah_release(n);
+    return rc;
   }
-  c->m.noah = 1;
-  c->diag = 1;  // MassBalance reads the last evaluation's fluxes
-  c->noah_first = 1;
-  return pihm_gpu_noah_set_state(c, s);
+  *out = n;
+  return PIHM_GPU_OK;
 }
 
-extern "C" int pihm_gpu_noah_set_forcing(pihm_gpu_ctx *c, const pihm_noah_forcing *f) {
-  if (!c || !c->noahlsm || !f || !f->prcp || !f->sfctmp || !f->rh || !f->sfcspd || !f->soldn || !f->longwave ||
+int noah_set_forcing(NoahInstance &n, const pihm_noah_forcing *f, const int32_t *perm, cudaStream_t st) {
+  if (!n.alloc || !f || !f->prcp || !f->sfctmp || !f->rh || !f->sfcspd || !f->soldn || !f->longwave ||
       !f->sfcprs || !f->lai)
     return PIHM_GPU_ERR_ARG;
-  NoahPlanes &P = *c->noahlsm;
+  NoahPlanes &P = *n.P;
   const double *src[] = {f->prcp, f->sfctmp, f->rh, f->sfcspd, f->soldn, f->longwave, f->sfcprs, f->lai};
   int rc = PIHM_GPU_OK;
-  for (int k = 0; k < 8 && !rc; k++) rc = upload_scalar(c, src[k], P.s[NS_PRCP + k]);
+  for (int k = 0; k < 8 && !rc; k++) rc = upload_scalar(perm, n.ne, src[k], P.s[NS_PRCP + k], st);
   return rc;
 }
 
-extern "C" int pihm_gpu_noah_step(pihm_gpu_ctx *c, double dt) {
-  if (!c || !c->noahlsm || !(dt > 0.0)) return PIHM_GPU_ERR_ARG;
-  const NoahPlanes &P = *c->noahlsm;
-  k_noah_step<<<(P.ne + kNoahBlock - 1) / kNoahBlock, kNoahBlock, 0, c->stream>>>(P, dt, c->m.err);
-  c->launches++;
-  return cuda_rc(cudaGetLastError()) ?: launch_inputs(c);
+int noah_launch_step(NoahInstance &n, double dt, unsigned int *err, cudaStream_t st, int64_t *launches) {
+  if (!n.alloc || !(dt > 0.0)) return PIHM_GPU_ERR_ARG;
+  k_noah_step<<<(n.ne + kNoahBlock - 1) / kNoahBlock, kNoahBlock, 0, st>>>(*n.P, dt, err);
+  ++*launches;
+  return cuda_rc(cudaGetLastError()) ?: launch_inputs(n, st, launches);
 }
 
-extern "C" int pihm_gpu_noah_begin(pihm_gpu_ctx *c, const double *y0_dev) {
-  if (!c || !c->noahlsm || !y0_dev) return PIHM_GPU_ERR_ARG;
-  const NoahPlanes &P = *c->noahlsm;
-  k_noah_begin<<<(P.ne + 255) / 256, 256, 0, c->stream>>>(P, y0_dev);
-  c->noah_first = 0;
-  c->launches++;
+int noah_launch_begin(NoahInstance &n, const double *y0, cudaStream_t st, int64_t *launches) {
+  if (!n.alloc || !y0) return PIHM_GPU_ERR_ARG;
+  k_noah_begin<<<(n.ne + 255) / 256, 256, 0, st>>>(*n.P, y0);
+  n.first = 0;
+  ++*launches;
   return cuda_rc(cudaGetLastError());
 }
 
-extern "C" int pihm_gpu_noah_post_step(pihm_gpu_ctx *c, const double *y_dev, double stepsize) {
-  if (!c || !c->noahlsm || !y_dev || !(stepsize > 0.0)) return PIHM_GPU_ERR_ARG;
-  const NoahPlanes &P = *c->noahlsm;
-  k_noah_post<<<(P.ne + kNoahBlock - 1) / kNoahBlock, kNoahBlock, 0, c->stream>>>(P, c->m, y_dev, stepsize,
-                                                                                  c->noah_first);
-  c->noah_first = 0;
-  c->launches++;
-  return cuda_rc(cudaGetLastError()) ?: launch_inputs(c);
+int noah_launch_post(NoahInstance &n, const double *y, double dt, cudaStream_t st, int64_t *launches) {
+  if (!n.alloc || !y || !(dt > 0.0)) return PIHM_GPU_ERR_ARG;
+  k_noah_post<<<(n.ne + kNoahBlock - 1) / kNoahBlock, kNoahBlock, 0, st>>>(*n.P, n.tg, y, dt, n.first);
+  n.first = 0;
+  ++*launches;
+  return cuda_rc(cudaGetLastError()) ?: launch_inputs(n, st, launches);
 }
 
-extern "C" int pihm_gpu_noah_get(pihm_gpu_ctx *c, int field, double *out) {
-  if (!c || !c->noahlsm || !out || field < 0 || field >= PIHM_NOAH_NFIELDS) return PIHM_GPU_ERR_ARG;
-  const NoahPlanes &P = *c->noahlsm;
-  const int ne = c->ne;
-  if (cudaStreamSynchronize(c->stream) != cudaSuccess) return PIHM_GPU_ERR_CUDA;
+int noah_get(NoahInstance &n, int field, const int32_t *perm, cudaStream_t st, double *out) {
+  if (!n.alloc || !out || field < 0 || field >= PIHM_NOAH_NFIELDS) return PIHM_GPU_ERR_ARG;
+  const NoahPlanes &P = *n.P;
+  const int ne = n.ne;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return PIHM_GPU_ERR_CUDA;
   static const int layer_of[] = {NL_SMC, NL_SH2O, NL_STC, NL_ET, NL_RUNOFF2_LYR, NL_SMFLXV};
   if (field < 6) {
     std::vector<double> h((size_t)noah::L * ne);
     if (cudaMemcpy(h.data(), P.l[layer_of[field]], sizeof(double) * h.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
       return PIHM_GPU_ERR_CUDA;
     for (int k = 0; k < noah::L; k++)
-      for (int i = 0; i < ne; i++) out[(size_t)noah::L * c->h_perm[i] + k] = h[(size_t)k * ne + i];
+      for (int i = 0; i < ne; i++) out[(size_t)noah::L * perm[i] + k] = h[(size_t)k * ne + i];
     return PIHM_GPU_OK;
   }
   static const int scalar_of[] = {NS_T1, NS_CMC, NS_SNEQV, NS_SNOWH, NS_SNDENS, NS_CH, NS_CM, NS_ALBEDO,
@@ -445,6 +424,83 @@ extern "C" int pihm_gpu_noah_get(pihm_gpu_ctx *c, int field, double *out) {
              cudaSuccess) {
     return PIHM_GPU_ERR_CUDA;
   }
-  for (int i = 0; i < ne; i++) out[c->h_perm[i]] = h[i];
+  for (int i = 0; i < ne; i++) out[perm[i]] = h[i];
   return PIHM_GPU_OK;
+}
+
+void noah_release(NoahInstance &n) {
+  if (n.alloc) cudaFree(n.alloc);
+  delete n.P;
+  n = NoahInstance();
+}
+
+}  // namespace pihm
+
+using namespace pihm;
+
+extern "C" int pihm_gpu_noah_set_state(pihm_gpu_ctx *c, const pihm_noah_state *s) {
+  if (!c || !c->noahlsm.alloc || !s) return PIHM_GPU_ERR_ARG;
+  return noah_set_state(c->noahlsm, s, c->h_perm, c->stream);
+}
+
+extern "C" int pihm_gpu_noah_init(pihm_gpu_ctx *c, const pihm_noah_params *p, const pihm_noah_state *s) {
+  if (!c || !p || !s || p->nelem != c->ne) return PIHM_GPU_ERR_ARG;
+  const size_t NE = c->ne;
+  // the right-hand side's Flux-PIHM input planes
+  if (!c->d_noah) {
+    const size_t nb = 3 * padded<double>(NE) + padded<int32_t>(NE);
+    if (cudaMalloc(&c->d_noah, nb) != cudaSuccess) {
+      c->d_noah = nullptr;
+      return PIHM_GPU_ERR_NOMEM;
+    }
+    char *q = (char *)c->d_noah;
+    c->m.noah_etgw = (double *)q; q += padded<double>(NE);
+    c->m.noah_satn = (double *)q; q += padded<double>(NE);
+    c->m.noah_fcr = (double *)q; q += padded<double>(NE);
+    c->m.noah_wtin = (int32_t *)q;
+  }
+  NoahTargets tg{c->m.d_sub, c->m.d_et, (int64_t)c->ne, const_cast<double *>(c->m.noah_etgw),
+                 const_cast<double *>(c->m.noah_satn), const_cast<double *>(c->m.noah_fcr),
+                 const_cast<double *>(c->m.edir), const_cast<double *>(c->m.ett), const_cast<double *>(c->m.pcpdrp),
+                 const_cast<int32_t *>(c->m.noah_wtin)};
+  noah_release(c->noahlsm);
+  const int rc = noah_build(p, s, c->h_perm, c->ne, tg, c->stream, &c->noahlsm);
+  if (rc != PIHM_GPU_OK) return rc;
+  c->m.noah = 1;
+  c->diag = 1;  // MassBalance reads the last evaluation's fluxes
+  return PIHM_GPU_OK;
+}
+
+extern "C" int pihm_gpu_noah_set_forcing(pihm_gpu_ctx *c, const pihm_noah_forcing *f) {
+  if (!c || !c->noahlsm.alloc) return PIHM_GPU_ERR_ARG;
+  return noah_set_forcing(c->noahlsm, f, c->h_perm, c->stream);
+}
+
+extern "C" int pihm_gpu_noah_step(pihm_gpu_ctx *c, double dt) {
+  if (!c || !c->noahlsm.alloc) return PIHM_GPU_ERR_ARG;
+  int64_t n = 0;
+  const int rc = noah_launch_step(c->noahlsm, dt, c->m.err, c->stream, &n);
+  c->launches += n;
+  return rc;
+}
+
+extern "C" int pihm_gpu_noah_begin(pihm_gpu_ctx *c, const double *y0_dev) {
+  if (!c || !c->noahlsm.alloc) return PIHM_GPU_ERR_ARG;
+  int64_t n = 0;
+  const int rc = noah_launch_begin(c->noahlsm, y0_dev, c->stream, &n);
+  c->launches += n;
+  return rc;
+}
+
+extern "C" int pihm_gpu_noah_post_step(pihm_gpu_ctx *c, const double *y_dev, double stepsize) {
+  if (!c || !c->noahlsm.alloc) return PIHM_GPU_ERR_ARG;
+  int64_t n = 0;
+  const int rc = noah_launch_post(c->noahlsm, y_dev, stepsize, c->stream, &n);
+  c->launches += n;
+  return rc;
+}
+
+extern "C" int pihm_gpu_noah_get(pihm_gpu_ctx *c, int field, double *out) {
+  if (!c || !c->noahlsm.alloc) return PIHM_GPU_ERR_ARG;
+  return noah_get(c->noahlsm, field, c->h_perm, c->stream, out);
 }

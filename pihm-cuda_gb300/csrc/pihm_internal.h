@@ -12,6 +12,7 @@
 
 #include "pihm_gpu.h"
 #include "pihm_land.h"
+#include "pihm_noah.h"
 
 namespace pihm {
 
@@ -193,6 +194,41 @@ int land_launch(LandInstance &li, int64_t t, double stepsize, const double *y_de
                 int64_t *launches);
 void land_release(LandInstance &li);
 
+// Where a Noah instance (noah.cu) reads the right-hand side's diagnostics of
+// the last evaluation and writes the right-hand side's Flux-PIHM inputs: one
+// watershed's elements, from its first element, with the planes' stride
+// (a context's own planes, or a range of the batch arena).
+struct NoahTargets {
+  const double *d_sub, *d_et;  // [3][stride], [5][stride]
+  int64_t stride;
+  double *etgw, *satn, *fcr, *edir, *ett, *pcpdrp;
+  int32_t *wtin;
+};
+struct NoahPlanes;
+// A Noah instance: its own allocation (parameters, forcing, state, outputs
+// in internal element order), the device view, and whether no model step has
+// ended yet (the first post-step takes the previous state from y).
+struct NoahInstance {
+  void *alloc = nullptr;
+  NoahPlanes *P = nullptr;
+  NoahTargets tg{};
+  int ne = 0;
+  int first = 1;
+};
+// pihm_gpu_noah_init's work for any targets (perm[internal] = reference element)
+int noah_build(const pihm_noah_params *p, const pihm_noah_state *s, const int32_t *perm, int ne,
+               const NoahTargets &tg, cudaStream_t st, NoahInstance *out);
+int noah_set_state(NoahInstance &n, const pihm_noah_state *s, const int32_t *perm, cudaStream_t st);
+int noah_set_forcing(NoahInstance &n, const pihm_noah_forcing *f, const int32_t *perm, cudaStream_t st);
+// Noah() over dt, then the right-hand side's inputs
+int noah_launch_step(NoahInstance &n, double dt, unsigned int *err, cudaStream_t st, int64_t *launches);
+// the state a run starts from (ws0 of MassBalance)
+int noah_launch_begin(NoahInstance &n, const double *y0, cudaStream_t st, int64_t *launches);
+// Summary's _NOAH_ part and NoahHydrol after a model step ending at y, then the inputs
+int noah_launch_post(NoahInstance &n, const double *y, double dt, cudaStream_t st, int64_t *launches);
+int noah_get(NoahInstance &n, int field, const int32_t *perm, cudaStream_t st, double *out);
+void noah_release(NoahInstance &n);
+
 // Optional per-kernel CUDA-event timing of the right-hand-side launches.
 struct Profiler {
   static constexpr int kKernels = 8;
@@ -234,10 +270,6 @@ cudaError_t launch_rhs(const DevMesh &m, const double *y, double *ydot, cudaStre
                        long long *launches, Profiler *prof, const RhsStreams *side = nullptr,
                        const double *y_ref = nullptr, const int32_t *iperm = nullptr);
 
-// Noah land-surface model planes (noah.cu, include/pihm_noah.h)
-struct NoahPlanes;
-void noah_free(pihm_gpu_ctx *c);
-
 }  // namespace pihm
 
 struct pihm_gpu_ctx {
@@ -264,7 +296,5 @@ struct pihm_gpu_ctx {
   void *d_noah;            // Flux-PIHM input planes, allocated on first use
   pihm::LandInstance land;  // land-surface model (pihm_gpu_land_init); alloc null when absent
   pihm::RhsStreams side;   // river kernel beside the element kernels
-  void *d_noahlsm;              // Noah land-surface model (pihm_gpu_noah_init), or null
-  pihm::NoahPlanes *noahlsm;    // its planes
-  int noah_first;               // no model step has ended since pihm_gpu_noah_init
+  pihm::NoahInstance noahlsm;   // Noah land-surface model (pihm_gpu_noah_init); alloc null when absent
 };
