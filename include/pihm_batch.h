@@ -30,6 +30,7 @@
 #include "pihm_bdf.h"
 #include "pihm_gpu.h"
 #include "pihm_land.h"
+#include "pihm_noah.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -82,6 +83,19 @@ typedef struct pihm_batch_job {
     const pihm_forcing_series *forcing;
     const double *cmc0, *sneqv0;
     int64_t start, lsm_step;
+    /* Flux-PIHM: Noah on the device (include/pihm_noah.h) instead of the
+     * uniform series, as the reference's _NOAH_ build runs it
+     * (src/pihm.c:21-123): the watershed's Noah parameters and initial
+     * state, and noah_nforcing forcing sets, the k-th for the land-surface
+     * step from model time k noah_lsm_step (Noah() runs over noah_lsm_step
+     * seconds), and after every model step Summary's _NOAH_ part and
+     * NoahHydrol.  Not with .land.  The pointers must stay valid until the
+     * watershed is released. */
+    const pihm_noah_params *noah;
+    const pihm_noah_state *noah_state;
+    const pihm_noah_forcing *noah_forcing;
+    int32_t noah_nforcing;
+    double noah_lsm_step;
 } pihm_batch_job;
 
 enum { PIHM_BATCH_RUNNING = 0, PIHM_BATCH_DONE = 1, PIHM_BATCH_FAILED = 2 };

@@ -95,13 +95,14 @@ Task<int> model_run(Sys *s) {
   for (int k = 0; k < s->nsteps; k++) {
     // the step's forcing: the uniform series, or the deck's boundary values
     // and land-surface step, which the round that runs this program applies
-    if (!s->land.alloc) co_await o.forcing(s->pcp[k], s->edir[k], s->ett[k]);
-    if (s->has_bc || s->land.alloc) s->pending_k = k;
+    if (!s->land.alloc && !s->noah.alloc) co_await o.forcing(s->pcp[k], s->edir[k], s->ett[k]);
+    if (s->has_bc || s->land.alloc || s->noah.alloc) s->pending_k = k;
     const double tout = (double)(k + 1) * ct.stepsize;
     if ((rc = c.set_stop_time(tout)) != bdf::SUCCESS) co_return rc;
     rc = co_await c.solve(tout, Y, &tret);
     if (rc < 0) co_return rc;
     co_await o.post_step(Y);
+    if (s->noah.alloc) s->pending_post = true;  // Summary's _NOAH_ part and NoahHydrol
     // AdjCVodeMaxStep, src/ode.c:601-661
     const double nsteps_d = (double)(c.nst - nst0);
     const double nfails = (double)(c.ncfn - ncfn0) / nsteps_d;
@@ -291,6 +292,11 @@ namespace batch {
 
 void free_ranges(pihm_batch *B, Sys *s) {
   DevMesh &m = B->A.m;
+  if (s->noah.alloc) {
+    cudaMemsetAsync(const_cast<int32_t *>(m.sys_noah) + s->slot, 0, sizeof(int32_t), B->st);
+    if (--B->noah_resident == 0) m.noah = m.diag = 0;
+    noah_release(s->noah);
+  }
   // mark the items free so the masked kernels skip them whatever the slot's next owner
   if (s->ne) cudaMemsetAsync((int32_t *)m.sys_elem + s->eoff, 0xff, sizeof(int32_t) * s->ne, B->st);
   if (s->nr) cudaMemsetAsync((int32_t *)m.sys_riv + s->roff, 0xff, sizeof(int32_t) * s->nr, B->st);
@@ -321,10 +327,13 @@ void resume(Sys *s) {
 
 // Validate a job and build everything the arena needs from it on the host.
 int prepare(const pihm_batch_job *job, int surf_mode, int riv_mode, int order, Prepared *p) {
-  if (!job || !job->mesh || !job->y0 || !p || job->nsteps < 0 ||
-      (job->nsteps > 0 && !job->land && (!job->pcpdrp || !job->edir || !job->ett)))
-    return PIHM_GPU_ERR_ARG;
+  if (!job || !job->mesh || !job->y0 || !p || job->nsteps < 0) return PIHM_GPU_ERR_ARG;
   if (job->land && (!job->forcing || job->lsm_step <= 0 || job->land->nelem != job->mesh->nelem))
+    return PIHM_GPU_ERR_ARG;
+  if (job->noah && (job->land || !job->noah_state || !job->noah_forcing || job->noah_nforcing < 1 ||
+                    !(job->noah_lsm_step > 0.0) || job->noah->nelem != job->mesh->nelem))
+    return PIHM_GPU_ERR_ARG;
+  if (job->nsteps > 0 && !job->land && !job->noah && (!job->pcpdrp || !job->edir || !job->ett))
     return PIHM_GPU_ERR_ARG;
   const pihm_step_control &c = job->ctrl;
   if (!(c.stepsize > 0.0) || c.reltol < 0 || c.abstol < 0 || !(c.decr > 0.0)) return PIHM_GPU_ERR_ARG;
@@ -336,7 +345,7 @@ int prepare(const pihm_batch_job *job, int surf_mode, int riv_mode, int order, P
   p->y0.assign(job->y0, job->y0 + neq);
   if (job->elem_bc) p->elem_bc.assign(job->elem_bc, job->elem_bc + 3 * (size_t)ne);
   if (job->river_bc) p->river_bc.assign(job->river_bc, job->river_bc + nr);
-  if (!job->land) {
+  if (!job->land && !job->noah) {
     p->pcp.assign(job->pcpdrp, job->pcpdrp + job->nsteps);
     p->edir.assign(job->edir, job->edir + job->nsteps);
     p->ett.assign(job->ett, job->ett + job->nsteps);
@@ -354,6 +363,16 @@ int prepare(const pihm_batch_job *job, int surf_mode, int riv_mode, int order, P
   p->forcing = job->forcing;
   p->start = job->start;
   p->lsm_step = job->lsm_step;
+  p->noah = job->noah;
+  p->noah_state = job->noah_state;
+  p->noah_forcing = job->noah_forcing;
+  p->noah_nforcing = job->noah_nforcing;
+  p->noah_lsm = job->noah_lsm_step;
+  if (job->noah) {
+    // every land-surface step of the run must have its forcing set
+    const double t_last = (double)(job->nsteps > 0 ? job->nsteps - 1 : 0) * c.stepsize;
+    if ((int64_t)(t_last / job->noah_lsm_step) >= job->noah_nforcing) return PIHM_GPU_ERR_ARG;
+  }
   if (job->land) {
     p->cmc0.assign(ne, 0.0);
     p->sneqv0.assign(ne, 0.0);
@@ -374,6 +393,30 @@ int attach_deck(pihm_batch *B, Sys *s, const Prepared &p) {
   if (s->has_bc && cudaMallocHost(&s->bc_stage, sizeof(double) * (3 * (size_t)s->ne + s->nr)) != cudaSuccess) {
     s->bc_stage = nullptr;
     return PIHM_GPU_ERR_NOMEM;
+  }
+  if (p.noah) {
+    DevMesh &m = B->A.m;
+    const int64_t eo = s->eoff, NE = B->ne_cap;
+    NoahTargets tg{m.d_sub + eo, m.d_et + eo, NE, const_cast<double *>(m.noah_etgw) + eo,
+                   const_cast<double *>(m.noah_satn) + eo, const_cast<double *>(m.noah_fcr) + eo,
+                   const_cast<double *>(m.edir) + eo, const_cast<double *>(m.ett) + eo,
+                   const_cast<double *>(m.pcpdrp) + eo, const_cast<int32_t *>(m.noah_wtin) + eo};
+    int rc = noah_build(p.noah, p.noah_state, p.im.perm.data(), s->ne, tg, B->st, &s->noah);
+    if (rc != PIHM_GPU_OK) return rc;
+    B->noah_resident++;  // free_ranges counts it back with the instance
+    int64_t n = 0;
+    rc = noah_launch_begin(s->noah, B->A.vec + s->soff, B->st, &n);  // ws0 of the first MassBalance
+    if (rc != PIHM_GPU_OK) return rc;
+    s->noah_forcing = p.noah_forcing;
+    s->noah_nforcing = p.noah_nforcing;
+    s->noah_lsm = p.noah_lsm;
+    const int32_t one = 1;
+    if (cudaMemcpyAsync(const_cast<int32_t *>(m.sys_noah) + s->slot, &one, sizeof(one), cudaMemcpyHostToDevice,
+                        B->st) != cudaSuccess ||
+        cudaStreamSynchronize(B->st) != cudaSuccess)
+      return PIHM_GPU_ERR_CUDA;
+    m.noah = 1;
+    m.diag = 1;  // MassBalance reads each watershed's last evaluation's fluxes
   }
   if (!p.land) return PIHM_GPU_OK;
   DevMesh &m = B->A.m;
@@ -520,7 +563,7 @@ int run_round(pihm_batch *B, bool *any) {
     r.ry = s->ry;
     r.pad0 = r.pad1 = 0;
     r.bstart = nblocks;
-    if (s->pending_k >= 0) forcing.push_back(s);
+    if (s->pending_k >= 0 || s->pending_post) forcing.push_back(s);
     std::memcpy(ops + nops, s->prog.data(), sizeof(Op) * s->prog.size());
     nops += (int)s->prog.size();
     nblocks += (int)pihm_nv::red_grid_for(s->neq);
@@ -556,22 +599,40 @@ int run_round(pihm_batch *B, bool *any) {
   B->launches++;
   if (B->profiling) cudaEventRecord(B->ev[1], st);
   if (tune) cudaEventRecord(B->tev[1], st);
-  // the land-surface step (src/pihm.c:30-66) after the program, which ends
-  // the previous model step's state in vector slot 0, and before the
-  // evaluation that starts the step
+  if (rhs && cudaMemsetAsync(B->err_sys, 0, sizeof(unsigned int) * B->max_sys, st) != cudaSuccess) return -1;
+  // after the program, which ends the previous model step's state in vector
+  // slot 0, and before the evaluation that starts the next step: Flux-PIHM's
+  // post-step (Summary's _NOAH_ part and NoahHydrol, src/update.c:34-41,
+  // src/noah/noah.c:57-160), then the land-surface step (src/pihm.c:30-66) or
+  // Noah() (src/pihm.c:50-58); a Noah error word joins the watershed's
+  // evaluation status
   for (Sys *s : forcing) {
-    const int64_t t = s->start + (int64_t)s->pending_k * (int64_t)s->ctrl.stepsize;
-    if (s->land.alloc && (t - s->start) % s->lsm_step == 0) {
-      int64_t n = 0;
-      if (land_launch(s->land, t, (double)s->lsm_step, B->A.vec + s->soff, st, &n) != PIHM_GPU_OK) return -1;
-      B->launches += n;
+    int64_t n = 0;
+    if (s->pending_post) {
+      if (noah_launch_post(s->noah, B->A.vec + s->soff, s->ctrl.stepsize, st, &n) != PIHM_GPU_OK) return -1;
+      s->pending_post = false;
     }
-    s->pending_k = -1;
+    if (s->pending_k >= 0) {
+      const int64_t t = s->start + (int64_t)s->pending_k * (int64_t)s->ctrl.stepsize;
+      if (s->land.alloc && (t - s->start) % s->lsm_step == 0 &&
+          land_launch(s->land, t, (double)s->lsm_step, B->A.vec + s->soff, st, &n) != PIHM_GPU_OK)
+        return -1;
+      if (s->noah.alloc) {
+        const double tm = (double)s->pending_k * s->ctrl.stepsize;
+        const double q = tm / s->noah_lsm;
+        if (q == std::floor(q)) {
+          if (noah_set_forcing(s->noah, s->noah_forcing + (int64_t)q, s->perm.data(), st) != PIHM_GPU_OK ||
+              noah_launch_step(s->noah, s->noah_lsm, B->err_sys + s->slot, st, &n) != PIHM_GPU_OK)
+            return -1;
+        }
+      }
+      s->pending_k = -1;
+    }
+    B->launches += n;
   }
   const bool stune = rhs && B->shape_forced < 0 && B->shape_tuning && el_req >= pihm_batch::kShapeMinElems;
   const int shape = B->shape_forced >= 0 ? B->shape_forced : (stune ? B->shape_next : B->shape_best);
   if (rhs) {
-    if (cudaMemsetAsync(B->err_sys, 0, sizeof(unsigned int) * B->max_sys, st) != cudaSuccess) return -1;
     B->A.m.main_shape = shape;
     if (stune) cudaEventRecord(B->sev[0], st);
     if (launch_rhs(B->A.m, B->A.rhs_in, B->A.rhs_out, st, &B->launches, nullptr, &B->side) != cudaSuccess)
@@ -786,6 +847,19 @@ int pihm_batch_create(const pihm_batch_limits *lim, int surf_mode, int riv_mode,
   m.sys_bank = sb;
   m.sys_dt = D(MS);
   m.sys_inv_dt = D(MS);
+  // Flux-PIHM watersheds: the right-hand side's Noah inputs, its diagnostics
+  // (MassBalance reads the last evaluation's fluxes) and the per-watershed flag
+  m.noah_etgw = D(NE);
+  m.noah_satn = D(NE);
+  m.noah_fcr = D(NE);
+  m.noah_wtin = I(NE);
+  m.d_ovl = D(3 * NE);
+  m.d_sub = D(3 * NE);
+  m.d_infil = D(NE);
+  m.d_rechg = D(NE);
+  m.d_et = D(5 * NE);
+  int32_t *snoah = I(MS);
+  m.sys_noah = snoah;
   DeviceArena &A = B->A;
   A.vec = D((size_t)kVecSlots * NEQ);
   A.neq_cap = NEQ;
@@ -822,6 +896,7 @@ int pihm_batch_create(const pihm_batch_limits *lim, int surf_mode, int riv_mode,
            cudaMemset(sed, 0xff, sizeof(int32_t) * NED) == cudaSuccess &&
            cudaMemset(sb, 0xff, sizeof(int32_t) * NE) == cudaSuccess &&
            cudaMemset(A.tickets, 0, sizeof(unsigned int) * MS) == cudaSuccess &&
+           cudaMemset(snoah, 0, sizeof(int32_t) * MS) == cudaSuccess &&
            cudaMemset(B->d_up, 0, up_bytes) == cudaSuccess &&
            cudaMemset(m.rivflow, 0, sizeof(double) * NUM_RIVFLX * NR) == cudaSuccess &&
            cudaMemset(m.carry_ovl, 0, sizeof(double) * 2 * NR) == cudaSuccess &&

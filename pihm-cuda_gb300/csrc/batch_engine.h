@@ -159,11 +159,18 @@ struct Sys {
   int64_t start = 0, lsm_step = 0;
   int32_t pending_k = -1;           // model step whose forcing the next round applies
   double *bc_stage = nullptr;       // pinned [3 ne + nr], internal order
+  // Flux-PIHM (pihm_batch_job.noah)
+  NoahInstance noah;                // alloc null when absent
+  const pihm_noah_forcing *noah_forcing = nullptr;
+  int32_t noah_nforcing = 0;
+  double noah_lsm = 0.0;
+  bool pending_post = false;        // Summary's _NOAH_ part and NoahHydrol after the step just ended
 
   Sys() = default;
   Sys(const Sys &) = delete;
   ~Sys() {
     land_release(land);
+    noah_release(noah);
     if (bc_stage) cudaFreeHost(bc_stage);
   }
 };
@@ -181,6 +188,11 @@ struct Prepared {
   const pihm_forcing_series *forcing = nullptr;
   std::vector<double> cmc0, sneqv0;
   int64_t start = 0, lsm_step = 0;
+  const pihm_noah_params *noah = nullptr;
+  const pihm_noah_state *noah_state = nullptr;
+  const pihm_noah_forcing *noah_forcing = nullptr;
+  int32_t noah_nforcing = 0;
+  double noah_lsm = 0.0;
 };
 
 }  // namespace batch
@@ -233,6 +245,7 @@ struct pihm_batch {
   double shape_ms_per_elem[kShapes] = {0};
   int shape_n[kShapes] = {0};
   cudaEvent_t sev[2] = {nullptr, nullptr};
+  int noah_resident = 0;  // Flux-PIHM watersheds resident (the arena's noah and diagnostics switch on)
   pihm::RhsStreams side;  // river kernel beside the element kernels
   int host_pageable = 0;  // the device can access pageable host memory (uploads by one gather kernel)
   // counters and timing (host: building rounds and running the coroutines;

@@ -122,6 +122,9 @@ struct DevMesh {
   const uint8_t *active;
   const double *sys_dt, *sys_inv_dt;
   unsigned int *err_sys;
+  // Batch engine: 1 for the watersheds that run Flux-PIHM (noah then marks
+  // that some do); null otherwise
+  const int32_t *sys_noah;
 
   // Flux-PIHM (_NOAH_) right-hand side, when noah != 0: per element, from
   // Noah's per-step outputs, the transpiration of the layers from the water

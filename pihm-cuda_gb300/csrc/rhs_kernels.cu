@@ -399,7 +399,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_elem_main(DevMesh m, const doub
   const double edir = m.edir[i], ett = m.ett[i];
   double edir_surf = 0.0, edir_unsat = 0.0, edir_gw = 0.0, ett_unsat = 0.0, ett_gw = 0.0;
   const bool gw_in_dinf = cmp::gt_v(gw, d_dinf);
-  if (m.noah) {
+  const bool noah = m.noah && (!m.sys_noah || m.sys_noah[sy]);
+  if (noah) {
     // Flux-PIHM (src/hydrol.c:43-55,79-83): no ponded-water source, and the
     // transpiration split by GwTransp (noah/lsm_func.c:163-185) over the
     // Noah layers from the water table down to the root depth
@@ -440,7 +441,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_elem_main(DevMesh m, const doub
   // Noah's top-layer moisture (src/vert_flow.c:94-98) and Recharge keeps
   // the column's
   double satn_i = satn, satkfunc_i = satkfunc, psi_i = psi_u, sq_i = sq;
-  if (m.noah && !gw_in_dinf) {
+  if (noah && !gw_in_dinf) {
     double s = m.noah_satn[i];
     s = cmp::gt_c(s, 1.0) ? 1.0 : s;
     s = cmp::lt_c(s, kSatMin) ? kSatMin : s;
@@ -497,7 +498,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_elem_main(DevMesh m, const doub
     infil = cmp::gt_v(infil, infil_max) ? infil_max : infil;
     infil *= wetfrac;
   }
-  if (m.noah) infil *= m.noah_fcr[i];  // frozen top soil, src/vert_flow.c:16-19
+  if (noah) infil *= m.noah_fcr[i];  // frozen top soil, src/vert_flow.c:16-19
   double rechg;
   if (gw_in_dinf) {
     rechg = infil;

@@ -187,7 +187,8 @@ extern "C" {
 
 int pihm_serve_submit(pihm_batch *B, const pihm_batch_job *job, double arrival_s, int32_t *ticket) {
   if (!B || !job || !job->mesh || !job->y0 || !ticket || job->nsteps < 0 ||
-      (job->nsteps > 0 && !job->land && (!job->pcpdrp || !job->edir || !job->ett)) || !(arrival_s >= 0.0))
+      (job->nsteps > 0 && !job->land && !job->noah && (!job->pcpdrp || !job->edir || !job->ett)) ||
+      !(arrival_s >= 0.0))
     return PIHM_GPU_ERR_ARG;
   pihm_serve_state *S = serve_state(B);
   auto r = std::make_unique<Request>();

@@ -43,7 +43,9 @@ class BatchJob(ctypes.Structure):
                 ("y0", _F64P), ("ctrl", StepControlC), ("nsteps", _I32), ("pcpdrp", _F64P),
                 ("edir", _F64P), ("ett", _F64P), ("outlet", _I32),
                 ("deck", _VP), ("land", _VP), ("forcing", _VP), ("cmc0", _F64P), ("sneqv0", _F64P),
-                ("start", _I64), ("lsm_step", _I64)]
+                ("start", _I64), ("lsm_step", _I64),
+                ("noah", _VP), ("noah_state", _VP), ("noah_forcing", _VP), ("noah_nforcing", _I32),
+                ("noah_lsm_step", _D)]
 
 
 class BatchInfo(ctypes.Structure):
@@ -103,6 +105,33 @@ def _deck_job(deck, nsteps: int | None, outlet: int):
     job.cmc0, job.sneqv0 = f64p(keep["cmc"]), f64p(keep["sneqv"])
     job.start = start
     job.lsm_step = int(ctrl.lsm_step)
+    return job, keep
+
+
+def _noah_job(ws, y0, ctrl, params: dict, state: dict, forcings, lsm_step: float, nsteps: int, outlet: int):
+    """A BatchJob running Flux-PIHM with Noah on the device: params, state
+    (pihm_gpu.noah.synthetic_noah's dicts, reference order) and one forcing
+    dict (pihm_gpu.noah.forcing) per land-surface step of lsm_step seconds;
+    and what it points at (keep both alive while the watershed runs)."""
+    from . import noah as N
+    zero = np.zeros(0)
+    job, keep = _job(ws, y0, ctrl, zero, zero, zero, outlet, None, None)
+    ps, kp = N.params_struct(params)
+    ss, ks = N.state_struct(state)
+    fs = (N.NoahForcing * len(forcings))()
+    kf = []
+    for k, f in enumerate(forcings):
+        one, keep_one = N.forcing_struct(f)
+        fs[k] = one
+        kf.append(keep_one)
+    keep.update(noah=(ps, kp, ss, ks, fs, kf), ws=ws)
+    job.nsteps = int(nsteps)
+    job.pcpdrp = job.edir = job.ett = None
+    job.noah = ctypes.cast(ctypes.pointer(ps), _VP)
+    job.noah_state = ctypes.cast(ctypes.pointer(ss), _VP)
+    job.noah_forcing = ctypes.cast(fs, _VP)
+    job.noah_nforcing = len(forcings)
+    job.noah_lsm_step = float(lsm_step)
     return job, keep
 
 
@@ -219,6 +248,20 @@ class Batch:
         self.keep[i.value] = keep
         return i.value
 
+    def add_noah(self, ws, y0, ctrl: StepControl, params: dict, state: dict, forcings, lsm_step: float,
+                 nsteps: int, outlet: int = -1) -> int | None:
+        """Admit a Flux-PIHM watershed with Noah on the device (see _noah_job);
+        None when the arena has no room for it now."""
+        job, keep = _noah_job(ws, y0, ctrl, params, state, forcings, lsm_step, nsteps, outlet)
+        i = _I32()
+        rc = self.lib.pihm_batch_add(self.h, ctypes.byref(job), ctypes.byref(i))
+        if rc == -5:
+            return None
+        capi._check("pihm_batch_add", rc)
+        self.jobs[i.value] = (ws, job.nsteps, outlet)
+        self.keep[i.value] = keep
+        return i.value
+
     def add_many(self, cases, threads: int = 16):
         """Admit many cases (dicts with ws, y0, ctrl, pcp, edir, ett, outlet),
         prepared in parallel on host threads; returns their ids (None where a
@@ -307,6 +350,18 @@ class Batch:
         capi._check("pihm_serve_submit", self.lib.pihm_serve_submit(self.h, ctypes.byref(job), float(arrival),
                                                                      ctypes.byref(t)))
         self.requests[t.value] = (keep["ws"], job.nsteps, outlet)
+        self.keep[("serve", t.value)] = keep
+        return t.value
+
+    def submit_noah(self, ws, y0, ctrl: StepControl, params: dict, state: dict, forcings, lsm_step: float,
+                    nsteps: int, arrival: float, outlet: int = -1) -> int:
+        """Queue a Flux-PIHM request (see _noah_job) arriving `arrival` seconds
+        after serve() starts."""
+        job, keep = _noah_job(ws, y0, ctrl, params, state, forcings, lsm_step, nsteps, outlet)
+        t = _I32()
+        capi._check("pihm_serve_submit", self.lib.pihm_serve_submit(self.h, ctypes.byref(job), float(arrival),
+                                                                     ctypes.byref(t)))
+        self.requests[t.value] = (ws, job.nsteps, outlet)
         self.keep[("serve", t.value)] = keep
         return t.value
 
