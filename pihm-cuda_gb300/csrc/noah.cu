@@ -55,6 +55,8 @@ struct NoahPlanes {
   double *s[NS_COUNT];
   double *l[NL_COUNT];
   int32_t *i[NI_COUNT];
+  int32_t *order;   // [ne] elements grouped by the branches Noah() will take (k_noah_classify)
+  int32_t *cls;     // [2 * kNoahClasses] class sizes, then cursors
   int ne;
 };
 
@@ -142,10 +144,55 @@ __device__ void store_col(const NoahPlanes &P, int i, const Col &c) {
 }
 
 constexpr int kNoahBlock = 128;
+constexpr int kNoahClasses = 8;
 
-__global__ void __launch_bounds__(kNoahBlock) k_noah_step(NoahPlanes P, double dt, unsigned int *err) {
+// The branch class of an element's next Noah() step: whether it will run the
+// snowpack path (snow on the ground, or precipitation that may fall as snow
+// or freezing rain), whether a soil layer or the skin is frozen (the
+// iterative frozen-water solution of FrH2O), whether it has vegetation (the
+// canopy resistance and transpiration).  Noah() is one thread per element and
+// GB300 retires 2 FP64 lanes per clock per SM, so a warp whose lanes take
+// different paths runs each path for all of them; grouping elements by class
+// keeps warps on one path.  Only the order of work changes: every element's
+// arithmetic, and so every result, is the same.
+__device__ __forceinline__ int noah_class(const NoahPlanes &P, int i) {
+  const double tf = 273.15;
+  const bool snow = P.s[NS_SNEQV][i] > 0.0 || (P.s[NS_PRCP][i] > 0.0 && P.s[NS_SFCTMP][i] <= tf + 1.0);
+  bool frozen = P.s[NS_T1][i] < tf;
+  const int nsoil = P.i[NI_NSOIL][i];
+  for (int k = 0; k < nsoil; k++) frozen = frozen || P.l[NL_STC][k * P.ne + i] < tf;
+  const bool veg = P.s[NS_SHDFAC][i] > 0.0;
+  return (snow ? 4 : 0) + (frozen ? 2 : 0) + (veg ? 1 : 0);
+}
+
+// class sizes (cls[0..7]; the caller zeroed cls)
+__global__ void __launch_bounds__(256) k_noah_count(NoahPlanes P) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.ne) return;
+  atomicAdd(&P.cls[noah_class(P, i)], 1);
+}
+
+// each element's place: its class's start (the sizes summed in class order)
+// plus a cursor; lanes of a warp in one class take consecutive places
+__global__ void __launch_bounds__(256) k_noah_place(NoahPlanes P) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool in = i < P.ne;
+  const int c = in ? noah_class(P, i) : kNoahClasses;
+  const unsigned mask = __match_any_sync(0xffffffffu, c);
+  if (!in) return;
+  const int lead = __ffs(mask) - 1, lane = threadIdx.x & 31;
+  int base = 0;
+  if (lane == lead) base = atomicAdd(&P.cls[kNoahClasses + c], __popc(mask));
+  base = __shfl_sync(mask, base, lead);
+  int start = 0;
+  for (int k = 0; k < c; k++) start += P.cls[k];
+  P.order[start + base + __popc(mask & ((1u << lane) - 1u))] = i;
+}
+
+__global__ void __launch_bounds__(kNoahBlock) k_noah_step(NoahPlanes P, double dt, unsigned int *err) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= P.ne) return;
+  const int i = P.order[t];
   Col c;
   load_col(P, i, c);
   noah::noah_step(c, dt);
@@ -305,7 +352,7 @@ int noah_build(const pihm_noah_params *p, const pihm_noah_state *s, const int32_
     return PIHM_GPU_ERR_ARG;
   const size_t NE = ne;
   const size_t bytes = NS_COUNT * padded<double>(NE) + NL_COUNT * padded<double>(noah::L * NE) +
-                       NI_COUNT * padded<int32_t>(NE);
+                       NI_COUNT * padded<int32_t>(NE) + padded<int32_t>(NE) + padded<int32_t>(2 * kNoahClasses);
   NoahInstance n;
   if (cudaMalloc(&n.alloc, bytes) != cudaSuccess) return PIHM_GPU_ERR_NOMEM;
   n.P = new NoahPlanes();
@@ -331,6 +378,9 @@ int noah_build(const pihm_noah_params *p, const pihm_noah_state *s, const int32_
     P.i[k] = (int32_t *)cur;
     cur += padded<int32_t>(NE);
   }
+  P.order = (int32_t *)cur;
+  cur += padded<int32_t>(NE);
+  P.cls = (int32_t *)cur;
   int rc = PIHM_GPU_OK;
   for (int k = 0; k < kParams && !rc; k++) rc = upload_scalar(perm, ne, params[k], P.s[k], st);
   // layer depths below the surface (DefSldpth, noah/lsm_func.c:152-156)
@@ -373,8 +423,12 @@ int noah_set_forcing(NoahInstance &n, const pihm_noah_forcing *f, const int32_t 
 
 int noah_launch_step(NoahInstance &n, double dt, unsigned int *err, cudaStream_t st, int64_t *launches) {
   if (!n.alloc || !(dt > 0.0)) return PIHM_GPU_ERR_ARG;
+  if (n.ne == 0) return PIHM_GPU_OK;
+  if (cudaMemsetAsync(n.P->cls, 0, sizeof(int32_t) * 2 * kNoahClasses, st) != cudaSuccess) return PIHM_GPU_ERR_CUDA;
+  k_noah_count<<<(n.ne + 255) / 256, 256, 0, st>>>(*n.P);
+  k_noah_place<<<(n.ne + 255) / 256, 256, 0, st>>>(*n.P);
   k_noah_step<<<(n.ne + kNoahBlock - 1) / kNoahBlock, kNoahBlock, 0, st>>>(*n.P, dt, err);
-  ++*launches;
+  *launches += 3;
   return cuda_rc(cudaGetLastError()) ?: launch_inputs(n, st, launches);
 }
 

@@ -190,11 +190,18 @@ def _main(argv=None):
     ap.add_argument("--model-steps", type=int, default=2)
     ap.add_argument("--deferred-scalars", type=int, default=-1, choices=[-1, 0, 1])
     ap.add_argument("--op-timing", action="store_true", help="host time inside the integrator's operations")
+    ap.add_argument("--noah", type=int, default=0, metavar="LAYERS",
+                    help="Flux-PIHM with Noah on the device, this many soil layers (hourly synthetic forcing)")
     a = ap.parse_args(argv)
     ws = W.generate(a.nelem, a.nriver or WL.river_count(a.nelem), seed=a.seed)
-    pcp, edir, ett = WL.step_forcing(ws, a.model_steps, 60.0, seed=8)
-    m = GpuWatershed(ws, W.relax_state(ws), pcp, edir, ett)
-    m.g.set_diagnostics(False)
+    if a.noah:
+        from . import noah as N
+        params, state = N.synthetic_noah(ws, seed=a.seed + 1, nlayers=a.noah)
+        m = NoahWatershed(ws, W.relax_state(ws), params, state, lambda h: N.forcing(ws, h, seed=a.seed + 2))
+    else:
+        pcp, edir, ett = WL.step_forcing(ws, a.model_steps, 60.0, seed=8)
+        m = GpuWatershed(ws, W.relax_state(ws), pcp, edir, ett)
+        m.g.set_diagnostics(False)
     try:
         t = time.perf_counter()
         r = run_steps(m, StepControl(), a.model_steps, m.set_forcing, deferred_scalars=a.deferred_scalars,
