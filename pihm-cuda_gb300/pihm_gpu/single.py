@@ -192,6 +192,9 @@ def _main(argv=None):
     ap.add_argument("--op-timing", action="store_true", help="host time inside the integrator's operations")
     ap.add_argument("--noah", type=int, default=0, metavar="LAYERS",
                     help="Flux-PIHM with Noah on the device, this many soil layers (hourly synthetic forcing)")
+    ap.add_argument("--mxstep", type=int, default=0, help="internal steps per model step (0: 10 x stepsize)")
+    ap.add_argument("--progress", type=int, default=0, metavar="K",
+                    help="print the wall time to stderr every K model steps")
     a = ap.parse_args(argv)
     ws = W.generate(a.nelem, a.nriver or WL.river_count(a.nelem), seed=a.seed)
     if a.noah:
@@ -203,8 +206,15 @@ def _main(argv=None):
         m = GpuWatershed(ws, W.relax_state(ws), pcp, edir, ett)
         m.g.set_diagnostics(False)
     try:
+        import sys
         t = time.perf_counter()
-        r = run_steps(m, StepControl(), a.model_steps, m.set_forcing, deferred_scalars=a.deferred_scalars,
+        forcing = m.set_forcing
+        if a.progress:
+            def forcing(k):
+                if k and k % a.progress == 0:
+                    print(f"model step {k}: {time.perf_counter() - t:.1f} s", file=sys.stderr, flush=True)
+                m.set_forcing(k)
+        r = run_steps(m, StepControl(mxstep=a.mxstep), a.model_steps, forcing, deferred_scalars=a.deferred_scalars,
                       op_timing=a.op_timing)
         m.read_state()
         wall = time.perf_counter() - t
