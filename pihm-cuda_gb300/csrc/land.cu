@@ -174,8 +174,8 @@ __global__ void __launch_bounds__(kLandBlock) k_land_step(LandDev L, const doubl
   const double radnet = sv[SV_SOLDN] * (1.0 - __ldg(&L.albedo[i]));
   const double vp = sv[SV_VP];
   const double pres = __ldg(&L.pres[i]);
-  const double qv = 0.622 * vp / pres;
-  const double qvsat = 0.622 * sv[SV_VPRH] / pres;
+  const double qv = div_any(0.622 * vp, pres);
+  const double qvsat = div_any(0.622 * sv[SV_VPRH], pres);
 
   // snow accumulation and melt
   const double frac_snow = sv[SV_FRAC_SNOW];
@@ -185,18 +185,18 @@ __global__ void __launch_bounds__(kLandBlock) k_land_step(LandDev L, const doubl
   if (sneqv > melt_rate * dt) {
     sneqv -= melt_rate * dt;
   } else {
-    melt_rate = sneqv / dt;
+    melt_rate = div_any(sneqv, dt);
     sneqv = 0.0;
   }
 
   // potential evaporation (Penman-Monteith)
   const double shdfac = __ldg(&L.shdfac[i]);
   const double intcp_max = __ldg(&L.cmcfactr[i]) * lai * shdfac;
-  const double ra = L.ra_num[i] / sv[SV_WIND016];
-  const double gamma = sv[SV_CGAMMA] / (pres / ra) + 1.0;
+  const double ra = div_any(L.ra_num[i], sv[SV_WIND016]);
+  const double gamma = div_any(sv[SV_CGAMMA], div_any(pres, ra)) + 1.0;
   const double delta = sv[SV_CDELTA] * qvsat;
-  const double etp =
-      (radnet * delta + gamma * (1.2 * kLvH2O * (qvsat - qv) / ra)) / (1000.0 * kLvH2O * (delta + gamma));
+  const double etp = div_any(radnet * delta + gamma * div_any(1.2 * kLvH2O * (qvsat - qv), ra),
+                             1000.0 * kLvH2O * (delta + gamma));
 
   // soil evaporation
   const double depth = __ldg(&L.depth[i]);
@@ -205,10 +205,10 @@ __global__ void __launch_bounds__(kLandBlock) k_land_step(LandDev L, const doubl
   if (depth - gw < __ldg(&L.rzd[i])) {
     satn = 1.0;
   } else {
-    const double r = unsat / (depth - gw);
+    const double r = div_any(unsat, depth - gw);
     satn = (r > 1.0) ? 1.0 : ((r < 0.0) ? 0.0 : 0.5 * (1.0 - cos(3.14 * r)));
   }
-  double betas = (satn * __ldg(&L.porosity[i]) + __ldg(&L.smcmin[i]) - __ldg(&L.smcwlt[i])) / __ldg(&L.dsmc[i]);
+  double betas = div_any(satn * __ldg(&L.porosity[i]) + __ldg(&L.smcmin[i]) - __ldg(&L.smcwlt[i]), __ldg(&L.dsmc[i]));
   betas = (betas < 0.0001) ? 0.0001 : ((betas > 1.0) ? 1.0 : betas);
   double edir = (1.0 - shdfac) * (betas * betas) * etp;
   edir *= L.cal_edir;
@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(kLandBlock) k_land_step(LandDev L, const doubl
     const double cm = (cmc < 0.0) ? 0.0 : ((cmc > intcp_max) ? intcp_max : cmc);
     // ec divides the clamped storage by intcp_max; ett's expression divides
     // only the unclamped branch (src/is_sm_et.c:128-131, 164-168)
-    const double base_ec = cm / intcp_max;
+    const double base_ec = div_any(cm, intcp_max);
     const double base_ett = (cmc < 0.0) ? 0.0 : base_ec;
     const double pw_ec = pow_fast(base_ec, cfactr);
     const double pw_ett = (__double_as_longlong(base_ett) == __double_as_longlong(base_ec)) ? pw_ec
@@ -231,42 +231,42 @@ __global__ void __launch_bounds__(kLandBlock) k_land_step(LandDev L, const doubl
     ec *= L.cal_ec;
     ec = (ec < 0.0) ? 0.0 : ec;
 
-    double fr = 1.1 * radnet / (__ldg(&L.rgl[i]) * lai);
+    double fr = div_any(1.1 * radnet, __ldg(&L.rgl[i]) * lai);
     fr = (fr < 0.0) ? 0.0 : fr;
-    double alphar = (1.0 + fr) / (fr + __ldg(&L.rs_ratio[i]));
+    double alphar = div_any(1.0 + fr, fr + __ldg(&L.rs_ratio[i]));
     alphar = (alphar > 10000.0) ? 10000.0 : alphar;
     const double dtopt = __ldg(&L.topt_c[i]) - sfctmp;
     double etas = 1.0 - 0.0016 * (dtopt * dtopt);
     etas = (etas < 0.0001) ? 0.0001 : etas;
     const double gammas = sv[SV_GAMMAS];
     const double rsmax = __ldg(&L.rsmax[i]);
-    double rs = __ldg(&L.rsmin[i]) * alphar / (betas * lai * etas * gammas);
+    double rs = div_any(__ldg(&L.rsmin[i]) * alphar, betas * lai * etas * gammas);
     rs = (rs > rsmax) ? rsmax : rs;
-    const double dg = delta / gamma;  // the reference forms it twice
-    const double pc = (1.0 + dg) / (1.0 + rs / ra + dg);
+    const double dg = div_any(delta, gamma);  // the reference forms it twice
+    const double pc = div_any(1.0 + dg, 1.0 + div_any(rs, ra) + dg);
     ett = shdfac * pc * (1.0 - pw_ett) * etp;
     ett *= L.cal_ett;
     ett = (ett < 0.0) ? 0.0 : ett;
     ett = ((gw < __ldg(&L.d_rzd[i])) && unsat <= 0.0) ? 0.0 : ett;
     // Rutter and Morton (1977): D0 = 6.52e-7 m s-1
-    drip = (cmc <= 0.0) ? 0.0 : 6.52E-7 * intcp_max * exp_l(3.89 * cmc / intcp_max);
+    drip = (cmc <= 0.0) ? 0.0 : 6.52E-7 * intcp_max * exp_l(div_any(3.89 * cmc, intcp_max));
   } else {
     ett = 0.0;
     ec = 0.0;
     drip = 0.0;
   }
   if (drip < 0.0) drip = 0.0;
-  if (drip * dt > cmc) drip = cmc / dt;
+  if (drip * dt > cmc) drip = div_any(cmc, dt);
 
   const double isval = cmc + (1.0 - frac_snow) * prcp * shdfac * dt - ec * dt - drip * dt;
   if (isval > intcp_max) {
     cmc = intcp_max;
-    drip += (isval - intcp_max) / dt;
+    drip += div_any(isval - intcp_max, dt);
   } else if (isval < 0.0) {
     cmc = 0.0;
     if (ec + drip > 0.0) {
-      ec = ec / (ec + drip) * (cmc + (1.0 - frac_snow) * prcp * shdfac * dt);
-      drip = drip / (ec + drip) * (cmc + (1.0 - frac_snow) * prcp * shdfac * dt);
+      ec = div_any(ec, ec + drip) * (cmc + (1.0 - frac_snow) * prcp * shdfac * dt);
+      drip = div_any(drip, ec + drip) * (cmc + (1.0 - frac_snow) * prcp * shdfac * dt);
     }
   } else {
     cmc = isval;
