@@ -176,3 +176,38 @@ def test_gpu_deferred_scalars_same_solve(case):
         [s1.nst, s1.nfe, s1.nni, s1.ncfn, s1.netf, s1.nli, s1.nfes]
     assert np.array_equal(res[0]["states"], res[-1]["states"])
     assert np.array_equal(res[0]["outlet"], res[-1]["outlet"])
+
+
+def test_deferred_scalars_follow_recoverable_rhs_failures_on_cpu():
+    """A right-hand side that reports recoverable failures (return +1): the
+    difference-quotient product retries with a quarter of the increment
+    (CVSpilsDQJtimes), a Newton evaluation makes CVODE retry the step.  The
+    GMRES iteration with its scalars kept aside (host values) must make the
+    same calls and the same solve as the plain iteration."""
+    import ctypes
+    ws, z, ctrl = _golden()
+    nsteps = 60
+    RHS = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p)
+    out = {}
+    for deferred in (0, 1):
+        b = OracleBackend(ws, z["y0"], z["pcp"], z["edir"], z["ett"])
+        inner = RHS(b.rhs.value)
+        calls = []
+
+        def flaky(t, y, ydot, ud, inner=inner, calls=calls):
+            rc = inner(t, y, ydot, ud)
+            calls.append(t)
+            return 1 if len(calls) % 37 == 0 else rc
+
+        cb = RHS(flaky)
+        b.rhs = ctypes.cast(cb, ctypes.c_void_p)
+        try:
+            r = run_steps(b, ctrl, nsteps, b.set_forcing, record_every=nsteps, deferred_scalars=deferred)
+        finally:
+            b.close()
+        s = r["stats"]
+        out[deferred] = (r["states"], [s.nst, s.nfe, s.nni, s.ncfn, s.netf, s.nli, s.nfes], calls)
+        assert r["deferred_scalars"] == deferred
+    assert out[0][1] == out[1][1], (out[0][1], out[1][1])
+    assert out[0][2] == out[1][2]
+    assert np.array_equal(out[0][0], out[1][0])
