@@ -449,9 +449,28 @@ def bench_flux_pihm():
     solve_s = time.perf_counter() - t
     noah_steps = m.noah_steps
     sneqv = m.g.noah_get("sneqv")
+    y_plain = m.read_state()
     m.close()
     evals = int(r["stats"].nfe + r["stats"].nfes)
     hours = FLUX_STEPS * 60.0 / 3600.0
+    # the same hour as a batch of one in the batch engine (Noah on the device
+    # there too; each round's vector operations fused per watershed)
+    engine = None
+    try:
+        from pihm_gpu.batch import Batch, limits_for
+        forcings = [N.forcing(ws, h, seed=2) for h in range(int(hours) + 1)]
+        b = Batch(limits_for([ws], FLUX_STEPS))
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        i = b.add_noah(ws, W.relax_state(ws), StepControl(), params, state, forcings, FLUX_LSM, FLUX_STEPS)
+        b.step()
+        got = b.result(i)
+        torch.cuda.synchronize()
+        ewall = time.perf_counter() - t
+        b.close()
+        engine = {"wall_s": ewall, "bit_identical_to_plain_path": bool(np.array_equal(got["y"], y_plain))}
+    except Exception as exc:
+        engine = {"error": repr(exc)}
     return {"metric": "Flux-PIHM RHS element-evals/s", "unit": "elem-evals/s", "value": res["noah"],
             "plain_rhs_value": res["plain"],
             "workload": f"{FLUX_NELEM} elements, {ws.nriver} segments, {FLUX_LAYERS} Noah soil layers, Noah on the "
@@ -464,6 +483,7 @@ def bench_flux_pihm():
                             "simulated_hours_per_wall_hour": hours * 3600.0 / solve_s,
                             "fraction_of_the_3_day_run": hours / 72.0,
                             "snow_covered_elements": int((sneqv > 0).sum()),
+                            "batch_engine": engine,
                             "workload": "RelaxIc, hourly synthetic Noah forcing (pihm_gpu.noah.forcing), land-surface "
                                         f"step {int(FLUX_LSM)} s, model step 60 s, reltol 1e-4"}}
 
