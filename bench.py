@@ -875,6 +875,44 @@ def main():
     e2e_copy_value = time_e2e(1)
     e2e_value = time_e2e(0)
     direct, pageable = g.host_path_info()
+    # pipelined: a second context on the same mesh and its own stream, the
+    # states alternating between the two through pihm_gpu_rhs_host_async /
+    # pihm_gpu_wait, so one evaluation's host-link transfers run beside the
+    # other's kernels (independent evaluations: an ensemble, not a CVODE
+    # sequence); same copies, same host buffers, host clock
+    pipelined = None
+    try:
+        stream2 = torch.cuda.Stream(device=dev)
+        g2 = GpuRhs(ws, stream=stream2.cuda_stream)
+        g2.set_forcing(*WL.rhs_forcing(ws))
+        g2.set_ws0_surf(base[:ws.nelem])
+        ctxs = (g, g2)
+
+        def submit(k):
+            c = ctxs[k % 2]
+            rc = lib.pihm_gpu_rhs_host_async(c.h, 0.0, ctypes.cast(y_host[k % NSTATES].data_ptr(), f64p),
+                                             ctypes.cast(yd_host[k % YDOT_RING].data_ptr(), f64p))
+            assert rc == 0, rc
+
+        def run(n):
+            for k in range(n):
+                if k >= 2:
+                    assert lib.pihm_gpu_wait(ctxs[k % 2].h) == 0
+                submit(k)
+            for c in ctxs:
+                assert lib.pihm_gpu_wait(c.h) == 0
+        run(4)
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        run(e2e_evals)
+        torch.cuda.synchronize()
+        ms_p = max_over_ranks((time.perf_counter() - t0) * 1e3, world, dev)
+        pipelined = {"value": replica_throughput(world, NELEM * e2e_evals, ms_p), "unit": UNIT, "contexts": 2,
+                     "evals": e2e_evals, "api": "pihm_gpu_rhs_host_async + pihm_gpu_wait, host clock"}
+        g2.close()
+    except Exception as exc:
+        pipelined = {"error": repr(exc)}
     host_path = ("direct: k_elem_prep reads y from and the reordering kernel writes ydot to pinned host memory"
                  if direct else "copy through device staging") + (
                  "; the device can access pageable host memory" if pageable else "")
@@ -980,7 +1018,8 @@ def main():
             "kernels": kernels, "dominant_kernel": dominant,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": bytes_state * STATES_PER_STEP,
                     "d2h_bytes_per_step": bytes_state * STATES_PER_STEP, "evals": e2e_evals,
-                    "host_path": host_path, "copy_path_value": e2e_copy_value},
+                    "host_path": host_path, "copy_path_value": e2e_copy_value,
+                    "pipelined": pipelined},
             "gpu_launches": launches,
             "clocks": clk.summary(),
             "cpu_baseline": cpu,

@@ -184,6 +184,17 @@ int pihm_gpu_rhs_host(pihm_gpu_ctx *ctx, double t, const double *y_host,
 /* pihm_gpu_rhs_host's path: mode 0 (default) reads and writes host arrays
  * directly where the device can address them, 1 always copies. */
 int pihm_gpu_set_host_path(pihm_gpu_ctx *ctx, int mode);
+/* pihm_gpu_rhs_host without waiting (no counterpart in the reference, whose
+ * evaluations are sequential): the evaluation is queued on the context's
+ * stream and pihm_gpu_wait returns its status; y_host must stay unchanged and
+ * both buffers valid until then, and the buffers should be pinned for the
+ * copies to be asynchronous.  Two contexts on one mesh, each on its own
+ * stream, then evaluate independent states with one's host-link transfers
+ * beside the other's kernels. */
+int pihm_gpu_rhs_host_async(pihm_gpu_ctx *ctx, double t, const double *y_host, double *ydot_host);
+/* Wait for the context's queued work: PIHM_GPU_OK, or PIHM_GPU_ERR_NAN if any
+ * of its evaluations since the last status read produced a NaN. */
+int pihm_gpu_wait(pihm_gpu_ctx *ctx);
 /* Whether the last pihm_gpu_rhs_host call accessed host memory directly, and
  * whether the device can access pageable host memory (either may be NULL). */
 int pihm_gpu_host_path_info(const pihm_gpu_ctx *ctx, int *last_direct, int *pageable_access);

@@ -409,8 +409,8 @@ int pihm_gpu_status(pihm_gpu_ctx *c) {
   return PIHM_GPU_OK;
 }
 
-int pihm_gpu_rhs_host(pihm_gpu_ctx *c, double t, const double *y_host, double *ydot_host) {
-  if (!c || !y_host || !ydot_host) return PIHM_GPU_ERR_ARG;
+// The host-buffer evaluation queued on the context's stream.
+static int rhs_host_enqueue(pihm_gpu_ctx *c, const double *y_host, double *ydot_host) {
   const size_t bytes = sizeof(double) * c->neq;
   // direct: k_elem_prep reads y from and the reordering kernel writes ydot to
   // host memory over the host link, in reference order (contiguous on the
@@ -429,8 +429,7 @@ int pihm_gpu_rhs_host(pihm_gpu_ctx *c, double t, const double *y_host, double *y
       e = launch_permute_ref(ydot_int, yd_dev, c->d_iperm, c->ne, c->nr, 0, c->stream);
       c->launches++;
     }
-    if (e != cudaSuccess) return PIHM_GPU_ERR_CUDA;
-    return pihm_gpu_status(c);
+    return e == cudaSuccess ? PIHM_GPU_OK : PIHM_GPU_ERR_CUDA;
   }
   // copy, then k_elem_prep reorders while preparing (the right-hand side
   // writes ydot over the reference-order copy once it has been read)
@@ -447,9 +446,23 @@ int pihm_gpu_rhs_host(pihm_gpu_ctx *c, double t, const double *y_host, double *y
   }
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(ydot_host, c->d_stage_out, bytes, cudaMemcpyDeviceToHost, c->stream);
-  if (e != cudaSuccess) return PIHM_GPU_ERR_CUDA;
-  return pihm_gpu_status(c);
+  return e == cudaSuccess ? PIHM_GPU_OK : PIHM_GPU_ERR_CUDA;
 }
+
+int pihm_gpu_rhs_host(pihm_gpu_ctx *c, double t, const double *y_host, double *ydot_host) {
+  (void)t;
+  if (!c || !y_host || !ydot_host) return PIHM_GPU_ERR_ARG;
+  const int rc = rhs_host_enqueue(c, y_host, ydot_host);
+  return rc != PIHM_GPU_OK ? rc : pihm_gpu_status(c);
+}
+
+int pihm_gpu_rhs_host_async(pihm_gpu_ctx *c, double t, const double *y_host, double *ydot_host) {
+  (void)t;
+  if (!c || !y_host || !ydot_host) return PIHM_GPU_ERR_ARG;
+  return rhs_host_enqueue(c, y_host, ydot_host);
+}
+
+int pihm_gpu_wait(pihm_gpu_ctx *c) { return pihm_gpu_status(c); }
 
 int pihm_gpu_set_host_path(pihm_gpu_ctx *c, int mode) {
   if (!c || (mode != 0 && mode != 1)) return PIHM_GPU_ERR_ARG;

@@ -50,6 +50,8 @@ def load() -> ctypes.CDLL:
         "pihm_gpu_destroy": ([_VP], None),
         "pihm_gpu_set_stream": ([_VP, _VP], ctypes.c_int),
         "pihm_gpu_set_kernel_shape": ([_VP, ctypes.c_int], ctypes.c_int),
+        "pihm_gpu_rhs_host_async": ([_VP, ctypes.c_double, _VP, _VP], ctypes.c_int),
+        "pihm_gpu_wait": ([_VP], ctypes.c_int),
         "pihm_gpu_sizes": ([_VP, _I32P, _I32P, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
         "pihm_gpu_get_permutation": ([_VP, _I32P, _I32P], ctypes.c_int),
         "pihm_gpu_set_forcing": ([_VP, _F64P, _F64P, _F64P], ctypes.c_int),

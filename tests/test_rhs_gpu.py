@@ -276,3 +276,49 @@ def test_element_kernel_shapes_give_the_same_bits():
     for shape in (1, 2):
         for k in range(3):
             assert np.array_equal(out[shape][k], out[0][k]), (shape, k)
+
+
+def test_async_host_evaluations_on_two_contexts_match_sync():
+    """pihm_gpu_rhs_host_async on two contexts of one mesh, each on its own
+    stream, alternating states (pinned buffers, direct host path): each
+    derivative equals the synchronous evaluation of the same state on a
+    context with the same call history."""
+    import ctypes
+    import torch
+    from pihm_gpu import workloads as WL
+    from pihm_gpu.capi import GpuRhs
+    ws = W.generate(20_000, WL.river_count(20_000), seed=14)
+    base = W.reference_state(ws, 14)
+    forcing = W.random_forcing(ws, 14)
+    states = [W.jitter(base, 900 + k) for k in range(6)]
+    f64p = ctypes.POINTER(ctypes.c_double)
+
+    def ctx(stream=None):
+        g = GpuRhs(ws, stream=stream)
+        g.set_forcing(*forcing)
+        g.set_ws0_surf(base[:ws.nelem])
+        return g
+
+    # synchronous reference: context k % 2 evaluates states k in order
+    want = []
+    refs = [ctx(), ctx()]
+    for k, y in enumerate(states):
+        got, rc = refs[k % 2].rhs_host(y)
+        assert rc == 0
+        want.append(got)
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    gs = [ctx(s1.cuda_stream), ctx(s2.cuda_stream)]
+    yh = [torch.from_numpy(y).pin_memory() for y in states]
+    ydh = [torch.empty(ws.neq, dtype=torch.float64).pin_memory() for _ in states]
+    lib = gs[0].lib
+    for k in range(len(states)):
+        if k >= 2:
+            assert lib.pihm_gpu_wait(gs[k % 2].h) == 0
+        assert lib.pihm_gpu_rhs_host_async(gs[k % 2].h, 0.0, ctypes.cast(yh[k].data_ptr(), f64p),
+                                           ctypes.cast(ydh[k].data_ptr(), f64p)) == 0
+    for g in gs:
+        assert lib.pihm_gpu_wait(g.h) == 0
+    for k in range(len(states)):
+        assert np.array_equal(ydh[k].numpy(), want[k]), k
+    for g in gs + refs:
+        g.close()
