@@ -12,8 +12,12 @@ L2, so no L2 flush is needed between evaluations.
 Printed (one JSON line, rank 0):
   value     element-evals/s with the states resident in HBM (device pointers,
             internal order), CUDA events on the library's stream
-  e2e       the same metric through the host-buffer C-ABI call
-            (pihm_gpu_rhs_host: pinned host y -> device, evaluate, -> host)
+  e2e       the same metric through the host-buffer C-ABI calls, every
+            state copied from pinned host memory and every derivative back
+            inside the timed region: the faster of pihm_gpu_rhs_host one
+            evaluation at a time (sync_value) and pihm_gpu_rhs_host_async on
+            two contexts of the mesh, whose copies run beside each other's
+            kernels (pipelined); mode says which
   roofline  the right-hand-side evaluation against the measured HBM copy
             bandwidth: algorithmic bytes (332 B per element + 184 B per
             segment) / device time of one evaluation
@@ -906,19 +910,36 @@ def main():
                 submit(k)
             for c in ctxs:
                 assert lib.pihm_gpu_wait(c.h) == 0
-        run(2 * nc)
-        barrier()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        run(e2e_evals)
-        torch.cuda.synchronize()
-        ms_p = max_over_ranks((time.perf_counter() - t0) * 1e3, world, dev)
-        pipelined = {"value": replica_throughput(world, NELEM * e2e_evals, ms_p), "unit": UNIT, "contexts": nc,
+        by_path = {}
+        for mode, name in ((0, "direct"), (1, "copy")):
+            # direct: the kernels read and write host memory (SM time on the
+            # link); copy: the copy engines move it, beside the other
+            # context's kernels
+            for c in ctxs:
+                c.set_host_path(mode)
+            run(2 * nc)
+            barrier()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            run(e2e_evals)
+            torch.cuda.synchronize()
+            ms_p = max_over_ranks((time.perf_counter() - t0) * 1e3, world, dev)
+            by_path[name] = replica_throughput(world, NELEM * e2e_evals, ms_p)
+        g.set_host_path(0)
+        best = max(by_path, key=by_path.get)
+        pipelined = {"value": by_path[best], "unit": UNIT, "contexts": nc, "host_path": best, "by_host_path": by_path,
                      "evals": e2e_evals, "api": "pihm_gpu_rhs_host_async + pihm_gpu_wait, host clock"}
         for _, gx in extra:
             gx.close()
     except Exception as exc:
         pipelined = {"error": repr(exc)}
+    # the headline e2e: the faster way through the C ABI for these 100
+    # independent states, every copy of every state inside the timed region
+    e2e_best, e2e_mode = e2e_value, "sync: pihm_gpu_rhs_host, one evaluation at a time"
+    if pipelined and "value" in pipelined and pipelined["value"] > e2e_value:
+        e2e_best = pipelined["value"]
+        e2e_mode = (f"pipelined: pihm_gpu_rhs_host_async on {pipelined['contexts']} contexts of the mesh, "
+                    f"{pipelined['host_path']} host path")
     host_path = ("direct: k_elem_prep reads y from and the reordering kernel writes ydot to pinned host memory"
                  if direct else "copy through device staging") + (
                  "; the device can access pageable host memory" if pageable else "")
@@ -1022,9 +1043,9 @@ def main():
                          "alg_bytes_per_eval": alg_bytes, "ms_per_eval": ms_per_eval,
                          "limit": "FP64 pipe (see fp64_pipe), not HBM", "fp64_pipe": fp64},
             "kernels": kernels, "dominant_kernel": dominant,
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": bytes_state * STATES_PER_STEP,
-                    "d2h_bytes_per_step": bytes_state * STATES_PER_STEP, "evals": e2e_evals,
-                    "host_path": host_path, "copy_path_value": e2e_copy_value,
+            "e2e": {"value": e2e_best, "unit": UNIT, "h2d_bytes_per_step": bytes_state * STATES_PER_STEP,
+                    "d2h_bytes_per_step": bytes_state * STATES_PER_STEP, "evals": e2e_evals, "mode": e2e_mode,
+                    "sync_value": e2e_value, "host_path": host_path, "copy_path_value": e2e_copy_value,
                     "pipelined": pipelined},
             "gpu_launches": launches,
             "clocks": clk.summary(),
