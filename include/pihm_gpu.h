@@ -188,7 +188,9 @@ int pihm_gpu_set_host_path(pihm_gpu_ctx *ctx, int mode);
  * evaluations are sequential): the evaluation is queued on the context's
  * stream and pihm_gpu_wait returns its status; y_host must stay unchanged and
  * both buffers valid until then, and the buffers should be pinned for the
- * copies to be asynchronous.  Two contexts on one mesh, each on its own
+ * copies to be asynchronous.  Several evaluations may be queued on one
+ * context before a wait; they run in the order queued, each seeing the
+ * carried state the previous one left.  Two contexts on one mesh, each on its own
  * stream, then evaluate independent states with one's host-link transfers
  * beside the other's kernels. */
 int pihm_gpu_rhs_host_async(pihm_gpu_ctx *ctx, double t, const double *y_host, double *ydot_host);

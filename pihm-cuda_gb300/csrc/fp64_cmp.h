@@ -115,5 +115,19 @@ PIHM_CMP_FN bool ge_v(double x, double y) { return le_v(y, x); }
 // |x| < c for a finite c > 0
 PIHM_CMP_FN bool abs_lt_c(double x, double c) { return (bits(x) & kMag) < bits(c); }
 
+PIHM_CMP_FN double from_bits(uint64_t b) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)b);
+#else
+  double x;
+  std::memcpy(&x, &b, sizeof x);
+  return x;
+#endif
+}
+
+// -x when neg is true, else x: the C unary minus flips the sign bit and
+// nothing else, so it too stays off the FP64 pipe
+PIHM_CMP_FN double neg_if(double x, bool neg) { return from_bits(bits(x) ^ ((uint64_t)neg << 63)); }
+
 }  // namespace cmp
 }  // namespace pihm

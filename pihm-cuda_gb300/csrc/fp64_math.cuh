@@ -171,13 +171,18 @@ __device__ __forceinline__ double pow_any(double x, double y) {
 // a / b and sqrt(x), correctly rounded: the integer-pipe paths where the
 // operands and the result are normal, the FP64 instructions otherwise (the
 // same bits either way)
+// The FP64 instructions sit out of line, as pow_any's fallback does: a
+// division or root inlined behind the test would be predicated rather than
+// branched around, and issued to the FP64 pipe by every warp.
+static __device__ __noinline__ double div_slow(double a, double b) { return a / b; }
+static __device__ __noinline__ double sqrt_slow(double x) { return sqrt(x); }
 __device__ __forceinline__ double div_any(double a, double b) {
   double q;
-  return im::div_i(a, b, q) ? q : a / b;
+  return im::div_i(a, b, q) ? q : div_slow(a, b);
 }
 __device__ __forceinline__ double sqrt_any(double x) {
   double r;
-  return im::sqrt_i(x, r) ? r : sqrt(x);
+  return im::sqrt_i(x, r) ? r : sqrt_slow(x);
 }
 
 // the Manning powers h^0.6666667 and h^(2/3)

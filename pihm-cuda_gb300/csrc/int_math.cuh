@@ -172,11 +172,17 @@ PIHM_IM_FN double exp2k(TVal t) {
   return bitsd(((uint64_t)(q + 1023) << 52) + (mant & kFrac));
 }
 
-// x^y on the integer path; false when x or y is outside its ranges
+// x^y on the integer path; false when x or y is outside its ranges.  +0 to
+// a positive power is +0 (C99 F.9.4.4), which a full soil column produces
+// (1 - satn^m == 0).
 PIHM_IM_FN bool pow_i(double x, double y, double &out) {
   int k;
   int64_t w;
   TVal t;
+  if (dbits(x) == 0 && dbits(y) - 1u < 0x7FF0000000000000ull) {
+    out = 0.0;
+    return true;
+  }
   if (!log2k(x, k, w) || !mul_t(y, k, w, t)) return false;
   out = exp2k(t);
   return true;
@@ -192,8 +198,10 @@ PIHM_IM_FN bool pow_i(double x, double y, double &out) {
 // rounding midpoint then decides the last bit.  The results are therefore
 // the IEEE quotient and root bit for bit, whatever the seed's own rounding
 // (the host build seeds with a correctly rounded float, the GPU with
-// rcp.approx / rsqrt.approx).  Operands or results outside the normal range
-// are declined (false) and the caller uses the FP64 instruction.
+// rcp.approx / rsqrt.approx).  A zero dividend over a normal divisor and the
+// root of a zero give the signed zero; other operands or results outside the
+// normal range are declined (false) and the caller uses the FP64
+// instruction.
 // ---------------------------------------------------------------------------
 
 PIHM_IM_FN float rcp_seed(float x) {
@@ -253,11 +261,16 @@ PIHM_IM_FN uint64_t seed_fixed(float r) {
   return v >> 63 ? 0x7FFFFFFFFFFFFFFFull : v;
 }
 
-// q = a / b for normal a, b with a normal quotient
+// q = a / b for normal (or zero) a and normal b with a normal quotient
 PIHM_IM_FN bool div_i(double a, double b, double &q) {
   const uint64_t ab = dbits(a), bb = dbits(b);
   const unsigned ea = (unsigned)(ab >> 52) & 2047u, eb = (unsigned)(bb >> 52) & 2047u;
-  if (ea - 1u >= 2046u || eb - 1u >= 2046u) return false;  // zero, subnormal, inf, nan
+  if (eb - 1u >= 2046u) return false;  // zero, subnormal, inf or nan divisor
+  if (ea - 1u >= 2046u) {
+    if (ab << 1) return false;  // subnormal, inf or nan dividend
+    q = bitsd((ab ^ bb) & (1ull << 63));
+    return true;
+  }
   const uint64_t Ma = (ab & kFrac) | (1ull << 52), Mb = (bb & kFrac) | (1ull << 52);
   // 1/mb, mb = Mb 2^-52 in [1, 2): R = r 2^63
   uint64_t R = seed_fixed(rcp_seed(bitsf(0x3F800000u | (uint32_t)((Mb & kFrac) >> 29))));
@@ -296,9 +309,13 @@ PIHM_IM_FN bool div_i(double a, double b, double &q) {
   return true;
 }
 
-// sqrt(x) for positive normal x
+// sqrt(x) for positive normal x, or a zero
 PIHM_IM_FN bool sqrt_i(double x, double &r) {
   const uint64_t xb = dbits(x);
+  if ((xb << 1) == 0) {  // sqrt(+-0) = +-0
+    r = x;
+    return true;
+  }
   const unsigned top = (unsigned)(xb >> 52);  // sign and biased exponent
   if (top - 1u >= 2046u) return false;       // not positive and normal
   const int ex = (int)top - 1023;

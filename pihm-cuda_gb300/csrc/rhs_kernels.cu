@@ -89,7 +89,7 @@ __device__ __forceinline__ void kr_psi(double satn, double vm, double vg_e, doub
   sq = sqrt_any(satn);
   const double t = 1.0 - pow_any(1.0 - pow_any(satn, vm), vg_e);
   satkfunc = sq * t * t;
-  psi = div_any(-pow_any(pow_any(div_any(1.0, satn), vm) - 1.0, vg_ib), alpha);
+  psi = cmp::neg_if(div_any(pow_any(pow_any(div_any(1.0, satn), vm) - 1.0, vg_ib), alpha), true);
 }
 
 // Batch engine: whether the watershed of item idx sits out this evaluation
@@ -360,12 +360,12 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_elem_main(DevMesh m, const doub
   for (int j = 0; j < 3; j++) {
     const int32_t code = m.emap[j * ne + i];
     riv[j] = false;
-    if (code > 0) {
-      ovl[j] = m.eflux_ovl[code - 1];
-      sub[j] = m.eflux_sub[code - 1];
-    } else if (code < 0) {
-      ovl[j] = -m.eflux_ovl[-code - 1];
-      sub[j] = -m.eflux_sub[-code - 1];
+    if (code != 0) {
+      // the edge's flux with the sign seen from this element (a negative
+      // code: the flux was computed from the neighbour's side)
+      const int e = (code > 0 ? code : -code) - 1;
+      ovl[j] = cmp::neg_if(m.eflux_ovl[e], code < 0);
+      sub[j] = cmp::neg_if(m.eflux_sub[e], code < 0);
     } else {
       const int32_t nb = m.nb[j * ne + i];
       if (nb != kBoundary) {

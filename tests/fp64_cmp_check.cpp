@@ -1,4 +1,5 @@
-// Checks every helper of fp64_cmp.h against the C comparison operators on
+// Checks every helper of fp64_cmp.h against the C comparison operators (and
+// the sign flip against the unary minus) on
 // signed zeros, subnormals, normals around the model constants, infinities,
 // NaNs of both signs and random bit patterns.  Prints the number of
 // mismatches and exits non-zero when there is any.
@@ -14,12 +15,6 @@
 #include "fp64_cmp.h"
 
 using namespace pihm::cmp;
-
-static double from_bits(uint64_t b) {
-  double x;
-  std::memcpy(&x, &b, sizeof x);
-  return x;
-}
 
 int main() {
   // the positive constants the kernels compare against, and a few others
@@ -63,6 +58,10 @@ int main() {
     check(le0(x), x <= 0.0, "le0", x, 0.0);
     check(eq0(x), x == 0.0, "eq0", x, 0.0);
     check(isnan_(x), std::isnan(x), "isnan_", x, 0.0);
+    // the unary minus, bit for bit
+    const double nx = -x;
+    check(bits(neg_if(x, true)) == bits(nx), true, "neg_if", x, 0.0);
+    check(bits(neg_if(x, false)) == bits(x), true, "neg_if0", x, 0.0);
     for (double c : consts) {
       check(gt_c(x, c), x > c, "gt_c", x, c);
       check(ge_c(x, c), x >= c, "ge_c", x, c);

@@ -79,14 +79,18 @@ def test_error_against_high_precision_references(host_lib):
 
 
 def test_exact_cases_and_declined_arguments(host_lib):
-    x = np.array([1.0, 0.5, 2.0, 4.0, 0.25, 8.0, 1.0, 0.0, -1.0, np.nan, np.inf, 1e-310, 2.0 ** 130, 2.0, 2.0])
-    y = np.array([3.7, 2.0, 10.0, 0.5, -1.5, 1.0 / 3.0, 0.0, 0.5, 0.5, 0.5, 0.5, 0.5, 0.5, 1e-9, 1e12])
+    x = np.array([1.0, 0.5, 2.0, 4.0, 0.25, 8.0, 0.0, 0.0,
+                  1.0, 0.0, 0.0, -0.0, -1.0, np.nan, np.inf, 1e-310, 2.0 ** 130, 2.0, 2.0])
+    y = np.array([3.7, 2.0, 10.0, 0.5, -1.5, 1.0 / 3.0, 0.5, 7.0,
+                  0.0, 0.0, -0.5, 0.5, 0.5, 0.5, 0.5, 0.5, 0.5, 1e-9, 1e12])
     got, ok = host_pow(host_lib, x, y)
-    assert ok[:6].all()
-    assert list(got[:6]) == [1.0, 0.25, 1024.0, 2.0, 8.0, 2.0]
-    # y = 0, zero, negative, NaN, infinite, subnormal or huge x, tiny or huge
-    # exponents: declined (the kernels use the FP64 path there)
-    assert not ok[6:].any()
+    assert ok[:8].all()
+    assert list(got[:8]) == [1.0, 0.25, 1024.0, 2.0, 8.0, 2.0, 0.0, 0.0]
+    assert not np.signbit(got[6:8]).any()
+    # y = 0, +0 to a non-positive power, -0, negative, NaN, infinite,
+    # subnormal or huge x, tiny or huge exponents: declined (the kernels use
+    # the FP64 path there)
+    assert not ok[8:].any()
 
 
 @pytest.mark.gpu
@@ -131,6 +135,7 @@ def div_sqrt_cases(rng, n):
         "integers": (rng.integers(1, 1 << 53, n).astype(np.float64), rng.integers(1, 1 << 26, n).astype(np.float64)),
         "squares": ((rng.integers(1, 1 << 26, n).astype(np.float64)) ** 2, np.full(n, 3.0)),
         "bit patterns": (np.abs(bits()), bits()),
+        "zero dividends": (np.zeros(n) * sign(), np.exp(rng.uniform(-340, 340, n)) * sign()),
     }
 
 
@@ -140,16 +145,19 @@ def test_division_and_sqrt_are_ieee_bit_for_bit(host_lib):
         q, okq, r, okr = host_div_sqrt(host_lib, a, b)
         with np.errstate(all="ignore"):
             wq, wr = a / b, np.sqrt(a)
-        assert okq.mean() > 0.7 and okr[a > 0].mean() > 0.99, name
+        assert okq.mean() > 0.7 and okr[a >= 0].mean() > 0.99, name
         assert np.array_equal(q[okq].view(np.int64), wq[okq].view(np.int64)), name
         assert np.array_equal(r[okr].view(np.int64), wr[okr].view(np.int64)), name
-    # zeros, subnormals, infinities, NaN and out-of-range quotients are
-    # declined; the square root declines negative arguments too
-    a = np.array([0.0, 5e-324, np.inf, np.nan, 1.0, 1e300, 1e-300, -4.0])
-    b = np.array([1.0, 1.0, 1.0, 1.0, 0.0, 1e-300, 1e300, 1.0])
-    q, okq, _, okr = host_div_sqrt(host_lib, a, b)
-    assert list(okq) == [False] * 7 + [True] and q[7] == -4.0
-    assert list(okr) == [False, False, False, False, True, True, True, False]
+    # a zero dividend gives the signed zero and the root of a zero is that
+    # zero; subnormals, infinities, NaN, zero divisors and out-of-range
+    # quotients are declined; the square root declines negative arguments too
+    a = np.array([0.0, -0.0, 5e-324, np.inf, np.nan, 1.0, 1e300, 1e-300, -4.0])
+    b = np.array([-1.0, 1.0, 1.0, 1.0, 1.0, 0.0, 1e-300, 1e300, 1.0])
+    q, okq, r, okr = host_div_sqrt(host_lib, a, b)
+    assert list(okq) == [True, True] + [False] * 6 + [True] and q[8] == -4.0
+    assert q[0] == 0.0 and np.signbit(q[0]) and q[1] == 0.0 and np.signbit(q[1])
+    assert list(okr) == [True, True, False, False, False, True, True, True, False]
+    assert r[0] == 0.0 and not np.signbit(r[0]) and np.signbit(r[1])
 
 
 @pytest.mark.gpu

@@ -278,11 +278,13 @@ def test_element_kernel_shapes_give_the_same_bits():
             assert np.array_equal(out[shape][k], out[0][k]), (shape, k)
 
 
-def test_async_host_evaluations_on_two_contexts_match_sync():
+@pytest.mark.parametrize("depth", [1, 3])
+def test_async_host_evaluations_on_two_contexts_match_sync(depth):
     """pihm_gpu_rhs_host_async on two contexts of one mesh, each on its own
-    stream, alternating states (pinned buffers, direct host path): each
-    derivative equals the synchronous evaluation of the same state on a
-    context with the same call history."""
+    stream, alternating states (pinned buffers, direct host path), with one
+    or several evaluations queued per context before a wait: each derivative
+    equals the synchronous evaluation of the same state on a context with the
+    same call history."""
     import ctypes
     import torch
     from pihm_gpu import workloads as WL
@@ -311,9 +313,12 @@ def test_async_host_evaluations_on_two_contexts_match_sync():
     yh = [torch.from_numpy(y).pin_memory() for y in states]
     ydh = [torch.empty(ws.neq, dtype=torch.float64).pin_memory() for _ in states]
     lib = gs[0].lib
+    queued = [0, 0]
     for k in range(len(states)):
-        if k >= 2:
+        if queued[k % 2] >= depth:
             assert lib.pihm_gpu_wait(gs[k % 2].h) == 0
+            queued[k % 2] = 0
+        queued[k % 2] += 1
         assert lib.pihm_gpu_rhs_host_async(gs[k % 2].h, 0.0, ctypes.cast(yh[k].data_ptr(), f64p),
                                            ctypes.cast(ydh[k].data_ptr(), f64p)) == 0
     for g in gs:
