@@ -340,10 +340,52 @@ __global__ void __launch_bounds__(kEdgeBlock) k_edge(DevMesh m, const double *RE
 // fastest on large meshes (276 against 298 and 294 us per 1M elements); on a
 // small mesh or a sparsely occupied batch arena the smaller blocks spread the
 // work over more SMs.  The batch engine tunes the shape per arena.
+//
+// Branch classes: a block first sorts its elements by the branches the
+// element rows take -- water table within the infiltration depth (no
+// Psi/KrFunc, Recharge = Infil), ponded surface (EffKinf's second case),
+// unsaturated zone deeper than the macropores (AvgKv's first case) -- so
+// that a warp's lanes mostly take the same ones, and each thread then
+// evaluates the element at its rank.  The classes only group; every element
+// is evaluated by the same code whatever its class, so the results do not
+// depend on the grouping.  Items that sit out (past the end, or a batch
+// watershed without an evaluation) sort last and leave as whole warps.
+constexpr int kElemClasses = 8;
+
+__device__ __forceinline__ int elem_class(const DevMesh &m, const double *RESTRICT y, int i) {
+  const int ne = m.ne;
+  const double gw = clamp0(y[2 * ne + i]);
+  const int ponded = cmp::gt_c(m.surfh[i], kDeprStg) ? 1 : 0;
+  if (cmp::gt_v(gw, m.d_dinf[i])) return 4 + ponded;
+  return 2 * ponded + (cmp::lt_v(gw, m.d_dmac[i]) ? 1 : 0);
+}
+
 template <int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) k_elem_main(DevMesh m, const double *RESTRICT y,
                                                     double *RESTRICT ydot) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ int s_count[kElemClasses];
+  __shared__ unsigned short s_order[BLOCK];
+  {
+    const int i0 = blockIdx.x * BLOCK + threadIdx.x;
+    int sy0;
+    const int cls = (i0 >= m.ne_run || skip_item(m, m.sys_elem, i0, &sy0)) ? kElemClasses - 1
+                                                                          : elem_class(m, y, i0);
+    if (threadIdx.x < kElemClasses) s_count[threadIdx.x] = 0;
+    __syncthreads();
+    // rank among the block's elements of the same class: one shared atomic
+    // per class present in the warp
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned peers = __match_any_sync(0xffffffffu, cls);
+    const int leader = __ffs(peers) - 1;
+    int rank = 0;
+    if ((int)lane == leader) rank = atomicAdd(&s_count[cls], __popc(peers));
+    rank = __shfl_sync(0xffffffffu, rank, leader) + __popc(peers & ((1u << lane) - 1u));
+    __syncthreads();
+    for (int c = 0; c < cls; c++) rank += s_count[c];
+    s_order[rank] = (unsigned short)threadIdx.x;
+    __syncthreads();
+  }
+  const int i = blockIdx.x * BLOCK + s_order[threadIdx.x];
   int sy;
   if (i >= m.ne_run || skip_item(m, m.sys_elem, i, &sy)) return;
   const int ne = m.ne;
