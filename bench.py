@@ -45,8 +45,9 @@ sys.path.insert(0, os.path.join(ROOT, "pihm-cuda_gb300"))
 NELEM, NRIVER = 1_000_000, 30_000
 NSTATES = 100
 STATES_PER_STEP = 100      # a step is one pass over the whole state set
-YDOT_RING = 10             # derivative buffers cycled through
+YDOT_RING = 12             # derivative buffers cycled through (a multiple of the context count)
 PIPE_DEPTH = 4             # evaluations queued per context in the pipelined end-to-end leg
+E2E_REPS = 3               # timed passes per pipelined configuration (the median is kept)
 BYTES_PER_ELEM, BYTES_PER_SEG = 332, 184
 METRIC = "RHS element-evals/s"
 UNIT = "elem-evals/s"
@@ -767,6 +768,10 @@ def main():
     ap.add_argument("--no-flux", action="store_true", help="skip the Flux-PIHM leg")
     ap.add_argument("--no-land", action="store_true", help="skip the land-surface leg")
     ap.add_argument("--no-scattered", action="store_true", help="skip the scattered-node mesh leg")
+    ap.add_argument("--contexts", type=int, default=RHS_CONTEXTS, choices=[1, 2, 3, 4],
+                    help="contexts of the mesh the states are spread over")
+    ap.add_argument("--shape", type=int, default=1, choices=[0, 1, 2],
+                    help="k_elem_main block shape of the headline contexts: 512x2, 256x4, 128x8 per SM")
     ap.add_argument("--solve-hours", type=float, default=0.5,
                     help="simulated hours of the 1M-element solve leg (0 skips it)")
     args = ap.parse_args()
@@ -807,17 +812,20 @@ def main():
     # RHS_CONTEXTS contexts of the mesh, each on its own stream, take the
     # states in turn: independent evaluations fill each other's kernel tails
     # and launch gaps (1: 2.23, 2: 2.48, 3: 2.51 G element-evals/s measured)
-    streams = [stream] + [torch.cuda.Stream(device=dev) for _ in range(RHS_CONTEXTS - 1)]
+    streams = [stream] + [torch.cuda.Stream(device=dev) for _ in range(args.contexts - 1)]
     ctxs = [g]
     for st in streams[1:]:
         gx = GpuRhs(ws, stream=st.cuda_stream)
         gx.set_forcing(*WL.rhs_forcing(ws))
         gx.set_ws0_surf(base[:ws.nelem])
         ctxs.append(gx)
+    for c in ctxs:
+        c.set_kernel_shape(args.shape)
     setup_s = time.perf_counter() - t_setup
 
     def step(s):
-        # ydot ring slots e % YDOT_RING: an even ring keeps each context on its own slots
+        # ydot ring slots e % YDOT_RING: the ring is a multiple of the context
+        # count, so each context keeps to its own slots
         for e in range(STATES_PER_STEP):
             k = (s * STATES_PER_STEP + e) % NSTATES
             ctxs[e % len(ctxs)].rhs_device(states[k].data_ptr(), ydot[e % YDOT_RING].data_ptr())
@@ -943,16 +951,20 @@ def main():
                 c.set_host_path(mode)
             for depth in (1, PIPE_DEPTH):
                 run(2 * nc, depth)
-                barrier()
-                torch.cuda.synchronize()
-                t0 = time.perf_counter()
-                run(e2e_evals, depth)
-                torch.cuda.synchronize()
-                ms_p = max_over_ranks((time.perf_counter() - t0) * 1e3, world, dev)
-                by_path[f"{name}, depth {depth}"] = replica_throughput(world, NELEM * e2e_evals, ms_p)
+                reps = []
+                for _ in range(E2E_REPS):
+                    barrier()
+                    torch.cuda.synchronize()
+                    t0 = time.perf_counter()
+                    run(e2e_evals, depth)
+                    torch.cuda.synchronize()
+                    ms_p = max_over_ranks((time.perf_counter() - t0) * 1e3, world, dev)
+                    reps.append(replica_throughput(world, NELEM * e2e_evals, ms_p))
+                by_path[f"{name}, depth {depth}"] = statistics.median(reps)
         g.set_host_path(0)
         best = max(by_path, key=by_path.get)
         pipelined = {"value": by_path[best], "unit": UNIT, "contexts": nc, "best": best,
+                     "statistic": f"median of {E2E_REPS} passes of {e2e_evals} evaluations per configuration",
                      "by_host_path_and_depth": by_path,
                      "evals": e2e_evals, "api": "pihm_gpu_rhs_host_async + pihm_gpu_wait, host clock"}
     except Exception as exc:
@@ -1068,7 +1080,7 @@ def main():
                          "alg_bytes_per_eval": alg_bytes, "ms_per_eval": ms_per_eval,
                          "limit": "FP64 pipe (see fp64_pipe), not HBM", "fp64_pipe": fp64},
             "kernels": kernels, "dominant_kernel": dominant,
-            "rhs_contexts": {"count": len(ctxs), "note": "the states are spread round-robin over contexts of the "
+            "rhs_contexts": {"count": len(ctxs), "k_elem_main_shape": ("512x2", "256x4", "128x8")[args.shape], "note": "the states are spread round-robin over contexts of the "
                              "mesh on their own streams; kernels and their shares are one context's"},
             "e2e": {"value": e2e_best, "unit": UNIT, "h2d_bytes_per_step": bytes_state * STATES_PER_STEP,
                     "d2h_bytes_per_step": bytes_state * STATES_PER_STEP, "evals": e2e_evals, "mode": e2e_mode,

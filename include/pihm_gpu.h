@@ -129,8 +129,8 @@ void pihm_gpu_destroy(pihm_gpu_ctx *ctx);
 int pihm_gpu_set_stream(pihm_gpu_ctx *ctx, void *stream);
 /* The stream the context issues its work on (NULL = legacy default). */
 void *pihm_gpu_get_stream(const pihm_gpu_ctx *ctx);
-/* Block shape of the element kernel: 0 (default) 512 threads x 2 blocks per
- * SM, 1: 256 x 4, 2: 128 x 8; identical results (the batch engine's
+/* Block shape of the element kernel: 0: 512 threads x 2 blocks per SM,
+ * 1 (default): 256 x 4, 2: 128 x 8; identical results (the batch engine's
  * pihm_batch_set_rhs_shape). */
 int pihm_gpu_set_kernel_shape(pihm_gpu_ctx *ctx, int shape);
 int pihm_gpu_sizes(const pihm_gpu_ctx *ctx, int32_t *nelem, int32_t *nriver,

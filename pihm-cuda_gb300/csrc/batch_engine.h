@@ -240,7 +240,7 @@ struct pihm_batch {
   // requesting element is kept.  Every shape gives the same bits.
   static constexpr int kShapes = 3;
   static constexpr int64_t kShapeMinElems = 20000;
-  int shape_best = 0, shape_forced = -1, shape_next = 0;
+  int shape_best = 1, shape_forced = -1, shape_next = 0;
   bool shape_tuning = true;
   double shape_ms_per_elem[kShapes] = {0};
   int shape_n[kShapes] = {0};

@@ -166,6 +166,7 @@ int pihm_gpu_create(const pihm_gpu_mesh *g, int surf_mode, int riv_mode, double 
   m.nr_run = nr;
   m.nedge_run = nedge;
   m.nbank_run = nbank;
+  m.main_shape = 1;  // k_elem_main at 256 x 4 per SM
 
   // dynamic block: inputs, scratch, diagnostics, staging, error word
   size_t dbytes = 0;

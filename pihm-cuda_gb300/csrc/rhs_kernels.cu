@@ -336,10 +336,12 @@ __global__ void __launch_bounds__(kEdgeBlock) k_edge(DevMesh m, const double *RE
 // k_elem_main
 // ---------------------------------------------------------------------------
 // Block shapes: the same 64-register budget (1,024 resident threads per
-// SM) cut into 512 x 2, 256 x 4 or 128 x 8 blocks.  The largest blocks are
-// fastest on large meshes (276 against 298 and 294 us per 1M elements); on a
-// small mesh or a sparsely occupied batch arena the smaller blocks spread the
-// work over more SMs.  The batch engine tunes the shape per arena.
+// SM) cut into 512 x 2, 256 x 4 or 128 x 8 blocks.  With the elements
+// ranked by branch class per block, 256 x 4 is fastest on large meshes (92
+// against 102 and 97 us per 400k elements): larger blocks group more
+// elements of a class but gather their loads from a wider window.  On a
+// small mesh or a sparsely occupied batch arena the smaller blocks spread
+// the work over more SMs.  The batch engine tunes the shape per arena.
 //
 // Branch classes: a block first sorts its elements by the branches the
 // element rows take -- water table within the infiltration depth (no
