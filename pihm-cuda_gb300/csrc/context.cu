@@ -225,8 +225,11 @@ static void free_profiler(Profiler *p) {
   delete p;
 }
 
+static void copy_path_release(pihm_gpu_ctx *c);
+
 void pihm_gpu_destroy(pihm_gpu_ctx *c) {
   if (!c) return;
+  copy_path_release(c);
   free_profiler(c->prof);
   if (c->d_static) cudaFree(c->d_static);
   if (c->d_dyn) cudaFree(c->d_dyn);
@@ -410,6 +413,47 @@ int pihm_gpu_status(pihm_gpu_ctx *c) {
   return PIHM_GPU_OK;
 }
 
+// The copy path's second staging pair, streams and events, on first use.
+static bool copy_path_init(pihm_gpu_ctx *c) {
+  auto &cp = c->cp;
+  if (cp.ready) return true;
+  const size_t bytes = sizeof(double) * c->neq;
+  const size_t half = (bytes + 255) & ~size_t(255);
+  if (cudaMalloc(&cp.second, 2 * half) != cudaSuccess) {
+    cp.second = nullptr;
+    return false;
+  }
+  cp.in[0] = c->d_stage_in;
+  cp.out[0] = c->d_stage_out;
+  cp.in[1] = (double *)cp.second;
+  cp.out[1] = (double *)((char *)cp.second + half);
+  bool ok = cudaStreamCreateWithFlags(&cp.h2d, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaStreamCreateWithFlags(&cp.d2h, cudaStreamNonBlocking) == cudaSuccess;
+  for (int k = 0; k < 2 && ok; k++)
+    ok = cudaEventCreateWithFlags(&cp.arrived[k], cudaEventDisableTiming) == cudaSuccess &&
+         cudaEventCreateWithFlags(&cp.done[k], cudaEventDisableTiming) == cudaSuccess &&
+         cudaEventCreateWithFlags(&cp.freed[k], cudaEventDisableTiming) == cudaSuccess;
+  if (!ok) {
+    copy_path_release(c);
+    return false;
+  }
+  cp.ready = true;
+  return true;
+}
+
+static void copy_path_release(pihm_gpu_ctx *c) {
+  auto &cp = c->cp;
+  if (cp.h2d) cudaStreamSynchronize(cp.h2d);
+  if (cp.d2h) cudaStreamSynchronize(cp.d2h);
+  for (int k = 0; k < 2; k++)
+    for (cudaEvent_t e : {cp.arrived[k], cp.done[k], cp.freed[k]})
+      if (e) cudaEventDestroy(e);
+  if (cp.h2d) cudaStreamDestroy(cp.h2d);
+  if (cp.d2h) cudaStreamDestroy(cp.d2h);
+  if (cp.second) cudaFree(cp.second);
+  cp = pihm_gpu_ctx::CopyPath{};
+}
+
 // The host-buffer evaluation queued on the context's stream.
 static int rhs_host_enqueue(pihm_gpu_ctx *c, const double *y_host, double *ydot_host) {
   const size_t bytes = sizeof(double) * c->neq;
@@ -433,28 +477,49 @@ static int rhs_host_enqueue(pihm_gpu_ctx *c, const double *y_host, double *ydot_
     return e == cudaSuccess ? PIHM_GPU_OK : PIHM_GPU_ERR_CUDA;
   }
   // copy, then k_elem_prep reorders while preparing (the right-hand side
-  // writes ydot over the reference-order copy once it has been read)
-  cudaError_t e = cudaMemcpyAsync(c->d_stage_in, y_host, bytes, cudaMemcpyHostToDevice, c->stream);
-  double *y_int = c->d_stage_out, *ydot_int = c->d_stage_in;
+  // writes ydot over the reference-order copy once it has been read).  The
+  // staging pairs alternate: the state of the evaluation after this one
+  // arrives on the h2d stream while this one's kernels run, and this one's
+  // derivative leaves on the d2h stream while the next one's kernels run.
+  // A pair is refilled only after the derivative it held two evaluations
+  // ago has left (freed), and the kernels start only after their state has
+  // arrived.
+  if (!copy_path_init(c)) return PIHM_GPU_ERR_NOMEM;
+  auto &cp = c->cp;
+  const int s = cp.slot;
+  cp.slot ^= 1;
+  double *in = cp.in[s], *out = cp.out[s];
+  cudaError_t e = cudaStreamWaitEvent(cp.h2d, cp.freed[s], 0);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(in, y_host, bytes, cudaMemcpyHostToDevice, cp.h2d);
+  if (e == cudaSuccess) e = cudaEventRecord(cp.arrived[s], cp.h2d);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, cp.arrived[s], 0);
   if (e == cudaSuccess) {
     c->m.diag = c->diag;
-    e = launch_rhs(c->m, y_int, ydot_int, c->stream, &c->launches, c->prof, &c->side, c->d_stage_in,
-                   c->d_iperm);
+    e = launch_rhs(c->m, out, in, c->stream, &c->launches, c->prof, &c->side, in, c->d_iperm);
   }
   if (e == cudaSuccess) {
-    e = launch_permute(ydot_int, c->d_stage_out, c->d_perm, c->ne, c->nr, 0, c->stream);
+    e = launch_permute(in, out, c->d_perm, c->ne, c->nr, 0, c->stream);
     c->launches++;
   }
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(ydot_host, c->d_stage_out, bytes, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(cp.done[s], c->stream);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(cp.d2h, cp.done[s], 0);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(ydot_host, out, bytes, cudaMemcpyDeviceToHost, cp.d2h);
+  if (e == cudaSuccess) e = cudaEventRecord(cp.freed[s], cp.d2h);
   return e == cudaSuccess ? PIHM_GPU_OK : PIHM_GPU_ERR_CUDA;
+}
+
+// Everything a host-buffer evaluation queued: the derivatives' copies out
+// (after their kernels), then the error word on the context's stream.
+static int host_wait(pihm_gpu_ctx *c) {
+  if (c->cp.ready && cudaStreamSynchronize(c->cp.d2h) != cudaSuccess) return PIHM_GPU_ERR_CUDA;
+  return pihm_gpu_status(c);
 }
 
 int pihm_gpu_rhs_host(pihm_gpu_ctx *c, double t, const double *y_host, double *ydot_host) {
   (void)t;
   if (!c || !y_host || !ydot_host) return PIHM_GPU_ERR_ARG;
   const int rc = rhs_host_enqueue(c, y_host, ydot_host);
-  return rc != PIHM_GPU_OK ? rc : pihm_gpu_status(c);
+  return rc != PIHM_GPU_OK ? rc : host_wait(c);
 }
 
 int pihm_gpu_rhs_host_async(pihm_gpu_ctx *c, double t, const double *y_host, double *ydot_host) {
@@ -463,7 +528,7 @@ int pihm_gpu_rhs_host_async(pihm_gpu_ctx *c, double t, const double *y_host, dou
   return rhs_host_enqueue(c, y_host, ydot_host);
 }
 
-int pihm_gpu_wait(pihm_gpu_ctx *c) { return pihm_gpu_status(c); }
+int pihm_gpu_wait(pihm_gpu_ctx *c) { return c ? host_wait(c) : PIHM_GPU_ERR_ARG; }
 
 int pihm_gpu_set_host_path(pihm_gpu_ctx *c, int mode) {
   if (!c || (mode != 0 && mode != 1)) return PIHM_GPU_ERR_ARG;

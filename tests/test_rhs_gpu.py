@@ -279,9 +279,11 @@ def test_element_kernel_shapes_give_the_same_bits():
 
 
 @pytest.mark.parametrize("depth", [1, 3])
-def test_async_host_evaluations_on_two_contexts_match_sync(depth):
+@pytest.mark.parametrize("host_path", [0, 1])
+def test_async_host_evaluations_on_two_contexts_match_sync(depth, host_path):
     """pihm_gpu_rhs_host_async on two contexts of one mesh, each on its own
-    stream, alternating states (pinned buffers, direct host path), with one
+    stream, alternating states (pinned buffers; the direct host path, or the
+    copy path with its alternating staging pairs and copy streams), with one
     or several evaluations queued per context before a wait: each derivative
     equals the synchronous evaluation of the same state on a context with the
     same call history."""
@@ -310,6 +312,8 @@ def test_async_host_evaluations_on_two_contexts_match_sync(depth):
         want.append(got)
     s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
     gs = [ctx(s1.cuda_stream), ctx(s2.cuda_stream)]
+    for g in gs:
+        g.set_host_path(host_path)
     yh = [torch.from_numpy(y).pin_memory() for y in states]
     ydh = [torch.empty(ws.neq, dtype=torch.float64).pin_memory() for _ in states]
     lib = gs[0].lib
