@@ -365,26 +365,50 @@ __device__ __forceinline__ int elem_class(const DevMesh &m, const double *RESTRI
 template <int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) k_elem_main(DevMesh m, const double *RESTRICT y,
                                                     double *RESTRICT ydot) {
-  __shared__ int s_count[kElemClasses];
+  // a stable ranking: class-major, then warp, then lane, so each class keeps
+  // the block's element order and a warp's elements lie close together
+  constexpr int kWarps = BLOCK / 32, kSlots = kElemClasses * kWarps;
+  __shared__ int s_off[kSlots];  // [class][warp]: count, then exclusive offset
   __shared__ unsigned short s_order[BLOCK];
   {
     const int i0 = blockIdx.x * BLOCK + threadIdx.x;
     int sy0;
     const int cls = (i0 >= m.ne_run || skip_item(m, m.sys_elem, i0, &sy0)) ? kElemClasses - 1
                                                                           : elem_class(m, y, i0);
-    if (threadIdx.x < kElemClasses) s_count[threadIdx.x] = 0;
+    for (int k = threadIdx.x; k < kSlots; k += BLOCK) s_off[k] = 0;
     __syncthreads();
-    // rank among the block's elements of the same class: one shared atomic
-    // per class present in the warp
     const unsigned lane = threadIdx.x & 31u;
+    const int warp = threadIdx.x >> 5;
     const unsigned peers = __match_any_sync(0xffffffffu, cls);
-    const int leader = __ffs(peers) - 1;
-    int rank = 0;
-    if ((int)lane == leader) rank = atomicAdd(&s_count[cls], __popc(peers));
-    rank = __shfl_sync(0xffffffffu, rank, leader) + __popc(peers & ((1u << lane) - 1u));
+    if ((int)lane == __ffs(peers) - 1) s_off[cls * kWarps + warp] = __popc(peers);
     __syncthreads();
-    for (int c = 0; c < cls; c++) rank += s_count[c];
-    s_order[rank] = (unsigned short)threadIdx.x;
+    if (warp == 0) {
+      // exclusive scan of the kSlots counts: each lane sums its run of
+      // consecutive slots, the lanes scan their sums, then write back
+      constexpr int kRun = (kSlots + 31) / 32;
+      int run[kRun], sum = 0;
+#pragma unroll
+      for (int r = 0; r < kRun; r++) {
+        const int k = (int)lane * kRun + r;
+        run[r] = k < kSlots ? s_off[k] : 0;
+        sum += run[r];
+      }
+      int incl = sum;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, d);
+        if ((int)lane >= d) incl += v;
+      }
+      int off = incl - sum;
+#pragma unroll
+      for (int r = 0; r < kRun; r++) {
+        const int k = (int)lane * kRun + r;
+        if (k < kSlots) s_off[k] = off;
+        off += run[r];
+      }
+    }
+    __syncthreads();
+    s_order[s_off[cls * kWarps + warp] + __popc(peers & ((1u << lane) - 1u))] = (unsigned short)threadIdx.x;
     __syncthreads();
   }
   const int i = blockIdx.x * BLOCK + s_order[threadIdx.x];
