@@ -11,14 +11,14 @@ L2, so no L2 flush is needed between evaluations.
 
 Printed (one JSON line, rank 0):
   value     element-evals/s with the states resident in HBM (device pointers,
-            internal order), the states spread over two contexts of the mesh
+            internal order), the states spread over four contexts of the mesh
             on their own streams, CUDA events from the first launch to the
             last stream's end
   e2e       the same metric through the host-buffer C-ABI calls, every
             state copied from pinned host memory and every derivative back
             inside the timed region: the faster of pihm_gpu_rhs_host one
             evaluation at a time (sync_value) and pihm_gpu_rhs_host_async on
-            two contexts of the mesh, whose transfers run beside each other's
+            four contexts of the mesh, whose transfers run beside each other's
             kernels, with one or four evaluations queued per context
             (pipelined); mode says which
   roofline  the right-hand-side evaluation against the measured HBM copy
@@ -327,7 +327,7 @@ def bench_batched():
 
 
 SCAT_STATES, SCAT_EVALS = 20, 60
-RHS_CONTEXTS = 2  # contexts of the mesh the states are spread over (value and pipelined e2e)
+RHS_CONTEXTS = 4  # contexts of the mesh the states are spread over (value and pipelined e2e)
 
 
 def bench_scattered():
@@ -811,7 +811,9 @@ def main():
     stream.synchronize()
     # RHS_CONTEXTS contexts of the mesh, each on its own stream, take the
     # states in turn: independent evaluations fill each other's kernel tails
-    # and launch gaps (1: 2.23, 2: 2.48, 3: 2.51 G element-evals/s measured)
+    # and launch gaps (1: 2.62, 2: 3.16, 3: 3.23, 4: 3.19 G element-evals/s
+    # measured), and in the pipelined end-to-end leg each context's copies
+    # run under the others' kernels (2: 1.39-2.45, 3: 2.56, 4: 2.64 G)
     streams = [stream] + [torch.cuda.Stream(device=dev) for _ in range(args.contexts - 1)]
     ctxs = [g]
     for st in streams[1:]:
@@ -911,10 +913,10 @@ def main():
     e2e_copy_value = time_e2e(1)
     e2e_value = time_e2e(0)
     direct, pageable = g.host_path_info()
-    # pipelined: a second context on the same mesh and its own stream, the
-    # states alternating between the two through pihm_gpu_rhs_host_async /
-    # pihm_gpu_wait, so one evaluation's host-link transfers run beside the
-    # other's kernels (independent evaluations: an ensemble, not a CVODE
+    # pipelined: the contexts of the mesh, each on its own stream, take the
+    # states in turn through pihm_gpu_rhs_host_async / pihm_gpu_wait, so one
+    # evaluation's host-link transfers run beside the others' kernels
+    # (independent evaluations: an ensemble, not a CVODE
     # sequence); same copies, same host buffers, host clock
     pipelined = None
     try:
