@@ -28,9 +28,14 @@
 
 namespace pihm_nv {
 
+// The FP64 division for operands outside the integer path's ranges, out of
+// line: inlined behind the test it would be predicated, and every warp
+// would issue it.
+static __device__ __noinline__ double div_rn_slow(double a, double b) { return __ddiv_rn(a, b); }
+
 __device__ __forceinline__ double div_rn(double a, double b) {
   double q;
-  return pihm::im::div_i(a, b, q) ? q : __ddiv_rn(a, b);
+  return pihm::im::div_i(a, b, q) ? q : div_rn_slow(a, b);
 }
 
 // z_i = OP(a, b, x_i, y_i, z_i)
