@@ -76,6 +76,22 @@ PIHM_IM_FN int64_t mulhi(int64_t a, int64_t b) {
 #endif
 }
 
+// the high half of a 32 x 32-bit signed product (one instruction on the GPU)
+PIHM_IM_FN int32_t mulhi32(int32_t a, int32_t b) {
+#if defined(__CUDA_ARCH__)
+  return __mulhi(a, b);
+#else
+  return (int32_t)(((int64_t)a * b) >> 32);
+#endif
+}
+
+// the polynomial constants (2^62 units) in 2^31 units, rounded, for the
+// 32-bit Horner steps
+#define PIHM_IM_Q31(c62) ((int32_t)(((c62) + (1ll << 30)) >> 31))
+constexpr int32_t kImL5q = PIHM_IM_Q31(kImL5), kImL4q = PIHM_IM_Q31(kImL4);
+constexpr int32_t kImE120q = PIHM_IM_Q31(kImE120), kImE24q = PIHM_IM_Q31(kImE24), kImE6q = PIHM_IM_Q31(kImE6);
+#undef PIHM_IM_Q31
+
 PIHM_IM_FN uint64_t dbits(double x) {
 #if defined(__CUDA_ARCH__)
   return (uint64_t)__double_as_longlong(x);
@@ -117,8 +133,11 @@ PIHM_IM_FN bool log2k(double x, int &k, int64_t &w) {
   // r 2^64 = M F_i - 2^64: the low 64 bits of the product, read as signed
   const int64_t R = (int64_t)(M * (uint64_t)PIHM_IM_LD(kImLogF[i]));
   const int64_t r = R * 256;  // r 2^72, |r 2^72| < 2^61.6
-  int64_t h = kImL5;          // T(r) 2^62 by Horner's rule
-  h = kImL4 + (mulhi(h, r) >> 8);
+  // T(r) 2^62 by Horner's rule; its first step, L4 + r L5, needs about 23
+  // bits (the later products scale its error by |r| < 2^-10.4 twice more and
+  // by r^2), so it runs in 32-bit fixed point (2^31 units)
+  const int32_t r32 = (int32_t)((r + (1ll << 39)) >> 40);  // r 2^32
+  int64_t h = (int64_t)(kImL4q + mulhi32(kImL5q, r32)) << 31;
   h = kImL3 + (mulhi(h, r) >> 8);
   h = kImL2 + (mulhi(h, r) >> 8);
   const int64_t r2 = mulhi(r, r);               // r^2 2^80
@@ -152,10 +171,13 @@ PIHM_IM_FN double exp2k(TVal t) {
   const unsigned j = (unsigned)t.n & 1023u;
   int q = (int)(t.n >> 10);
   const int64_t r = mulhi(t.f, kImLn2) >> 1;   // f ln2 / 1024 in units of 2^-72
-  int64_t h = kImE120;                         // E(r) 2^62
-  h = kImE24 + (mulhi(h, r) >> 8);
-  h = kImE6 + (mulhi(h, r) >> 8);
-  h = kImE2 + (mulhi(h, r) >> 8);
+  // E(r) 2^62 by Horner's rule; E6 + r (E24 + r E120) needs about 30 bits
+  // (expm1 = r + r^2 E with |r| <= 2^-11.5), so its two steps run in 32-bit
+  // fixed point (2^31 units, error below 2^-30.9)
+  const int32_t r32 = (int32_t)((r + (1ll << 39)) >> 40);  // r 2^32
+  int32_t h31 = kImE24q + mulhi32(kImE120q, r32);
+  h31 = kImE6q + mulhi32(h31, r32);
+  const int64_t h = kImE2 + (mulhi((int64_t)h31 << 31, r) >> 8);
   const int64_t r2 = mulhi(r, r);              // r^2 2^80
   const int64_t e = r + (mulhi(r2, h) >> 6);   // expm1(r) 2^72
   const uint64_t T = PIHM_IM_LD(kImExpT[j]);   // 2^(j/1024) 2^63
@@ -224,6 +246,14 @@ PIHM_IM_FN float rsqrt_seed(float x) {
 #endif
 }
 
+PIHM_IM_FN uint32_t umulhi32(uint32_t a, uint32_t b) {
+#if defined(__CUDA_ARCH__)
+  return __umulhi(a, b);
+#else
+  return (uint32_t)(((uint64_t)a * b) >> 32);
+#endif
+}
+
 PIHM_IM_FN uint64_t umulhi(uint64_t a, uint64_t b) {
 #if defined(__CUDA_ARCH__)
   return __umul64hi(a, b);
@@ -272,12 +302,17 @@ PIHM_IM_FN bool div_i(double a, double b, double &q) {
     return true;
   }
   const uint64_t Ma = (ab & kFrac) | (1ull << 52), Mb = (bb & kFrac) | (1ull << 52);
-  // 1/mb, mb = Mb 2^-52 in [1, 2): R = r 2^63
-  uint64_t R = seed_fixed(rcp_seed(bitsf(0x3F800000u | (uint32_t)((Mb & kFrac) >> 29))));
-  const uint64_t B = Mb << 11;  // mb 2^63
-#pragma unroll
-  for (int it = 0; it < 2; it++) {
-    // e = 1 - mb r in units of 2^-62; r <- r (1 + e)
+  // 1/mb, mb = Mb 2^-52 in [1, 2): R = r 2^63.  Newton's step r <- r (1 + e),
+  // e = 1 - mb r, never overshoots 1/mb in exact arithmetic; the first step
+  // (from the seed's 2^-23 to about 2^-30) runs in 32-bit fixed point, the
+  // second (to about 2^-60) in 64-bit
+  const uint64_t R0 = seed_fixed(rcp_seed(bitsf(0x3F800000u | (uint32_t)((Mb & kFrac) >> 29))));
+  const int32_t R32 = (int32_t)(R0 >> 32);                  // r 2^31 (< 2^31)
+  const int32_t e32 = (int32_t)((1u << 30) - umulhi32((uint32_t)(Mb >> 21), (uint32_t)R32));  // e 2^30
+  uint64_t R = (uint64_t)(R32 + mulhi32(R32, e32) * 4) << 32;
+  {
+    const uint64_t B = Mb << 11;  // mb 2^63
+    // e = 1 - mb r in units of 2^-62
     const int64_t e = (int64_t)((1ull << 62) - umulhi(B, R));
     R = (uint64_t)((int64_t)R + mulhi((int64_t)R, e) * 4);
   }
@@ -323,11 +358,16 @@ PIHM_IM_FN bool sqrt_i(double x, double &r) {
   // x = m 2^(ex - odd), m = M 2^-52 in [1, 4)
   const uint64_t M = ((xb & kFrac) | (1ull << 52)) << odd;
   const float mf = bitsf((uint32_t)(0x3F800000u + ((uint32_t)odd << 23)) | (uint32_t)((xb & kFrac) >> 29));
-  uint64_t Y = seed_fixed(rsqrt_seed(mf));  // 1/sqrt(m) 2^63
-  const uint64_t Mm = M << 10;               // m 2^62
-#pragma unroll
-  for (int it = 0; it < 2; it++) {
-    // e = 1 - m y^2 in units of 2^-60; y <- y (1 + e / 2)
+  // 1/sqrt(m) by Newton's step y <- y (1 + e / 2), e = 1 - m y^2, which
+  // never overshoots in exact arithmetic: the first step (from the seed's
+  // 2^-23 to about 2^-29) in 32-bit fixed point, the second in 64-bit
+  const int32_t Y32 = (int32_t)(seed_fixed(rsqrt_seed(mf)) >> 32);  // y 2^31 (y < 1)
+  const uint32_t y2_32 = (uint32_t)(((uint64_t)Y32 * (uint64_t)Y32) >> 30);  // y^2 2^32
+  const int32_t e32 = (int32_t)((1u << 30) - umulhi32((uint32_t)(M >> 22), y2_32));  // e 2^30
+  uint64_t Y = (uint64_t)(Y32 + mulhi32(Y32, e32) * 2) << 32;  // y 2^63
+  const uint64_t Mm = M << 10;  // m 2^62
+  {
+    // e = 1 - m y^2 in units of 2^-60
     const uint64_t y2 = umulhi(Y, Y);  // y^2 2^62
     const int64_t e = (int64_t)((1ull << 60) - umulhi(Mm, y2));
     Y = (uint64_t)((int64_t)Y + mulhi((int64_t)Y, e) * 8);
