@@ -194,6 +194,31 @@ PIHM_IM_FN double exp2k(TVal t) {
   return bitsd(((uint64_t)(q + 1023) << 52) + (mant & kFrac));
 }
 
+// 1024 log2 q for q = fl(1/x), the correctly rounded reciprocal of x, from
+// x's own (k, w): q x = 1 + d exactly, with d = D 2^(ex + eq - 104) and D
+// the low 64 bits of the product of the two 53-bit mantissas (the product
+// is 2^(104 - ex - eq) + D, |D| <= 2^52), so 1024 log2 q = -(1024 k + w
+// 2^-53) + (1024/ln 2) d, the d^2 term being below 2^-100.  Saves the
+// logarithm of q where x^y and (1/x)^y are both wanted.  False unless q is
+// positive and normal with q x within 2^-51 of 1.
+PIHM_IM_FN bool log2k_recip(double x, double q, int k, int64_t w, int &kq, int64_t &wq) {
+  const uint64_t xb = dbits(x), qb = dbits(q);
+  const int ex = (int)((xb >> 52) & 2047u), eq = (int)((qb >> 52) & 2047u);
+  if (eq - 1u >= 2046u || (qb >> 63)) return false;
+  const int s = 104 - (ex - 1023) - (eq - 1023);  // q x = (Mx Mq) 2^-s
+  if (s != 104 && s != 105) return false;
+  const uint64_t Mx = (xb & kFrac) | (1ull << 52), Mq = (qb & kFrac) | (1ull << 52);
+  const int64_t D = (int64_t)(Mx * Mq);  // Mx Mq - 2^s (2^s vanishes mod 2^64)
+  if (D > (1ll << 53) || D < -(1ll << 53)) return false;  // |D| <= 2^52 for a correctly rounded q
+  // (1024/ln 2) D 2^-s in units of 2^-53: mulhi(D 2^8, kImK) is
+  // (1024/ln 2) D 2^-4 (kImK = (1024/ln 2) 2^52), rounded by 2^(57 - s)
+  const int sh = s - 57;  // 47 or 48
+  const int64_t c = (mulhi(D * 256, kImK) + (1ll << (sh - 1))) >> sh;
+  kq = -k;
+  wq = -w + c;
+  return true;
+}
+
 // x^y on the integer path; false when x or y is outside its ranges.  +0 to
 // a positive power is +0 (C99 F.9.4.4), which a full soil column produces
 // (1 - satn^m == 0).

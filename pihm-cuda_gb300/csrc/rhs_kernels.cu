@@ -84,12 +84,29 @@ __device__ __forceinline__ double overland_flow(double avg_h, double grad_h, dou
 // (pow_any), and 1/satn and the division by alpha are IEEE divisions as in
 // the reference.  The powers run on the integer pipe.
 // sq returns sqrt(satn), which EffKinf's macropore branch needs too.
+// satn^m and (1/satn)^m share satn's logarithm: the second is the power of
+// the rounded reciprocal fl(1/satn), whose logarithm follows from satn's and
+// the exact residual of the division (im::log2k_recip), within the same
+// 0.502 ulp as a power of its own.
 __device__ __forceinline__ void kr_psi(double satn, double vm, double vg_e, double vg_ib, double alpha,
                                        double &satkfunc, double &psi, double &sq) {
   sq = sqrt_any(satn);
-  const double t = 1.0 - pow_any(1.0 - pow_any(satn, vm), vg_e);
+  const double q = div_any(1.0, satn);
+  double pm, qm;  // satn^m, (1/satn)^m
+  int k, kq;
+  int64_t w, wq;
+  im::TVal t1, t3;
+  if (im::log2k(satn, k, w) && im::mul_t(vm, k, w, t1) && im::log2k_recip(satn, q, k, w, kq, wq) &&
+      im::mul_t(vm, kq, wq, t3)) {
+    pm = im::exp2k(t1);
+    qm = im::exp2k(t3);
+  } else {
+    pm = pow_any(satn, vm);
+    qm = pow_any(q, vm);
+  }
+  const double t = 1.0 - pow_any(1.0 - pm, vg_e);
   satkfunc = sq * t * t;
-  psi = cmp::neg_if(div_any(pow_any(pow_any(div_any(1.0, satn), vm) - 1.0, vg_ib), alpha), true);
+  psi = cmp::neg_if(div_any(pow_any(qm - 1.0, vg_ib), alpha), true);
 }
 
 // Batch engine: whether the watershed of item idx sits out this evaluation

@@ -52,3 +52,21 @@ void im_sqrt(const double *x, double *r, int32_t *ok, int64_t n) {
   }
 }
 }
+
+extern "C" {
+// out[i] = fl(1/x[i])^y[i] through the logarithm of x[i] (log2k_recip);
+// ok[i] = 0 where a step declines
+void im_pow_recip(const double *x, const double *y, double *out, int32_t *ok, int64_t n) {
+  for (int64_t i = 0; i < n; i++) {
+    double q = 0.0, r = 0.0;
+    int k = 0, kq = 0;
+    int64_t w = 0, wq = 0;
+    pihm::im::TVal t{0, 0};
+    const bool good = pihm::im::div_i(1.0, x[i], q) && pihm::im::log2k(x[i], k, w) &&
+                      pihm::im::log2k_recip(x[i], q, k, w, kq, wq) && pihm::im::mul_t(y[i], kq, wq, t);
+    if (good) r = pihm::im::exp2k(t);
+    ok[i] = good ? 1 : 0;
+    out[i] = r;
+  }
+}
+}
