@@ -413,20 +413,22 @@ int pihm_gpu_status(pihm_gpu_ctx *c) {
   return PIHM_GPU_OK;
 }
 
-// The copy path's second staging pair, streams and events, on first use.
+// The copy path's staging pairs, streams and events, on first use.
 static bool copy_path_init(pihm_gpu_ctx *c) {
   auto &cp = c->cp;
   if (cp.ready) return true;
   const size_t bytes = sizeof(double) * c->neq;
-  const size_t half = (bytes + 255) & ~size_t(255);
-  if (cudaMalloc(&cp.second, 2 * half) != cudaSuccess) {
-    cp.second = nullptr;
+  const size_t one = (bytes + 255) & ~size_t(255);
+  // staging of its own: the direct path's kernels use d_stage_in/out on the
+  // context's stream, which this path's copy streams are not ordered after
+  if (cudaMalloc(&cp.staging, 4 * one) != cudaSuccess) {
+    cp.staging = nullptr;
     return false;
   }
-  cp.in[0] = c->d_stage_in;
-  cp.out[0] = c->d_stage_out;
-  cp.in[1] = (double *)cp.second;
-  cp.out[1] = (double *)((char *)cp.second + half);
+  for (int k = 0; k < 2; k++) {
+    cp.in[k] = (double *)((char *)cp.staging + (2 * k) * one);
+    cp.out[k] = (double *)((char *)cp.staging + (2 * k + 1) * one);
+  }
   bool ok = cudaStreamCreateWithFlags(&cp.h2d, cudaStreamNonBlocking) == cudaSuccess &&
             cudaStreamCreateWithFlags(&cp.d2h, cudaStreamNonBlocking) == cudaSuccess;
   for (int k = 0; k < 2 && ok; k++)
@@ -450,7 +452,7 @@ static void copy_path_release(pihm_gpu_ctx *c) {
       if (e) cudaEventDestroy(e);
   if (cp.h2d) cudaStreamDestroy(cp.h2d);
   if (cp.d2h) cudaStreamDestroy(cp.d2h);
-  if (cp.second) cudaFree(cp.second);
+  if (cp.staging) cudaFree(cp.staging);
   cp = pihm_gpu_ctx::CopyPath{};
 }
 

@@ -286,13 +286,13 @@ struct pihm_gpu_ctx {
   void *d_dyn;     // inputs + scratch
   size_t dyn_bytes;
   double *d_stage_in, *d_stage_out;   // host-path staging [neq]
-  // Copy path of the host-buffer evaluation: two staging pairs, so the next
-  // evaluation's state can arrive while this one's kernels run, and one
-  // stream per copy direction, so a copy never waits behind a kernel it does
-  // not depend on (created on the first copy-path evaluation).
+  // Copy path of the host-buffer evaluation: two staging pairs of its own,
+  // so the next evaluation's state can arrive while this one's kernels run,
+  // and one stream per copy direction, so a copy never waits behind a kernel
+  // it does not depend on (created on the first copy-path evaluation).
   struct CopyPath {
     double *in[2] = {nullptr, nullptr}, *out[2] = {nullptr, nullptr};
-    void *second = nullptr;  // allocation holding in[1], out[1]
+    void *staging = nullptr;  // allocation holding both pairs
     cudaStream_t h2d = nullptr, d2h = nullptr;
     cudaEvent_t arrived[2] = {nullptr, nullptr}, done[2] = {nullptr, nullptr}, freed[2] = {nullptr, nullptr};
     int slot = 0;

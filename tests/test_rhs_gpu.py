@@ -331,3 +331,45 @@ def test_async_host_evaluations_on_two_contexts_match_sync(depth, host_path):
         assert np.array_equal(ydh[k].numpy(), want[k]), k
     for g in gs + refs:
         g.close()
+
+
+def test_async_host_paths_switched_with_evaluations_in_flight():
+    """One context queues evaluations on the copy path, switches to the
+    direct path and queues more before waiting: the copy path stages through
+    buffers of its own, so every derivative equals the synchronous
+    evaluation of the same state in the same order."""
+    import ctypes
+    import torch
+    from pihm_gpu import workloads as WL
+    from pihm_gpu.capi import GpuRhs
+    ws = W.generate(20_000, WL.river_count(20_000), seed=15)
+    base = W.reference_state(ws, 15)
+    forcing = W.random_forcing(ws, 15)
+    states = [W.jitter(base, 950 + k) for k in range(6)]
+    f64p = ctypes.POINTER(ctypes.c_double)
+
+    def ctx(stream=None):
+        g = GpuRhs(ws, stream=stream)
+        g.set_forcing(*forcing)
+        g.set_ws0_surf(base[:ws.nelem])
+        return g
+
+    ref = ctx()
+    want = []
+    for y in states:
+        got, rc = ref.rhs_host(y)
+        assert rc == 0
+        want.append(got)
+    st = torch.cuda.Stream()
+    g = ctx(st.cuda_stream)
+    yh = [torch.from_numpy(y).pin_memory() for y in states]
+    ydh = [torch.empty(ws.neq, dtype=torch.float64).pin_memory() for _ in states]
+    for k in range(len(states)):
+        g.set_host_path(1 if k % 3 != 2 else 0)
+        assert g.lib.pihm_gpu_rhs_host_async(g.h, 0.0, ctypes.cast(yh[k].data_ptr(), f64p),
+                                             ctypes.cast(ydh[k].data_ptr(), f64p)) == 0
+    assert g.lib.pihm_gpu_wait(g.h) == 0
+    for k in range(len(states)):
+        assert np.array_equal(ydh[k].numpy(), want[k]), k
+    for c in (g, ref):
+        c.close()
