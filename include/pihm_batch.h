@@ -171,11 +171,11 @@ int pihm_batch_set_program_variant(pihm_batch *b, int32_t variant);
 
 /* The right-hand side's element kernel (k_elem_main) comes in three block
  * shapes with the same register budget -- 0: 512 threads x 2 blocks per SM,
- * 1: 256 x 4, 2: 128 x 8 -- that give identical results: large blocks are
- * fastest over large arenas, small ones spread a small or sparsely occupied
- * arena over more SMs.  By default (-1) the engine times them on its first
- * evaluations over at least 20,000 elements and keeps the fastest per
- * element; 0..2 forces one. */
+ * 1: 256 x 4, 2: 128 x 8 -- that give identical results: 256 x 4 is fastest
+ * on one large mesh, smaller blocks spread a small or sparsely occupied
+ * arena over more SMs.  By default (-1) the engine uses 256 x 4 until it has
+ * timed the three on its first evaluations over at least 20,000 elements,
+ * then keeps the fastest per element; 0..2 forces one. */
 int pihm_batch_set_rhs_shape(pihm_batch *b, int32_t shape);
 
 /* ---- serving --------------------------------------------------------------
