@@ -15,7 +15,8 @@ by up to 6.2e-3 of its peak and single storages by up to 17 % of
 max(|storage|, 1 mm) after 2 days.  The GPU right-hand side differs from the
 reference's by about an ulp (pow, fused multiply-adds, reciprocals, reduction
 order), so its end-to-end run is held to that envelope: no farther from the
-reference than twice the farthest perturbed run, in each measure."""
+reference than the farthest perturbed run, in each measure (the GPU run sits
+at about 0.6 of the hydrograph envelope and 0.3 of the storage envelope)."""
 import os
 
 import numpy as np
@@ -130,8 +131,8 @@ def test_gpu_solve_hydrograph_and_storages():
     print(f"GPU solve: nst {s.nst} nfe {s.nfe} (reference {z['stats'][0]} {z['stats'][1]}); "
           f"hydrograph err {qerr:.2e} (envelope {qenv:.2e}), storage err {serr:.2e} "
           f"(envelope {senv:.2e})")
-    assert qerr <= 2 * qenv
-    assert serr <= 2 * senv
+    assert qerr <= qenv
+    assert serr <= senv
     span = nmax - nmin
     assert nmin - span <= s.nst <= nmax + span
     # mass balance: the cumulative residual is no worse than the reference
