@@ -4,12 +4,15 @@
 // seven launches with no host synchronisation, the two river kernels on a
 // second stream beside k_elem_grad/k_edge/k_elem_main (k_edge is listed at
 // its definition: each interior edge is evaluated once and read with a sign
-// by both elements).  GB300 issues ~2 FP64 instructions per clock per SM,
-// so the kernels are FP64-issue bound: powers go through the table-driven
-// pow_fast (fp64_math.cuh), divisions by static quantities are multiplications
-// by reciprocals computed at load, and sub-expressions the reference
-// re-evaluates (EffKh per edge side, KrFunc/Psi in Infil and Recharge) are
-// computed once.
+// by both elements).  GB300 issues ~2 FP64 lanes per clock per SM, so the
+// FP64 pipe is the scarce one: the element rows' powers, divisions and
+// square roots run in fixed point on the integer pipe (int_math.cuh; the
+// divisions and roots IEEE-exact), comparisons and sign flips on the
+// integer pipe too (fp64_cmp.h), divisions by static quantities are
+// multiplications by reciprocals computed at load, sub-expressions the
+// reference re-evaluates (EffKh per edge side, KrFunc/Psi in Infil and
+// Recharge) are computed once, and each block ranks its elements by branch
+// class so that a warp's lanes share their branches.
 //
 //   k_elem_prep   per element: clamp y (src/ode.c:25-49), SurfH
 //                 (src/hydrol.c:100-134), surface head zmax + surfh and the
