@@ -930,7 +930,7 @@ def main():
 
         def run(n, depth):
             # up to depth evaluations queued per context: pihm_gpu_wait
-            # drains one context while the other's queue keeps the device busy
+            # drains one context while the others' queues keep the device busy
             queued = [0] * nc
             for k in range(n):
                 c = k % nc
@@ -944,11 +944,10 @@ def main():
         by_path = {}
         for mode, name in ((0, "direct"), (1, "copy")):
             # direct: the kernels read and write host memory (SM time on the
-            # link); copy: the copy engines move it, beside the other
-            # context's kernels.  Copies queued behind a context's unfinished
-            # kernels can hold up the other context's copies, so each path
-            # is timed with one and with PIPE_DEPTH evaluations queued per
-            # context
+            # link); copy: each context's copy streams move it, beside the
+            # other contexts' kernels.  Each path is timed with one and with
+            # PIPE_DEPTH evaluations queued per context (a wait drains a
+            # whole context, so the best depth depends on the path)
             for c in ctxs:
                 c.set_host_path(mode)
             for depth in (1, PIPE_DEPTH):
